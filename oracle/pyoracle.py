@@ -1,0 +1,135 @@
+"""ctypes front end of the oracle library (oracle/_build/liboracle_pgl.so) and of
+the reference harness (oracle/_ref/ref_harness, x86 hosts with the reference
+tree only).  Test infrastructure: used by tests/, __graft_entry__.smoke() and
+bench.py's CPU baseline, never by the product.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle_pgl.so")
+REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+
+QUERY_OUT_DTYPE = np.dtype(
+    [("ok", "<u4"), ("id", "<u4"), ("sample1d", "<f4"), ("dir", "<f4", (3,)), ("pdf", "<f4"), ("pdfLi", "<f4")]
+)
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        lib = ctypes.CDLL(LIB_PATH)
+        vp, u64 = ctypes.c_void_p, ctypes.c_uint64
+        lib.orc_field_new.restype = vp
+        lib.orc_field_new.argtypes = [ctypes.c_int, u64, ctypes.c_int]
+        lib.orc_field_free.argtypes = [vp]
+        lib.orc_field_update.argtypes = [vp, vp, u64]
+        lib.orc_field_iteration.restype = u64
+        lib.orc_field_iteration.argtypes = [vp]
+        lib.orc_field_store.restype = u64
+        lib.orc_field_store.argtypes = [vp, ctypes.c_char_p, u64]
+        lib.orc_field_query.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, u64]
+        lib.orc_field_leaf_of.argtypes = [vp, ctypes.c_int, vp, vp, u64]
+        lib.orc_field_set_scene_bounds.argtypes = [vp, vp]
+        for n in ("orc_fexp", "orc_flog", "orc_rcp", "orc_rsqrt"):
+            getattr(lib, n).restype = ctypes.c_float
+            getattr(lib, n).argtypes = [ctypes.c_float]
+        _lib = lib
+    return _lib
+
+
+class OracleField:
+    """Oracle restatement of a kd-tree PA-VMM field (deterministic CPU_8)."""
+
+    def __init__(self, max_samples_per_leaf=32000, deterministic=True, threads=1):
+        self.lib = load()
+        self.h = self.lib.orc_field_new(int(deterministic), int(max_samples_per_leaf), int(threads))
+
+    def close(self):
+        if self.h:
+            self.lib.orc_field_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_scene_bounds(self, lower, upper):
+        b = np.ascontiguousarray(np.concatenate([lower, upper]).astype(np.float32))
+        self.lib.orc_field_set_scene_bounds(self.h, b.ctypes.data)
+
+    def update(self, samples):
+        s = np.ascontiguousarray(samples)
+        self.lib.orc_field_update(self.h, s.ctypes.data, len(s))
+
+    @property
+    def iteration(self):
+        return int(self.lib.orc_field_iteration(self.h))
+
+    def field_bytes(self):
+        n = self.lib.orc_field_store(self.h, None, 0)
+        buf = ctypes.create_string_buffer(int(n))
+        self.lib.orc_field_store(self.h, buf, n)
+        return buf.raw
+
+    def query(self, queries, volume=False, cosine=True):
+        q = np.ascontiguousarray(queries)
+        out = np.zeros(len(q), dtype=QUERY_OUT_DTYPE)
+        self.lib.orc_field_query(self.h, int(volume), int(cosine), q.ctypes.data, out.ctypes.data, len(q))
+        return out
+
+    def leaf_of(self, positions, volume=False):
+        p = np.ascontiguousarray(np.asarray(positions, np.float32).reshape(-1, 3))
+        out = np.zeros(len(p), dtype=np.int32)
+        self.lib.orc_field_leaf_of(self.h, int(volume), p.ctypes.data, out.ctypes.data, len(p))
+        return out
+
+
+def reference_available():
+    return os.path.exists(REF_HARNESS)
+
+
+def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministic=True, threads=1, device=8):
+    """Runs the reference library on ``frames`` (list of sample arrays) and
+    returns (field file bytes, per-frame update ms, surface query out, volume
+    query out)."""
+    import sys
+
+    sys.path.insert(0, os.path.dirname(HERE))
+    from openpgl_gb300 import synthetic
+
+    with tempfile.TemporaryDirectory() as td:
+        fpath = os.path.join(td, "frames.bin")
+        with open(fpath, "wb") as f:
+            f.write(synthetic.frames_blob(frames))
+        args = [REF_HARNESS, fpath, os.path.join(td, "ref"), str(device), str(threads),
+                str(max_samples_per_leaf), str(int(deterministic))]
+        if queries is not None:
+            qpath = os.path.join(td, "q.bin")
+            with open(qpath, "wb") as f:
+                f.write(synthetic.queries_blob(queries))
+            args.append(qpath)
+        env = dict(os.environ)
+        env["PGL_ORACLE_THREADS"] = str(threads)
+        subprocess.run(args, check=True, env=env)
+        field = open(os.path.join(td, "ref.field"), "rb").read()
+        times = [float(x) for x in open(os.path.join(td, "ref.times")).read().split()]
+        sq = vq = None
+        if queries is not None:
+            sq = np.fromfile(os.path.join(td, "ref.surfq.bin"), dtype=QUERY_OUT_DTYPE)
+            vq = np.fromfile(os.path.join(td, "ref.volq.bin"), dtype=QUERY_OUT_DTYPE)
+        return field, times, sq, vq

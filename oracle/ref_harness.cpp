@@ -1,0 +1,136 @@
+// Drives the UNMODIFIED reference library (oracle/_ref/libopenpgl_ref.so)
+// through its own public C++ wrapper only, the way a renderer would.  Used to
+// produce golden outputs (tests/golden/) and to time the reference CPU path.
+// Test infrastructure; never part of the product.
+//
+// usage: ref_harness <frames.bin> <out_prefix> <device 4|8> <threads>
+//                    <maxSamplesPerLeaf> <deterministic 0|1> [queries.bin]
+// frames.bin : u64 numFrames, then per frame u64 n + n * PGLSampleData (40 B)
+// queries.bin: u64 n, then n * {pos f3, normal f3, sample1D f, u f2} (36 B)
+// outputs    : <out_prefix>.field      (reference field file after the last frame)
+//              <out_prefix>.times      (per-frame Update wall time in ms, text)
+//              <out_prefix>.surfq.bin  n * {ok u32, id u32, s1d f, dir f3, pdf f,
+//                                           pdfLi f} (surface queries)
+//              <out_prefix>.volq.bin   same for the volume field
+#include <openpgl/cpp/OpenPGL.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+struct Query {
+  float pos[3], normal[3], s1d, u[2];
+};
+struct QueryOut {
+  uint32_t ok, id;
+  float s1d, dir[3], pdf, pdfLi;
+};
+
+bool readAll(const char *path, std::vector<char> &buf) {
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return false;
+  std::fseek(f, 0, SEEK_END);
+  long sz = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  buf.resize(size_t(sz));
+  size_t got = std::fread(buf.data(), 1, buf.size(), f);
+  std::fclose(f);
+  return got == buf.size();
+}
+}  // namespace
+
+int main(int argc, char **argv) {
+  if (argc < 7) {
+    std::fprintf(stderr, "usage: %s frames.bin out_prefix device threads maxSamplesPerLeaf deterministic [queries.bin]\n", argv[0]);
+    return 2;
+  }
+  const std::string prefix = argv[2];
+  const int dev = std::atoi(argv[3]);
+  const int threads = std::atoi(argv[4]);
+  const size_t maxLeaf = std::strtoull(argv[5], nullptr, 10);
+  const bool deterministic = std::atoi(argv[6]) != 0;
+
+  std::vector<char> frames;
+  if (!readAll(argv[1], frames)) {
+    std::fprintf(stderr, "cannot read %s\n", argv[1]);
+    return 1;
+  }
+
+  openpgl::cpp::Device device(dev == 4 ? PGL_DEVICE_TYPE_CPU_4 : PGL_DEVICE_TYPE_CPU_8, size_t(threads));
+  openpgl::cpp::FieldConfig cfg;
+  cfg.Init(PGL_SPATIAL_STRUCTURE_KDTREE, PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM, deterministic, maxLeaf);
+  openpgl::cpp::Field field(&device, cfg);
+  openpgl::cpp::SampleStorage storage;
+
+  const char *p = frames.data();
+  uint64_t numFrames;
+  std::memcpy(&numFrames, p, 8);
+  p += 8;
+  FILE *times = std::fopen((prefix + ".times").c_str(), "w");
+  for (uint64_t f = 0; f < numFrames; ++f) {
+    uint64_t n;
+    std::memcpy(&n, p, 8);
+    p += 8;
+    storage.AddSamples(reinterpret_cast<const PGLSampleData *>(p), size_t(n));
+    p += n * sizeof(PGLSampleData);
+    auto t0 = std::chrono::steady_clock::now();
+    field.Update(storage);
+    auto t1 = std::chrono::steady_clock::now();
+    storage.Clear();
+    std::fprintf(times, "%.6f\n", std::chrono::duration<double, std::milli>(t1 - t0).count());
+  }
+  std::fclose(times);
+  field.Store(prefix + ".field");
+
+  if (argc > 7) {
+    std::vector<char> qbuf;
+    if (!readAll(argv[7], qbuf)) return 1;
+    uint64_t nq;
+    std::memcpy(&nq, qbuf.data(), 8);
+    const Query *q = reinterpret_cast<const Query *>(qbuf.data() + 8);
+    std::vector<QueryOut> surf(nq), vol(nq);
+    openpgl::cpp::SurfaceSamplingDistribution ssd(&field);
+    openpgl::cpp::VolumeSamplingDistribution vsd(&field);
+    for (uint64_t i = 0; i < nq; ++i) {
+      pgl_point3f pos = {q[i].pos[0], q[i].pos[1], q[i].pos[2]};
+      pgl_vec3f nrm = {q[i].normal[0], q[i].normal[1], q[i].normal[2]};
+      pgl_point2f u = {q[i].u[0], q[i].u[1]};
+      QueryOut &o = surf[i];
+      std::memset(&o, 0, sizeof(o));
+      float s1d = q[i].s1d;
+      o.ok = ssd.Init(&field, pos, s1d) ? 1u : 0u;
+      o.s1d = s1d;
+      if (o.ok) {
+        ssd.ApplyCosineProduct(nrm);
+        pgl_vec3f d;
+        o.pdf = ssd.SamplePDF(u, d);
+        o.dir[0] = d.x; o.dir[1] = d.y; o.dir[2] = d.z;
+        o.pdfLi = ssd.IncomingRadiancePDF(d);
+        o.id = ssd.GetId();
+      }
+      QueryOut &v = vol[i];
+      std::memset(&v, 0, sizeof(v));
+      float s1dv = q[i].s1d;
+      v.ok = vsd.Init(&field, pos, s1dv) ? 1u : 0u;
+      v.s1d = s1dv;
+      if (v.ok) {
+        pgl_vec3f d;
+        v.pdf = vsd.SamplePDF(u, d);
+        v.dir[0] = d.x; v.dir[1] = d.y; v.dir[2] = d.z;
+        v.pdfLi = vsd.IncomingRadiancePDF(d);
+        v.id = vsd.GetId();
+      }
+    }
+    FILE *fs = std::fopen((prefix + ".surfq.bin").c_str(), "wb");
+    std::fwrite(surf.data(), sizeof(QueryOut), surf.size(), fs);
+    std::fclose(fs);
+    FILE *fv = std::fopen((prefix + ".volq.bin").c_str(), "wb");
+    std::fwrite(vol.data(), sizeof(QueryOut), vol.size(), fv);
+    std::fclose(fv);
+  }
+  return 0;
+}

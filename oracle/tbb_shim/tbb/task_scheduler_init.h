@@ -1,0 +1,3 @@
+// Forwarding header of the oracle-only TBB stand-in.
+#pragma once
+#include "../tbb_shim.h"
