@@ -1,0 +1,22 @@
+// Umbrella header of the C API (reference: include/openpgl/openpgl.h).
+#pragma once
+
+#define OPENPGL_INLINE inline
+
+#ifndef OPENPGL_DISABLE_ASSERTS
+#include <assert.h>
+#define OPENPGL_ASSERT(cond) assert(cond);
+#else
+#define OPENPGL_ASSERT(cond)
+#endif
+
+#include "common.h"
+#include "data.h"
+#include "device.h"
+#include "field.h"
+#include "fieldstatistics.h"
+#include "pathsegmentstorage.h"
+#include "region.h"
+#include "samplestorage.h"
+#include "surfacesamplingdistribution.h"
+#include "volumesamplingdistribution.h"

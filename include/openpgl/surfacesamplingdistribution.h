@@ -1,0 +1,29 @@
+// Surface sampling distribution (reference: include/openpgl/surfacesamplingdistribution.h:24-46;
+// api.cpp:587-657).
+#pragma once
+#include "common.h"
+#include "region.h"
+#ifdef __cplusplus
+extern "C" {
+struct SurfaceSamplingDistribution;
+#endif
+typedef struct SurfaceSamplingDistribution *PGLSurfaceSamplingDistribution;
+
+OPENPGL_CORE_INTERFACE void pglReleaseSurfaceSamplingDistribution(PGLSurfaceSamplingDistribution d);
+OPENPGL_CORE_INTERFACE void pglSurfaceSamplingDistributionApplyCosineProduct(PGLSurfaceSamplingDistribution d,
+                                                                             pgl_vec3f normal);
+OPENPGL_CORE_INTERFACE bool pglSurfaceSamplingDistributionSupportsApplyCosineProduct(PGLSurfaceSamplingDistribution d);
+OPENPGL_CORE_INTERFACE pgl_vec3f pglSurfaceSamplingDistributionSample(PGLSurfaceSamplingDistribution d,
+                                                                      pgl_point2f sample);
+OPENPGL_CORE_INTERFACE float pglSurfaceSamplingDistributionPDF(PGLSurfaceSamplingDistribution d, pgl_vec3f direction);
+OPENPGL_CORE_INTERFACE float pglSurfaceSamplingDistributionSamplePDF(PGLSurfaceSamplingDistribution d,
+                                                                     pgl_point2f sample, pgl_vec3f &direction);
+OPENPGL_CORE_INTERFACE float pglSurfaceSamplingDistributionIncomingRadiancePDF(PGLSurfaceSamplingDistribution d,
+                                                                               pgl_vec3f direction);
+OPENPGL_CORE_INTERFACE uint32_t pglSurfaceSamplingDistributionGetId(PGLSurfaceSamplingDistribution d);
+OPENPGL_CORE_INTERFACE bool pglSurfaceSamplingDistributionValidate(PGLSurfaceSamplingDistribution d);
+OPENPGL_CORE_INTERFACE void pglSurfaceSamplingDistributionClear(PGLSurfaceSamplingDistribution d);
+OPENPGL_CORE_INTERFACE PGLRegion pglSurfaceSamplingGetRegion(PGLSurfaceSamplingDistribution d);
+#ifdef __cplusplus
+}
+#endif

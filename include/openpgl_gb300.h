@@ -1,0 +1,60 @@
+// Entry points appended to the Open PGL C API by the GB300 library.  They have
+// no counterpart in the reference; they expose the batched GPU forms of the
+// guided query and of the sample ingest, and diagnostics.
+#pragma once
+
+#include "openpgl/openpgl.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// One guided query: position, normal (for the cosine product), the 1D random
+// number of the stochastic region choice, and the 2D random number of the
+// direction sample (36 bytes).
+typedef struct {
+  pgl_point3f position;
+  pgl_vec3f normal;
+  float sample1D;
+  pgl_point2f sample2D;
+} PGLGuidedQuery;
+
+// Result of Init + (cosine product) + SamplePDF + IncomingRadiancePDF (32 bytes).
+typedef struct {
+  uint32_t valid;     // Init succeeded
+  uint32_t id;        // kd leaf (GetId)
+  float sample1D;     // sample1D after the region choice rescaled it
+  pgl_vec3f direction;
+  float pdf;          // SamplePDF
+  float pdfLi;        // IncomingRadiancePDF(direction)
+} PGLGuidedQueryResult;
+
+// Guided queries on host buffers: copies the queries in, runs one kernel,
+// copies the results out.  Same results as the per-object calls.
+OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceBatch(PGLField field, const PGLGuidedQuery *queries, size_t n,
+                                                       PGLGuidedQueryResult *results, bool cosineProduct);
+OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatch(PGLField field, const PGLGuidedQuery *queries, size_t n,
+                                                      PGLGuidedQueryResult *results);
+// Guided queries on device buffers, enqueued on `cudaStream` (a cudaStream_t,
+// or null for the library's stream); does not synchronise.
+OPENPGL_CORE_INTERFACE bool pglFieldSampleBatchDevice(PGLField field, bool volume, const PGLGuidedQuery *dQueries,
+                                                      size_t n, PGLGuidedQueryResult *dResults, bool cosineProduct,
+                                                      void *cudaStream);
+// Adds samples that already live in device memory.
+OPENPGL_CORE_INTERFACE void pglSampleStorageAddSamplesDevice(PGLSampleStorage sampleStorage,
+                                                             const PGLSampleData *dSamples, size_t numSamples);
+// Serialised field (the bytes pglFieldStoreToFile writes); returns the size,
+// copies when buffer holds at least that many bytes.
+OPENPGL_CORE_INTERFACE size_t pglFieldStoreToBuffer(PGLField field, char *buffer, size_t capacity);
+// Milliseconds of the last Update of the surface (0) or volume (1) field:
+// total, sample copy, spatial structure, directional fitting.
+OPENPGL_CORE_INTERFACE bool pglFieldGetLastUpdateTimings(PGLField field, int volume, float out4[4]);
+// Per-region counters of the last Update: region, EM iterations, splits,
+// merges, components (5 x u32 per region); returns the region count.
+OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int volume, uint32_t *out, size_t capacity);
+// Message of the last error raised on this thread ("" if none).
+OPENPGL_CORE_INTERFACE const char *pglGetLastError();
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,394 @@
+"""Python front end of libopenpgl_gb300.so, the GB300 implementation of Open
+PGL's field-training and guided-query path behind the Open PGL C API.
+
+The classes mirror the reference's C++ wrapper (openpgl/include/openpgl/cpp/:
+Device, FieldConfig, Field, SampleStorage, SurfaceSamplingDistribution,
+VolumeSamplingDistribution) and call the exported C functions through ctypes.
+There is no fallback: if the library cannot be loaded, or no GPU is present,
+constructing a Device raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .synthetic import PGL_QUERY_DTYPE, PGL_SAMPLE_DTYPE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libopenpgl_gb300.so")
+
+PGL_DEVICE_TYPE_CPU_4, PGL_DEVICE_TYPE_CPU_8, PGL_DEVICE_TYPE_CPU_16, PGL_DEVICE_TYPE_NONE = 0, 1, 2, 3
+PGL_DEVICE_TYPE_GPU_SM103 = 4
+PGL_SPATIAL_STRUCTURE_KDTREE = 0
+PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM = 0
+
+QUERY_RESULT_DTYPE = np.dtype(
+    [("ok", "<u4"), ("id", "<u4"), ("sample1d", "<f4"), ("dir", "<f4", (3,)), ("pdf", "<f4"), ("pdfLi", "<f4")]
+)
+assert QUERY_RESULT_DTYPE.itemsize == 32
+
+
+class Vec3(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_float), ("y", ctypes.c_float), ("z", ctypes.c_float)]
+
+
+class Vec2(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_float), ("y", ctypes.c_float)]
+
+
+class Box3(ctypes.Structure):
+    _fields_ = [("lower", Vec3), ("upper", Vec3)]
+
+
+class SampleData(ctypes.Structure):
+    _fields_ = [("position", Vec3), ("direction", Vec3), ("weight", ctypes.c_float), ("pdf", ctypes.c_float),
+                ("distance", ctypes.c_float), ("flags", ctypes.c_uint32)]
+
+
+class FieldArguments(ctypes.Structure):  # PGLFieldArguments (config.h)
+    _fields_ = [("spatialStructureType", ctypes.c_int), ("spatialStructureArguments", ctypes.c_void_p),
+                ("directionalDistributionType", ctypes.c_int), ("directionalDistributionArguments", ctypes.c_void_p),
+                ("deterministic", ctypes.c_bool), ("fitRegions", ctypes.c_bool)]
+
+
+class PGLString(ctypes.Structure):
+    _fields_ = [("m_str", ctypes.c_char_p), ("m_size", ctypes.c_size_t)]
+
+
+# Exported symbols of include/openpgl/*.h and include/openpgl_gb300.h.
+C_API = {
+    "pglNewDevice": (ctypes.c_void_p, [ctypes.c_int, ctypes.c_size_t]),
+    "pglReleaseDevice": (None, [ctypes.c_void_p]),
+    "pglDeviceNewField": (ctypes.c_void_p, [ctypes.c_void_p, FieldArguments]),
+    "pglDeviceNewFieldFromFile": (ctypes.c_void_p, [ctypes.c_void_p, ctypes.c_char_p]),
+    "pglFieldArgumentsSetDefaults": (None, [ctypes.POINTER(FieldArguments), ctypes.c_int, ctypes.c_int, ctypes.c_bool,
+                                            ctypes.c_size_t]),
+    "pglReleaseField": (None, [ctypes.c_void_p]),
+    "pglFieldStoreToFile": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_char_p]),
+    "pglFieldGetIteration": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "pglFieldSetSceneBounds": (None, [ctypes.c_void_p, Box3]),
+    "pglFieldGetSceneBounds": (Box3, [ctypes.c_void_p]),
+    "pglFieldUpdate": (None, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pglFieldUpdateSurface": (None, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pglFieldUpdateVolume": (None, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pglFieldReset": (None, [ctypes.c_void_p]),
+    "pglFieldNewSurfaceSamplingDistribution": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "pglFieldInitSurfaceSamplingDistribution": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, Vec3,
+                                                                ctypes.POINTER(ctypes.c_float)]),
+    "pglFieldNewVolumeSamplingDistribution": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "pglFieldInitVolumeSamplingDistribution": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, Vec3,
+                                                               ctypes.POINTER(ctypes.c_float)]),
+    "pglFieldValidate": (ctypes.c_bool, [ctypes.c_void_p]),
+    "pglFieldCompare": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pglFieldGetSurfaceStatistics": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "pglFieldGetVolumeStatistics": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "pglReleaseFieldStatistics": (None, [ctypes.c_void_p]),
+    "pglFieldStatisticsToString": (PGLString, [ctypes.c_void_p]),
+    "pglFieldStatisticsHeaderCSVString": (PGLString, [ctypes.c_void_p]),
+    "pglFieldStatisticsToCSVString": (PGLString, [ctypes.c_void_p]),
+    "pglReleaseString": (None, [PGLString]),
+    "pglNewSampleStorage": (ctypes.c_void_p, []),
+    "pglNewSampleStorageFromFile": (ctypes.c_void_p, [ctypes.c_char_p]),
+    "pglReleaseSampleStorage": (None, [ctypes.c_void_p]),
+    "pglSampleStorageStoreToFile": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_char_p]),
+    "pglSampleStorageAddSample": (None, [ctypes.c_void_p, ctypes.POINTER(SampleData)]),
+    "pglSampleStorageAddSamples": (None, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "pglSampleStorageReserve": (None, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]),
+    "pglSampleStorageClear": (None, [ctypes.c_void_p]),
+    "pglSampleStorageClearSurface": (None, [ctypes.c_void_p]),
+    "pglSampleStorageClearVolume": (None, [ctypes.c_void_p]),
+    "pglSampleStorageGetSizeSurface": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "pglSampleStorageGetSizeVolume": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "pglSampleStorageGetSampleSurface": (SampleData, [ctypes.c_void_p, ctypes.c_int]),
+    "pglSampleStorageGetSampleVolume": (SampleData, [ctypes.c_void_p, ctypes.c_int]),
+    "pglSampleStorageValidate": (ctypes.c_bool, [ctypes.c_void_p]),
+    "pglSampleStorageCompare": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pglReleaseSurfaceSamplingDistribution": (None, [ctypes.c_void_p]),
+    "pglSurfaceSamplingDistributionApplyCosineProduct": (None, [ctypes.c_void_p, Vec3]),
+    "pglSurfaceSamplingDistributionSupportsApplyCosineProduct": (ctypes.c_bool, [ctypes.c_void_p]),
+    "pglSurfaceSamplingDistributionSample": (Vec3, [ctypes.c_void_p, Vec2]),
+    "pglSurfaceSamplingDistributionPDF": (ctypes.c_float, [ctypes.c_void_p, Vec3]),
+    "pglSurfaceSamplingDistributionSamplePDF": (ctypes.c_float, [ctypes.c_void_p, Vec2, ctypes.POINTER(Vec3)]),
+    "pglSurfaceSamplingDistributionIncomingRadiancePDF": (ctypes.c_float, [ctypes.c_void_p, Vec3]),
+    "pglSurfaceSamplingDistributionGetId": (ctypes.c_uint32, [ctypes.c_void_p]),
+    "pglSurfaceSamplingDistributionValidate": (ctypes.c_bool, [ctypes.c_void_p]),
+    "pglSurfaceSamplingDistributionClear": (None, [ctypes.c_void_p]),
+    "pglSurfaceSamplingGetRegion": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "pglReleaseVolumeSamplingDistribution": (None, [ctypes.c_void_p]),
+    "pglVolumeSamplingDistributionSample": (Vec3, [ctypes.c_void_p, Vec2]),
+    "pglVolumeSamplingDistributionPDF": (ctypes.c_float, [ctypes.c_void_p, Vec3]),
+    "pglVolumeSamplingDistributionSamplePDF": (ctypes.c_float, [ctypes.c_void_p, Vec2, ctypes.POINTER(Vec3)]),
+    "pglVolumeSamplingDistributionIncomingRadiancePDF": (ctypes.c_float, [ctypes.c_void_p, Vec3]),
+    "pglVolumeSamplingDistributionGetId": (ctypes.c_uint32, [ctypes.c_void_p]),
+    "pglVolumeSamplingDistributionValidate": (ctypes.c_bool, [ctypes.c_void_p]),
+    "pglVolumeSamplingDistributionClear": (None, [ctypes.c_void_p]),
+    "pglVolumeSamplingDistributionApplySingleLobeHenyeyGreensteinProduct": (None, [ctypes.c_void_p, Vec3,
+                                                                                   ctypes.c_float]),
+    "pglVolumeSamplingDistributionSupportsApplySingleLobeHenyeyGreensteinProduct": (ctypes.c_bool,
+                                                                                    [ctypes.c_void_p]),
+    "pglVolumeSamplingGetRegion": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "pglFieldSampleSurfaceBatch": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                   ctypes.c_void_p, ctypes.c_bool]),
+    "pglFieldSampleVolumeBatch": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                  ctypes.c_void_p]),
+    "pglFieldSampleBatchDevice": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_bool, ctypes.c_void_p, ctypes.c_size_t,
+                                                  ctypes.c_void_p, ctypes.c_bool, ctypes.c_void_p]),
+    "pglSampleStorageAddSamplesDevice": (None, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "pglFieldStoreToBuffer": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
+    "pglFieldGetLastUpdateTimings": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    "pglFieldGetLastUpdateReports": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                       ctypes.c_size_t]),
+    "pglGetLastError": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    """Loads the in-tree library (building it first if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            if not build_if_missing:
+                raise OSError(f"{LIB_PATH} is missing; run openpgl_gb300/build.py")
+            from . import build as _b
+
+            _b.build()
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in C_API.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def last_error():
+    return load().pglGetLastError().decode()
+
+
+def _check(ok, what):
+    if not ok:
+        raise RuntimeError(f"{what} failed: {last_error()}")
+
+
+class Device:
+    def __init__(self, device_type=PGL_DEVICE_TYPE_CPU_8, num_threads=0):
+        self.lib = load()
+        self.h = self.lib.pglNewDevice(device_type, num_threads)
+        _check(self.h, "pglNewDevice")
+
+    def release(self):
+        if self.h:
+            self.lib.pglReleaseDevice(self.h)
+            self.h = None
+
+
+class FieldConfig:
+    """FieldConfig::Init (cpp/FieldConfig.h:62-64)."""
+
+    def __init__(self, deterministic=True, max_samples_per_leaf=32000):
+        self.args = FieldArguments()
+        load().pglFieldArgumentsSetDefaults(ctypes.byref(self.args), PGL_SPATIAL_STRUCTURE_KDTREE,
+                                            PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM, deterministic,
+                                            max_samples_per_leaf)
+
+
+class SampleStorage:
+    def __init__(self):
+        self.lib = load()
+        self.h = self.lib.pglNewSampleStorage()
+        _check(self.h, "pglNewSampleStorage")
+
+    def add_samples(self, samples):
+        s = np.ascontiguousarray(samples, dtype=PGL_SAMPLE_DTYPE)
+        self.lib.pglSampleStorageAddSamples(self.h, s.ctypes.data, len(s))
+
+    def add_sample(self, sample):
+        s = np.ascontiguousarray(np.asarray([sample], dtype=PGL_SAMPLE_DTYPE))
+        self.lib.pglSampleStorageAddSample(self.h, ctypes.cast(s.ctypes.data, ctypes.POINTER(SampleData)))
+
+    def clear(self):
+        self.lib.pglSampleStorageClear(self.h)
+
+    def clear_surface(self):
+        self.lib.pglSampleStorageClearSurface(self.h)
+
+    def clear_volume(self):
+        self.lib.pglSampleStorageClearVolume(self.h)
+
+    def reserve(self, ns, nv):
+        self.lib.pglSampleStorageReserve(self.h, ns, nv)
+
+    @property
+    def size_surface(self):
+        return int(self.lib.pglSampleStorageGetSizeSurface(self.h))
+
+    @property
+    def size_volume(self):
+        return int(self.lib.pglSampleStorageGetSizeVolume(self.h))
+
+    def sample(self, idx, volume=False):
+        fn = self.lib.pglSampleStorageGetSampleVolume if volume else self.lib.pglSampleStorageGetSampleSurface
+        d = fn(self.h, idx)
+        out = np.zeros(1, dtype=PGL_SAMPLE_DTYPE)
+        ctypes.memmove(out.ctypes.data, ctypes.byref(d), 40)
+        return out[0]
+
+    def validate(self):
+        return bool(self.lib.pglSampleStorageValidate(self.h))
+
+    def compare(self, other):
+        return bool(self.lib.pglSampleStorageCompare(self.h, other.h))
+
+    def store(self, path):
+        return bool(self.lib.pglSampleStorageStoreToFile(self.h, path.encode()))
+
+    def release(self):
+        if self.h:
+            self.lib.pglReleaseSampleStorage(self.h)
+            self.h = None
+
+
+class Field:
+    def __init__(self, device, config):
+        self.lib = load()
+        self.h = self.lib.pglDeviceNewField(device.h, config.args)
+        _check(self.h, "pglDeviceNewField")
+
+    def update(self, storage):
+        self.lib.pglFieldUpdate(self.h, storage.h)
+        err = last_error()
+        if err:
+            raise RuntimeError(err)
+
+    def update_surface(self, storage):
+        self.lib.pglFieldUpdateSurface(self.h, storage.h)
+
+    def update_volume(self, storage):
+        self.lib.pglFieldUpdateVolume(self.h, storage.h)
+
+    def reset(self):
+        self.lib.pglFieldReset(self.h)
+
+    @property
+    def iteration(self):
+        return int(self.lib.pglFieldGetIteration(self.h))
+
+    def set_scene_bounds(self, lower, upper):
+        self.lib.pglFieldSetSceneBounds(self.h, Box3(Vec3(*lower), Vec3(*upper)))
+
+    def scene_bounds(self):
+        b = self.lib.pglFieldGetSceneBounds(self.h)
+        return (b.lower.x, b.lower.y, b.lower.z), (b.upper.x, b.upper.y, b.upper.z)
+
+    def validate(self):
+        return bool(self.lib.pglFieldValidate(self.h))
+
+    def compare(self, other):
+        return bool(self.lib.pglFieldCompare(self.h, other.h))
+
+    def field_bytes(self):
+        n = self.lib.pglFieldStoreToBuffer(self.h, None, 0)
+        buf = ctypes.create_string_buffer(int(n))
+        self.lib.pglFieldStoreToBuffer(self.h, buf, n)
+        return buf.raw
+
+    def store(self, path):
+        return bool(self.lib.pglFieldStoreToFile(self.h, path.encode()))
+
+    def timings(self, volume=False):
+        out = (ctypes.c_float * 4)()
+        self.lib.pglFieldGetLastUpdateTimings(self.h, int(volume), out)
+        return dict(total=out[0], copy=out[1], spatial=out[2], directional=out[3])
+
+    def reports(self, volume=False):
+        n = self.lib.pglFieldGetLastUpdateReports(self.h, int(volume), None, 0)
+        out = np.zeros((n, 5), dtype=np.uint32)
+        self.lib.pglFieldGetLastUpdateReports(self.h, int(volume), out.ctypes.data, n)
+        return out
+
+    def statistics_string(self, volume=False):
+        s = (self.lib.pglFieldGetVolumeStatistics if volume else self.lib.pglFieldGetSurfaceStatistics)(self.h)
+        p = self.lib.pglFieldStatisticsToString(s)
+        text = ctypes.string_at(p.m_str).decode()
+        self.lib.pglReleaseString(p)
+        self.lib.pglReleaseFieldStatistics(s)
+        return text
+
+    def sample_batch(self, queries, volume=False, cosine=True):
+        """Guided queries (Init + cosine product + SamplePDF + pdfLi) in one launch."""
+        q = np.ascontiguousarray(queries, dtype=PGL_QUERY_DTYPE)
+        out = np.zeros(len(q), dtype=QUERY_RESULT_DTYPE)
+        if volume:
+            ok = self.lib.pglFieldSampleVolumeBatch(self.h, q.ctypes.data, len(q), out.ctypes.data)
+        else:
+            ok = self.lib.pglFieldSampleSurfaceBatch(self.h, q.ctypes.data, len(q), out.ctypes.data, cosine)
+        _check(ok, "pglFieldSampleBatch")
+        return out
+
+    def sample_batch_device(self, q_ptr, n, out_ptr, volume=False, cosine=True, stream=None):
+        ok = self.lib.pglFieldSampleBatchDevice(self.h, volume, q_ptr, n, out_ptr, cosine, stream)
+        _check(ok, "pglFieldSampleBatchDevice")
+
+    def release(self):
+        if self.h:
+            self.lib.pglReleaseField(self.h)
+            self.h = None
+
+
+class SurfaceSamplingDistribution:
+    """Per-object sampling distribution (one launch chain per call)."""
+
+    volume = False
+
+    def __init__(self, field):
+        self.lib = load()
+        self.field = field
+        fn = (self.lib.pglFieldNewVolumeSamplingDistribution if self.volume
+              else self.lib.pglFieldNewSurfaceSamplingDistribution)
+        self.h = fn(field.h)
+        _check(self.h, "pglFieldNew*SamplingDistribution")
+        pre = "pglVolumeSamplingDistribution" if self.volume else "pglSurfaceSamplingDistribution"
+        self._sample_pdf = getattr(self.lib, pre + "SamplePDF")
+        self._pdf = getattr(self.lib, pre + "PDF")
+        self._pdf_li = getattr(self.lib, pre + "IncomingRadiancePDF")
+        self._get_id = getattr(self.lib, pre + "GetId")
+
+    def init(self, position, sample1d):
+        s = ctypes.c_float(sample1d)
+        fn = (self.lib.pglFieldInitVolumeSamplingDistribution if self.volume
+              else self.lib.pglFieldInitSurfaceSamplingDistribution)
+        ok = fn(self.field.h, self.h, Vec3(*position), ctypes.byref(s))
+        return bool(ok), s.value
+
+    def apply_cosine_product(self, normal):
+        self.lib.pglSurfaceSamplingDistributionApplyCosineProduct(self.h, Vec3(*normal))
+
+    def sample_pdf(self, u):
+        d = Vec3()
+        pdf = self._sample_pdf(self.h, Vec2(*u), ctypes.byref(d))
+        return (d.x, d.y, d.z), pdf
+
+    def pdf(self, direction):
+        return self._pdf(self.h, Vec3(*direction))
+
+    def incoming_radiance_pdf(self, direction):
+        return self._pdf_li(self.h, Vec3(*direction))
+
+    def get_id(self):
+        return int(self._get_id(self.h))
+
+    def release(self):
+        if self.h:
+            fn = (self.lib.pglReleaseVolumeSamplingDistribution if self.volume
+                  else self.lib.pglReleaseSurfaceSamplingDistribution)
+            fn(self.h)
+            self.h = None
+
+
+class VolumeSamplingDistribution(SurfaceSamplingDistribution):
+    volume = True

@@ -1,0 +1,724 @@
+// The Open PGL C API (extern "C", plain pointers) implemented on the GPU field.
+// Every function replaces the reference function of the same name in
+// openpgl/api/api.cpp; error handling follows api.cpp:33-72: exceptions never
+// cross the ABI, the message is printed and a neutral value returned.  The
+// message is also kept for pglGetLastError (appended symbol).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+
+#include "../../include/openpgl_gb300.h"
+#include "field.h"
+
+using namespace pgl;
+
+namespace {
+thread_local std::string g_lastError;
+
+struct DeviceImpl {
+  PGL_DEVICE_TYPE type;
+  size_t numThreads;
+};
+
+struct StatsImpl {
+  size_t numRegions = 0, numNodes = 0, maxDepth = 0;
+  size_t sizePerRegion = 0;
+  float timeUpdate = 0, timeCopy = 0, timeSpatial = 0, timeDirectional = 0;
+  float minK = 0, maxK = 0, avgK = 0, secondMomentK = 0;
+};
+
+PGLString make_string(const std::string &s) {
+  PGLString p;
+  p.m_size = s.size() + 1;
+  p.m_str = new char[p.m_size];
+  std::memcpy(p.m_str, s.c_str(), p.m_size);
+  return p;
+}
+
+void fail(const char *fn, const std::exception &e) {
+  g_lastError = std::string(fn) + ": " + e.what();
+  std::cout << g_lastError << std::endl;
+}
+
+GpuField *F(PGLField f) { return reinterpret_cast<GpuField *>(f); }
+Storage *S(PGLSampleStorage s) { return reinterpret_cast<Storage *>(s); }
+GpuSamplingDistribution *D(void *d) { return reinterpret_cast<GpuSamplingDistribution *>(d); }
+
+static_assert(sizeof(PGLSampleData) == sizeof(PGLSampleRecord), "sample record layout");
+static_assert(sizeof(PGLGuidedQuery) == sizeof(QueryIn), "query layout");
+static_assert(sizeof(PGLGuidedQueryResult) == sizeof(QueryOut), "query result layout");
+
+#define PGL_TRY try {
+#define PGL_CATCH(ret)            \
+  }                               \
+  catch (const std::exception &e) { \
+    fail(__func__, e);            \
+    return ret;                   \
+  }
+#define PGL_CATCH_VOID            \
+  }                               \
+  catch (const std::exception &e) { \
+    fail(__func__, e);            \
+    return;                       \
+  }
+
+FieldConfig config_from(const PGLFieldArguments &args) {  // Device.h:99-136
+  if (args.spatialStructureType != PGL_SPATIAL_STRUCTURE_KDTREE ||
+      args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM)
+    throw std::runtime_error("only the kd-tree + parallax-aware VMM field runs on the GPU");
+  FieldConfig c;
+  const PGLKDTreeArguments *kd = static_cast<const PGLKDTreeArguments *>(args.spatialSturctureArguments);
+  const PGLVMMFactoryArguments *vm = static_cast<const PGLVMMFactoryArguments *>(args.directionalDistributionArguments);
+  if (!kd || !vm) throw std::runtime_error("null field arguments");
+  c.deterministic = args.deterministic ? 1u : 0u;
+  c.fitRegions = args.debugArguments.fitRegions ? 1u : 0u;
+  c.knn = kd->knnLookup ? 1u : 0u;
+  c.minSamples = kd->minSamples;
+  c.maxSamples = kd->maxSamples;
+  c.maxDepth = kd->maxDepth;
+  c.initK = uint32_t(vm->initK);
+  c.initKappa = vm->initKappa;
+  c.maxK = uint32_t(vm->maxK);
+  c.maxIter = uint32_t(vm->maxEMIterrations);
+  c.maxKappa = vm->maxKappa;
+  c.maxMeanCosine = kappa_to_mean_cosine(c.maxKappa);
+  c.convergence = vm->convergenceThreshold;
+  c.weightPrior = vm->weightPrior;
+  c.mcPriorStrength = vm->meanCosinePriorStrength;
+  c.mcPrior = vm->meanCosinePrior;
+  c.splitThreshold = vm->splittingThreshold;
+  c.mergeThreshold = vm->mergingThreshold;
+  c.partialReFit = vm->partialReFit ? 1u : 0u;
+  c.maxSplitItr = vm->maxSplitItr;
+  c.useSplitMerge = vm->useSplitAndMerge ? 1u : 0u;
+  c.minSplit = vm->minSamplesForSplitting;
+  c.minRefit = vm->minSamplesForPartialRefitting;
+  c.minMerge = vm->minSamplesForMerging;
+  c.maxKappaSplit = 32000.0f;
+  c.maxMeanCosineSplit = kappa_to_mean_cosine(32000.0f);
+  c.laneWidth = 8;
+  // the reference takes ownership of the argument structs (Device.h:109,136)
+  delete kd;
+  delete vm;
+  return c;
+}
+
+StatsImpl *make_stats(const SubField &f) {  // Field::getStatistics (Field.h:604-638)
+  StatsImpl *s = new StatsImpl();
+  s->numRegions = f.regions.size();
+  s->numNodes = f.nodes.size();
+  s->sizePerRegion = sizeof(RegionDir) + sizeof(RegionHost);
+  s->timeUpdate = f.timings.total;
+  s->timeCopy = f.timings.copy;
+  s->timeSpatial = f.timings.spatial;
+  s->timeDirectional = f.timings.directional;
+  // depth
+  std::vector<std::pair<uint32_t, uint32_t>> st;
+  if (!f.nodes.empty()) st.push_back({0, 1});
+  while (!st.empty()) {
+    auto it = st.back();
+    st.pop_back();
+    s->maxDepth = std::max<size_t>(s->maxDepth, it.second);
+    const KDNode &n = f.nodes[it.first];
+    if ((n.bits >> 30) != 3u) {
+      st.push_back({(n.bits & 0x3FFFFFFFu), it.second + 1});
+      st.push_back({(n.bits & 0x3FFFFFFFu) + 1, it.second + 1});
+    }
+  }
+  std::vector<RegionDir> r = f.downloadRegions();
+  if (!r.empty()) {
+    s->minK = 1e10f;
+    for (const RegionDir &d : r) {
+      float k = float(d.vmm.K);
+      s->minK = std::min(s->minK, k);
+      s->maxK = std::max(s->maxK, k);
+      s->avgK += k;
+      s->secondMomentK += k * k;
+    }
+    s->avgK /= float(r.size());
+    s->secondMomentK = std::sqrt(s->secondMomentK / float(r.size()));
+  }
+  return s;
+}
+}  // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------------ device (api.cpp:83-114)
+OPENPGL_CORE_INTERFACE PGLDevice pglNewDevice(PGL_DEVICE_TYPE deviceType, size_t numThreads) {
+  PGL_TRY
+  Context::get();  // fails loudly without a usable GPU
+  return reinterpret_cast<PGLDevice>(new DeviceImpl{deviceType, numThreads});
+  PGL_CATCH(nullptr)
+}
+OPENPGL_CORE_INTERFACE void pglReleaseDevice(PGLDevice device) { delete reinterpret_cast<DeviceImpl *>(device); }
+
+OPENPGL_CORE_INTERFACE PGLField pglDeviceNewField(PGLDevice device, PGLFieldArguments args) {
+  PGL_TRY
+  if (!device) throw std::runtime_error("null handle provided to pglDeviceNewField");
+  return reinterpret_cast<PGLField>(new GpuField(config_from(args)));
+  PGL_CATCH(nullptr)
+}
+OPENPGL_CORE_INTERFACE PGLField pglDeviceNewFieldFromFile(PGLDevice, const char *) {
+  PGL_TRY
+  throw std::runtime_error("loading a field from a file is not supported by the GPU library yet");
+  PGL_CATCH(nullptr)
+}
+
+OPENPGL_CORE_INTERFACE void pglFieldArgumentsSetDefaults(PGLFieldArguments &a, const PGL_SPATIAL_STRUCTURE_TYPE,
+                                                         const PGL_DIRECTIONAL_DISTRIBUTION_TYPE directionalType,
+                                                         const bool deterministic, const size_t maxSamplesPerLeaf) {
+  // api.cpp:755-787
+  a.spatialStructureType = PGL_SPATIAL_STRUCTURE_KDTREE;
+  PGLKDTreeArguments *kd = new PGLKDTreeArguments();
+  kd->maxSamples = maxSamplesPerLeaf;
+  a.spatialSturctureArguments = kd;
+  a.deterministic = deterministic;
+  a.debugArguments.fitRegions = true;
+  if (directionalType == PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE) {
+    a.directionalDistributionType = PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE;
+    a.directionalDistributionArguments = new PGLDQTFactoryArguments();
+  } else {
+    a.directionalDistributionType = directionalType == PGL_DIRECTIONAL_DISTRIBUTION_VMM
+                                        ? PGL_DIRECTIONAL_DISTRIBUTION_VMM
+                                        : PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM;
+    a.directionalDistributionArguments = new PGLVMMFactoryArguments(maxSamplesPerLeaf);
+  }
+}
+
+// ------------------------------------------------------------------ field (api.cpp:115-280)
+OPENPGL_CORE_INTERFACE void pglReleaseField(PGLField field) {
+  PGL_TRY
+  delete F(field);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE bool pglFieldStoreToFile(PGLField field, const char *fieldFileName) {
+  PGL_TRY
+  if (!field || !fieldFileName) throw std::runtime_error("null handle or file name");
+  std::string b = F(field)->serialize();
+  std::ofstream os(fieldFileName, std::ios::binary);
+  if (!os) throw std::runtime_error("error: couldn't open file!");
+  os.write(b.data(), std::streamsize(b.size()));
+  return bool(os);
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE size_t pglFieldGetIteration(PGLField field) {
+  PGL_TRY
+  return F(field)->iteration;
+  PGL_CATCH(0)
+}
+OPENPGL_CORE_INTERFACE void pglFieldSetSceneBounds(PGLField field, pgl_box3f bounds) {
+  PGL_TRY
+  float b[6] = {bounds.lower.x, bounds.lower.y, bounds.lower.z, bounds.upper.x, bounds.upper.y, bounds.upper.z};
+  F(field)->setSceneBounds(b);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE pgl_box3f pglFieldGetSceneBounds(PGLField field) {
+  pgl_box3f r{};
+  PGL_TRY
+  float b[6];
+  F(field)->sceneBounds(b);
+  r.lower = pgl_vec3f{b[0], b[1], b[2]};
+  r.upper = pgl_vec3f{b[3], b[4], b[5]};
+  return r;
+  PGL_CATCH(r)
+}
+OPENPGL_CORE_INTERFACE void pglFieldUpdate(PGLField field, PGLSampleStorage sampleStorage) {
+  PGL_TRY
+  F(field)->update(*S(sampleStorage), true, true);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglFieldUpdateSurface(PGLField field, PGLSampleStorage sampleStorage) {
+  PGL_TRY
+  F(field)->update(*S(sampleStorage), true, false);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglFieldUpdateVolume(PGLField field, PGLSampleStorage sampleStorage) {
+  PGL_TRY
+  F(field)->update(*S(sampleStorage), false, true);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglFieldReset(PGLField field) {
+  PGL_TRY
+  F(field)->reset();
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE bool pglFieldValidate(PGLField field) {
+  PGL_TRY
+  GpuField *f = F(field);
+  bool v = true;
+  if (f->surface.initialized) v = v && f->surface.valid();
+  if (f->volume.initialized) v = v && f->volume.valid();
+  return v;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglFieldCompare(PGLField a, PGLField b) {
+  PGL_TRY
+  return F(a)->equals(*F(b));
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE PGLFieldStatistics pglFieldGetSurfaceStatistics(PGLField field) {
+  PGL_TRY
+  return reinterpret_cast<PGLFieldStatistics>(make_stats(F(field)->surface));
+  PGL_CATCH(nullptr)
+}
+OPENPGL_CORE_INTERFACE PGLFieldStatistics pglFieldGetVolumeStatistics(PGLField field) {
+  PGL_TRY
+  return reinterpret_cast<PGLFieldStatistics>(make_stats(F(field)->volume));
+  PGL_CATCH(nullptr)
+}
+
+// ------------------------------------------------------------------ per-object sampling distributions
+OPENPGL_CORE_INTERFACE PGLSurfaceSamplingDistribution pglFieldNewSurfaceSamplingDistribution(PGLField field) {
+  PGL_TRY
+  return reinterpret_cast<PGLSurfaceSamplingDistribution>(new GpuSamplingDistribution(F(field), false));
+  PGL_CATCH(nullptr)
+}
+OPENPGL_CORE_INTERFACE PGLVolumeSamplingDistribution pglFieldNewVolumeSamplingDistribution(PGLField field) {
+  PGL_TRY
+  return reinterpret_cast<PGLVolumeSamplingDistribution>(new GpuSamplingDistribution(F(field), true));
+  PGL_CATCH(nullptr)
+}
+static bool init_distribution(GpuField *f, GpuSamplingDistribution *d, bool volume, pgl_point3f p, float *s1d) {
+  // SurfaceVolumeField::init{Surface,Volume}SamplingDistribution (SurfaceVolumeField.h:50-85)
+  Context &c = Context::get();
+  const SubField &sf = volume ? f->volume : f->surface;
+  float in = s1d ? *s1d : -1.0f;
+  check(launch_ssd_init(sf.view(), p.x, p.y, p.z, in, d->dState, d->hRes, c.stream), "init");
+  check(cudaStreamSynchronize(c.stream), "init");
+  if (s1d) *s1d = d->hRes->s1d;
+  if (!d->hRes->ok) return false;
+  d->numDistributions = 1;
+  d->id = d->hRes->id;
+  d->regionTag = reinterpret_cast<const void *>(uintptr_t(d->hRes->id) + 1u);
+  return true;
+}
+OPENPGL_CORE_INTERFACE bool pglFieldInitSurfaceSamplingDistribution(PGLField field, PGLSurfaceSamplingDistribution d,
+                                                                    pgl_point3f position, float *sample1D) {
+  PGL_TRY
+  return init_distribution(F(field), D(d), false, position, sample1D);
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglFieldInitVolumeSamplingDistribution(PGLField field, PGLVolumeSamplingDistribution d,
+                                                                   pgl_point3f position, float *sample1D) {
+  PGL_TRY
+  return init_distribution(F(field), D(d), true, position, sample1D);
+  PGL_CATCH(false)
+}
+static pgl_vec3f dist_sample(GpuSamplingDistribution *d, pgl_point2f u, float *pdf) {
+  Context &c = Context::get();
+  check(launch_ssd_sample(d->dState, u.x, u.y, pdf ? 1 : 0, d->hRes, c.stream), "sample");
+  check(cudaStreamSynchronize(c.stream), "sample");
+  if (pdf) *pdf = d->hRes->pdf;
+  return pgl_vec3f{d->hRes->dx, d->hRes->dy, d->hRes->dz};
+}
+static float dist_pdf(GpuSamplingDistribution *d, pgl_vec3f dir, bool li) {
+  Context &c = Context::get();
+  check(launch_ssd_pdf(d->dState, dir.x, dir.y, dir.z, li ? 1 : 0, d->hRes, c.stream), "pdf");
+  check(cudaStreamSynchronize(c.stream), "pdf");
+  return d->hRes->pdf;
+}
+OPENPGL_CORE_INTERFACE void pglReleaseSurfaceSamplingDistribution(PGLSurfaceSamplingDistribution d) {
+  PGL_TRY
+  delete D(d);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglReleaseVolumeSamplingDistribution(PGLVolumeSamplingDistribution d) {
+  PGL_TRY
+  delete D(d);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglSurfaceSamplingDistributionApplyCosineProduct(PGLSurfaceSamplingDistribution d,
+                                                                             pgl_vec3f normal) {
+  PGL_TRY
+  if (D(d)->numDistributions == 0) return;  // VMMSurfaceSamplingDistribution.h:52-60
+  Context &c = Context::get();
+  check(launch_ssd_cosine(D(d)->dState, normal.x, normal.y, normal.z, 2.18853f, cosine_lobe_normalization(), c.stream),
+        "cosine product");
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE bool pglSurfaceSamplingDistributionSupportsApplyCosineProduct(PGLSurfaceSamplingDistribution) {
+  return true;
+}
+OPENPGL_CORE_INTERFACE pgl_vec3f pglSurfaceSamplingDistributionSample(PGLSurfaceSamplingDistribution d,
+                                                                      pgl_point2f sample) {
+  PGL_TRY
+  return dist_sample(D(d), sample, nullptr);
+  PGL_CATCH(pgl_vec3f{})
+}
+OPENPGL_CORE_INTERFACE float pglSurfaceSamplingDistributionPDF(PGLSurfaceSamplingDistribution d, pgl_vec3f direction) {
+  PGL_TRY
+  return dist_pdf(D(d), direction, false);
+  PGL_CATCH(0.0f)
+}
+OPENPGL_CORE_INTERFACE float pglSurfaceSamplingDistributionSamplePDF(PGLSurfaceSamplingDistribution d,
+                                                                     pgl_point2f sample, pgl_vec3f &direction) {
+  PGL_TRY
+  float pdf = 0.0f;
+  direction = dist_sample(D(d), sample, &pdf);
+  return pdf;
+  PGL_CATCH(0.0f)
+}
+OPENPGL_CORE_INTERFACE float pglSurfaceSamplingDistributionIncomingRadiancePDF(PGLSurfaceSamplingDistribution d,
+                                                                               pgl_vec3f direction) {
+  PGL_TRY
+  return dist_pdf(D(d), direction, true);
+  PGL_CATCH(0.0f)
+}
+OPENPGL_CORE_INTERFACE uint32_t pglSurfaceSamplingDistributionGetId(PGLSurfaceSamplingDistribution d) {
+  return D(d)->id;
+}
+OPENPGL_CORE_INTERFACE bool pglSurfaceSamplingDistributionValidate(PGLSurfaceSamplingDistribution d) {
+  return D(d)->numDistributions > 0;
+}
+OPENPGL_CORE_INTERFACE void pglSurfaceSamplingDistributionClear(PGLSurfaceSamplingDistribution d) {
+  D(d)->numDistributions = 0;
+}
+OPENPGL_CORE_INTERFACE PGLRegion pglSurfaceSamplingGetRegion(PGLSurfaceSamplingDistribution d) {
+  return reinterpret_cast<PGLRegion>(const_cast<void *>(D(d)->regionTag));
+}
+OPENPGL_CORE_INTERFACE pgl_vec3f pglVolumeSamplingDistributionSample(PGLVolumeSamplingDistribution d,
+                                                                     pgl_point2f sample) {
+  PGL_TRY
+  return dist_sample(D(d), sample, nullptr);
+  PGL_CATCH(pgl_vec3f{})
+}
+OPENPGL_CORE_INTERFACE float pglVolumeSamplingDistributionPDF(PGLVolumeSamplingDistribution d, pgl_vec3f direction) {
+  PGL_TRY
+  return dist_pdf(D(d), direction, false);
+  PGL_CATCH(0.0f)
+}
+OPENPGL_CORE_INTERFACE float pglVolumeSamplingDistributionSamplePDF(PGLVolumeSamplingDistribution d,
+                                                                    pgl_point2f sample, pgl_vec3f &direction) {
+  PGL_TRY
+  float pdf = 0.0f;
+  direction = dist_sample(D(d), sample, &pdf);
+  return pdf;
+  PGL_CATCH(0.0f)
+}
+OPENPGL_CORE_INTERFACE float pglVolumeSamplingDistributionIncomingRadiancePDF(PGLVolumeSamplingDistribution d,
+                                                                              pgl_vec3f direction) {
+  PGL_TRY
+  return dist_pdf(D(d), direction, true);
+  PGL_CATCH(0.0f)
+}
+OPENPGL_CORE_INTERFACE uint32_t pglVolumeSamplingDistributionGetId(PGLVolumeSamplingDistribution d) {
+  return D(d)->id;
+}
+OPENPGL_CORE_INTERFACE bool pglVolumeSamplingDistributionValidate(PGLVolumeSamplingDistribution d) {
+  return D(d)->numDistributions > 0;
+}
+OPENPGL_CORE_INTERFACE void pglVolumeSamplingDistributionClear(PGLVolumeSamplingDistribution d) {
+  D(d)->numDistributions = 0;
+}
+OPENPGL_CORE_INTERFACE void pglVolumeSamplingDistributionApplySingleLobeHenyeyGreensteinProduct(
+    PGLVolumeSamplingDistribution, pgl_vec3f, const float) {
+  PGL_TRY
+  throw std::runtime_error("the Henyey-Greenstein product is not supported by the GPU library yet");
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE bool pglVolumeSamplingDistributionSupportsApplySingleLobeHenyeyGreensteinProduct(
+    PGLVolumeSamplingDistribution) {
+  return false;
+}
+OPENPGL_CORE_INTERFACE PGLRegion pglVolumeSamplingGetRegion(PGLVolumeSamplingDistribution d) {
+  return reinterpret_cast<PGLRegion>(const_cast<void *>(D(d)->regionTag));
+}
+
+// ------------------------------------------------------------------ sample storage (api.cpp:328-400)
+OPENPGL_CORE_INTERFACE PGLSampleStorage pglNewSampleStorage() {
+  PGL_TRY
+  Context::get();
+  return reinterpret_cast<PGLSampleStorage>(new Storage());
+  PGL_CATCH(nullptr)
+}
+static const char kStorageHeader[] = "OPENPGL_0.6.0_SAMPLE_STORAGE";
+OPENPGL_CORE_INTERFACE PGLSampleStorage pglNewSampleStorageFromFile(const char *fileName) {
+  PGL_TRY
+  if (!fileName) throw std::runtime_error("null string provided to pglNewSampleStorageFromFile");
+  std::ifstream is(fileName, std::ios::binary);
+  if (!is) throw std::runtime_error("error: couldn't open file");
+  char hdr[sizeof(kStorageHeader)];
+  is.read(hdr, sizeof(hdr));
+  if (!is) throw std::runtime_error("error: invalid file header");
+  Storage *s = new Storage();
+  for (int side = 0; side < 2; ++side) {  // SampleDataStorage.h:176-216
+    uint64_t n = 0;
+    is.read(reinterpret_cast<char *>(&n), 8);
+    std::vector<PGLSampleRecord> v(n);
+    is.read(reinterpret_cast<char *>(v.data()), std::streamsize(n * sizeof(PGLSampleRecord)));
+    s->add(v.data(), v.size());
+  }
+  s->flush();
+  return reinterpret_cast<PGLSampleStorage>(s);
+  PGL_CATCH(nullptr)
+}
+OPENPGL_CORE_INTERFACE void pglReleaseSampleStorage(PGLSampleStorage s) {
+  PGL_TRY
+  delete S(s);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE bool pglSampleStorageStoreToFile(PGLSampleStorage s, const char *fileName) {
+  PGL_TRY
+  if (!s || !fileName) throw std::runtime_error("null handle or file name");
+  std::ofstream os(fileName, std::ios::binary);
+  if (!os) throw std::runtime_error("error: couldn't open file!");
+  os.write(kStorageHeader, sizeof(kStorageHeader));
+  for (bool vol : {false, true}) {
+    std::vector<PGLSampleRecord> v = S(s)->download(vol);
+    uint64_t n = v.size();
+    os.write(reinterpret_cast<const char *>(&n), 8);
+    os.write(reinterpret_cast<const char *>(v.data()), std::streamsize(n * sizeof(PGLSampleRecord)));
+  }
+  return bool(os);
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE void pglSampleStorageAddSample(PGLSampleStorage s, PGLSampleData &sample) {
+  PGL_TRY
+  S(s)->add(reinterpret_cast<const PGLSampleRecord *>(&sample), 1);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglSampleStorageAddSamples(PGLSampleStorage s, const PGLSampleData *samples, size_t n) {
+  PGL_TRY
+  S(s)->add(reinterpret_cast<const PGLSampleRecord *>(samples), n);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglSampleStorageReserve(PGLSampleStorage s, const size_t ns, const size_t nv) {
+  PGL_TRY
+  S(s)->reserve(ns, nv);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglSampleStorageClear(PGLSampleStorage s) {
+  PGL_TRY
+  S(s)->clearSurface();
+  S(s)->clearVolume();
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglSampleStorageClearSurface(PGLSampleStorage s) {
+  PGL_TRY
+  S(s)->clearSurface();
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE void pglSampleStorageClearVolume(PGLSampleStorage s) {
+  PGL_TRY
+  S(s)->clearVolume();
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE size_t pglSampleStorageGetSizeSurface(PGLSampleStorage s) {
+  PGL_TRY
+  return S(s)->sizeSurface();
+  PGL_CATCH(0)
+}
+OPENPGL_CORE_INTERFACE size_t pglSampleStorageGetSizeVolume(PGLSampleStorage s) {
+  PGL_TRY
+  return S(s)->sizeVolume();
+  PGL_CATCH(0)
+}
+OPENPGL_CORE_INTERFACE PGLSampleData pglSampleStorageGetSampleSurface(PGLSampleStorage s, const int idx) {
+  PGLSampleData d{};
+  PGL_TRY
+  PGLSampleRecord r = S(s)->get(false, uint64_t(idx));
+  std::memcpy(&d, &r, sizeof(d));
+  return d;
+  PGL_CATCH(d)
+}
+OPENPGL_CORE_INTERFACE PGLSampleData pglSampleStorageGetSampleVolume(PGLSampleStorage s, const int idx) {
+  PGLSampleData d{};
+  PGL_TRY
+  PGLSampleRecord r = S(s)->get(true, uint64_t(idx));
+  std::memcpy(&d, &r, sizeof(d));
+  return d;
+  PGL_CATCH(d)
+}
+OPENPGL_CORE_INTERFACE bool pglSampleStorageValidate(PGLSampleStorage s) {
+  PGL_TRY
+  return S(s)->validate();
+  PGL_CATCH(false)
+}
+static bool sample_less(const PGLSampleRecord &a, const PGLSampleRecord &b) {  // SampleData.h:82-93
+  if (a.weight != b.weight) return a.weight < b.weight;
+  if (a.pdf != b.pdf) return a.pdf < b.pdf;
+  if (a.distance != b.distance) return a.distance < b.distance;
+  if (a.px != b.px) return a.px < b.px;
+  if (a.py != b.py) return a.py < b.py;
+  if (a.pz != b.pz) return a.pz < b.pz;
+  if (a.dx != b.dx) return a.dx < b.dx;
+  if (a.dy != b.dy) return a.dy < b.dy;
+  return a.dz < b.dz;
+}
+OPENPGL_CORE_INTERFACE bool pglSampleStorageCompare(PGLSampleStorage a, PGLSampleStorage b) {
+  // SampleDataStorage::operator== (SampleDataStorage.h:230-279): both sides
+  // sorted, compared over the first storage's size (its size check is missing)
+  PGL_TRY
+  for (bool vol : {false, true}) {
+    std::vector<PGLSampleRecord> x = S(a)->download(vol), y = S(b)->download(vol);
+    std::sort(x.begin(), x.end(), sample_less);
+    std::sort(y.begin(), y.end(), sample_less);
+    for (size_t i = 0; i < x.size() && i < y.size(); ++i)
+      if (std::memcmp(&x[i], &y[i], sizeof(PGLSampleRecord)) != 0) return false;
+  }
+  return true;
+  PGL_CATCH(false)
+}
+
+// ------------------------------------------------------------------ statistics strings (api.cpp:788-846)
+OPENPGL_CORE_INTERFACE void pglReleaseFieldStatistics(PGLFieldStatistics s) {
+  delete reinterpret_cast<StatsImpl *>(s);
+}
+OPENPGL_CORE_INTERFACE PGLString pglFieldStatisticsToString(PGLFieldStatistics p) {
+  const StatsImpl &s = *reinterpret_cast<StatsImpl *>(p);
+  std::stringstream ss;
+  ss << "FieldStatistics:\n  numCacheRegions = " << s.numRegions << "\n  sizePerCacheRegions = " << s.sizePerRegion
+     << "\n  timeLastUpdate = " << s.timeUpdate << " ms\n  timeLastUpdateCopySamples = " << s.timeCopy
+     << " ms\n  timeLastUpdateSpatialStructureUpdate = " << s.timeSpatial
+     << " ms\n  timeLastUpdateDirectionalDistriubtionUpdate = " << s.timeDirectional
+     << " ms\nKDTreeStatistics:\n  numberOfNodes = " << s.numNodes << "\n  maxDepth = " << s.maxDepth
+     << "\nDirectionalDistributionStatistics:\n  minNumberOfComponents = " << s.minK
+     << "\n  maxNumberOfComponents = " << s.maxK << "\n  averageNumberOfComponents = " << s.avgK
+     << "\n  secondMomentNumberOfComponents = " << s.secondMomentK << "\n";
+  return make_string(ss.str());
+}
+OPENPGL_CORE_INTERFACE PGLString pglFieldStatisticsHeaderCSVString(PGLFieldStatistics) {
+  return make_string(
+      "FieldStatistics: , numCacheRegions , sizePerCacheRegions(bs) , timeUpdate(ms) , timeCopySamples(ms) , "
+      "timeSpatialStructureUpdate(ms) , timeDirectionalDistriubtionUpdate(ms) , KDTreeStatistics: , numberOfNodes , "
+      "maxDepth , DirectionalDistributionStatistics: , minNumberOfComponents , maxNumberOfComponents , "
+      "averageNumberOfComponents , secondMomentNumberOfComponents , ");
+}
+OPENPGL_CORE_INTERFACE PGLString pglFieldStatisticsToCSVString(PGLFieldStatistics p) {
+  const StatsImpl &s = *reinterpret_cast<StatsImpl *>(p);
+  std::stringstream ss;
+  ss << "  , " << s.numRegions << " , " << s.sizePerRegion << " , " << s.timeUpdate << " , " << s.timeCopy << " , "
+     << s.timeSpatial << " , " << s.timeDirectional << " ,   , " << s.numNodes << " , " << s.maxDepth << " ,   , "
+     << s.minK << " , " << s.maxK << " , " << s.avgK << " , " << s.secondMomentK << " , ";
+  return make_string(ss.str());
+}
+OPENPGL_CORE_INTERFACE void pglReleaseString(PGLString str) { delete[] str.m_str; }
+
+// ------------------------------------------------------------------ path segments: outside the GPU path
+#define PGL_UNSUPPORTED(ret)                                                                          \
+  {                                                                                                   \
+    g_lastError = std::string(__func__) + ": path segment storage is not part of the GPU library"; \
+    return ret;                                                                                       \
+  }
+OPENPGL_CORE_INTERFACE PGLPathSegmentStorage pglNewPathSegmentStorage() PGL_UNSUPPORTED(nullptr)
+OPENPGL_CORE_INTERFACE void pglReleasePathSegmentStorage(PGLPathSegmentStorage) {}
+OPENPGL_CORE_INTERFACE void pglPathSegmentStorageReserve(PGLPathSegmentStorage, size_t) PGL_UNSUPPORTED()
+OPENPGL_CORE_INTERFACE void pglPathSegmentStorageClear(PGLPathSegmentStorage) PGL_UNSUPPORTED()
+OPENPGL_CORE_INTERFACE void pglPathSegmentSetMaxDistance(PGLPathSegmentStorage, float) PGL_UNSUPPORTED()
+OPENPGL_CORE_INTERFACE float pglPathSegmentGetMaxDistance(PGLPathSegmentStorage) PGL_UNSUPPORTED(0.0f)
+OPENPGL_CORE_INTERFACE int pglPathSegmentGetNumSegments(PGLPathSegmentStorage) PGL_UNSUPPORTED(0)
+OPENPGL_CORE_INTERFACE int pglPathSegmentGetNumSamples(PGLPathSegmentStorage) PGL_UNSUPPORTED(0)
+OPENPGL_CORE_INTERFACE size_t pglPathSegmentStoragePrepareSamples(PGLPathSegmentStorage, const bool, const bool,
+                                                                  const bool) PGL_UNSUPPORTED(0)
+OPENPGL_CORE_INTERFACE pgl_vec3f pglPathSegmentStorageCalculatePixelEstimate(PGLPathSegmentStorage, const bool)
+    PGL_UNSUPPORTED(pgl_vec3f{})
+OPENPGL_CORE_INTERFACE const PGLSampleData *pglPathSegmentStorageGetSamples(PGLPathSegmentStorage, size_t &n) {
+  n = 0;
+  PGL_UNSUPPORTED(nullptr)
+}
+OPENPGL_CORE_INTERFACE void pglPathSegmentStorageAddSample(PGLPathSegmentStorage, PGLSampleData) PGL_UNSUPPORTED()
+OPENPGL_CORE_INTERFACE PGLPathSegmentData *pglPathSegmentStorageNextSegment(PGLPathSegmentStorage)
+    PGL_UNSUPPORTED(nullptr)
+OPENPGL_CORE_INTERFACE void pglPathSegmentStorageAddSegment(PGLPathSegmentStorage, PGLPathSegmentData)
+    PGL_UNSUPPORTED()
+OPENPGL_CORE_INTERFACE bool pglPathSegmentStorageValidateSamples(PGLPathSegmentStorage) PGL_UNSUPPORTED(false)
+OPENPGL_CORE_INTERFACE bool pglPathSegmentStorageValidateSegments(PGLPathSegmentStorage) PGL_UNSUPPORTED(false)
+OPENPGL_CORE_INTERFACE void pglPathSegmentStoragePropagateSamples(PGLPathSegmentStorage, PGLSampleStorage, bool, bool,
+                                                                  bool) PGL_UNSUPPORTED()
+
+// ------------------------------------------------------------------ appended entry points (openpgl_gb300.h)
+OPENPGL_CORE_INTERFACE bool pglFieldSampleBatchDevice(PGLField field, bool volume, const PGLGuidedQuery *dQueries,
+                                                      size_t n, PGLGuidedQueryResult *dResults, bool cosineProduct,
+                                                      void *cudaStream) {
+  PGL_TRY
+  Context &c = Context::get();
+  const SubField &sf = volume ? F(field)->volume : F(field)->surface;
+  QueryParams p{};
+  p.f = sf.view();
+  p.cosKappa = 2.18853f;
+  p.cosNorm = cosine_lobe_normalization();
+  p.cosine = cosineProduct ? 1 : 0;
+  p.samplesPerQuery = 1;
+  cudaStream_t s = cudaStream ? static_cast<cudaStream_t>(cudaStream) : c.stream;
+  check(launch_query(p, reinterpret_cast<const QueryIn *>(dQueries), reinterpret_cast<QueryOut *>(dResults),
+                     uint32_t(n), s),
+        "query");
+  return true;
+  PGL_CATCH(false)
+}
+static bool sample_batch_host(PGLField field, bool volume, const PGLGuidedQuery *q, size_t n, PGLGuidedQueryResult *r,
+                              bool cosine) {
+  Context &c = Context::get();
+  static thread_local DevArray<QueryIn> dq;
+  static thread_local DevArray<QueryOut> dr;
+  dq.reserve(n);
+  dr.reserve(n);
+  check(cudaMemcpyAsync(dq.p, q, n * sizeof(QueryIn), cudaMemcpyHostToDevice, c.stream), "H2D queries");
+  if (!pglFieldSampleBatchDevice(field, volume, reinterpret_cast<const PGLGuidedQuery *>(dq.p), n,
+                                 reinterpret_cast<PGLGuidedQueryResult *>(dr.p), cosine, c.stream))
+    return false;
+  check(cudaMemcpyAsync(r, dr.p, n * sizeof(QueryOut), cudaMemcpyDeviceToHost, c.stream), "D2H results");
+  check(cudaStreamSynchronize(c.stream), "queries");
+  return true;
+}
+OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceBatch(PGLField field, const PGLGuidedQuery *queries, size_t n,
+                                                       PGLGuidedQueryResult *results, bool cosineProduct) {
+  PGL_TRY
+  return sample_batch_host(field, false, queries, n, results, cosineProduct);
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatch(PGLField field, const PGLGuidedQuery *queries, size_t n,
+                                                      PGLGuidedQueryResult *results) {
+  PGL_TRY
+  return sample_batch_host(field, true, queries, n, results, false);
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE void pglSampleStorageAddSamplesDevice(PGLSampleStorage s, const PGLSampleData *d, size_t n) {
+  PGL_TRY
+  std::vector<PGLSampleRecord> h(n);
+  check(cudaMemcpy(h.data(), d, n * sizeof(PGLSampleRecord), cudaMemcpyDeviceToHost), "D2H samples");
+  S(s)->add(h.data(), n);
+  S(s)->flush();
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE size_t pglFieldStoreToBuffer(PGLField field, char *buffer, size_t capacity) {
+  PGL_TRY
+  std::string b = F(field)->serialize();
+  if (buffer && capacity >= b.size()) std::memcpy(buffer, b.data(), b.size());
+  return b.size();
+  PGL_CATCH(0)
+}
+OPENPGL_CORE_INTERFACE bool pglFieldGetLastUpdateTimings(PGLField field, int volume, float out4[4]) {
+  PGL_TRY
+  const UpdateTimings &t = volume ? F(field)->volume.timings : F(field)->surface.timings;
+  out4[0] = t.total;
+  out4[1] = t.copy;
+  out4[2] = t.spatial;
+  out4[3] = t.directional;
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int volume, uint32_t *out, size_t cap) {
+  PGL_TRY
+  const SubField &sf = volume ? F(field)->volume : F(field)->surface;
+  size_t n = sf.lastReports.size();
+  if (out && cap >= n)
+    for (size_t i = 0; i < n; ++i) {
+      out[5 * i + 0] = sf.lastReportRegion[i];
+      out[5 * i + 1] = sf.lastReports[i].emIterations;
+      out[5 * i + 2] = sf.lastReports[i].splits;
+      out[5 * i + 3] = sf.lastReports[i].merges;
+      out[5 * i + 4] = sf.lastReports[i].K;
+    }
+  return n;
+  PGL_CATCH(0)
+}
+OPENPGL_CORE_INTERFACE const char *pglGetLastError() { return g_lastError.c_str(); }
+
+}  // extern "C"

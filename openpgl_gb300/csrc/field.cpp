@@ -1,0 +1,880 @@
+// Host orchestration of the GPU guiding field.  Compiled with
+// -ffp-contract=off: the float code here (statistics merge/split, split
+// decisions, quantisation frames) must produce the reference's bits.
+#include "field.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace pgl {
+
+void check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+Context &Context::get() {
+  static Context c;
+  static bool init = false;
+  if (!init) {
+    check(cudaGetDevice(&c.device), "cudaGetDevice");
+    check(cudaDeviceGetAttribute(&c.numSMs, cudaDevAttrMultiProcessorCount, c.device), "SM count");
+    check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
+    check(em_upload_tables(), "tables (em)");
+    check(spatial_upload_tables(), "tables (spatial)");
+    check(query_upload_tables(), "tables (query)");
+    init = true;
+  }
+  return c;
+}
+
+template <typename T>
+void DevArray<T>::reserve(size_t n, bool keep) {
+  if (n <= cap && p) return;
+  size_t want = std::max<size_t>(n + n / 4, 64);
+  T *np = nullptr;
+  check(cudaMalloc(&np, want * sizeof(T)), "cudaMalloc");
+  if (keep && p && cap) check(cudaMemcpy(np, p, cap * sizeof(T), cudaMemcpyDeviceToDevice), "grow copy");
+  if (p) cudaFree(p);
+  p = np;
+  cap = want;
+}
+template <typename T>
+void DevArray<T>::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+}
+template struct DevArray<float4>;
+template struct DevArray<float>;
+template struct DevArray<uint32_t>;
+template struct DevArray<RegionDir>;
+template struct DevArray<KDNode>;
+template struct DevArray<Neighbours>;
+template struct DevArray<PGLSampleRecord>;
+
+// ------------------------------------------------------------------ statistics (host)
+// IntegerSampleStatistics frame (SampleStatistics.h:227-241), SSE rcp form.
+void quant_frame(const float b[6], float c[3], float inv[3]) {
+  for (int d = 0; d < 3; ++d) {
+    float ext = b[3 + d] - b[d];
+    float half = ext * 0.5f;
+    inv[d] = rcp_sse(half);
+    c[d] = b[d] + half;
+  }
+}
+// IntegerSampleStatistics::getSampleStatistics (SampleStatistics.h:297-340)
+Stats stats_from_acc(const IStatsAcc &a, const float b[6]) {
+  Stats s;
+  if (a.n == 0) return s;
+  float half[3], center[3];
+  for (int d = 0; d < 3; ++d) {
+    float ext = b[3 + d] - b[d];
+    half[d] = ext * 0.5f;
+    center[d] = b[d] + half[d];
+  }
+  uint32_t n = uint32_t(a.n);
+  float invN = 1.f / float(n);
+  float mean[3], var[3];
+  for (int d = 0; d < 3; ++d) {
+    mean[d] = (float(a.m[d]) / 4096.f) * invN;
+    var[d] = (float(a.v[d]) / 4096.f) * invN;
+  }
+  for (int d = 0; d < 3; ++d) var[d] -= mean[d] * mean[d];
+  for (int d = 0; d < 3; ++d) var[d] = std::fabs(var[d]);
+  for (int d = 0; d < 3; ++d) {
+    mean[d] = mean[d] * half[d];
+    mean[d] += center[d];
+    var[d] = var[d] * (half[d] * half[d]);
+  }
+  for (int d = 0; d < 3; ++d) {
+    s.mean[d] = mean[d];
+    s.var[d] = var[d] * float(n);
+    float lw = (float(a.lo[d]) - 0.0f) / 4096.f;
+    lw = lw * half[d];
+    lw = lw + center[d];
+    float up = (float(a.hi[d]) + 0.0f) / 4096.f;
+    up = up * half[d];
+    up = up + center[d];
+    s.lo[d] = lw;
+    s.hi[d] = up;
+  }
+  s.n = float(n);
+  return s;
+}
+// SampleStatistics::merge (SampleStatistics.h:101-118)
+void stats_merge(Stats &a, const Stats &b) {
+  float mA[3], mB[3], vA[3], vB[3];
+  std::memcpy(mA, a.mean, 12);
+  std::memcpy(mB, b.mean, 12);
+  std::memcpy(vA, a.var, 12);
+  std::memcpy(vB, b.var, 12);
+  float nA = a.n, nB = b.n;
+  for (int d = 0; d < 3; ++d) a.mean[d] = mA[d] * nA + mB[d] * nB;
+  a.n += nB;
+  for (int d = 0; d < 3; ++d) a.mean[d] /= a.n;
+  for (int d = 0; d < 3; ++d)
+    a.var[d] = (((vA[d] + (nA * mA[d]) * mA[d]) + vB[d]) + (nB * mB[d]) * mB[d]) - (a.n * a.mean[d]) * a.mean[d];
+  for (int d = 0; d < 3; ++d) {
+    a.lo[d] = emin(a.lo[d], b.lo[d]);
+    a.hi[d] = emax(a.hi[d], b.hi[d]);
+  }
+}
+// SampleStatistics::split (SampleStatistics.h:68-99)
+void stats_split(Stats &s, int dim, float pos, float decay, bool lower) {
+  if (s.n > 0.f) {
+    float variance = s.var[dim] / s.n;
+    float sd = std::sqrt(variance);
+    float nv = variance - variance / 4.0f;
+    s.var[dim] = nv * s.n;
+    if (lower) {
+      s.lo[dim] = smax(pos, s.lo[dim]);
+      s.mean[dim] = smin(s.hi[dim], s.mean[dim] + sd / 2.0f);
+    } else {
+      s.hi[dim] = smin(pos, s.hi[dim]);
+      s.mean[dim] = smax(s.lo[dim], s.mean[dim] - sd / 2.0f);
+    }
+    s.n *= decay;
+    for (int d = 0; d < 3; ++d) s.var[d] *= decay;
+  }
+}
+float kappa_to_mean_cosine(float k) {  // PAVMM.h:910-918 (scalar, libm tanhf)
+  float m = 1.0f / std::tanh(k) - 1.0f / k;
+  return k > 0.0f ? m : 0.0f;
+}
+float cosine_lobe_normalization() {  // VMMSurfaceSamplingDistribution.h:52-60
+  return float(double(2.18853f) / (2.0 * kPiD * double(1.0f - std::exp(-2.0f * 2.18853f))));
+}
+
+// ------------------------------------------------------------------ storage
+void SampleSide::reserve(uint64_t count) {
+  P.reserve(count, true);
+  D.reserve(count, true);
+  pdf.reserve(count, true);
+  flags.reserve(count, true);
+}
+
+void Storage::add(const PGLSampleRecord *s, size_t n) {
+  pending_.insert(pending_.end(), s, s + n);
+  if (pending_.size() >= (1u << 16)) flush();
+}
+
+void Storage::reserve(size_t ns, size_t nv) {
+  flush();
+  if (ns > surf.n) surf.reserve(ns);
+  if (nv > vol.n) vol.reserve(nv);
+}
+
+void Storage::flush() {
+  if (pending_.empty()) return;
+  Context &c = Context::get();
+  const uint32_t n = uint32_t(pending_.size());
+  staging_.reserve(n);
+  check(cudaMemcpyAsync(staging_.p, pending_.data(), size_t(n) * sizeof(PGLSampleRecord), cudaMemcpyHostToDevice,
+                        c.stream),
+        "H2D samples");
+  lastH2DBytes += uint64_t(n) * sizeof(PGLSampleRecord);
+  // worst case: every sample in one class
+  surf.reserve(surf.n + n);
+  vol.reserve(vol.n + n);
+  SoAView sv{surf.P.p, surf.D.p, surf.pdf.p, surf.flags.p, surf.n};
+  SoAView vv{vol.P.p, vol.D.p, vol.pdf.p, vol.flags.p, vol.n};
+  uint32_t numVol = 0;
+  check(ingest_samples(staging_.p, n, scratch_, sv, vv, &numVol, c.stream), "ingest");
+  vol.n += numVol;
+  surf.n += n - numVol;
+  pending_.clear();
+}
+
+std::vector<PGLSampleRecord> Storage::download(bool volume) {
+  flush();
+  SampleSide &s = volume ? vol : surf;
+  std::vector<PGLSampleRecord> out(s.n);
+  if (s.n == 0) return out;
+  Context &c = Context::get();
+  DevArray<PGLSampleRecord> tmp;
+  tmp.reserve(s.n);
+  check(export_samples(s.P.p, s.D.p, s.pdf.p, s.flags.p, s.n, tmp.p, c.stream), "export");
+  check(cudaMemcpyAsync(out.data(), tmp.p, s.n * sizeof(PGLSampleRecord), cudaMemcpyDeviceToHost, c.stream), "D2H");
+  check(cudaStreamSynchronize(c.stream), "sync");
+  return out;
+}
+
+PGLSampleRecord Storage::get(bool volume, uint64_t idx) {
+  flush();
+  SampleSide &s = volume ? vol : surf;
+  PGLSampleRecord r{};
+  if (idx >= s.n) return r;
+  Context &c = Context::get();
+  float4 p, d;
+  float pdf;
+  uint32_t fl;
+  check(cudaMemcpyAsync(&p, s.P.p + idx, sizeof(p), cudaMemcpyDeviceToHost, c.stream), "D2H");
+  check(cudaMemcpyAsync(&d, s.D.p + idx, sizeof(d), cudaMemcpyDeviceToHost, c.stream), "D2H");
+  check(cudaMemcpyAsync(&pdf, s.pdf.p + idx, sizeof(pdf), cudaMemcpyDeviceToHost, c.stream), "D2H");
+  check(cudaMemcpyAsync(&fl, s.flags.p + idx, sizeof(fl), cudaMemcpyDeviceToHost, c.stream), "D2H");
+  check(cudaStreamSynchronize(c.stream), "sync");
+  r = PGLSampleRecord{p.x, p.y, p.z, d.x, d.y, d.z, d.w, pdf, p.w, fl};
+  return r;
+}
+
+static bool valid_sample(const PGLSampleRecord &s) {  // SampleData.h:25-46
+  bool v = isvalidf(s.px) && isvalidf(s.py) && isvalidf(s.pz);
+  v = v && isvalidf(s.dx) && isvalidf(s.dy) && isvalidf(s.dz);
+  v = v && isvalidf(s.weight) && s.weight >= 0.f;
+  v = v && isvalidf(s.pdf) && s.pdf > 0.f;
+  v = v && isvalidf(s.distance) && s.distance > 0.f;
+  return v;
+}
+bool Storage::validate() {
+  for (bool v : {false, true})
+    for (const PGLSampleRecord &s : download(v))
+      if (!valid_sample(s)) return false;
+  return true;
+}
+
+// ------------------------------------------------------------------ sub-field
+void SubField::ensureUniformDirs() {
+  if (dUniformDirs.p) return;
+  // Spherical Fibonacci directions (WEMFactory.h:668-700), with libm as in the reference
+  std::vector<float> d(kMaxK * kMaxK * 3);
+  const float gr = 1.618033988749895f;
+  for (uint32_t l = 0; l < uint32_t(kMaxK); ++l)
+    for (uint32_t n = 0; n < uint32_t(kMaxK); ++n) {
+      float *o = &d[(l * kMaxK + n) * 3];
+      if (n < l + 1) {
+        float phi = float(2.0 * kPiD * double(float(n) / gr));
+        float z = 1.0f - ((2.0f * float(n) + 1.0f) / float(l + 1));
+        float theta = std::acos(z);
+        float ct = std::cos(theta), st = std::sin(theta), cp = std::cos(phi), sp = std::sin(phi);
+        o[0] = st * cp;
+        o[1] = st * sp;
+        o[2] = ct;
+      } else {
+        o[0] = 0.0f;
+        o[1] = 0.0f;
+        o[2] = 1.0f;
+      }
+    }
+  dUniformDirs.reserve(d.size());
+  check(cudaMemcpy(dUniformDirs.p, d.data(), d.size() * sizeof(float), cudaMemcpyHostToDevice), "uniform dirs");
+}
+
+static inline bool is_leaf(const KDNode &n) { return (n.bits >> 30) == 3u; }
+static inline uint32_t child_of(const KDNode &n) { return n.bits & 0x3FFFFFFFu; }
+
+void SubField::buildTree(uint32_t n, const float4 *P) {
+  Context &c = Context::get();
+  struct Front {
+    uint32_t node, depth;
+    float b[6];
+    uint32_t begin, end;
+    Stats st;
+  };
+  std::vector<Front> front;
+  Stats rootStats;
+  if (is_leaf(nodes[0])) {  // KDTreeBuilder.h:94-115
+    KdJob j{};
+    quant_frame(kdBounds, j.c, j.inv);
+    acc_.reserve(1);
+    check(init_acc(acc_.p, 1, c.stream), "init acc");
+    check(kd_root_stats(posA_.p, n, j, acc_.p, c.stream), "root stats");
+    IStatsAcc a;
+    check(cudaMemcpyAsync(&a, acc_.p, sizeof(a), cudaMemcpyDeviceToHost, c.stream), "D2H");
+    check(cudaStreamSynchronize(c.stream), "sync");
+    rootStats = stats_from_acc(a, kdBounds);
+  }
+  Front root{0, 1, {}, 0, n, rootStats};
+  std::memcpy(root.b, kdBounds, 24);
+  front.push_back(root);
+  check(cudaMemsetAsync(node_.p, 0, size_t(n) * 4, c.stream), "node ids");
+
+  std::vector<KdJob> jobs;
+  std::vector<const Front *> jobFront;
+  std::vector<uint32_t> nodeToJob;
+  std::vector<IStatsAcc> acc;
+  const uint32_t oldRegions = uint32_t(regions.size());
+  while (!front.empty()) {
+    jobs.clear();
+    jobFront.clear();
+    for (Front &f : front) {
+      if (f.end == f.begin) continue;
+      if (is_leaf(nodes[f.node])) {
+        uint32_t r = child_of(nodes[f.node]);
+        if (f.depth < cfg.maxDepth && regions[r].stats.n + float(f.end - f.begin) > float(cfg.maxSamples)) {
+          // split (KDTreeBuilder.h:252-284)
+          Stats merged = regions[r].stats;
+          stats_merge(merged, f.st);
+          float v[3] = {merged.var[0] / merged.n, merged.var[1] / merged.n, merged.var[2] / merged.n};
+          int i = v[1] > v[0] ? 1 : 0;
+          int dim = v[i] > v[2] ? i : 2;
+          float pos = merged.mean[dim];
+          RegionHost right = regions[r];
+          stats_split(regions[r].stats, dim, pos, 0.25f, false);
+          stats_split(right.stats, dim, pos, 0.25f, true);
+          regions[r].splitFlag = true;
+          right.splitFlag = true;
+          regions[r].bounds[3 + dim] = pos;
+          right.bounds[dim] = pos;
+          regions.push_back(right);
+          uint32_t rightIdx = uint32_t(regions.size() - 1);
+          regionOrigin_.push_back(r < oldRegions ? r : regionOrigin_[r - oldRegions]);
+          uint32_t lr0 = uint32_t(nodes.size());
+          nodes.push_back(KDNode{0.0f, (3u << 30) | r});
+          nodes.push_back(KDNode{0.0f, (3u << 30) | rightIdx});
+          nodes[f.node].split = pos;
+          nodes[f.node].bits = (uint32_t(dim) << 30) | lr0;
+          splitNodes_.push_back(f.node);
+        } else {
+          stats_merge(regions[r].stats, f.st);
+          regions[r].rb = f.begin;
+          regions[r].re = f.end;
+          continue;
+        }
+      }
+      const KDNode &nd = nodes[f.node];
+      KdJob j{};
+      j.begin = f.begin;
+      j.end = f.end;
+      j.dim = nd.bits >> 30;
+      j.left = child_of(nd);
+      j.pos = nd.split;
+      j.needStats = (is_leaf(nodes[j.left]) || is_leaf(nodes[j.left + 1])) ? 1u : 0u;
+      quant_frame(f.b, j.c, j.inv);
+      jobs.push_back(j);
+      jobFront.push_back(&f);
+    }
+    if (jobs.empty()) break;
+    nodeToJob.assign(nodes.size(), ~0u);
+    for (size_t k = 0; k < jobs.size(); ++k) nodeToJob[jobFront[k]->node] = uint32_t(k);
+    jobs_.reserve(jobs.size());
+    nodeToJob_.reserve(nodeToJob.size());
+    acc_.reserve(2 * jobs.size());
+    check(cudaMemcpyAsync(jobs_.p, jobs.data(), jobs.size() * sizeof(KdJob), cudaMemcpyHostToDevice, c.stream), "jobs");
+    check(cudaMemcpyAsync(nodeToJob_.p, nodeToJob.data(), nodeToJob.size() * 4, cudaMemcpyHostToDevice, c.stream),
+          "node map");
+    check(kd_job_of(node_.p, n, nodeToJob_.p, jobOf_.p, c.stream), "job of");
+    check(init_acc(acc_.p, uint32_t(2 * jobs.size()), c.stream), "init acc");
+    check(kd_level(posA_.p, jobOf_.p, n, jobs_.p, isLeft_.p, scanLeft_.p, acc_.p, posB_.p, nodeB_.p, scratch_,
+                   c.stream),
+          "kd level");
+    std::swap(posA_.p, posB_.p);
+    std::swap(posA_.cap, posB_.cap);
+    std::swap(node_.p, nodeB_.p);
+    std::swap(node_.cap, nodeB_.cap);
+    acc.resize(2 * jobs.size());
+    check(cudaMemcpyAsync(acc.data(), acc_.p, acc.size() * sizeof(IStatsAcc), cudaMemcpyDeviceToHost, c.stream),
+          "D2H acc");
+    check(cudaStreamSynchronize(c.stream), "sync");
+    std::vector<Front> next;
+    next.reserve(2 * jobs.size());
+    for (size_t k = 0; k < jobs.size(); ++k) {
+      const KdJob &j = jobs[k];
+      const Front &f = *jobFront[k];
+      uint32_t nL = uint32_t(acc[2 * k].n), nR = uint32_t(acc[2 * k + 1].n);
+      Front L{j.left, f.depth + 1, {}, j.begin, j.begin + nL, Stats()};
+      Front R{j.left + 1, f.depth + 1, {}, j.begin + nL, j.begin + nL + nR, Stats()};
+      std::memcpy(L.b, f.b, 24);
+      std::memcpy(R.b, f.b, 24);
+      L.b[3 + j.dim] = j.pos;
+      R.b[j.dim] = j.pos;
+      if (j.needStats) {
+        L.st = stats_from_acc(acc[2 * k], f.b);
+        R.st = stats_from_acc(acc[2 * k + 1], f.b);
+      }
+      next.push_back(L);
+      next.push_back(R);
+    }
+    front.swap(next);
+  }
+}
+
+// Region and node numbering of the reference's depth-first build: the pair of
+// children of a split node is appended when the node is split, and splits
+// happen in depth-first, left-first order (KDTreeBuilder.h:271-280,346-349).
+void SubField::renumber(uint32_t oldNodes, uint32_t oldRegions) {
+  const uint32_t numSplits = uint32_t(splitNodes_.size());
+  if (numSplits == 0) return;
+  std::vector<uint32_t> splitIdx(nodes.size(), ~0u);
+  for (uint32_t k = 0; k < numSplits; ++k) splitIdx[splitNodes_[k]] = k;
+  std::vector<uint32_t> ord(numSplits, ~0u);
+  uint32_t next = 0;
+  std::vector<uint32_t> stack{0};
+  while (!stack.empty()) {
+    uint32_t i = stack.back();
+    stack.pop_back();
+    if (splitIdx[i] != ~0u) ord[splitIdx[i]] = next++;
+    if (!is_leaf(nodes[i])) {
+      stack.push_back(child_of(nodes[i]) + 1);
+      stack.push_back(child_of(nodes[i]));
+    }
+  }
+  auto mapNode = [&](uint32_t i) -> uint32_t {
+    if (i < oldNodes) return i;
+    uint32_t k = (i - oldNodes) / 2, c = (i - oldNodes) % 2;
+    return oldNodes + 2 * ord[k] + c;
+  };
+  auto mapRegion = [&](uint32_t r) -> uint32_t { return r < oldRegions ? r : oldRegions + ord[r - oldRegions]; };
+  std::vector<KDNode> nn(nodes.size());
+  for (uint32_t i = 0; i < nodes.size(); ++i) {
+    KDNode d = nodes[i];
+    if (is_leaf(d))
+      d.bits = (3u << 30) | mapRegion(child_of(d));
+    else
+      d.bits = (d.bits & 0xC0000000u) | mapNode(child_of(d));
+    nn[mapNode(i)] = d;
+  }
+  nodes.swap(nn);
+  std::vector<RegionHost> nr(regions.size());
+  std::vector<uint32_t> no(regionOrigin_.size());
+  for (uint32_t r = 0; r < regions.size(); ++r) nr[mapRegion(r)] = regions[r];
+  for (uint32_t k = 0; k < regionOrigin_.size(); ++k) no[ord[k]] = regionOrigin_[k];
+  regions.swap(nr);
+  regionOrigin_.swap(no);
+}
+
+void SubField::update(SampleSide &in) {
+  Context &c = Context::get();
+  const uint32_t n = uint32_t(in.n);
+  if (n == 0) return;
+  cudaEvent_t ev[5];
+  for (auto &e : ev) check(cudaEventCreate(&e), "event");
+  check(cudaEventRecord(ev[0], c.stream), "event");
+  const bool first = !initialized;
+  if (first) {
+    iteration = 0;
+    totalSPP = 0;
+  }
+  for (DevArray<float4> *a : {&posA_, &posB_, &sP_, &sD_, &tmpP_, &tmpD_}) a->reserve(n);
+  for (DevArray<float> *a : {&sPdf_, &tmpPdf_, &dist_}) a->reserve(n);
+  for (DevArray<uint32_t> *a : {&node_, &nodeB_, &jobOf_, &isLeft_, &scanLeft_}) a->reserve(n);
+  keys_.reserve(2 * size_t(n));
+  vals_.reserve(2 * size_t(n));
+  check(init_posidx(in.P.p, n, posA_.p, c.stream), "copy samples");
+  check(cudaEventRecord(ev[1], c.stream), "event");
+
+  if (first) {
+    if (!boundsSet) {  // Field.h:326-344
+      bounds6_.reserve(6);
+      check(scene_bounds(in.P.p, n - 1, bounds6_.p, c.stream), "bounds");
+      uint32_t o[6];
+      check(cudaMemcpyAsync(o, bounds6_.p, sizeof(o), cudaMemcpyDeviceToHost, c.stream), "D2H");
+      check(cudaStreamSynchronize(c.stream), "sync");
+      float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {FLT_MIN, FLT_MIN, FLT_MIN};
+      if (n > 1)
+        for (int d = 0; d < 3; ++d) {
+          uint32_t a = o[d], b = o[3 + d];
+          uint32_t ua = (a & 0x80000000u) ? (a & 0x7FFFFFFFu) : ~a;
+          uint32_t ub = (b & 0x80000000u) ? (b & 0x7FFFFFFFu) : ~b;
+          float fa, fb;
+          std::memcpy(&fa, &ua, 4);
+          std::memcpy(&fb, &ub, 4);
+          lo[d] = emin(FLT_MAX, fa);
+          hi[d] = emax(FLT_MIN, fb);
+        }
+      for (int d = 0; d < 3; ++d) {
+        float ctr = (lo[d] + hi[d]) / 2.0f;
+        sceneBounds[d] = ctr + 3.0f * (lo[d] - ctr);
+        sceneBounds[3 + d] = ctr + 3.0f * (hi[d] - ctr);
+      }
+      boundsSet = true;
+    }
+    std::memcpy(kdBounds, sceneBounds, 24);
+    kdInit = true;
+    nodes.assign(1, KDNode{0.0f, (3u << 30) | 0u});
+    regions.assign(1, RegionHost());
+    std::memcpy(regions[0].bounds, sceneBounds, 24);
+    dRegions.reserve(1);
+    check(cudaMemsetAsync(dRegions.p, 0, sizeof(RegionDir), c.stream), "region 0");
+  }
+  const uint32_t oldNodes = uint32_t(nodes.size()), oldRegions = uint32_t(regions.size());
+  splitNodes_.clear();
+  regionOrigin_.clear();
+  buildTree(n, in.P.p);
+  renumber(oldNodes, oldRegions);
+  const uint32_t R = uint32_t(regions.size());
+  dRegions.reserve(R, true);
+  if (R > oldRegions) {  // new regions start as copies of the region they split from
+    std::vector<uint32_t> idx(2 * (R - oldRegions));
+    for (uint32_t k = 0; k < R - oldRegions; ++k) {
+      idx[k] = oldRegions + k;
+      idx[(R - oldRegions) + k] = regionOrigin_[k];
+    }
+    copyIdx_.reserve(idx.size());
+    check(cudaMemcpyAsync(copyIdx_.p, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, c.stream), "copy idx");
+    check(copy_regions(dRegions.p, copyIdx_.p, copyIdx_.p + (R - oldRegions), R - oldRegions, c.stream), "copy");
+  }
+  if (cfg.knn) {  // Field.h:362-387 -> KNN.h:189-266
+    std::vector<float4> m(R);
+    for (uint32_t r = 0; r < R; ++r) m[r] = make_float4(regions[r].stats.mean[0], regions[r].stats.mean[1],
+                                                        regions[r].stats.mean[2], 0.0f);
+    means_.reserve(R);
+    dNbrs.reserve(R);
+    check(cudaMemcpyAsync(means_.p, m.data(), R * sizeof(float4), cudaMemcpyHostToDevice, c.stream), "means");
+    check(build_knn(means_.p, R, dNbrs.p, c.stream), "knn");
+  }
+  dNodes.reserve(nodes.size());
+  check(cudaMemcpyAsync(dNodes.p, nodes.data(), nodes.size() * sizeof(KDNode), cudaMemcpyHostToDevice, c.stream),
+        "nodes");
+  check(cudaEventRecord(ev[2], c.stream), "event");
+
+  // leaves in sample order, then the per-leaf deterministic order
+  std::vector<uint32_t> leafRegions;
+  for (uint32_t r = 0; r < R; ++r)
+    if (regions[r].re > regions[r].rb) leafRegions.push_back(r);
+  std::sort(leafRegions.begin(), leafRegions.end(),
+            [&](uint32_t a, uint32_t b) { return regions[a].rb < regions[b].rb; });
+  const uint32_t L = uint32_t(leafRegions.size());
+  std::vector<uint32_t> seg(3 * size_t(L));
+  for (uint32_t k = 0; k < L; ++k) {
+    seg[k] = uint32_t(regions[leafRegions[k]].rb);
+    seg[L + k] = uint32_t(regions[leafRegions[k]].re);
+    seg[2 * L + k] = uint32_t(regions[leafRegions[k]].re - regions[leafRegions[k]].rb);
+  }
+  leafSeg_.reserve(seg.size());
+  check(cudaMemcpyAsync(leafSeg_.p, seg.data(), seg.size() * 4, cudaMemcpyHostToDevice, c.stream), "segments");
+  check(gather_and_order(posA_.p, n, in.P.p, in.D.p, in.pdf.p, leafSeg_.p, leafSeg_.p + 2 * L, L, cfg.deterministic,
+                         tmpP_.p, tmpD_.p, tmpPdf_.p, keys_.p, vals_.p, sP_.p, sD_.p, sPdf_.p, scratch_, c.stream),
+        "gather");
+
+  // directional fit / update of every region (Field.h:389-511)
+  std::vector<LeafTask> tasks(R);
+  for (uint32_t r = 0; r < R; ++r) {
+    LeafTask &t = tasks[r];
+    const RegionHost &h = regions[r];
+    t.region = r;
+    t.begin = uint32_t(h.rb);
+    t.count = uint32_t(h.re - h.rb);
+    t.flags = (first ? kTaskFit : 0u) | (h.splitFlag ? kTaskDecay : 0u);
+    for (int d = 0; d < 3; ++d) {
+      t.mean[d] = h.stats.mean[d];
+      t.varOverN[d] = h.stats.var[d] / h.stats.n;
+    }
+  }
+  std::stable_sort(tasks.begin(), tasks.end(), [](const LeafTask &a, const LeafTask &b) { return a.count > b.count; });
+  tasks_.reserve(R);
+  reports_.reserve(R);
+  queue_.reserve(1);
+  check(cudaMemcpyAsync(tasks_.p, tasks.data(), R * sizeof(LeafTask), cudaMemcpyHostToDevice, c.stream), "tasks");
+  check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), c.stream), "queue");
+  ensureUniformDirs();
+  if (cfg.fitRegions) {
+    int blocks = std::min<int>(int(R), c.numSMs * 2);
+    check(launch_em(tasks_.p, R, queue_.p, dRegions.p, sP_.p, sD_.p, sPdf_.p, dist_.p, cfg, dUniformDirs.p, reports_.p,
+                    std::max(blocks, 1), c.stream),
+          "em");
+  }
+  check(cudaEventRecord(ev[3], c.stream), "event");
+  lastReports.resize(R);
+  check(cudaMemcpyAsync(lastReports.data(), reports_.p, R * sizeof(LeafReport), cudaMemcpyDeviceToHost, c.stream),
+        "reports");
+  check(cudaStreamSynchronize(c.stream), "update");
+  lastReportRegion.resize(R);
+  for (uint32_t k = 0; k < R; ++k) lastReportRegion[k] = tasks[k].region;
+  float ms[4];
+  check(cudaEventElapsedTime(&ms[0], ev[0], ev[3]), "timing");
+  check(cudaEventElapsedTime(&ms[1], ev[0], ev[1]), "timing");
+  check(cudaEventElapsedTime(&ms[2], ev[1], ev[2]), "timing");
+  check(cudaEventElapsedTime(&ms[3], ev[2], ev[3]), "timing");
+  timings = UpdateTimings{ms[0], ms[1], ms[2], ms[3]};
+  for (auto &e : ev) cudaEventDestroy(e);
+  for (RegionHost &h : regions) {
+    h.splitFlag = false;
+    h.rb = h.re = 0;
+  }
+  initialized = true;
+  iteration++;
+}
+
+void SubField::reset() {  // Field.h:222-233
+  iteration = 0;
+  totalSPP = 0;
+  boundsSet = false;
+  initialized = false;
+  kdInit = false;
+  nodes.clear();
+  regions.clear();
+}
+
+FieldView SubField::view() const {
+  FieldView v{};
+  v.nodes = dNodes.p;
+  v.regions = dRegions.p;
+  v.nbrs = dNbrs.p;
+  std::memcpy(v.bounds, kdBounds, 24);
+  v.iteration = (initialized && !nodes.empty()) ? uint32_t(iteration) : 0u;
+  v.knn = cfg.knn;
+  v.numNodes = uint32_t(nodes.size());
+  return v;
+}
+
+std::vector<RegionDir> SubField::downloadRegions() const {
+  std::vector<RegionDir> r(regions.size());
+  if (r.empty()) return r;
+  Context &c = Context::get();
+  check(cudaMemcpyAsync(r.data(), dRegions.p, r.size() * sizeof(RegionDir), cudaMemcpyDeviceToHost, c.stream), "D2H");
+  check(cudaStreamSynchronize(c.stream), "sync");
+  return r;
+}
+
+void SubField::uploadRegions(const std::vector<RegionDir> &r) {
+  if (r.empty()) return;
+  dRegions.reserve(r.size());
+  check(cudaMemcpy(dRegions.p, r.data(), r.size() * sizeof(RegionDir), cudaMemcpyHostToDevice), "H2D regions");
+}
+
+bool SubField::valid() const {  // Field::isValid (Field.h:307-317)
+  for (const RegionDir &r : downloadRegions())
+    if (!r.valid) return false;
+  return true;
+}
+
+// ------------------------------------------------------------------ field
+GpuField::GpuField(const FieldConfig &cfg) {
+  surface.cfg = cfg;
+  volume.cfg = cfg;
+  surface.isSurface = true;
+  volume.isSurface = false;
+}
+
+void GpuField::update(Storage &s, bool doSurface, bool doVolume) {  // SurfaceVolumeField.h:102-148
+  s.flush();
+  if (doSurface && s.surf.n > 0) surface.update(s.surf);
+  if (doVolume && s.vol.n > 0) volume.update(s.vol);
+  iteration++;
+}
+
+void GpuField::setSceneBounds(const float b[6]) {  // SurfaceVolumeField.h:87-93
+  float e[6];
+  for (int d = 0; d < 3; ++d) {
+    e[d] = b[d] - 1.01f * std::fabs(b[d]);
+    e[3 + d] = b[3 + d] + 1.01f * std::fabs(b[3 + d]);
+  }
+  for (SubField *f : {&surface, &volume}) {
+    std::memcpy(f->sceneBounds, e, 24);
+    f->boundsSet = true;
+  }
+}
+
+void GpuField::sceneBounds(float out[6]) const {
+  for (int d = 0; d < 3; ++d) {
+    out[d] = emin(surface.sceneBounds[d], volume.sceneBounds[d]);
+    out[3 + d] = emax(surface.sceneBounds[3 + d], volume.sceneBounds[3 + d]);
+  }
+}
+
+void GpuField::reset() {
+  iteration = 0;
+  totalSPP = 0;
+  surface.reset();
+  volume.reset();
+}
+
+// ------------------------------------------------------------------ serialisation
+namespace {
+struct Writer {
+  std::string b;
+  void raw(const void *p, size_t n) { b.append(reinterpret_cast<const char *>(p), n); }
+  template <typename T>
+  void put(const T &v) { raw(&v, sizeof(T)); }
+  void lanes(const float *a, int v) { raw(a + v * kLanes, sizeof(float) * kLanes); }
+};
+void write_sub(Writer &w, const SubField &f) {  // Field::serialize (Field.h:240-267), CPU_8 lane layout
+  const FieldConfig &c = f.cfg;
+  w.put<uint8_t>(f.isSurface);
+  w.put<float>(c.decayOnSpatialSplit);
+  w.put<uint64_t>(f.iteration);
+  w.put<uint64_t>(f.totalSPP);
+  w.put<uint8_t>(c.deterministic != 0);
+  w.put<uint8_t>(c.fitRegions != 0);
+  w.put<uint8_t>(f.boundsSet);
+  w.raw(f.sceneBounds, 24);
+  w.put<uint8_t>(f.initialized);
+  float t[4] = {0, 0, 0, 0};
+  w.raw(t, 16);
+  w.put<uint64_t>(c.initK);
+  w.put<float>(c.initKappa);
+  w.put<uint64_t>(c.maxK);
+  w.put<uint64_t>(c.maxIter);
+  w.put<float>(c.maxKappa);
+  w.put<float>(c.maxMeanCosine);
+  w.put<float>(c.convergence);
+  w.put<float>(c.weightPrior);
+  w.put<float>(c.mcPriorStrength);
+  w.put<float>(c.mcPrior);
+  w.put<float>(c.splitThreshold);
+  w.put<float>(c.mergeThreshold);
+  w.put<uint8_t>(c.partialReFit != 0);
+  w.put<int32_t>(c.maxSplitItr);
+  w.put<int32_t>(c.minSplit);
+  w.put<int32_t>(c.minMerge);
+  w.put<int32_t>(c.minRefit);
+  w.put<uint64_t>(c.minSamples);
+  w.put<uint64_t>(c.maxSamples);
+  w.put<uint64_t>(c.maxDepth);
+  w.put<uint8_t>(f.kdInit);
+  w.raw(f.kdBounds, 24);
+  w.put<uint64_t>(f.nodes.size());
+  for (const KDNode &n : f.nodes) {
+    w.put<float>(n.split);
+    w.put<uint32_t>(n.bits);
+  }
+  std::vector<RegionDir> dir = f.downloadRegions();
+  w.put<uint64_t>(f.regions.size());
+  for (size_t i = 0; i < f.regions.size(); ++i) {
+    const RegionDir &r = dir[i];
+    const RegionHost &h = f.regions[i];
+    w.put<uint8_t>(r.valid != 0);
+    for (int v = 0; v < kMaxK / kLanes; ++v) {
+      w.lanes(r.vmm.w, v);
+      w.lanes(r.vmm.kappa, v);
+      w.lanes(r.vmm.mx, v);
+      w.lanes(r.vmm.my, v);
+      w.lanes(r.vmm.mz, v);
+      w.lanes(r.vmm.norm, v);
+      w.lanes(r.vmm.e2k, v);
+      w.lanes(r.vmm.mc, v);
+      w.lanes(r.vmm.dist, v);
+    }
+    w.put<uint64_t>(r.vmm.K);
+    w.raw(r.vmm.pivot, 12);
+    w.raw(h.bounds, 24);
+    for (int v = 0; v < kMaxK / kLanes; ++v) {
+      w.lanes(r.suff.dx, v);
+      w.lanes(r.suff.dy, v);
+      w.lanes(r.suff.dz, v);
+      w.lanes(r.suff.w, v);
+      w.lanes(r.suff.dw, v);
+    }
+    w.put<float>(r.suff.sumWeights);
+    w.put<float>(r.suff.numSamples);
+    w.put<float>(r.suff.overallNumSamples);
+    w.put<uint64_t>(r.suff.K);
+    w.put<uint8_t>(r.suff.normalized != 0);
+    for (int v = 0; v < kMaxK / kLanes; ++v) {
+      w.lanes(r.split.chi2, v);
+      w.lanes(r.split.mx, v);
+      w.lanes(r.split.my, v);
+      w.lanes(r.split.cx, v);
+      w.lanes(r.split.cy, v);
+      w.lanes(r.split.cz, v);
+      w.lanes(r.split.n, v);
+      w.lanes(r.split.sw, v);
+      w.lanes(r.split.sa, v);
+    }
+    w.put<uint64_t>(r.split.K);
+    w.put<uint64_t>(r.afterSplit);
+    w.put<uint64_t>(r.afterMerge);
+    w.raw(h.stats.mean, 12);
+    w.raw(h.stats.var, 12);
+    w.put<float>(h.stats.n);
+    w.raw(h.stats.lo, 12);
+    w.raw(h.stats.hi, 12);
+    w.put<uint8_t>(h.splitFlag);
+    w.put<uint64_t>(h.rb);
+    w.put<uint64_t>(h.re);
+  }
+  w.put<uint8_t>(c.knn != 0);
+  bool built = c.knn && !f.regions.empty() && f.initialized;
+  w.put<uint8_t>(built);
+  if (built) {
+    w.put<uint32_t>(uint32_t(f.regions.size()));
+    for (const RegionHost &h : f.regions) {
+      float p[4] = {h.stats.mean[0], h.stats.mean[1], h.stats.mean[2], 0.0f};
+      w.raw(p, 16);
+    }
+  }
+}
+}  // namespace
+
+std::string GpuField::serialize() const {  // SurfaceVolumeField::storeToFile (SurfaceVolumeField.h:171-214)
+  Writer w;
+  const char hdr[] = "OPENPGL_0.6.0_FIELD";
+  w.raw(hdr, sizeof(hdr));
+  w.put<int32_t>(0);
+  w.put<int32_t>(0);
+  w.put<uint64_t>(iteration);
+  w.put<uint64_t>(totalSPP);
+  write_sub(w, surface);
+  write_sub(w, volume);
+  return w.b;
+}
+
+// Field::operator== (Field.h:552-601): exact comparison after the canonical
+// depth-first relabelling of the trees (KDTree.h:256-283); timings are not
+// compared, as in the reference.
+namespace {
+void canonical(const std::vector<KDNode> &nodes, std::vector<KDNode> &out, std::vector<uint32_t> &leafData) {
+  out.clear();
+  leafData.clear();
+  if (nodes.empty()) return;
+  struct Item {
+    uint32_t src, dst;
+  };
+  out.push_back(nodes[0]);
+  std::vector<Item> stack{{0, 0}};
+  while (!stack.empty()) {
+    Item it = stack.back();
+    stack.pop_back();
+    const KDNode &n = nodes[it.src];
+    if (!is_leaf(n)) {
+      uint32_t l = child_of(n);
+      uint32_t nl = uint32_t(out.size());
+      out[it.dst].bits = (out[it.dst].bits & 0xC0000000u) | nl;
+      out.push_back(nodes[l]);
+      out.push_back(nodes[l + 1]);
+      stack.push_back({l + 1, nl + 1});
+      stack.push_back({l, nl});
+    } else {
+      out[it.dst].bits = (3u << 30) | uint32_t(leafData.size());
+      leafData.push_back(child_of(n));
+    }
+  }
+}
+bool sub_equal(const SubField &a, const SubField &b) {
+  if (!a.initialized && !b.initialized) return true;
+  bool eq = a.isSurface == b.isSurface && a.iteration == b.iteration && a.totalSPP == b.totalSPP &&
+            a.boundsSet == b.boundsSet && a.initialized == b.initialized &&
+            std::memcmp(a.sceneBounds, b.sceneBounds, 24) == 0 &&
+            std::memcmp(&a.cfg, &b.cfg, sizeof(FieldConfig)) == 0;
+  std::vector<KDNode> na, nb;
+  std::vector<uint32_t> da, db;
+  canonical(a.nodes, na, da);
+  canonical(b.nodes, nb, db);
+  if (na.size() != nb.size() || da.size() != db.size() || a.regions.size() != b.regions.size()) return false;
+  for (size_t i = 0; i < na.size(); ++i)
+    if (na[i].split != nb[i].split || na[i].bits != nb[i].bits) eq = false;
+  std::vector<RegionDir> ra = a.downloadRegions(), rb = b.downloadRegions();
+  for (size_t i = 0; i < da.size(); ++i) {
+    const RegionDir &x = ra[da[i]], &y = rb[db[i]];
+    const RegionHost &hx = a.regions[da[i]], &hy = b.regions[db[i]];
+    if (std::memcmp(&x.vmm, &y.vmm, sizeof(VMMState)) != 0) eq = false;
+    if (std::memcmp(&x.suff, &y.suff, sizeof(SuffState)) != 0) eq = false;
+    if (std::memcmp(&x.split, &y.split, sizeof(SplitState)) != 0) eq = false;
+    if (x.afterSplit != y.afterSplit || x.afterMerge != y.afterMerge) eq = false;
+    if (std::memcmp(&hx.stats, &hy.stats, sizeof(Stats)) != 0 || hx.splitFlag != hy.splitFlag) eq = false;
+    if (std::memcmp(hx.bounds, hy.bounds, 24) != 0 || hx.rb != hy.rb || hx.re != hy.re) eq = false;
+  }
+  return eq;
+}
+}  // namespace
+
+bool GpuField::equals(const GpuField &o) const {
+  return iteration == o.iteration && totalSPP == o.totalSPP && sub_equal(surface, o.surface) &&
+         sub_equal(volume, o.volume);
+}
+
+// ------------------------------------------------------------------ sampling distributions
+GpuSamplingDistribution::GpuSamplingDistribution(GpuField *f, bool vol) : field(f), volume(vol) {
+  check(cudaMalloc(&dState, sizeof(SSDState)), "ssd state");
+  check(cudaMallocHost(&hRes, sizeof(SSDResult)), "ssd result");
+  std::memset(hRes, 0, sizeof(SSDResult));
+}
+GpuSamplingDistribution::~GpuSamplingDistribution() {
+  if (dState) cudaFree(dState);
+  if (hRes) cudaFreeHost(hRes);
+}
+
+}  // namespace pgl

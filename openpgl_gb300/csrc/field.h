@@ -1,0 +1,167 @@
+// Host side of the GPU guiding field: device-resident sample storage, the
+// surface/volume sub-fields and their Update and query paths.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "launch.h"
+#include "pgl_internal.h"
+
+namespace pgl {
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string &m) : std::runtime_error(m) {}
+};
+void check(cudaError_t e, const char *what);
+
+// Process-wide CUDA state: the stream every object uses, constant tables.
+struct Context {
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int numSMs = 0;
+  static Context &get();
+};
+
+template <typename T>
+struct DevArray {
+  T *p = nullptr;
+  size_t cap = 0;
+  void reserve(size_t n, bool keep = false);
+  void release();
+  ~DevArray() { release(); }
+  DevArray() = default;
+  DevArray(const DevArray &) = delete;
+  DevArray &operator=(const DevArray &) = delete;
+};
+
+struct SampleSide {
+  DevArray<float4> P, D;
+  DevArray<float> pdf;
+  DevArray<uint32_t> flags;
+  uint64_t n = 0;
+  void reserve(uint64_t count);
+};
+
+// SampleDataStorage on the device (SampleDataStorage.h:18-324): surface and
+// volume samples as structure-of-arrays.  Samples added one by one are kept
+// in a host buffer and moved to the device in one copy when needed.
+class Storage {
+ public:
+  SampleSide surf, vol;
+  void add(const PGLSampleRecord *s, size_t n);
+  void flush();
+  void reserve(size_t ns, size_t nv);
+  void clearSurface() { flush(); surf.n = 0; }
+  void clearVolume() { flush(); vol.n = 0; }
+  uint64_t sizeSurface() { flush(); return surf.n; }
+  uint64_t sizeVolume() { flush(); return vol.n; }
+  PGLSampleRecord get(bool volume, uint64_t idx);
+  std::vector<PGLSampleRecord> download(bool volume);
+  bool validate();
+  uint64_t lastH2DBytes = 0;
+
+ private:
+  std::vector<PGLSampleRecord> pending_;
+  DevArray<PGLSampleRecord> staging_;
+  Scratch scratch_;
+};
+
+struct RegionHost {
+  Stats stats;
+  float bounds[6] = {0, 0, 0, 0, 0, 0};
+  bool splitFlag = false;
+  uint64_t rb = 0, re = 0;
+};
+
+// Per-phase timings of the last Update (FieldStatistics, Field.h:153-216).
+struct UpdateTimings {
+  float total = 0, copy = 0, spatial = 0, directional = 0;
+};
+
+class SubField {
+ public:
+  FieldConfig cfg;
+  bool isSurface = true;
+  uint64_t iteration = 0, totalSPP = 0;
+  bool boundsSet = false, initialized = false, kdInit = false;
+  float sceneBounds[6] = {0, 0, 0, 0, 0, 0};
+  float kdBounds[6] = {0, 0, 0, 0, 0, 0};
+  std::vector<KDNode> nodes;
+  std::vector<RegionHost> regions;
+  UpdateTimings timings;
+  std::vector<LeafReport> lastReports;
+  std::vector<uint32_t> lastReportRegion;
+
+  DevArray<RegionDir> dRegions;
+  DevArray<KDNode> dNodes;
+  DevArray<Neighbours> dNbrs;
+  DevArray<float> dUniformDirs;
+
+  void update(SampleSide &in);
+  void reset();
+  FieldView view() const;
+  std::vector<RegionDir> downloadRegions() const;
+  void uploadRegions(const std::vector<RegionDir> &r);
+  bool valid() const;
+
+ private:
+  void buildTree(uint32_t n, const float4 *P);
+  void renumber(uint32_t oldNodes, uint32_t oldRegions);
+  void ensureUniformDirs();
+
+  // working buffers (sized to the largest update seen)
+  DevArray<float4> posA_, posB_, sP_, sD_, tmpP_, tmpD_;
+  DevArray<float> sPdf_, tmpPdf_, dist_;
+  DevArray<uint32_t> node_, nodeB_, jobOf_, isLeft_, scanLeft_, keys_, vals_, nodeToJob_, leafSeg_, copyIdx_;
+  DevArray<KdJob> jobs_;
+  DevArray<IStatsAcc> acc_;
+  DevArray<LeafTask> tasks_;
+  DevArray<LeafReport> reports_;
+  DevArray<float4> means_;
+  DevArray<unsigned int> queue_;
+  DevArray<uint32_t> bounds6_;
+  Scratch scratch_;
+  std::vector<uint32_t> splitNodes_;        // nodes split in this update (creation order)
+  std::vector<uint32_t> regionOrigin_;      // origin region of every region created in this update
+};
+
+class GpuField {
+ public:
+  explicit GpuField(const FieldConfig &cfg);
+  SubField surface, volume;
+  uint64_t iteration = 0, totalSPP = 0;
+  void update(Storage &s, bool doSurface, bool doVolume);
+  void setSceneBounds(const float b[6]);
+  void sceneBounds(float out[6]) const;
+  void reset();
+  std::string serialize() const;  // byte layout of pglFieldStoreToFile (CPU_8 lanes)
+  bool equals(const GpuField &o) const;
+};
+
+// Per-object sampling distribution (plain drop-in path).
+struct GpuSamplingDistribution {
+  GpuField *field = nullptr;
+  bool volume = false;
+  SSDState *dState = nullptr;
+  SSDResult *hRes = nullptr;  // pinned
+  uint32_t numDistributions = 0;
+  uint32_t id = 0;
+  const void *regionTag = nullptr;
+  GpuSamplingDistribution(GpuField *f, bool vol);
+  ~GpuSamplingDistribution();
+};
+
+// Host reproductions of the reference's scalar statistics code.
+Stats stats_from_acc(const IStatsAcc &a, const float bounds[6]);
+void stats_merge(Stats &a, const Stats &b);
+void stats_split(Stats &s, int dim, float pos, float decay, bool lower);
+void quant_frame(const float bounds[6], float c[3], float inv[3]);
+float kappa_to_mean_cosine(float k);
+float cosine_lobe_normalization();
+
+}  // namespace pgl

@@ -1,0 +1,67 @@
+// Host-callable launchers of the library's CUDA kernels (defined next to the
+// kernels in em_kernel.cu, spatial_kernels.cu, query_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pgl_internal.h"
+
+namespace pgl {
+
+// Growable device scratch buffer.
+struct Scratch {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+cudaError_t scratch_reserve(Scratch &s, size_t bytes);
+void scratch_free(Scratch &s);
+
+struct SoAView {
+  float4 *P;       // position xyz, distance
+  float4 *D;       // direction xyz, weight
+  float *pdf;
+  uint32_t *flags;
+  uint64_t base;   // append offset
+};
+
+cudaError_t em_upload_tables();
+cudaError_t spatial_upload_tables();
+cudaError_t query_upload_tables();
+
+// ingest: AoS batch (device) -> surface / volume SoA, stable per class.
+cudaError_t ingest_samples(const PGLSampleRecord *in, uint32_t n, Scratch &scratch, SoAView surf, SoAView vol,
+                           uint32_t *numVolume, cudaStream_t s);
+cudaError_t export_samples(const float4 *P, const float4 *D, const float *pdf, const uint32_t *flags, uint64_t n,
+                           PGLSampleRecord *out, cudaStream_t s);
+// min/max over positions [0, n) as order-preserving integers (6 x u32, device)
+cudaError_t scene_bounds(const float4 *P, uint64_t n, uint32_t *d6, cudaStream_t s);
+
+cudaError_t init_posidx(const float4 *P, uint32_t n, float4 *posIdx, cudaStream_t s);
+cudaError_t init_acc(IStatsAcc *acc, uint32_t count, cudaStream_t s);
+cudaError_t kd_root_stats(const float4 *pos, uint32_t n, const KdJob &job, IStatsAcc *acc, cudaStream_t s);
+cudaError_t kd_job_of(const uint32_t *node, uint32_t n, const uint32_t *nodeToJob, uint32_t *jobOf, cudaStream_t s);
+cudaError_t kd_level(const float4 *pos, const uint32_t *jobOf, uint32_t n, const KdJob *jobs, uint32_t *isLeft,
+                     uint32_t *scanLeft, IStatsAcc *acc, float4 *posOut, uint32_t *nodeOut, Scratch &scratch,
+                     cudaStream_t s);
+// Gathers samples into leaf order and applies the deterministic per-leaf
+// order (SampleDataLess) when `sorted`; leafBegin/leafCount are device arrays.
+cudaError_t gather_and_order(const float4 *posIdx, uint32_t n, const float4 *P, const float4 *D, const float *pdf,
+                             const uint32_t *leafBegin, const uint32_t *leafCount, uint32_t numLeaves, bool sorted,
+                             float4 *tmpP, float4 *tmpD, float *tmpPdf, uint32_t *keys, uint32_t *vals,
+                             float4 *oP, float4 *oD, float *oPdf, Scratch &scratch, cudaStream_t s);
+cudaError_t copy_regions(RegionDir *regions, const uint32_t *dst, const uint32_t *src, uint32_t n, cudaStream_t s);
+cudaError_t build_knn(const float4 *means, uint32_t R, Neighbours *out, cudaStream_t s);
+
+size_t em_shared_bytes();
+cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
+                      float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
+                      LeafReport *reports, int numBlocks, cudaStream_t stream);
+
+cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s);
+cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,
+                            cudaStream_t s);
+cudaError_t launch_ssd_cosine(SSDState *st, float nx, float ny, float nz, float ck, float cn, cudaStream_t s);
+cudaError_t launch_ssd_sample(const SSDState *st, float ux, float uy, int withPdf, SSDResult *res, cudaStream_t s);
+cudaError_t launch_ssd_pdf(const SSDState *st, float dx, float dy, float dz, int li, SSDResult *res, cudaStream_t s);
+
+}  // namespace pgl

@@ -1,0 +1,294 @@
+// Scalar arithmetic of the guiding field, shared by host and device code.
+//
+// Open PGL's CPU_8 device (the reference) runs its math on 8-wide AVX2
+// vectors.  To give the same numbers, every function here performs the same
+// IEEE operations in the same order:
+//  * translation units that include this file are compiled with FMA
+//    contraction disabled (nvcc --fmad=false, g++ -ffp-contract=off); FMAs
+//    are written out (fmaf) exactly where embree's madd/msub/fnmadd are
+//    (third-party/embreeSrc/common/math/vec3.h:204-209, linearspace3.h:150);
+//  * approximate reciprocals start from the x86 RCPSS/RSQRTSS values, held in
+//    tables measured on x86 (x86_approx_tables.h), then take the same Newton
+//    step as embree::rcp/rsqrt (math/emath.h:61-145, simd/vfloat8_avx.h:254-290);
+//  * fast exp/log/sin/acos follow the published ispc/syrah polynomials that
+//    the reference vendors (math/transcendental.h:18-472);
+//  * horizontal sums over a group of 8 lanes use the vfloat8 reduce tree
+//    ((0+1)+(2+3))+((4+5)+(6+7)) (simd/vfloat8_avx.h:677-683).
+#pragma once
+
+#include <cstdint>
+#include <cmath>
+#include <cfloat>
+
+#ifdef __CUDACC__
+#define PGL_HD __host__ __device__ __forceinline__
+#else
+#define PGL_HD inline
+#endif
+
+namespace pgl {
+
+constexpr int kLanes = 8;       // SIMD width of the CPU_8 reference
+constexpr int kMaxK = 32;       // PGL_VMM_MAX_COMPONENTS
+constexpr float kInv4Pi = 0.07957747154594767f;
+constexpr float kTwoPiF = 6.28318530717958647692f;  // (float)(2*M_PI)
+constexpr double kPiD = 3.14159265358979323846;
+
+}  // namespace pgl
+#include "x86_approx_tables.h"
+namespace pgl {
+// rcp/rsqrt seed tables: the host reads the static arrays of
+// x86_approx_tables.h; every CUDA translation unit has its own constant-memory
+// copy, filled by the upload function that PGL_DEFINE_TABLE_UPLOAD defines.
+#ifdef __CUDACC__
+static __constant__ uint32_t d_rcp_table[2048];
+static __constant__ uint32_t d_rsqrt_table[2048];
+#define PGL_DEFINE_TABLE_UPLOAD(fn)                                                                  \
+  cudaError_t fn() {                                                                                 \
+    cudaError_t e = cudaMemcpyToSymbol(d_rcp_table, pgl_x86_rcp_table, sizeof(pgl_x86_rcp_table));     \
+    if (e != cudaSuccess) return e;                                                                  \
+    return cudaMemcpyToSymbol(d_rsqrt_table, pgl_x86_rsqrt_table, sizeof(pgl_x86_rsqrt_table));       \
+  }
+#endif
+
+PGL_HD uint32_t f2u(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  uint32_t u;
+  __builtin_memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+PGL_HD float u2f(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f;
+  __builtin_memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+PGL_HD uint32_t rcp_seed(uint32_t idx) {
+#ifdef __CUDA_ARCH__
+  return d_rcp_table[idx];
+#else
+  return pgl_x86_rcp_table[idx];
+#endif
+}
+PGL_HD uint32_t rsqrt_seed(uint32_t idx) {
+#ifdef __CUDA_ARCH__
+  return d_rsqrt_table[idx];
+#else
+  return pgl_x86_rsqrt_table[idx];
+#endif
+}
+PGL_HD float fmaf_(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return std::fmaf(a, b, c);
+#endif
+}
+
+// x86 RCPSS: 12-bit reciprocal estimate (sign/zero/inf/denormal handling of the
+// instruction; the mantissa comes from the measured table).
+PGL_HD float rcpss(float x) {
+  uint32_t u = f2u(x), s = u & 0x80000000u, e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+  if (e == 0) return u2f(s | 0x7F800000u);
+  if (e == 255) return m ? x : u2f(s);
+  uint32_t t = rcp_seed(m >> 12);
+  int re = int((t >> 23) & 0xFFu) - (int(e) - 127);
+  if (re <= 0) return u2f(s);
+  if (re >= 255) return u2f(s | 0x7F800000u);
+  return u2f(s | (uint32_t(re) << 23) | (t & 0x7FFFFFu));
+}
+// x86 RSQRTSS
+PGL_HD float rsqrtss(float x) {
+  uint32_t u = f2u(x), e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+  if (u & 0x80000000u) return (e == 0 && m == 0) ? -INFINITY : NAN;
+  if (e == 0) return INFINITY;
+  if (e == 255) return m ? x : 0.0f;
+  int ue = int(e) - 127, p = ue & 1, q = ue >> 1;
+  uint32_t t = rsqrt_seed(uint32_t(p) * 1024u + (m >> 13));
+  int re = int((t >> 23) & 0xFFu) - q;
+  return u2f((uint32_t(re) << 23) | (t & 0x7FFFFFu));
+}
+// embree::rcp(float) in an AVX2 unit: r * fnmadd(r, a, 2)
+PGL_HD float rcp_avx2(float a) {
+  float r = rcpss(a);
+  return r * fmaf_(-r, a, 2.0f);
+}
+// embree::rcp(float) in an SSE unit: r * (2 - r*a).  The kd-tree statistics
+// use this form on every device: their inline members are emitted by the
+// SSE translation unit first and the linker keeps that copy.
+PGL_HD float rcp_sse(float a) {
+  float r = rcpss(a);
+  return r * (2.0f - r * a);
+}
+// embree::rsqrt(float) (no FMA in the scalar form)
+PGL_HD float rsqrt_scalar(float a) {
+  float r = rsqrtss(a);
+  return (1.5f * r) + (((a * -0.5f) * r) * (r * r));
+}
+// embree::rsqrt(vfloat8), AVX2 form
+PGL_HD float rsqrt_lane(float a) {
+  float r = rsqrtss(a);
+  return fmaf_(1.5f, r, ((a * -0.5f) * r) * (r * r));
+}
+
+PGL_HD float emin(float a, float b) { return a < b ? a : b; }   // embree::min, MINPS
+PGL_HD float emax(float a, float b) { return a < b ? b : a; }   // embree::max
+PGL_HD float smin(float a, float b) { return (b < a) ? b : a; }  // std::min
+PGL_HD float smax(float a, float b) { return (a < b) ? b : a; }  // std::max
+PGL_HD bool isvalidf(float v) { return (v > -1.844E18f) & (v < 1.844E18f); }
+
+PGL_HD float floorf_(float x) {
+#ifdef __CUDA_ARCH__
+  return floorf(x);
+#else
+  return std::floor(x);
+#endif
+}
+
+// fastapprox::exp
+PGL_HD float fexp(float v) {
+  const float ln2Part1 = float(0.6931457519), ln2Part2 = float(1.4286067653e-6);
+  const float oneOverLn2 = 1.44269502162933349609375f;
+  float scaled = v * oneOverLn2;
+  float kReal = floorf_(scaled);
+  int k = int(kReal);
+  float x = v - kReal * ln2Part1;
+  x -= kReal * ln2Part2;
+  float r = x * 2.7555381529964506626129150390625e-4f + 1.304379315115511417388916015625e-3f;
+  r = x * r + 8.378830738365650177001953125e-3f;
+  r = x * r + 4.16539050638675689697265625e-2f;
+  r = x * r + 0.166668415069580078125f;
+  r = x * r + 0.4999999105930328369140625f;
+  r = x * r + 1.0f;
+  r = x * r + 1.0f;
+  r *= u2f(uint32_t((k + 127) << 23));
+  if (kReal > 127.0f) r = INFINITY;
+  if (kReal <= -127.0f) r = 0.0f;
+  return r;
+}
+// fastapprox::log
+PGL_HD float flog(float v) {
+  bool useNan = v < 0.0f, useInf = v == 0.0f;
+  float patched = (useNan || useInf) ? 1.0f : v;
+  int32_t iv = int32_t(f2u(patched));
+  int exponent = ((iv >> 23) + 1) - 127;
+  float reduced = u2f(uint32_t((iv & int32_t(0x807FFFFF)) | (126 << 23)));
+  float x1 = 1.0f - reduced;
+  float r = x1 * 1.7491014003753662109375f + -2.4899270534515380859375f;
+  r = x1 * r + 1.98442304134368896484375f;
+  r = x1 * r + -0.599632322788238525390625f;
+  r = x1 * r + 0.3424419462680816650390625f;
+  r = x1 * r + 0.17541764676570892333984375f;
+  r = x1 * r + 0.2519190013408660888671875f;
+  r = x1 * r + 0.33326041698455810546875f;
+  r = x1 * r + 0.50000095367431640625f;
+  r = x1 * r + 1.0f;
+  r *= -x1;
+  r += float(exponent) * 0.693147182464599609375f;
+  if (useNan) return NAN;
+  if (useInf) return -INFINITY;
+  return r;
+}
+// fastapprox::sin
+PGL_HD float fsin(float v) {
+  float scaled = v * 0.636619746685028076171875f;
+  float kReal = floorf_(scaled);
+  int k = int(kReal);
+  float x = v - kReal * 1.57079637050628662109375f;
+  int m4 = k & 3;
+  bool useCos = (m4 == 1) | (m4 == 3);
+  bool flip = m4 > 1;
+  float outside = useCos ? 1.0f : x;
+  float c2 = useCos ? -0.5f : -0.16666667163372039794921875f;
+  float c4 = useCos ? 4.166664183139801025390625e-2f : 8.333347737789154052734375e-3f;
+  float c6 = useCos ? -1.388833043165504932403564453125e-3f : -1.9842604524455964565277099609375e-4f;
+  float c8 = useCos ? 2.47562347794882953166961669921875e-5f : 2.760012648650445044040679931640625e-6f;
+  float c10 = useCos ? -2.59630184018533327616751194000244140625e-7f : -2.50293279435709337121807038784027099609375e-8f;
+  float x2 = x * x;
+  float f = x2 * c10 + c8;
+  f = x2 * f + c6;
+  f = x2 * f + c4;
+  f = x2 * f + c2;
+  f = x2 * f + 1.0f;
+  f *= outside;
+  return flip ? -f : f;
+}
+// fastapprox::acos (= pi/2 - asin)
+PGL_HD float facos(float x0) {
+  bool neg = x0 < 0.0f;
+  float x = fabsf(x0);
+  bool nanres = x > 1.0f;
+  float v = 1.57079517841339111328125f +
+            x * (-0.21450997889041900634765625f +
+                 x * (8.78556668758392333984375e-2f +
+                      x * (-4.489909112453460693359375e-2f +
+                           x * (1.928029954433441162109375e-2f + x * (-4.3095736764371395111083984375e-3f)))));
+  v *= -sqrtf(1.0f - x);
+  v = v + 1.57079637050628662109375f;
+  v = (v < 0.0f) ? 0.0f : v;
+  v = neg ? -v : v;
+  v = nanres ? NAN : v;
+  return 1.57079637050628662109375f - v;
+}
+
+struct V3 {
+  float x, y, z;
+};
+PGL_HD V3 mk(float x, float y, float z) { return V3{x, y, z}; }
+PGL_HD V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+PGL_HD V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+PGL_HD V3 operator*(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }
+PGL_HD V3 operator/(V3 a, float s) { return V3{a.x / s, a.y / s, a.z / s}; }
+// embree::dot = madd(a.x,b.x, madd(a.y,b.y, a.z*b.z))
+PGL_HD float dot(V3 a, V3 b) { return fmaf_(a.x, b.x, fmaf_(a.y, b.y, a.z * b.z)); }
+PGL_HD V3 cross(V3 a, V3 b) {
+  return V3{fmaf_(a.y, b.z, -(a.z * b.y)), fmaf_(a.z, b.x, -(a.x * b.z)), fmaf_(a.x, b.y, -(a.y * b.x))};
+}
+PGL_HD float length(V3 a) { return sqrtf(dot(a, a)); }
+
+struct Frame {
+  V3 vx, vy, vz;
+};
+// embree::frame(N); lane=true picks the vector rsqrt refinement
+PGL_HD Frame frame_of(V3 N, bool lane) {
+  V3 dx0 = mk(0.0f, N.z, -N.y), dx1 = mk(-N.z, 0.0f, N.x);
+  V3 d = dot(dx0, dx0) > dot(dx1, dx1) ? dx0 : dx1;
+  float r = lane ? rsqrt_lane(dot(d, d)) : rsqrt_scalar(dot(d, d));
+  V3 dx = d * r;
+  V3 c = cross(N, dx);
+  float r2 = lane ? rsqrt_lane(dot(c, c)) : rsqrt_scalar(dot(c, c));
+  return Frame{dx, c * r2, N};
+}
+PGL_HD V3 xfm(const Frame &f, V3 b) {
+  return V3{fmaf_(b.x, f.vx.x, fmaf_(b.y, f.vy.x, b.z * f.vz.x)),
+            fmaf_(b.x, f.vx.y, fmaf_(b.y, f.vy.y, b.z * f.vz.y)),
+            fmaf_(b.x, f.vx.z, fmaf_(b.y, f.vy.z, b.z * f.vz.z))};
+}
+PGL_HD Frame inverse_of(const Frame &a) {
+  V3 c0 = cross(a.vy, a.vz), c1 = cross(a.vz, a.vx), c2 = cross(a.vx, a.vy);
+  float det = dot(a.vx, c0);
+  return Frame{mk(c0.x, c1.x, c2.x) / det, mk(c0.y, c1.y, c2.y) / det, mk(c0.z, c1.z, c2.z) / det};
+}
+
+PGL_HD float reduce8(const float *l) {
+  float a0 = l[0] + l[1], a2 = l[2] + l[3], a4 = l[4] + l[5], a6 = l[6] + l[7];
+  return (a0 + a2) + (a4 + a6);
+}
+PGL_HD int vec_count(int K) { return (K + kLanes - 1) / kLanes; }
+
+PGL_HD float mean_cosine_to_kappa(float mc) {
+  float mc2 = mc * mc;
+  return (mc * 3.0f - mc * mc2) / (1.0f - mc2);
+}
+
+// (float)(k / (2*pi*(1-e))) evaluated in double, as the reference's scalar
+// code does where a float meets the M_PI literal.
+PGL_HD float vmf_norm_double(float k, float e) { return float(double(k) / (2.0 * kPiD * double(1.0f - e))); }
+
+}  // namespace pgl

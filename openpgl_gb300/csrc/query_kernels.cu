@@ -1,0 +1,288 @@
+// Guided queries: kd lookup, stochastic nearest-region choice, parallax shift
+// of the region's mixture to the query point, cosine product, sampling and
+// pdf evaluation (Field.h:109-145, KNN.h:22-28,134-148,
+// VMMSurfaceSamplingDistribution.h:37-108, PAVMM.h:609-831).
+//
+// One warp per query, lane k owning mixture lobe k, which mirrors the
+// reference's 8-wide SIMD lanes: per-lane arithmetic is the reference's, and
+// horizontal sums use shuffles in the vfloat8 reduce order (lanes j, j+8, j+16,
+// j+24 summed in vector order, then the 8-lane tree).
+#include <cuda_runtime.h>
+
+#include "launch.h"
+#include "pgl_internal.h"
+
+namespace pgl {
+
+
+
+
+// (p[dim] >= pivot) goes right (KDTree.h:390-393); treelets give the same leaf.
+__device__ __forceinline__ uint32_t kd_leaf(const FieldView &f, float p0, float p1, float p2) {
+  uint32_t i = 0;
+  KDNode n = f.nodes[0];
+  while ((n.bits >> 30) != 3u) {
+    uint32_t dim = n.bits >> 30;
+    float c = dim == 0 ? p0 : (dim == 1 ? p1 : p2);
+    i = (n.bits & 0x3FFFFFFFu) + (c >= n.split ? 1u : 0u);
+    n = f.nodes[i];
+  }
+  return n.bits & 0x3FFFFFFFu;
+}
+
+// Returns the region to use, updating s1d (KNN.h:22-28, 134-148).
+__device__ uint32_t choose_region(const FieldView &f, uint32_t leaf, float p0, float p1, float p2, float &s1d,
+                                  int lane) {
+  const Neighbours &nb = f.nbrs[leaf];
+  uint32_t size = min(4u, nb.size);
+  uint32_t sel = uint32_t(s1d * float(size));
+  s1d = (s1d - float(sel) / float(size)) * float(size);
+  sel = min(sel, size - 1);
+  uint32_t key = 0xFFFFFFFFu;
+  if (lane < 8) {
+    V3 d = mk(nb.px[lane] - p0, nb.py[lane] - p1, nb.pz[lane] - p2);
+    float dd = dot(d, d);
+    key = (f2u(dd) & ~7u) | uint32_t(lane);
+    if (nb.ids[lane] == ~0u) key = f2u(INFINITY);
+  }
+  // rank among the 8 keys (all finite keys are distinct)
+  uint32_t rank = 0;
+  for (int j = 0; j < 8; ++j) {
+    uint32_t kj = __shfl_sync(0xFFFFFFFFu, key, j);
+    float fj = u2f(kj), fk = u2f(key);
+    rank += (fj < fk) ? 1u : 0u;
+  }
+  uint32_t hit = __ballot_sync(0xFFFFFFFFu, lane < 8 && rank == sel && key != f2u(INFINITY));
+  int src = __ffs(hit) - 1;
+  uint32_t chosenKey = __shfl_sync(0xFFFFFFFFu, key, src < 0 ? 0 : src);
+  return nb.ids[chosenKey & 7u];
+}
+
+// vfloat8 horizontal sum of lane values over the mixture: per group lane j
+// sums lanes j, j+8, ... over cnt vectors, then the 8-lane tree.
+__device__ __forceinline__ float lane_sum(float v, int cnt, int lane) {
+  float acc = 0.0f;
+  for (int q = 0; q < cnt; ++q) acc += __shfl_sync(0xFFFFFFFFu, v, (q * kLanes + (lane & 7)) & 31);
+  acc += __shfl_xor_sync(0xFFFFFFFFu, acc, 1);
+  acc += __shfl_xor_sync(0xFFFFFFFFu, acc, 2);
+  acc += __shfl_xor_sync(0xFFFFFFFFu, acc, 4);
+  return __shfl_sync(0xFFFFFFFFu, acc, 0);
+}
+
+// Copy of the region's lobe with the parallax shift to the query point.
+__device__ __forceinline__ Lobe load_shifted(const VMMState &v, int lane, float p0, float p1, float p2) {
+  Lobe L;
+  L.w = v.w[lane]; L.kappa = v.kappa[lane]; L.norm = v.norm[lane]; L.e2k = v.e2k[lane];
+  float dist = v.dist[lane];
+  V3 mu = mk(v.mx[lane], v.my[lane], v.mz[lane]);
+  V3 s = mk(v.pivot[0] - p0, v.pivot[1] - p1, v.pivot[2] - p2);
+  V3 p = mu * dist + s;
+  float len = length(p);
+  p = p / len;
+  bool cond = (dist > 0.0f) && (dist >= -FLT_MAX) && (dist <= FLT_MAX);
+  if (cond) mu = p;
+  L.mx = mu.x; L.my = mu.y; L.mz = mu.z;
+  return L;
+}
+
+// PAVMM::product with a single lobe (the cosine lobe)
+__device__ __forceinline__ Lobe product_lobe(Lobe L, V3 n, float kappa, float normalization, int cnt, int lane,
+                                             float &integral) {
+  V3 mu = mk(L.mx, L.my, L.mz);
+  V3 nm = mu * L.kappa + n * kappa;
+  float nk = sqrtf(dot(nm, nm));
+  bool chk = nk > 1e-3f;
+  nk = chk ? nk : 0.0f;
+  nm = chk ? nm / nk : mu;
+  float ne = fexp(-2.0f * nk);
+  float nn = nk / (kTwoPiF * (1.0f - ne));
+  nn = chk ? nn : kInv4Pi;
+  float scale = (L.norm * normalization) / nn;
+  float c0 = dot(mu, nm), c1 = dot(n, nm);
+  float ev = fexp(L.kappa * (c0 - 1.0f) + kappa * (c1 - 1.0f));
+  scale *= ev;
+  scale *= L.w * 1.0f;
+  Lobe R;
+  R.w = scale; R.kappa = nk; R.mx = nm.x; R.my = nm.y; R.mz = nm.z; R.norm = nn; R.e2k = ne;
+  integral = lane_sum(lane < cnt * kLanes ? R.w : 0.0f, cnt, lane);
+  R.w /= integral;
+  return R;
+}
+
+__device__ __forceinline__ float mixture_pdf(const Lobe &L, V3 d, int cnt, int lane) {
+  float ct = dot(d, mk(L.mx, L.my, L.mz));
+  float cm1 = emin(ct - 1.0f, 0.0f);
+  float ev = L.norm * fexp(L.kappa * cm1);
+  float t = lane < cnt * kLanes ? L.w * ev : 0.0f;
+  return lane_sum(t, cnt, lane);
+}
+
+// PAVMM::sample (PAVMM.h:737-806)
+__device__ V3 mixture_sample(const Lobe &L, int K, float ux, float uy, int lane) {
+  // per-vector sums of the weights
+  float g = L.w;
+  g += __shfl_xor_sync(0xFFFFFFFFu, g, 1);
+  g += __shfl_xor_sync(0xFFFFFFFFu, g, 2);
+  g += __shfl_xor_sync(0xFFFFFFFFu, g, 4);
+  float vecSum[4];
+  for (int q = 0; q < 4; ++q) vecSum[q] = __shfl_sync(0xFFFFFFFFu, g, q * kLanes);
+  uint32_t sv = 0, sc = 0;
+  float searched = uy, sumW = 0.0f, cdf = 0.0f;
+  uint32_t quot = uint32_t((K - 1) / kLanes), rem = uint32_t((K - 1) % kLanes);
+  for (;;) {
+    cdf = vecSum[sv];
+    if (sumW + cdf >= searched || sv + 1 >= quot + 1) break;
+    sumW += cdf;
+    sv++;
+  }
+  uint32_t maxSel = (sv == quot) ? rem + 1 : kLanes;
+  for (;;) {
+    cdf = __shfl_sync(0xFFFFFFFFu, L.w, int(sv * kLanes + sc));
+    if (sumW + cdf >= searched || sc + 1 >= maxSel) break;
+    sumW += cdf;
+    sc++;
+  }
+  float u1 = smin(1.0f - FLT_EPSILON, (searched - sumW) / cdf);
+  int s = int(sv * kLanes + sc);
+  float k = __shfl_sync(0xFFFFFFFFu, L.kappa, s), e2k = __shfl_sync(0xFFFFFFFFu, L.e2k, s);
+  V3 mu = mk(__shfl_sync(0xFFFFFFFFu, L.mx, s), __shfl_sync(0xFFFFFFFFu, L.my, s), __shfl_sync(0xFFFFFFFFu, L.mz, s));
+  V3 d;
+  if (k == 0.0f) {
+    float z = 1.0f - 2.0f * u1;
+    float r = sqrtf(smax(0.f, (1.0f - z * z)));
+    float sp, cp;
+    sincosf(float(2.0 * kPiD * double(ux)), &sp, &cp);
+    d = mk(r * cp, r * sp, z);
+  } else {
+    float ct = 1.f + (flog(1.0f + ((e2k - 1.f) * ux))) / k;
+    ct = smin(1.0f, smax(ct, -1.f));
+    float st = sqrtf(1.f - ct * ct);
+    float phi = float(2.0 * kPiD * double(u1));
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    d = mk(st * cp, st * sp, ct);
+  }
+  return xfm(frame_of(mu, false), d);
+}
+
+
+// Batched guided query: Init + optional cosine product + SamplePDF (+ pdfLi).
+__global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, uint32_t n) {
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= n) return;
+  const QueryIn q = in[gw];
+  const FieldView &f = P.f;
+  QueryOut o;
+  o.ok = 0; o.id = 0; o.s1d = q.s1d; o.dx = o.dy = o.dz = 0.0f; o.pdf = 0.0f; o.pdfLi = 0.0f;
+  bool inside = f.iteration > 0 && q.px >= f.bounds[0] && q.px <= f.bounds[3] && q.py >= f.bounds[1] &&
+                q.py <= f.bounds[4] && q.pz >= f.bounds[2] && q.pz <= f.bounds[5];
+  if (inside) {
+    uint32_t leaf = kd_leaf(f, q.px, q.py, q.pz);
+    uint32_t reg = leaf;
+    float s1d = q.s1d;
+    if (f.knn && s1d >= 0.f) reg = choose_region(f, leaf, q.px, q.py, q.pz, s1d, lane);
+    o.s1d = s1d;
+    const RegionDir &R = f.regions[reg];
+    if (R.valid) {
+      const int K = int(R.vmm.K), cnt = vec_count(K);
+      Lobe li = load_shifted(R.vmm, lane, q.px, q.py, q.pz);
+      Lobe g = li;
+      if (P.cosine) {
+        float integral;
+        g = product_lobe(li, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, cnt, lane, integral);
+      }
+      V3 d = mixture_sample(g, K, (q.ux - 0.0f) / 1.0f, q.uy, lane);
+      o.ok = 1;
+      o.id = leaf;
+      o.dx = d.x; o.dy = d.y; o.dz = d.z;
+      o.pdf = 0.0f + 1.0f * mixture_pdf(g, d, cnt, lane);
+      o.pdfLi = mixture_pdf(li, d, cnt, lane);
+    }
+  }
+  if (lane == 0) out[gw] = o;
+}
+
+// ---------------------------------------------------------------- per-object path
+// State of one SurfaceSamplingDistribution / VolumeSamplingDistribution on the
+// device: the shifted mixture (for IncomingRadiancePDF) and the product one.
+
+__global__ void ssd_init_kernel(FieldView f, float px, float py, float pz, float s1dIn, SSDState *st, SSDResult *res) {
+  const int lane = threadIdx.x & 31;
+  SSDResult r{0, 0, s1dIn, 0, 0, 0, 0};
+  bool inside = f.iteration > 0 && px >= f.bounds[0] && px <= f.bounds[3] && py >= f.bounds[1] && py <= f.bounds[4] &&
+                pz >= f.bounds[2] && pz <= f.bounds[5];
+  if (inside) {
+    uint32_t leaf = kd_leaf(f, px, py, pz);
+    uint32_t reg = leaf;
+    float s1d = s1dIn;
+    if (f.knn && s1d >= 0.f) reg = choose_region(f, leaf, px, py, pz, s1d, lane);
+    r.s1d = s1d;
+    const RegionDir &R = f.regions[reg];
+    if (R.valid) {
+      Lobe li = load_shifted(R.vmm, lane, px, py, pz);
+      st->li[lane] = li;
+      st->g[lane] = li;
+      if (lane == 0) st->K = R.vmm.K;
+      r.ok = 1;
+      r.id = leaf;
+    }
+  }
+  if (lane == 0) *res = r;
+}
+__global__ void ssd_cosine_kernel(SSDState *st, float nx, float ny, float nz, float cosKappa, float cosNorm) {
+  const int lane = threadIdx.x & 31;
+  const int cnt = vec_count(int(st->K));
+  float integral;
+  Lobe g = product_lobe(st->g[lane], mk(nx, ny, nz), cosKappa, cosNorm, cnt, lane, integral);
+  __syncwarp();
+  st->g[lane] = g;
+}
+__global__ void ssd_sample_kernel(const SSDState *st, float ux, float uy, int withPdf, SSDResult *res) {
+  const int lane = threadIdx.x & 31;
+  const int K = int(st->K), cnt = vec_count(K);
+  Lobe g = st->g[lane];
+  V3 d = mixture_sample(g, K, (ux - 0.0f) / 1.0f, uy, lane);
+  float pdf = withPdf ? 0.0f + 1.0f * mixture_pdf(g, d, cnt, lane) : 0.0f;
+  if (lane == 0) {
+    res->dx = d.x; res->dy = d.y; res->dz = d.z; res->pdf = pdf;
+  }
+}
+__global__ void ssd_pdf_kernel(const SSDState *st, float dx, float dy, float dz, int li, SSDResult *res) {
+  const int lane = threadIdx.x & 31;
+  const int cnt = vec_count(int(st->K));
+  Lobe L = li ? st->li[lane] : st->g[lane];
+  float pdf = li ? mixture_pdf(L, mk(dx, dy, dz), cnt, lane) : 0.0f + 1.0f * mixture_pdf(L, mk(dx, dy, dz), cnt, lane);
+  if (lane == 0) res->pdf = pdf;
+}
+
+// ---------------------------------------------------------------- launchers
+PGL_DEFINE_TABLE_UPLOAD(query_upload_tables)
+
+cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const unsigned threads = 256;
+  const uint64_t warps = n;
+  unsigned blocks = unsigned((warps * 32 + threads - 1) / threads);
+  query_kernel<<<blocks, threads, 0, s>>>(p, in, out, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,
+                            cudaStream_t s) {
+  ssd_init_kernel<<<1, 32, 0, s>>>(f, px, py, pz, s1d, st, res);
+  return cudaGetLastError();
+}
+cudaError_t launch_ssd_cosine(SSDState *st, float nx, float ny, float nz, float ck, float cn, cudaStream_t s) {
+  ssd_cosine_kernel<<<1, 32, 0, s>>>(st, nx, ny, nz, ck, cn);
+  return cudaGetLastError();
+}
+cudaError_t launch_ssd_sample(const SSDState *st, float ux, float uy, int withPdf, SSDResult *res, cudaStream_t s) {
+  ssd_sample_kernel<<<1, 32, 0, s>>>(st, ux, uy, withPdf, res);
+  return cudaGetLastError();
+}
+cudaError_t launch_ssd_pdf(const SSDState *st, float dx, float dy, float dz, int li, SSDResult *res, cudaStream_t s) {
+  ssd_pdf_kernel<<<1, 32, 0, s>>>(st, dx, dy, dz, li, res);
+  return cudaGetLastError();
+}
+
+}  // namespace pgl

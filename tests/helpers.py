@@ -1,0 +1,68 @@
+"""Comparison helpers shared by the parity tests."""
+
+import numpy as np
+
+import fieldfile
+
+
+def direction_grid(n=64):
+    """Equal-area 64x64 grid of directions (z = 1 - 2u, phi = 2 pi v)."""
+    u = (np.arange(n) + 0.5) / n
+    z = 1.0 - 2.0 * u
+    phi = 2.0 * np.pi * u
+    zz, pp = np.meshgrid(z, phi, indexing="ij")
+    r = np.sqrt(np.maximum(0.0, 1.0 - zz * zz))
+    return np.stack([r * np.cos(pp), r * np.sin(pp), zz], axis=-1).reshape(-1, 3)
+
+
+def vmm_pdf64(vmm, dirs):
+    """Mixture pdf evaluated in FP64 from the stored lobe parameters."""
+    K = int(vmm["K"])
+    w = vmm["w"][:K].astype(np.float64)
+    k = vmm["kappa"][:K].astype(np.float64)
+    mu = np.stack([vmm["mx"][:K], vmm["my"][:K], vmm["mz"][:K]], axis=1).astype(np.float64)
+    norm = np.where(k > 0, k / (2 * np.pi * (1 - np.exp(-2 * k))), 1 / (4 * np.pi))
+    ct = dirs @ mu.T
+    return (w * norm * np.exp(k * np.minimum(ct - 1.0, 0.0))).sum(axis=1)
+
+
+def compare_fields(gpu_bytes, orc_bytes, side="surface"):
+    """Returns a dict describing how the GPU field matches the oracle field."""
+    A = fieldfile.read_field_file(gpu_bytes)[side]
+    B = fieldfile.read_field_file(orc_bytes)[side]
+    ca, cb = fieldfile.canonical_tree(A), fieldfile.canonical_tree(B)
+    res = dict(tree_equal=bool(len(ca["dim"]) == len(cb["dim"]) and np.array_equal(ca["dim"], cb["dim"])
+                               and np.array_equal(ca["split"], cb["split"])),
+               numbering_equal=bool(len(A["nodes"]) == len(B["nodes"])
+                                    and np.array_equal(A["nodes"]["bits"], B["nodes"]["bits"])),
+               regions=len(A["regions"]))
+    if not res["tree_equal"] or len(A["regions"]) != len(B["regions"]):
+        return res
+    dirs = direction_grid()
+    bit = 0
+    kdiff = 0
+    worst = 0.0
+    stats_equal = True
+    rel_errs = []
+    for ra, rb in zip(A["regions"], B["regions"]):
+        for key in ("mean", "var", "bounds"):
+            if not np.array_equal(ra["stats"][key].view(np.uint32), rb["stats"][key].view(np.uint32)):
+                stats_equal = False
+        if ra["stats"]["n"] != rb["stats"]["n"]:
+            stats_equal = False
+        va, vb = ra["vmm"], rb["vmm"]
+        exact = va["K"] == vb["K"] and all(
+            np.array_equal(va[k].view(np.uint32), vb[k].view(np.uint32))
+            for k in ("w", "kappa", "mx", "my", "mz", "norm", "e2k", "mc", "dist"))
+        bit += int(exact)
+        if not (ra["valid"] and rb["valid"]):
+            continue
+        if va["K"] != vb["K"]:
+            kdiff += 1
+        pa, pb = vmm_pdf64(va, dirs), vmm_pdf64(vb, dirs)
+        rel = np.abs(pa - pb) / np.maximum(np.abs(pb), 1e-12)
+        rel_errs.append(rel.max())
+        worst = max(worst, float(rel.max()))
+    res.update(bit_exact_regions=bit, k_differs=kdiff, worst_pdf_rel=worst, stats_equal=stats_equal,
+               rel_errs=np.array(rel_errs))
+    return res
