@@ -79,7 +79,7 @@ def build(verbose=False, ptxas_info=False):
                 if verbose and out.strip():
                     print(out)
     if _stale(LIB, objs):
-        _run([nvcc, GENCODE, "-shared", "-o", LIB] + objs + ["-lcudart"])
+        _run([nvcc, GENCODE, "-shared", "-Xlinker", "--no-undefined", "-o", LIB] + objs + ["-lcudart"])
     return LIB
 
 

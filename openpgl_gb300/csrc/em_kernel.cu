@@ -123,7 +123,7 @@ __device__ void vmm_merge(VMMState &v, int i0, int i1) {  // PAVMM.h:259-343
     mc = sqrtf(mc);
     kappa = mean_cosine_to_kappa(mc);
     kappa = kappa < 1e-3f ? 0.f : kappa;
-    e2k = expf(-2.0f * kappa);
+    e2k = lib_expf(-2.0f * kappa);
     nrm = vmf_norm_double(kappa, e2k);
     mx /= mc; my /= mc; mz /= mc;
   } else {
@@ -344,7 +344,7 @@ __device__ V3 map2d_to_3d(float x, float y) {  // Splitter.h:174-186
   V3 r;
   r.x = len > 0.0f ? x * sinc : 0.0f;
   r.y = len > 0.0f ? y * sinc : 0.0f;
-  r.z = cosf(len);
+  r.z = lib_cosf(len);
   return r;
 }
 
@@ -393,7 +393,7 @@ __device__ float product_scale(V3 m0, float k0, float n0, V3 m1, float k1, float
   pk = sqrtf(dot(pm, pm));
   pn = float(1.0 / (4.0 * kPiD));
   if (pk > 1e-3f) {
-    float pe = expf(-2.0f * pk);
+    float pe = lib_expf(-2.0f * pk);
     pn = vmf_norm_double(pk, pe);
     pm = pm / pk;
   } else {
@@ -402,7 +402,7 @@ __device__ float product_scale(V3 m0, float k0, float n0, V3 m1, float k1, float
   }
   float scale = (n0 * n1) / pn;
   float c0 = dot(m0, pm), c1 = dot(m1, pm);
-  scale *= expf(k0 * (c0 - 1.0f) + k1 * (c1 - 1.0f));
+  scale *= lib_expf(k0 * (c0 - 1.0f) + k1 * (c1 - 1.0f));
   return scale;
 }
 __device__ float integrated_division(V3 m0, float k0, float n0, V3 m1, float k1, float n1, float e2k1) {  // Merger.h:337-365
@@ -410,7 +410,7 @@ __device__ float integrated_division(V3 m0, float k0, float n0, V3 m1, float k1,
   float pk = sqrtf(dot(pm, pm));
   float pn = float(1.0 / (4.0 * kPiD));
   if (pk > 1e-3f) {
-    float pe = expf(-2.0f * pk);
+    float pe = lib_expf(-2.0f * pk);
     pn = vmf_norm_double(pk, pe);
     pm = pm / pk;
   } else {
@@ -419,7 +419,7 @@ __device__ float integrated_division(V3 m0, float k0, float n0, V3 m1, float k1,
   float scale = (n0 * n1) / pn;
   float c0 = dot(m0, pm), c1 = dot(m1, pm);
   scale = float(double(scale) * ((4.0 * kPiD * kPiD * double(1.0f - e2k1)) / double(k1 * k1)));
-  scale *= expf((k0 * (c0 - 1.0f) + k1 * (c1 - 1.0f)) + (2.0f * k1));
+  scale *= lib_expf((k0 * (c0 - 1.0f) + k1 * (c1 - 1.0f)) + (2.0f * k1));
   return scale;
 }
 __device__ float merge_cost(const VMMState &v, int i0, int i1) {  // Merger.h:92-177
@@ -435,7 +435,7 @@ __device__ float merge_cost(const VMMState &v, int i0, int i1) {  // Merger.h:92
     mc = sqrtf(mc);
     kappa = mean_cosine_to_kappa(mc);
     kappa = kappa < 1e-3f ? 0.f : kappa;
-    e2k = expf(-2.0f * kappa);
+    e2k = lib_expf(-2.0f * kappa);
     nrm = vmf_norm_double(kappa, e2k);
     m = m / mc;
   } else {
@@ -535,7 +535,7 @@ __device__ void phase_a(EmShared &S, const LeafSamples &L, uint32_t base, int nI
       if (pdf > 1e-16f) {
         valid = 1;
         inv = rcp_avx2(pdf);
-        lt = dw.w * logf(pdf);
+        lt = dw.w * lib_logf(pdf);
       }
     }
     S.svalid[s] = valid;

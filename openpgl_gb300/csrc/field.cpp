@@ -54,6 +54,12 @@ template struct DevArray<RegionDir>;
 template struct DevArray<KDNode>;
 template struct DevArray<Neighbours>;
 template struct DevArray<PGLSampleRecord>;
+template struct DevArray<KdJob>;
+template struct DevArray<LeafTask>;
+template struct DevArray<LeafReport>;
+template struct DevArray<IStatsAcc>;
+template struct DevArray<QueryIn>;
+template struct DevArray<QueryOut>;
 
 // ------------------------------------------------------------------ statistics (host)
 // IntegerSampleStatistics frame (SampleStatistics.h:227-241), SSE rcp form.
@@ -833,12 +839,24 @@ void canonical(const std::vector<KDNode> &nodes, std::vector<KDNode> &out, std::
     }
   }
 }
+// Member-wise (FieldConfig has tail padding, so no memcmp).
+bool config_equal(const FieldConfig &a, const FieldConfig &b) {
+  return a.maxSamples == b.maxSamples && a.maxDepth == b.maxDepth && a.minSamples == b.minSamples &&
+         a.deterministic == b.deterministic && a.knn == b.knn && a.fitRegions == b.fitRegions &&
+         a.decayOnSpatialSplit == b.decayOnSpatialSplit && a.initK == b.initK && a.initKappa == b.initKappa &&
+         a.maxK == b.maxK && a.maxIter == b.maxIter && a.maxKappa == b.maxKappa &&
+         a.maxMeanCosine == b.maxMeanCosine && a.convergence == b.convergence && a.weightPrior == b.weightPrior &&
+         a.mcPriorStrength == b.mcPriorStrength && a.mcPrior == b.mcPrior && a.splitThreshold == b.splitThreshold &&
+         a.mergeThreshold == b.mergeThreshold && a.useSplitMerge == b.useSplitMerge &&
+         a.partialReFit == b.partialReFit && a.maxSplitItr == b.maxSplitItr && a.minSplit == b.minSplit &&
+         a.minRefit == b.minRefit && a.minMerge == b.minMerge;
+}
 bool sub_equal(const SubField &a, const SubField &b) {
   if (!a.initialized && !b.initialized) return true;
   bool eq = a.isSurface == b.isSurface && a.iteration == b.iteration && a.totalSPP == b.totalSPP &&
             a.boundsSet == b.boundsSet && a.initialized == b.initialized &&
             std::memcmp(a.sceneBounds, b.sceneBounds, 24) == 0 &&
-            std::memcmp(&a.cfg, &b.cfg, sizeof(FieldConfig)) == 0;
+            config_equal(a.cfg, b.cfg);
   std::vector<KDNode> na, nb;
   std::vector<uint32_t> da, db;
   canonical(a.nodes, na, da);

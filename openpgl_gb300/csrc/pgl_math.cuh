@@ -151,6 +151,45 @@ PGL_HD float floorf_(float x) {
 #endif
 }
 
+// Single-precision exp/log/cos/sin/sincos as the host C library returns them
+// (std::exp(float) etc. on the reference side).  On the device each is
+// evaluated in double and rounded once to float: that is the correctly rounded
+// result except where the exact value lies within ~2^-29 ulp of a rounding
+// boundary, and it equals the C library's float result wherever that one is
+// correctly rounded (glibc's expf/logf/sinf/cosf are, bar rare inputs).
+PGL_HD float lib_expf(float x) {
+#ifdef __CUDA_ARCH__
+  return float(exp(double(x)));
+#else
+  return std::exp(x);
+#endif
+}
+PGL_HD float lib_logf(float x) {
+#ifdef __CUDA_ARCH__
+  return float(log(double(x)));
+#else
+  return std::log(x);
+#endif
+}
+PGL_HD float lib_cosf(float x) {
+#ifdef __CUDA_ARCH__
+  return float(cos(double(x)));
+#else
+  return std::cos(x);
+#endif
+}
+PGL_HD void lib_sincosf(float x, float *s, float *c) {
+#ifdef __CUDA_ARCH__
+  double sd, cd;
+  sincos(double(x), &sd, &cd);
+  *s = float(sd);
+  *c = float(cd);
+#else
+  *s = std::sin(x);
+  *c = std::cos(x);
+#endif
+}
+
 // fastapprox::exp
 PGL_HD float fexp(float v) {
   const float ln2Part1 = float(0.6931457519), ln2Part2 = float(1.4286067653e-6);

@@ -151,7 +151,7 @@ __device__ V3 mixture_sample(const Lobe &L, int K, float ux, float uy, int lane)
     float z = 1.0f - 2.0f * u1;
     float r = sqrtf(smax(0.f, (1.0f - z * z)));
     float sp, cp;
-    sincosf(float(2.0 * kPiD * double(ux)), &sp, &cp);
+    lib_sincosf(float(2.0 * kPiD * double(ux)), &sp, &cp);
     d = mk(r * cp, r * sp, z);
   } else {
     float ct = 1.f + (flog(1.0f + ((e2k - 1.f) * ux))) / k;
@@ -159,7 +159,7 @@ __device__ V3 mixture_sample(const Lobe &L, int K, float ux, float uy, int lane)
     float st = sqrtf(1.f - ct * ct);
     float phi = float(2.0 * kPiD * double(u1));
     float sp, cp;
-    sincosf(phi, &sp, &cp);
+    lib_sincosf(phi, &sp, &cp);
     d = mk(st * cp, st * sp, ct);
   }
   return xfm(frame_of(mu, false), d);
