@@ -1,0 +1,404 @@
+#!/usr/bin/env python3
+"""Benchmark of the field-training (Update) and guided-query path on one GB300.
+
+Workload (multi-frame, plain drop-in): 8 frames x 2,097,152 PGLSampleData
+records (16,777,216 samples per step) from the cube-face generator, 25 % of
+them flagged inside-volume (interior positions, one lobe with kappa 20);
+maxSamplesPerLeaf 32000, deterministic.  One step = a fresh field, then for
+every frame: clear the storage, add that frame's samples, pglFieldUpdate.
+The metric is milliseconds per 16M (2^24) samples, lower is better.  Beside it
+the guided queries of the cube workload (1,048,576 queries: Init + cosine
+product + Sample + PDF) on the trained field, as queries/s.
+
+`value` is timed with CUDA events on the library's stream with the samples
+already in device memory; `e2e` adds each frame's host-to-device copy from
+pinned memory (pglSampleStorageAddSamples on host records) and the read-back
+of the per-region update reports.  The inputs (16.8M x 40 B = 671 MB) are
+larger than L2 (129 MB), so no flush is needed between steps.
+
+`--impl reference` times the CPU restatement of the reference algorithm (the
+oracle, built with the reference's arithmetic) with all host threads on a
+bounded sample of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FRAMES = 8
+FRAME_SAMPLES = 2_097_152
+SAMPLES_PER_STEP = FRAMES * FRAME_SAMPLES  # 16,777,216
+UNIT_SAMPLES = 16_777_216
+MAX_SAMPLES_PER_LEAF = 32000
+QUERIES = 1_048_576
+METRIC = "Update ms/16M samples; guided queries/s @p99; batched vs plain GPU vs host CPU"
+UNIT = "ms/16M samples"
+WORKLOAD = ("multi-frame: 8 frames x 2,097,152 samples (25% inside-volume, cube faces, 3-lobe vMF per octant), "
+            "maxSamplesPerLeaf 32000, deterministic; plus 1,048,576 guided queries (cosine product, 1 SamplePDF)")
+# algorithmic bytes of one EM launch: each sample's position+distance and
+# direction+weight read once (2 x 16 B), each region's directional state
+# (3008 B) read and written once
+EM_BYTES_PER_SAMPLE = 32
+REGION_STATE_BYTES = 3008
+# DRAM traffic of the EM kernel per sample, from the ncu capture summarised in
+# profiles/em_leaf_kernel_multiframe.md (None until captured)
+EM_TRAFFIC_PER_SAMPLE = None
+
+
+def frame_seed(f):
+    return 9000 + f
+
+
+def make_frames():
+    from openpgl_gb300 import synthetic as syn
+
+    return [syn.cube_face_samples(FRAME_SAMPLES, frame_seed(f), volume_fraction=0.25) for f in range(FRAMES)]
+
+
+def make_queries():
+    from openpgl_gb300 import synthetic as syn
+
+    return syn.queries(QUERIES, 4242)
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) != 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[2:]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- CPU baseline
+def cpu_baseline(frames, budget_s=20.0, threads=None):
+    """Times the oracle (the CPU restatement of the reference's Update, with the
+    reference's arithmetic) on the first frames of the workload, as many as
+    fit in about budget_s, and scales to ms per 16M samples."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    threads = threads or os.cpu_count()
+    orc = pyoracle.OracleField(MAX_SAMPLES_PER_LEAF, deterministic=True, threads=threads)
+    done, t_total = 0, 0.0
+    for f in frames:
+        t0 = time.perf_counter()
+        orc.update(f)
+        t_total += time.perf_counter() - t0
+        done += 1
+        if t_total >= budget_s:
+            break
+    orc.close()
+    samples = done * FRAME_SAMPLES
+    value = t_total * 1e3 * UNIT_SAMPLES / samples
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"frames 1-{done} of 8 ({samples} samples, fresh field), oracle Update wall time scaled to "
+                      f"16,777,216 samples"}
+
+
+def cpu_queries(frames, queries, threads=None, n=131072):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    threads = threads or os.cpu_count()
+    orc = pyoracle.OracleField(MAX_SAMPLES_PER_LEAF, deterministic=True, threads=threads)
+    orc.update(frames[0])
+    t0 = time.perf_counter()
+    orc.query(queries[:n])
+    dt = time.perf_counter() - t0
+    orc.close()
+    return n / dt
+
+
+# ----------------------------------------------------------------- GPU arm
+def run_gpu(args, rank, world, local_rank):
+    import torch
+
+    import openpgl_gb300 as pgl
+
+    torch.cuda.set_device(local_rank)
+    frames = make_frames()
+    queries = make_queries()
+    dev = pgl.Device()
+    stream = torch.cuda.ExternalStream(dev.cuda_stream())
+    field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF))
+    storage = pgl.SampleStorage()
+    d_frames = [torch.from_numpy(f.view(np.uint8)).to("cuda") for f in frames]
+    torch.cuda.synchronize()
+
+    em_ms, em_launches, em_bytes, em_samples = [0.0], [0], [0], [0]
+
+    def step(record=False):
+        field.reset()
+        for f, d in zip(frames, d_frames):
+            storage.clear()
+            storage.add_samples_device(d.data_ptr(), len(f))
+            field.update(storage)
+            if record:
+                for vol in (False, True):
+                    ph = field.phases(vol)
+                    if ph["samples"] > 0:
+                        em_ms[0] += ph["em_kernel"]
+                        em_launches[0] += 1
+                        em_samples[0] += int(ph["samples"])
+                        em_bytes[0] += int(ph["samples"]) * EM_BYTES_PER_SAMPLE + \
+                            int(ph["regions"]) * 2 * REGION_STATE_BYTES
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    barrier()
+    launches0 = pgl.kernel_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step(record=True)
+    ev1.record(stream)
+    barrier()
+    launches = pgl.kernel_launch_count() - launches0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    clk = clocks.stop()
+
+    # ---- guided queries on the trained field (device buffers)
+    qdev = torch.from_numpy(queries.view(np.uint8)).to("cuda")
+    rdev = torch.empty(QUERIES * 32, dtype=torch.uint8, device="cuda")
+    for _ in range(max(args.warmup, 3)):
+        field.sample_batch_device(qdev.data_ptr(), QUERIES, rdev.data_ptr(), stream=dev.cuda_stream())
+    torch.cuda.synchronize()
+    lat = []
+    q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(args.steps, 5)
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        field.sample_batch_device(qdev.data_ptr(), QUERIES, rdev.data_ptr(), stream=dev.cuda_stream())
+        b.record(stream)
+        lat.append((a, b))
+    torch.cuda.synchronize()
+    lat_ms = sorted(a.elapsed_time(b) for a, b in lat)
+    q_ms = statistics.median(lat_ms)
+    # host-buffer queries (copies inside)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        field.sample_batch(queries)
+    q_e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
+
+    # ---- end to end: host (pinned) sample records through the C API
+    pinned = [torch.from_numpy(f.view(np.uint8)).pin_memory() for f in frames]
+    host_views = [p.numpy().view(frames[0].dtype) for p in pinned]
+    d2h = [0]
+
+    def e2e_step():
+        field.reset()
+        for f in host_views:
+            storage.clear()
+            storage.add_samples(f)
+            field.update(storage)
+            for vol in (False, True):
+                rep = field.reports(vol)
+                d2h[0] += rep.nbytes if hasattr(rep, "nbytes") else 0
+
+    e2e_step()
+    barrier()
+    d2h[0] = 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_wall = (time.perf_counter() - t0) * 1e3 / args.steps
+
+    # max over ranks
+    vals = torch.tensor([ms, e2e_ms, q_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(vals, op=torch.distributed.ReduceOp.MAX)
+    ms, e2e_ms, q_ms = vals.tolist()
+    if rank != 0:
+        return None
+
+    em_avg_ms = em_ms[0] / max(em_launches[0], 1)
+    em_bytes_per_launch = em_bytes[0] / max(em_launches[0], 1)
+    achieved = em_bytes_per_launch / (em_avg_ms * 1e-3) / 1e9
+    peak = measured_peak("hbm_gbs", 6800.0)
+    traffic = None
+    if EM_TRAFFIC_PER_SAMPLE is not None:
+        traffic = EM_TRAFFIC_PER_SAMPLE * em_samples[0] / max(em_launches[0], 1)
+    out = {
+        "metric": METRIC,
+        "value": round(ms * UNIT_SAMPLES / (SAMPLES_PER_STEP * world), 3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 3),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded generators of the configured shapes)",
+        "config": {"workload": WORKLOAD, "samples_per_step": SAMPLES_PER_STEP, "frames": FRAMES,
+                   "max_samples_per_leaf": MAX_SAMPLES_PER_LEAF, "l2": "inputs (671 MB) larger than L2",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"kernel": "em_leaf_kernel", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak[0],
+                     "peak_source": peak[1], "unit": "GB/s", "frac": round(achieved / peak[0], 4),
+                     "traffic": traffic, "avg_launch_ms": round(em_avg_ms, 3),
+                     "algorithmic_bytes_per_launch": int(em_bytes_per_launch),
+                     "em_share_of_step": round(em_ms[0] / args.steps / ms, 3),
+                     "note": "EM is FP32/SFU-bound; HBM fraction shown against minimum algorithmic bytes"},
+        "e2e": {"value": round(e2e_ms * UNIT_SAMPLES / (SAMPLES_PER_STEP * world), 3), "unit": UNIT,
+                "h2d_bytes_per_step": SAMPLES_PER_STEP * 40, "d2h_bytes_per_step": d2h[0] // max(args.steps, 1),
+                "wall_ms_per_step": round(e2e_wall, 3)},
+        "queries": {"queries_per_s": round(QUERIES / (q_ms * 1e-3)), "batch": QUERIES,
+                    "p50_ms": round(statistics.median(lat_ms), 3),
+                    "p99_ms": round(lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))], 3),
+                    "e2e_queries_per_s": round(QUERIES / (q_e2e_ms * 1e-3))},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(frames, budget_s=args.cpu_budget)
+        out["cpu_baseline"]["queries_per_s"] = round(cpu_queries(frames, queries))
+    return out
+
+
+def measured_peak(key, fallback):
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            v = json.load(f).get(key)
+        if v:
+            return float(v), "measured"
+    except (OSError, ValueError):
+        pass
+    return fallback, "fallback"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    frames = make_frames()
+    threads = os.cpu_count()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    # each step: a fresh field trained on the first frame (a bounded sample of
+    # the workload), scaled to ms per 16M samples
+    for _ in range(args.warmup):
+        pass
+    times = []
+    for _ in range(args.steps):
+        orc = pyoracle.OracleField(MAX_SAMPLES_PER_LEAF, deterministic=True, threads=threads)
+        t0 = time.perf_counter()
+        orc.update(frames[0])
+        times.append(time.perf_counter() - t0)
+        orc.close()
+    ms = statistics.median(times) * 1e3
+    value = ms * UNIT_SAMPLES / FRAME_SAMPLES
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "samples_per_step": FRAME_SAMPLES,
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "frame 1 of 8 (2,097,152 samples, fresh field) per step, scaled to 16,777,216"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        if world > 1:
+            import torch
+
+            torch.cuda.set_device(local_rank)
+            torch.distributed.init_process_group("nccl")
+        out = run_gpu(args, rank, world, local_rank)
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -49,10 +49,31 @@ OPENPGL_CORE_INTERFACE size_t pglFieldStoreToBuffer(PGLField field, char *buffer
 // Milliseconds of the last Update of the surface (0) or volume (1) field:
 // total, sample copy, spatial structure, directional fitting.
 OPENPGL_CORE_INTERFACE bool pglFieldGetLastUpdateTimings(PGLField field, int volume, float out4[4]);
+// Phases of the last Update of the surface (0) or volume (1) field, from CUDA
+// events on the library's stream: total, sample copy, spatial structure,
+// directional (= gather + EM kernel), gather, EM kernel (ms), then the number
+// of samples and of regions.  Returns 8; writes when capacity >= 8.
+OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdatePhases(PGLField field, int volume, double *out, size_t capacity);
+// The cudaStream_t every kernel of the library is launched on (one per
+// process), for callers that order their own work or events against it.
+OPENPGL_CORE_INTERFACE void *pglDeviceGetCudaStream(PGLDevice device);
+// Number of the library's own CUDA kernels launched so far by this process
+// (the scan and sort kernels of CUB that it calls are not counted).
+OPENPGL_CORE_INTERFACE uint64_t pglGetKernelLaunchCount();
 // Per-region counters of the last Update: region, EM iterations, splits,
 // merges, components (5 x u32 per region); returns the region count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int volume, uint32_t *out, size_t capacity);
-// Message of the last error raised on this thread ("" if none).
+// Where the EM kernel spent the last Update, per region (15 x u64 each):
+// region, samples, E-step passes, distance passes, split-statistics passes,
+// then SM clock cycles in E-steps, distance passes, split-statistics passes,
+// merging, M-steps and in total, then inside the passes the cycles of the
+// producing threads and of the slowest summing thread, for E-steps and for
+// split-statistics passes.  Returns the region count; writes when
+// capacity >= 15 x count.
+OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int volume, uint64_t *out,
+                                                           size_t capacity);
+// Message of the error raised by the last library call on this thread ("" if
+// that call succeeded).
 OPENPGL_CORE_INTERFACE const char *pglGetLastError();
 
 #ifdef __cplusplus

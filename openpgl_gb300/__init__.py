@@ -142,6 +142,11 @@ C_API = {
     "pglFieldGetLastUpdateReports": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                        ctypes.c_size_t]),
     "pglGetLastError": (ctypes.c_char_p, []),
+    "pglFieldGetLastUpdatePhases": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                                      ctypes.c_size_t]),
+    "pglDeviceGetCudaStream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "pglGetKernelLaunchCount": (ctypes.c_uint64, []),
+    "pglFieldGetLastUpdateProfile": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
 }
 
 _lib = None
@@ -166,6 +171,11 @@ def load(build_if_missing=True):
     return _lib
 
 
+def kernel_launch_count():
+    """Kernels of this library launched so far by the process."""
+    return int(load().pglGetKernelLaunchCount())
+
+
 def last_error():
     return load().pglGetLastError().decode()
 
@@ -180,6 +190,10 @@ class Device:
         self.lib = load()
         self.h = self.lib.pglNewDevice(device_type, num_threads)
         _check(self.h, "pglNewDevice")
+
+    def cuda_stream(self):
+        """The cudaStream_t (as an int) the library launches on."""
+        return self.lib.pglDeviceGetCudaStream(self.h) or 0
 
     def release(self):
         if self.h:
@@ -206,6 +220,13 @@ class SampleStorage:
     def add_samples(self, samples):
         s = np.ascontiguousarray(samples, dtype=PGL_SAMPLE_DTYPE)
         self.lib.pglSampleStorageAddSamples(self.h, s.ctypes.data, len(s))
+
+    def add_samples_device(self, ptr, n):
+        """Adds n PGLSampleData records that live in device memory at ptr."""
+        self.lib.pglSampleStorageAddSamplesDevice(self.h, ptr, n)
+        err = last_error()
+        if err:
+            raise RuntimeError(err)
 
     def add_sample(self, sample):
         s = np.ascontiguousarray(np.asarray([sample], dtype=PGL_SAMPLE_DTYPE))
@@ -304,6 +325,20 @@ class Field:
         out = (ctypes.c_float * 4)()
         self.lib.pglFieldGetLastUpdateTimings(self.h, int(volume), out)
         return dict(total=out[0], copy=out[1], spatial=out[2], directional=out[3])
+
+    def profile(self, volume=False):
+        """Per-region EM profile of the last Update (see pglFieldGetLastUpdateProfile)."""
+        n = self.lib.pglFieldGetLastUpdateProfile(self.h, int(volume), None, 0)
+        out = np.zeros((n, 15), dtype=np.uint64)
+        if n:
+            self.lib.pglFieldGetLastUpdateProfile(self.h, int(volume), out.ctypes.data, out.size)
+        return out
+
+    def phases(self, volume=False):
+        out = (ctypes.c_double * 8)()
+        self.lib.pglFieldGetLastUpdatePhases(self.h, int(volume), out, 8)
+        keys = ("total", "copy", "spatial", "directional", "gather", "em_kernel", "samples", "regions")
+        return dict(zip(keys, list(out)))
 
     def reports(self, volume=False):
         n = self.lib.pglFieldGetLastUpdateReports(self.h, int(volume), None, 0)

@@ -53,7 +53,9 @@ static_assert(sizeof(PGLSampleData) == sizeof(PGLSampleRecord), "sample record l
 static_assert(sizeof(PGLGuidedQuery) == sizeof(QueryIn), "query layout");
 static_assert(sizeof(PGLGuidedQueryResult) == sizeof(QueryOut), "query result layout");
 
-#define PGL_TRY try {
+#define PGL_TRY \
+  try {         \
+    g_lastError.clear();
 #define PGL_CATCH(ret)            \
   }                               \
   catch (const std::exception &e) { \
@@ -681,10 +683,7 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatch(PGLField field, const PGLG
 }
 OPENPGL_CORE_INTERFACE void pglSampleStorageAddSamplesDevice(PGLSampleStorage s, const PGLSampleData *d, size_t n) {
   PGL_TRY
-  std::vector<PGLSampleRecord> h(n);
-  check(cudaMemcpy(h.data(), d, n * sizeof(PGLSampleRecord), cudaMemcpyDeviceToHost), "D2H samples");
-  S(s)->add(h.data(), n);
-  S(s)->flush();
+  S(s)->ingestDevice(reinterpret_cast<const PGLSampleRecord *>(d), n);
   PGL_CATCH_VOID
 }
 OPENPGL_CORE_INTERFACE size_t pglFieldStoreToBuffer(PGLField field, char *buffer, size_t capacity) {
@@ -703,6 +702,50 @@ OPENPGL_CORE_INTERFACE bool pglFieldGetLastUpdateTimings(PGLField field, int vol
   out4[3] = t.directional;
   return true;
   PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdatePhases(PGLField field, int volume, double *out, size_t cap) {
+  PGL_TRY
+  const UpdateTimings &t = volume ? F(field)->volume.timings : F(field)->surface.timings;
+  const double v[8] = {t.total, t.copy, t.spatial, t.directional, t.gather, t.emKernel, double(t.samples),
+                       double(t.regions)};
+  if (out && cap >= 8)
+    for (int i = 0; i < 8; ++i) out[i] = v[i];
+  return 8;
+  PGL_CATCH(0)
+}
+OPENPGL_CORE_INTERFACE uint64_t pglGetKernelLaunchCount() { return kernel_launches(); }
+OPENPGL_CORE_INTERFACE void *pglDeviceGetCudaStream(PGLDevice device) {
+  PGL_TRY
+  (void)device;
+  return static_cast<void *>(Context::get().stream);
+  PGL_CATCH(nullptr)
+}
+OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int volume, uint64_t *out, size_t cap) {
+  PGL_TRY
+  const SubField &sf = volume ? F(field)->volume : F(field)->surface;
+  size_t n = sf.lastProfiles.size();
+  if (out && cap >= n)
+    for (size_t i = 0; i < n; ++i) {
+      const LeafProfile &p = sf.lastProfiles[i];
+      uint64_t *o = out + 15 * i;
+      o[0] = sf.lastReportRegion[i];
+      o[1] = p.count;
+      o[2] = p.estepPasses;
+      o[3] = p.distPasses;
+      o[4] = p.splitPasses;
+      o[5] = p.cycEstep;
+      o[6] = p.cycDist;
+      o[7] = p.cycSplit;
+      o[8] = p.cycMerge;
+      o[9] = p.cycMstep;
+      o[10] = p.cycTotal;
+      o[11] = p.cycProdE;
+      o[12] = p.cycConsE;
+      o[13] = p.cycProdS;
+      o[14] = p.cycConsS;
+    }
+  return n;
+  PGL_CATCH(0)
 }
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int volume, uint32_t *out, size_t cap) {
   PGL_TRY

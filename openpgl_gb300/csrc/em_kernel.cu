@@ -9,25 +9,25 @@
 // and merger of VMMChiSquareComponentSplitter.h / VMMChiSquareComponentMerger.h.
 //
 // How it is laid out for the GPU: a pass over a leaf's samples (E-step,
-// distance pass, split-statistics pass) streams the samples in chunks of
-// kChunk.  Phase A computes every per-(sample, lobe) term in parallel (4 threads
-// per sample, one per group of 8 lobes) into shared memory; phase B runs one
-// thread per accumulator (for example the x component of lobe 7's weighted
-// direction sum) that adds the chunk's terms in sample order.  That keeps the
-// reference's summation order (sequential over samples within each SIMD
-// lane), so every accumulator gets the reference's bits, while the 4K+1 to
-// 6K accumulators of many leaves keep the SM busy.  Scalar per-leaf logic (M
-// step, split/merge bookkeeping) runs on thread 0 between passes.
+// distance pass, split-statistics pass) streams the samples in chunks through
+// a two-stage producer/consumer pipeline (see "sample passes" below):
+// producer threads compute each sample's lobe terms and pdf, consumer threads
+// (one per accumulator, e.g. the x component of lobe 7's weighted direction
+// sum) add the chunk's terms in sample order.  That keeps the reference's
+// summation order (sequential over samples within each SIMD lane), so every
+// accumulator gets the reference's bits.  Scalar per-leaf logic (M step,
+// split/merge bookkeeping) runs on thread 0 between passes.
 #include <cuda_runtime.h>
+
+#include <cstddef>
 
 #include "launch.h"
 #include "pgl_internal.h"
 
 namespace pgl {
 
-constexpr int kEmThreads = 256;
-constexpr int kChunk = 64;
-constexpr int kTermStride = kChunk + 1;  // pad: conflict-free for both phases
+constexpr int kEmThreads = 512;
+constexpr int kStageFloats = 19200;  // floats per pipeline stage (two stages, 150 KB)
 constexpr int kMaxPairs = kMaxK * (kMaxK - 1) / 2;
 
 struct Unassigned {
@@ -42,10 +42,12 @@ struct EmShared {
   SuffState temp;     // statistics of a partial refit
   SplitState lsplit;  // split statistics used by the recursive splitting
   Frame invFrame[kMaxK];
-  float term[6][kMaxK][kTermStride];
-  float sdx[kChunk], sdy[kChunk], sdz[kChunk], sw[kChunk], spdf[kChunk], sinv[kChunk], lterm[kChunk], ssd[kChunk],
-      sSamplePdf[kChunk];
-  int svalid[kChunk];
+  __align__(16) float pbuf[2 * kStageFloats];  // the two pipeline stages
+  __align__(16) float4 lobeA[kMaxK];  // mean direction, kappa
+  float2 lobeB[kMaxK];                // normalisation, weight
+  float lobeWInv[kMaxK];              // RN(1 / weight) for div_rcp
+  float xch[2][kMaxK];
+  uint32_t rcpTab[2048];
   float cost[kMaxPairs];
   float ll;
   Unassigned un;
@@ -58,7 +60,16 @@ struct EmShared {
   float mcEstimate;
   int iterations;
   LeafReport report;
+  LeafProfile prof;
 };
+static_assert(offsetof(EmShared, pbuf) % 16 == 0 &&
+                  offsetof(EmShared, lobeA) % 16 == 0,
+              "128-bit shared loads");
+
+// cycle accounting of thread 0 (LeafProfile)
+#define PGL_PROF_BEGIN(t) const long long t = clock64();
+#define PGL_PROF_END(t, field) \
+  if (threadIdx.x == 0) S.prof.field += uint64_t(clock64() - (t));
 
 // ---------------------------------------------------------------- scalar helpers (thread 0)
 
@@ -482,6 +493,26 @@ __device__ void split_merge_stats(SplitState &s, int I, int J, float wI, V3 muI,
 }
 
 // ---------------------------------------------------------------- sample passes
+//
+// Every pass over a leaf's samples (E-step, distance pass, split-statistics
+// pass) runs as a two-stage pipeline over chunks of samples, with one
+// __syncthreads per chunk and two shared-memory stages:
+//   producers (threads [0, P)): one sample per thread; all lobe terms of the
+//     sample in registers, its pdf, then the per-(lobe, sample) values of the
+//     pass written to stage (c & 1);
+//   consumers (threads [P, 512)): one thread per accumulator (for example
+//     the x component of lobe 7's weighted direction sum), adding the chunk in
+//     stage ((c - 1) & 1) in sample order.
+// The consumers keep the reference's summation order (sequential over samples
+// within each SIMD lane).  Samples that the reference skips (pdf <= 1e-16)
+// contribute a term of exactly +-0, which leaves an accumulator unchanged:
+// accumulators start at +0 and a round-to-nearest sum that starts at +0
+// never becomes -0.  The producers write each accumulator's finished term,
+// so a consumer lane only loads and adds, and chain warps do not diverge
+// (chi-square lanes have warps of their own).  Each pass
+// gives the consumers only the warps its chains need and the producers the
+// rest; the chunk is one sample per producer thread, bounded by the stage
+// memory.
 
 struct LeafSamples {
   const float4 *dirw;  // direction xyz, weight
@@ -492,155 +523,398 @@ struct LeafSamples {
 
 enum PassKind { kPassEStep = 0, kPassDistance = 1, kPassSplit = 2 };
 
-// Phase A for one chunk: responsibilities (and pass-specific terms) of sample
-// s = tid % kChunk for lobes [8v, 8v+8), v = tid / kChunk.
-__device__ void phase_a(EmShared &S, const LeafSamples &L, uint32_t base, int nIn, PassKind kind) {
-  const int tid = threadIdx.x;
-  const int s = tid % kChunk, v = tid / kChunk;
-  const VMMState &vm = S.vmm;
-  const int cnt = vec_count(int(vm.K));
-  bool have = s < nIn;
-  float4 dw = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (have) dw = L.dirw[base + s];
-  if (v == 0) {
-    S.sdx[s] = dw.x; S.sdy[s] = dw.y; S.sdz[s] = dw.z; S.sw[s] = dw.w;
-    if (have && kind != kPassEStep) {
-      if (kind == kPassDistance) S.ssd[s] = rcp_avx2(L.dist[base + s]);
-      else S.sSamplePdf[s] = L.pdf[base + s];
-    }
+// Thread roles and stage layout of one pass (the same in every thread).
+struct PassShape {
+  int P;       // producer threads [0, P); consumers [P, kEmThreads)
+  int C;       // samples per chunk (<= P)
+  int R;       // row stride of the per-(lobe, sample) rows: C + 4 floats
+  int stage;   // floats per stage
+};
+template <PassKind kind>
+__device__ __forceinline__ PassShape pass_shape(int Kp) {
+  // rows: one per (accumulator, lobe); extra: per-sample arrays
+  int consWarps, rows, extra;
+  if (kind == kPassEStep) {  // 4 Kp lobe chains, then LL and 4 unassigned sums
+    consWarps = Kp / 8 + 1;
+    rows = 4 * Kp;
+    extra = 5;
+  } else if (kind == kPassDistance) {  // 2 Kp chains
+    consWarps = (2 * Kp + 31) / 32;
+    rows = 2 * Kp;
+    extra = 0;
+  } else {  // 5 Kp product chains, then (from a warp boundary) Kp chi-square chains
+    consWarps = (5 * Kp + 31) / 32 + 1;
+    rows = 6 * Kp;
+    extra = 1;
   }
-  const V3 d = mk(dw.x, dw.y, dw.z);
-  if (have && v < cnt) {
-#pragma unroll
-    for (int j = 0; j < kLanes; ++j) {
-      int k = v * kLanes + j;
-      float ct = dot(d, mk(vm.mx[k], vm.my[k], vm.mz[k]));
-      float cm1 = emin(ct - 1.0f, 0.0f);
-      float ev = vm.norm[k] * fexp(vm.kappa[k] * cm1);
-      S.term[0][k][s] = vm.w[k] * ev;
-    }
-  }
-  __syncthreads();
-  if (v == 0) {
-    int valid = 0;
-    float pdf = 0.0f, inv = 0.0f, lt = 0.0f;
-    if (have) {
-      float pv[kLanes];
-#pragma unroll
-      for (int j = 0; j < kLanes; ++j) pv[j] = 0.0f;
-      for (int vv = 0; vv < cnt; ++vv)
-#pragma unroll
-        for (int j = 0; j < kLanes; ++j) pv[j] += S.term[0][vv * kLanes + j][s];
-      pdf = reduce8(pv);
-      if (pdf > 1e-16f) {
-        valid = 1;
-        inv = rcp_avx2(pdf);
-        lt = dw.w * lib_logf(pdf);
-      }
-    }
-    S.svalid[s] = valid;
-    S.spdf[s] = pdf;
-    S.sinv[s] = inv;
-    S.lterm[s] = lt;
-  }
-  __syncthreads();
-  if (have && v < cnt && S.svalid[s]) {
-    const float inv = S.sinv[s], pdf = S.spdf[s];
-#pragma unroll
-    for (int j = 0; j < kLanes; ++j) {
-      int k = v * kLanes + j;
-      float a = S.term[0][k][s] * inv;
-      if (kind == kPassEStep) {
-        S.term[0][k][s] = a;
-      } else if (kind == kPassDistance) {
-        float wts = (dw.w * a) * ((a * pdf) / vm.w[k]);
-        S.term[0][k][s] = wts;
-        S.term[1][k][s] = wts * S.ssd[s];
-      } else {
-        float spdfv = S.sSamplePdf[s];
-        float value = dw.w * spdfv;
-        float mcEst = S.mcEstimate;
-        float vmf = a * pdf;
-        float pvp = vmf * value;
-        pvp /= (mcEst * pdf);
-        float chi = (value * value) * vmf;
-        chi /= ((mcEst * mcEst) * pdf) * pdf;
-        chi -= 2.0f * pvp;
-        chi += vmf;
-        chi /= spdfv;
-        chi = a > 0.0f ? chi : 0.0f;
-        V3 ld = xfm(S.invFrame[k], d);
-        float aw = a * dw.w;
-        S.term[0][k][s] = a;
-        S.term[1][k][s] = chi;
-        S.term[2][k][s] = aw;
-        S.term[3][k][s] = aw * (ld.x * ld.x);
-        S.term[4][k][s] = aw * (ld.y * ld.y);
-        S.term[5][k][s] = aw * (ld.x * ld.y);
-      }
-    }
-  }
-  __syncthreads();
+  PassShape p;
+  p.P = kEmThreads - 32 * consWarps;
+  int c = (kStageFloats - 4 * rows) / (rows + extra);
+  c = c < p.P ? c : p.P;
+  p.C = c & ~31;
+  p.R = p.C + 4;
+  p.stage = rows * p.R + extra * p.C;
+  return p;
 }
 
-// E-step (WEMFactory.h:847-892).  Accumulators: t < 128 -> (component t/32,
-// lobe t%32) of the weighted direction/weight sums, 128 -> log-likelihood,
-// 129..132 -> unassigned weight and direction.
+// x86 RCPSS from the block's shared copy of the table (per-lane gathers from
+// constant memory would serialise)
+__device__ __forceinline__ float rcp_avx2_tab(float a, const uint32_t *tab) {
+  uint32_t u = f2u(a), s = u & 0x80000000u, e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+  float r;
+  if (e == 0) {
+    r = u2f(s | 0x7F800000u);
+  } else if (e == 255) {
+    r = m ? a : u2f(s);
+  } else {
+    uint32_t t = tab[m >> 12];
+    int re = int((t >> 23) & 0xFFu) - (int(e) - 127);
+    r = re <= 0 ? u2f(s) : (re >= 255 ? u2f(s | 0x7F800000u) : u2f(s | (uint32_t(re) << 23) | (t & 0x7FFFFFu)));
+  }
+  return r * fmaf_(-r, a, 2.0f);
+}
+
+// Lobe parameters packed for the producers' broadcast loads.
+__device__ void pack_lobes(EmShared &S, int Kp) {
+  const int tid = threadIdx.x;
+  if (tid < Kp) {
+    const VMMState &v = S.vmm;
+    S.lobeA[tid] = make_float4(v.mx[tid], v.my[tid], v.mz[tid], v.kappa[tid]);
+    S.lobeB[tid] = make_float2(v.norm[tid], v.w[tid]);
+    S.lobeWInv[tid] = rcp_for_div(v.w[tid]);
+  }
+}
+
+// Producer side of one sample: the E-step terms of all lobes, the sample pdf
+// (vfloat8 lane sums over the lobe vectors, then the 8-lane reduction) and
+// 1/pdf.
+struct SampleTerms {
+  float t[kMaxK];
+  float pdf, inv;
+  bool valid;
+};
+__device__ __forceinline__ void sample_terms(const EmShared &S, int cnt, V3 d, SampleTerms &T) {
+  float pv[kLanes];
+#pragma unroll
+  for (int j = 0; j < kLanes; ++j) pv[j] = 0.0f;
+#pragma unroll
+  for (int v = 0; v < kMaxK / kLanes; ++v) {
+    if (v < cnt) {
+#pragma unroll
+      for (int j = 0; j < kLanes; ++j) {
+        const int k = v * kLanes + j;
+        const float4 A = S.lobeA[k];
+        const float2 B = S.lobeB[k];
+        float ct = dot(d, mk(A.x, A.y, A.z));
+        float cm1 = emin(ct - 1.0f, 0.0f);
+        float ev = B.x * fexp(A.w * cm1);
+        T.t[k] = B.y * ev;
+        pv[j] += T.t[k];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kLanes; ++j) T.t[v * kLanes + j] = 0.0f;
+    }
+  }
+  T.pdf = reduce8(pv);
+  T.valid = T.pdf > 1e-16f;
+  T.inv = T.valid ? rcp_avx2_tab(T.pdf, S.rcpTab) : 0.0f;
+}
+
+struct SampleIn {
+  float4 dw;
+  float x;  // pdf (split pass) or distance (distance pass)
+  bool have;
+};
+template <PassKind kind>
+__device__ __forceinline__ SampleIn load_sample(const LeafSamples &L, uint32_t idx) {
+  SampleIn r;
+  r.have = idx < L.count;
+  r.dw = make_float4(0.f, 0.f, 0.f, 0.f);
+  r.x = 0.0f;
+  if (r.have) {
+    r.dw = L.dirw[idx];
+    if constexpr (kind == kPassDistance) r.x = L.dist[idx];
+    else if constexpr (kind == kPassSplit) r.x = L.pdf[idx];
+  }
+  return r;
+}
+
+// Producer: fill stage `st` (base pointer B) for the sample in slot s.
+template <PassKind kind>
+__device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cnt, int Kp, int s, const SampleIn &in,
+                                        float *B) {
+  SampleTerms T;
+  const V3 d = mk(in.dw.x, in.dw.y, in.dw.z);
+  const float w = in.dw.w;
+  if (in.have) {
+    sample_terms(S, cnt, d, T);
+  } else {
+    T.valid = false;
+    T.pdf = 0.0f;
+    T.inv = 0.0f;
+  }
+  const bool valid = in.have && T.valid;
+  const int R = sh.R, C = sh.C;
+  if constexpr (kind == kPassEStep) {
+    // rows q Kp + k: (dx a) w, (dy a) w, (dz a) w, a w; then LL and the
+    // unassigned sums per sample
+#pragma unroll
+    for (int k = 0; k < kMaxK; ++k) {
+      if (k < Kp) {
+        float px = 0.0f, py = 0.0f, pz = 0.0f, pw = 0.0f;
+        if (valid) {
+          const float a = T.t[k] * T.inv;
+          px = (d.x * a) * w;
+          py = (d.y * a) * w;
+          pz = (d.z * a) * w;
+          pw = a * w;
+        }
+        B[k * R + s] = px;
+        B[(Kp + k) * R + s] = py;
+        B[(2 * Kp + k) * R + s] = pz;
+        B[(3 * Kp + k) * R + s] = pw;
+      }
+    }
+    float *X = B + 4 * Kp * R;
+    // the log-likelihood only drives the convergence test (its relative
+    // change against 0.005); it is not stored, so the single-precision logf
+    // (<= 1 ulp) stands in for the C library's here
+    X[s] = valid ? w * logf(T.pdf) : 0.0f;
+    const bool un = in.have && !T.valid;
+    X[C + s] = un ? w : 0.0f;
+    X[2 * C + s] = un ? d.x * w : 0.0f;
+    X[3 * C + s] = un ? d.y * w : 0.0f;
+    X[4 * C + s] = un ? d.z * w : 0.0f;
+  } else if constexpr (kind == kPassDistance) {
+    // rows k: wts * rcp(distance); rows Kp + k: wts
+    const VMMState &vm = S.vmm;
+    const float sd = valid ? rcp_avx2_tab(in.x, S.rcpTab) : 0.0f;
+#pragma unroll
+    for (int k = 0; k < kMaxK; ++k) {
+      if (k < Kp) {
+        float wts = 0.0f;
+        if (valid) {
+          float a = T.t[k] * T.inv;
+          wts = (w * a) * div_rcp(a * T.pdf, vm.w[k], S.lobeWInv[k]);
+        }
+        B[k * R + s] = wts * sd;
+        B[(Kp + k) * R + s] = wts;
+      }
+    }
+  } else {
+    // rows r Kp + k: a, a w, (a w)(lx lx), (a w)(ly ly), (a w)(lx ly), chi;
+    // then the validity per sample
+    const float spdfv = in.x;
+    const float value = w * spdfv;
+    const float mcEst = S.mcEstimate;
+    // the three divisors are per sample: one reciprocal each, then Markstein
+    const float den1 = mcEst * T.pdf, den2 = ((mcEst * mcEst) * T.pdf) * T.pdf;
+    const float y1 = rcp_for_div(den1), y2 = rcp_for_div(den2), y3 = rcp_for_div(spdfv);
+#pragma unroll
+    for (int k = 0; k < kMaxK; ++k) {
+      if (k < Kp) {
+        float a = 0.0f, aw = 0.0f, cxx = 0.0f, cyy = 0.0f, cxy = 0.0f, chi = 0.0f;
+        if (valid) {
+          a = T.t[k] * T.inv;
+          float vmf = a * T.pdf;
+          float pvp = vmf * value;
+          pvp = div_rcp(pvp, den1, y1);
+          chi = (value * value) * vmf;
+          chi = div_rcp(chi, den2, y2);
+          chi -= 2.0f * pvp;
+          chi += vmf;
+          chi = div_rcp(chi, spdfv, y3);
+          chi = a > 0.0f ? chi : 0.0f;
+          V3 ld = xfm(S.invFrame[k], d);
+          aw = a * w;
+          cxx = aw * (ld.x * ld.x);
+          cyy = aw * (ld.y * ld.y);
+          cxy = aw * (ld.x * ld.y);
+        }
+        B[k * R + s] = a;
+        B[(Kp + k) * R + s] = aw;
+        B[(2 * Kp + k) * R + s] = cxx;
+        B[(3 * Kp + k) * R + s] = cyy;
+        B[(4 * Kp + k) * R + s] = cxy;
+        B[(5 * Kp + k) * R + s] = chi;
+      }
+    }
+    B[6 * Kp * R + s] = valid ? 1.0f : 0.0f;
+  }
+}
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+
+// Sum of one row (the terms of one accumulator) in sample order; loads run a
+// group of 4 samples ahead of the additions.
+__device__ __forceinline__ void row_chain(const float *row, int n4, float &acc) {
+  float4 v = ld4(row);
+  for (int s = 0; s < n4; s += 4) {
+    const int sn = s + 4 < n4 ? s + 4 : s;
+    const float4 v1 = ld4(row + sn);
+    acc += v.x;
+    acc += v.y;
+    acc += v.z;
+    acc += v.w;
+    v = v1;
+  }
+}
+
+// E-step (WEMFactory.h:847-892): lanes c < 4 Kp sum row c ((d_q a_k) w for
+// q = c / Kp < 3, a_k w for q = 3), then the log-likelihood and the four
+// unassigned-sample sums.
+__device__ __forceinline__ void estep_chain(const float *B, const PassShape &sh, int c, int Kp, int n4, float &acc) {
+  if (c < 4 * Kp) {
+    row_chain(B + c * sh.R, n4, acc);
+  } else {
+    const int e = c - 4 * Kp;
+    if (e < 5) row_chain(B + 4 * Kp * sh.R + e * sh.C, n4, acc);
+  }
+}
+
+// Distance pass (WEMFactory.h:1199-1326): lanes c < Kp sum wts * rcp(distance),
+// lanes Kp <= c < 2 Kp sum wts.
+__device__ __forceinline__ void distance_chain(const float *B, const PassShape &sh, int c, int Kp, int n4,
+                                               float &acc) {
+  if (c < 2 * Kp) row_chain(B + c * sh.R, n4, acc);
+}
+
+// One step of chi2 += (x - chi2) / n with y = RN(1/n); `bad` records a step
+// outside the range where div_rcp's FMA steps are exact.
+__device__ __forceinline__ float chi_step(float acc, float x, float n, float y, float v, bool &bad) {
+  const float num = x - acc;
+  const float q0 = num * y;
+  const float r = fmaf_(-q0, n, num);
+  const float q = fmaf_(r, y, q0);
+  const float an = fabsf(num), aq = fabsf(q);
+  bad |= (v != 0.0f) && !(an >= 1e-30f && an <= 1e30f && aq >= 1e-30f && aq <= 1e30f) && (num != 0.0f);
+  return v != 0.0f ? acc + q : acc;
+}
+
+// Split-statistics pass (Splitter.h:439-523).  Lanes c < 5 Kp sum row c
+// (r = c / Kp: sumAssignedSamples a, sumWeights a w, then the 2D covariance
+// sums (a w)(lx lx), (a w)(ly ly), (a w)(lx ly)).  Chi-square lanes start at
+// the next warp: the running mean chi2 += (chi - chi2) / n over the valid
+// samples.
+__device__ __forceinline__ int split_chi_base(int Kp) { return ((5 * Kp + 31) / 32) * 32; }
+__device__ __forceinline__ void split_chain(const float *B, const PassShape &sh, int c, int Kp, int n4, float &acc,
+                                            float &accN) {
+  const int R = sh.R;
+  const int chiBase = split_chi_base(Kp);
+  const float *Vr = B + 6 * Kp * R;
+  if (c < 5 * Kp) {
+    row_chain(B + c * R, n4, acc);
+  } else if (c >= chiBase && c < chiBase + Kp) {
+    // the counts and their reciprocals do not depend on chi2: only the
+    // subtract, three FMA-unit operations and the add stay on the chain
+    const int k = c - chiBase;
+    const float *cr = B + (5 * Kp + k) * R;
+    float4 x = ld4(cr), v = ld4(Vr);
+    for (int s = 0; s < n4; s += 4) {
+      const int sn = s + 4 < n4 ? s + 4 : s;
+      const float4 x1 = ld4(cr + sn), v1 = ld4(Vr + sn);
+      const float n1 = accN + v.x, n2 = n1 + v.y, n3 = n2 + v.z, n4v = n3 + v.w;
+      const float y1 = __frcp_rn(n1), y2 = __frcp_rn(n2), y3 = __frcp_rn(n3), y4 = __frcp_rn(n4v);
+      const float acc0 = acc;
+      bool bad = false;
+      acc = chi_step(acc, x.x, n1, y1, v.x, bad);
+      acc = chi_step(acc, x.y, n2, y2, v.y, bad);
+      acc = chi_step(acc, x.z, n3, y3, v.z, bad);
+      acc = chi_step(acc, x.w, n4v, y4, v.w, bad);
+      if (bad) {  // out of the exact range: redo the group with the division
+        acc = acc0;
+        if (v.x != 0.0f) acc += (x.x - acc) / n1;
+        if (v.y != 0.0f) acc += (x.y - acc) / n2;
+        if (v.z != 0.0f) acc += (x.z - acc) / n3;
+        if (v.w != 0.0f) acc += (x.w - acc) / n4v;
+      }
+      accN = n4v;
+      x = x1;
+      v = v1;
+    }
+  }
+}
+
+// Runs one pass over the leaf's samples.  `acc`/`accN` are the consumer's
+// accumulators (initialised by the caller); the producer side is driven here.
+template <PassKind kind>
+__device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const PassShape &sh, int cnt, float &acc,
+                                      float &accN) {
+  const int tid = threadIdx.x;
+  const int Kp = cnt * kLanes;
+  const int C = sh.C;
+  const uint32_t numChunks = (L.count + C - 1) / C;
+  const bool producer = tid < C;
+  const bool consumer = tid >= sh.P;
+  const int c = tid - sh.P;
+  SampleIn next;
+  if (producer) next = load_sample<kind>(L, uint32_t(tid));
+  long long cycP = 0, cycC = 0;
+  for (uint32_t it = 0; it <= numChunks; ++it) {
+    if (producer && it < numChunks) {
+      const long long t0 = clock64();
+      const SampleIn cur = next;
+      if (it + 1 < numChunks) next = load_sample<kind>(L, (it + 1) * C + tid);
+      produce<kind>(S, sh, cnt, Kp, tid, cur, S.pbuf + (it & 1) * sh.stage);
+      cycP += clock64() - t0;
+    }
+    if (consumer && it >= 1) {
+      const long long t0 = clock64();
+      const uint32_t prev = it - 1;
+      const int n = int(min(uint32_t(C), L.count - prev * C));
+      const int n4 = (n + 3) & ~3;
+      const float *B = S.pbuf + (prev & 1) * sh.stage;
+      if constexpr (kind == kPassEStep) estep_chain(B, sh, c, Kp, n4, acc);
+      else if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
+      else split_chain(B, sh, c, Kp, n4, acc, accN);
+      cycC += clock64() - t0;
+    }
+    __syncthreads();
+  }
+  const int probe = kind == kPassSplit ? split_chi_base(Kp) : 0;
+  if (tid == 0) {
+    if (kind == kPassSplit) S.prof.cycProdS += uint64_t(cycP);
+    else if (kind == kPassEStep) S.prof.cycProdE += uint64_t(cycP);
+  }
+  if (c == probe) {
+    if (kind == kPassSplit) S.prof.cycConsS += uint64_t(cycC);
+    else if (kind == kPassEStep) S.prof.cycConsE += uint64_t(cycC);
+  }
+}
+
+// E-step over all samples into S.cur, S.ll and S.un.
 __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
   const int tid = threadIdx.x;
+  const int cnt = vec_count(int(S.vmm.K));
+  const int Kp = cnt * kLanes;
+  const PassShape sh = pass_shape<kPassEStep>(Kp);
   if (tid == 0) {
     S.un = Unassigned{0.f, 0.f, 0.f, 0.f};
     suff_clear(S.cur, S.vmm.K);
     S.cur.K = S.vmm.K;
     S.cur.numSamples = float(L.count);
   }
+  pack_lobes(S, Kp);
   __syncthreads();
-  const int cnt = vec_count(int(S.vmm.K));
-  const int q = tid / kMaxK, k = tid % kMaxK;
-  const bool lobeChain = tid < 4 * kMaxK && k < cnt * kLanes;
-  float acc = 0.0f;
-  for (uint32_t base = 0; base < L.count; base += kChunk) {
-    int nIn = int(min(uint32_t(kChunk), L.count - base));
-    phase_a(S, L, base, nIn, kPassEStep);
-    if (lobeChain) {
-      for (int s = 0; s < nIn; ++s) {
-        if (!S.svalid[s]) continue;
-        float a = S.term[0][k][s], w = S.sw[s];
-        if (q == 0) acc += (S.sdx[s] * a) * w;
-        else if (q == 1) acc += (S.sdy[s] * a) * w;
-        else if (q == 2) acc += (S.sdz[s] * a) * w;
-        else acc += a * w;
-      }
-    } else if (tid == 128) {
-      for (int s = 0; s < nIn; ++s)
-        if (S.svalid[s]) acc += S.lterm[s];
-    } else if (tid >= 129 && tid <= 132) {
-      for (int s = 0; s < nIn; ++s) {
-        if (S.svalid[s]) continue;
-        float w = S.sw[s];
-        if (tid == 129) acc += w;
-        else if (tid == 130) acc = acc + (S.sdx[s] * w);
-        else if (tid == 131) acc = acc + (S.sdy[s] * w);
-        else acc = acc + (S.sdz[s] * w);
-      }
+  float acc = 0.0f, accN = 0.0f;
+  run_pass<kPassEStep>(S, L, sh, cnt, acc, accN);
+  const int c = tid - sh.P;
+  if (c >= 0) {
+    if (c < 4 * Kp) {
+      const int q = c / Kp, k = c % Kp;
+      if (q == 0) S.cur.dx[k] = acc;
+      else if (q == 1) S.cur.dy[k] = acc;
+      else if (q == 2) S.cur.dz[k] = acc;
+      else S.cur.w[k] = acc;
+    } else {
+      const int e = c - 4 * Kp;
+      if (e == 0) S.ll = acc;
+      else if (e == 1) S.un.sw = acc;
+      else if (e == 2) S.un.dx = acc;
+      else if (e == 3) S.un.dy = acc;
+      else if (e == 4) S.un.dz = acc;
     }
-    __syncthreads();
-  }
-  if (lobeChain) {
-    if (q == 0) S.cur.dx[k] = acc;
-    else if (q == 1) S.cur.dy[k] = acc;
-    else if (q == 2) S.cur.dz[k] = acc;
-    else S.cur.w[k] = acc;
-  } else if (tid == 128) {
-    S.ll = acc;
-  } else if (tid == 129) {
-    S.un.sw = acc;
-  } else if (tid == 130) {
-    S.un.dx = acc;
-  } else if (tid == 131) {
-    S.un.dy = acc;
-  } else if (tid == 132) {
-    S.un.dz = acc;
   }
   __syncthreads();
 }
@@ -649,26 +923,22 @@ __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
 __device__ void pass_distances(EmShared &S, const LeafSamples &L, bool init) {
   const int tid = threadIdx.x;
   const int cnt = vec_count(int(S.vmm.K));
-  const int q = tid / kMaxK, k = tid % kMaxK;
-  const bool chain = tid < 2 * kMaxK && k < cnt * kLanes;
-  float acc = 0.0f;
-  for (uint32_t base = 0; base < L.count; base += kChunk) {
-    int nIn = int(min(uint32_t(kChunk), L.count - base));
-    phase_a(S, L, base, nIn, kPassDistance);
-    if (chain)
-      for (int s = 0; s < nIn; ++s)
-        if (S.svalid[s]) acc += S.term[q == 0 ? 1 : 0][k][s];  // q0: distances, q1: weights
-    __syncthreads();
-  }
-  // exchange: bd in term[0][k][0], bw in term[1][k][0]
-  if (chain) S.term[q][k][0] = acc;
+  const int Kp = cnt * kLanes;
+  const PassShape sh = pass_shape<kPassDistance>(Kp);
+  pack_lobes(S, Kp);
+  __syncthreads();
+  float acc = 0.0f, accN = 0.0f;
+  run_pass<kPassDistance>(S, L, sh, cnt, acc, accN);
+  // exchange: bd in xch[0][k], bw in xch[1][k]
+  const int c = tid - sh.P;
+  if (c >= 0 && c < 2 * Kp) S.xch[c / Kp][c % Kp] = acc;
   __syncthreads();
   if (tid == 0) {
     VMMState &v = S.vmm;
     SuffState &s = S.suff;
-    int c = vec_count(int(v.K)), rem = int(v.K % kLanes);
-    for (int kk = 0; kk < c * kLanes; ++kk) {
-      float bd = S.term[0][kk][0], bw = S.term[1][kk][0];
+    int cc = vec_count(int(v.K)), rem = int(v.K % kLanes);
+    for (int kk = 0; kk < cc * kLanes; ++kk) {
+      float bd = S.xch[0][kk], bw = S.xch[1][kk];
       if (init) {
         s.dw[kk] = bw;
         v.dist[kk] = s.dw[kk] / bd;
@@ -680,7 +950,7 @@ __device__ void pass_distances(EmShared &S, const LeafSamples &L, bool init) {
       }
     }
     if (rem > 0)
-      for (int i = rem; i < kLanes; ++i) { v.dist[(c - 1) * kLanes + i] = 0.0f; s.dw[(c - 1) * kLanes + i] = 0.0f; }
+      for (int i = rem; i < kLanes; ++i) { v.dist[(cc - 1) * kLanes + i] = 0.0f; s.dw[(cc - 1) * kLanes + i] = 0.0f; }
   }
   __syncthreads();
 }
@@ -689,46 +959,32 @@ __device__ void pass_distances(EmShared &S, const LeafSamples &L, bool init) {
 __device__ void pass_split_stats(EmShared &S, const LeafSamples &L, SplitState &sp) {
   const int tid = threadIdx.x;
   const int cnt = vec_count(int(sp.K));
-  if (tid < cnt * kLanes) S.invFrame[tid] = inverse_of(frame_of(mk(S.vmm.mx[tid], S.vmm.my[tid], S.vmm.mz[tid]), true));
+  const int Kp = cnt * kLanes;
+  const PassShape sh = pass_shape<kPassSplit>(Kp);
+  if (tid < Kp) S.invFrame[tid] = inverse_of(frame_of(mk(S.vmm.mx[tid], S.vmm.my[tid], S.vmm.mz[tid]), true));
+  pack_lobes(S, Kp);
   __syncthreads();
-  const int q = tid / kMaxK, k = tid % kMaxK;
-  const bool chain = tid < 6 * kMaxK && k < cnt * kLanes;
+  const int c = tid - sh.P;
+  const int chiBase = split_chi_base(Kp);
   float acc = 0.0f, accN = 0.0f;
-  if (chain) {
-    switch (q) {
-      case 0: acc = sp.sa[k]; break;
-      case 1: acc = sp.chi2[k]; accN = sp.n[k]; break;
-      case 2: acc = sp.sw[k]; break;
-      case 3: acc = sp.cx[k]; break;
-      case 4: acc = sp.cy[k]; break;
-      default: acc = sp.cz[k]; break;
-    }
+  if (c >= 0 && c < 5 * Kp) {
+    const int r = c / Kp, k = c % Kp;
+    acc = r == 0 ? sp.sa[k] : r == 1 ? sp.sw[k] : r == 2 ? sp.cx[k] : r == 3 ? sp.cy[k] : sp.cz[k];
+  } else if (c >= chiBase && c < chiBase + Kp) {
+    acc = sp.chi2[c - chiBase];
+    accN = sp.n[c - chiBase];
   }
-  for (uint32_t base = 0; base < L.count; base += kChunk) {
-    int nIn = int(min(uint32_t(kChunk), L.count - base));
-    phase_a(S, L, base, nIn, kPassSplit);
-    if (chain) {
-      for (int s = 0; s < nIn; ++s) {
-        if (!S.svalid[s]) continue;
-        if (q == 1) {
-          accN += 1.0f;
-          acc += (S.term[1][k][s] - acc) / accN;
-        } else {
-          acc += S.term[q == 0 ? 0 : q][k][s];
-        }
-      }
-    }
-    __syncthreads();
-  }
-  if (chain) {
-    switch (q) {
-      case 0: sp.sa[k] = acc; break;
-      case 1: sp.chi2[k] = acc; sp.n[k] = accN; break;
-      case 2: sp.sw[k] = acc; break;
-      case 3: sp.cx[k] = acc; break;
-      case 4: sp.cy[k] = acc; break;
-      default: sp.cz[k] = acc; break;
-    }
+  run_pass<kPassSplit>(S, L, sh, cnt, acc, accN);
+  if (c >= 0 && c < 5 * Kp) {
+    const int r = c / Kp, k = c % Kp;
+    if (r == 0) sp.sa[k] = acc;
+    else if (r == 1) sp.sw[k] = acc;
+    else if (r == 2) sp.cx[k] = acc;
+    else if (r == 3) sp.cy[k] = acc;
+    else sp.cz[k] = acc;
+  } else if (c >= chiBase && c < chiBase + Kp) {
+    sp.chi2[c - chiBase] = acc;
+    sp.n[c - chiBase] = accN;
   }
   __syncthreads();
 }
@@ -748,8 +1004,12 @@ __device__ int em_loop(EmShared &S, const LeafSamples &L, SuffState &prev, bool 
   }
   __syncthreads();
   while (S.loopFlag) {
+    PGL_PROF_BEGIN(t0)
     pass_estep(S, L);
+    PGL_PROF_END(t0, cycEstep)
+    PGL_PROF_BEGIN(t1)
     if (tid == 0) {
+      S.prof.estepPasses++;
       if (S.un.sw > 0.0f && S.cur.K < kMaxK) {  // handleUnassignedSampleStats (WEMFactory.h:731-748)
         int t = int(S.cur.K);
         S.cur.K++;
@@ -771,6 +1031,7 @@ __device__ int em_loop(EmShared &S, const LeafSamples &L, SuffState &prev, bool 
       }
       S.loopFlag = (!converged && uint32_t(S.iterations) < cfg.maxIter) ? 1 : 0;
     }
+    PGL_PROF_END(t1, cycMstep)
     __syncthreads();
   }
   if (tid == 0) suff_add(prev, S.cur);
@@ -855,7 +1116,12 @@ __device__ void recursive_splitting(EmShared &S, const LeafSamples &L, const Fie
       split_clear(S.lsplit, S.vmm.K);
     }
     __syncthreads();
-    pass_split_stats(S, L, S.lsplit);
+    {
+      PGL_PROF_BEGIN(tp0)
+      if (threadIdx.x == 0) S.prof.splitPasses++;
+      pass_split_stats(S, L, S.lsplit);
+      PGL_PROF_END(tp0, cycSplit)
+    }
     if (tid == 0) {
       sort_candidates(S, S.lsplit);
       for (int k = 0; k < kMaxK; ++k) S.mask[k] = 0;
@@ -894,18 +1160,35 @@ __device__ void asm_fit(EmShared &S, const LeafSamples &L, const FieldConfig &cf
   }
   __syncthreads();
   S.report.emIterations += em_loop(S, L, S.suff, false, cfg);
-  pass_distances(S, L, true);
+  {
+    PGL_PROF_BEGIN(tp0)
+    if (threadIdx.x == 0) S.prof.distPasses++;
+    pass_distances(S, L, true);
+    PGL_PROF_END(tp0, cycDist)
+  }
   if (cfg.useSplitMerge) {
     if (tid == 0) S.mcEstimate = S.suff.sumWeights / S.suff.numSamples;
     __syncthreads();
     recursive_splitting(S, L, cfg);
     if (tid == 0) split_clear(S.split, S.vmm.K);
     __syncthreads();
-    pass_split_stats(S, L, S.split);
+    {
+      PGL_PROF_BEGIN(tp1)
+      if (threadIdx.x == 0) S.prof.splitPasses++;
+      pass_split_stats(S, L, S.split);
+      PGL_PROF_END(tp1, cycSplit)
+    }
+    PGL_PROF_BEGIN(tm)
     int m = perform_merging(S, cfg);
+    PGL_PROF_END(tm, cycMerge)
     if (tid == 0) S.report.merges += uint32_t(m);
   }
-  pass_distances(S, L, true);
+  {
+    PGL_PROF_BEGIN(tp1)
+    if (threadIdx.x == 0) S.prof.distPasses++;
+    pass_distances(S, L, true);
+    PGL_PROF_END(tp1, cycDist)
+  }
 }
 
 // Update (later frames) of one leaf (ASMF.h:352-462)
@@ -926,7 +1209,12 @@ __device__ void asm_update(EmShared &S, const LeafSamples &L, const FieldConfig 
       afterMerge += L.count;
     }
     __syncthreads();
-    pass_split_stats(S, L, S.split);
+    {
+      PGL_PROF_BEGIN(tp2)
+      if (threadIdx.x == 0) S.prof.splitPasses++;
+      pass_split_stats(S, L, S.split);
+      PGL_PROF_END(tp2, cycSplit)
+    }
     if (afterSplit >= uint64_t(int64_t(cfg.minSplit))) {
       if (tid == 0) {
         for (int k = 0; k < kMaxK; ++k) S.mask[k] = 0;
@@ -960,12 +1248,19 @@ __device__ void asm_update(EmShared &S, const LeafSamples &L, const FieldConfig 
       __syncthreads();
     }
     if (afterMerge >= uint64_t(int64_t(cfg.minMerge))) {
+      PGL_PROF_BEGIN(tm)
       int m = perform_merging(S, cfg);
+      PGL_PROF_END(tm, cycMerge)
       if (tid == 0) { S.report.merges += uint32_t(m); afterMerge = 0; }
       __syncthreads();
     }
   }
-  pass_distances(S, L, false);
+  {
+    PGL_PROF_BEGIN(tp2)
+    if (threadIdx.x == 0) S.prof.distPasses++;
+    pass_distances(S, L, false);
+    PGL_PROF_END(tp2, cycDist)
+  }
 }
 
 // Reprojection of a leaf's samples to the region's sample mean
@@ -994,11 +1289,12 @@ __device__ void reproject_leaf(const LeafTask &t, float4 *pd, float4 *dirw, floa
 __global__ void __launch_bounds__(kEmThreads)
 em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
                float4 *dirw, const float *pdf, float *dist, FieldConfig cfg, const float *uniformDirs,
-               LeafReport *reports) {
+               LeafReport *reports, LeafProfile *profiles) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EmShared &S = *reinterpret_cast<EmShared *>(smem_raw);
   __shared__ uint32_t taskId;
   __shared__ uint64_t afterSplit, afterMerge;
+  for (int i = threadIdx.x; i < 2048; i += blockDim.x) S.rcpTab[i] = rcp_seed(uint32_t(i));
   for (;;) {
     if (threadIdx.x == 0) taskId = atomicAdd(queue, 1u);
     __syncthreads();
@@ -1017,7 +1313,9 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
       dst = reinterpret_cast<uint32_t *>(&S.split);
       for (int i = threadIdx.x; i < int(sizeof(SplitState) / 4); i += blockDim.x) dst[i] = src[i];
     }
+    const long long leafStart = clock64();
     if (threadIdx.x == 0) {
+      S.prof = LeafProfile{t.count, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
       afterSplit = R.afterSplit;
       afterMerge = R.afterMerge;
       S.report = LeafReport{0, 0, 0, 0};
@@ -1073,6 +1371,10 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
       R.valid = valid;
       S.report.K = S.vmm.K;
       if (reports) reports[taskId] = S.report;
+      if (profiles) {
+        S.prof.cycTotal = uint64_t(clock64() - leafStart);
+        profiles[taskId] = S.prof;
+      }
     }
     __syncthreads();
   }
@@ -1084,7 +1386,7 @@ size_t em_shared_bytes() { return sizeof(EmShared); }
 
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
                       float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
-                      LeafReport *reports, int numBlocks, cudaStream_t stream) {
+                      LeafReport *reports, LeafProfile *profiles, int numBlocks, cudaStream_t stream) {
   static bool attrSet = false;
   const size_t smem = sizeof(EmShared);
   if (!attrSet) {
@@ -1092,8 +1394,9 @@ cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *qu
     if (e != cudaSuccess) return e;
     attrSet = true;
   }
+  count_launch();
   em_leaf_kernel<<<numBlocks, kEmThreads, smem, stream>>>(tasks, numTasks, queue, regions, pd, dirw, pdf, dist, cfg,
-                                                          uniformDirs, reports);
+                                                          uniformDirs, reports, profiles);
   return cudaGetLastError();
 }
 

@@ -57,6 +57,7 @@ template struct DevArray<PGLSampleRecord>;
 template struct DevArray<KdJob>;
 template struct DevArray<LeafTask>;
 template struct DevArray<LeafReport>;
+template struct DevArray<LeafProfile>;
 template struct DevArray<IStatsAcc>;
 template struct DevArray<QueryIn>;
 template struct DevArray<QueryOut>;
@@ -163,6 +164,11 @@ void SampleSide::reserve(uint64_t count) {
 }
 
 void Storage::add(const PGLSampleRecord *s, size_t n) {
+  if (n >= (1u << 16)) {  // large batches go to the device straight from the caller's buffer
+    flush();
+    ingest(s, n);
+    return;
+  }
   pending_.insert(pending_.end(), s, s + n);
   if (pending_.size() >= (1u << 16)) flush();
 }
@@ -175,23 +181,41 @@ void Storage::reserve(size_t ns, size_t nv) {
 
 void Storage::flush() {
   if (pending_.empty()) return;
+  std::vector<PGLSampleRecord> p;
+  p.swap(pending_);
+  ingest(p.data(), p.size());
+}
+void Storage::flushIfPending() {
+  if (!pending_.empty()) flush();
+}
+
+// Copies n host records to the device and splits them into the surface and
+// volume arrays.  Returns after the copy has completed (ingest_samples
+// synchronises), so the caller may reuse its buffer.
+void Storage::ingest(const PGLSampleRecord *src, size_t count) {
   Context &c = Context::get();
-  const uint32_t n = uint32_t(pending_.size());
+  const uint32_t n = uint32_t(count);
   staging_.reserve(n);
-  check(cudaMemcpyAsync(staging_.p, pending_.data(), size_t(n) * sizeof(PGLSampleRecord), cudaMemcpyHostToDevice,
-                        c.stream),
+  check(cudaMemcpyAsync(staging_.p, src, size_t(n) * sizeof(PGLSampleRecord), cudaMemcpyHostToDevice, c.stream),
         "H2D samples");
   lastH2DBytes += uint64_t(n) * sizeof(PGLSampleRecord);
+  ingestDevice(staging_.p, count);
+}
+
+// Splits n device-resident records into the surface and volume arrays.
+void Storage::ingestDevice(const PGLSampleRecord *dsrc, size_t count) {
+  flushIfPending();
+  Context &c = Context::get();
+  const uint32_t n = uint32_t(count);
   // worst case: every sample in one class
   surf.reserve(surf.n + n);
   vol.reserve(vol.n + n);
   SoAView sv{surf.P.p, surf.D.p, surf.pdf.p, surf.flags.p, surf.n};
   SoAView vv{vol.P.p, vol.D.p, vol.pdf.p, vol.flags.p, vol.n};
   uint32_t numVol = 0;
-  check(ingest_samples(staging_.p, n, scratch_, sv, vv, &numVol, c.stream), "ingest");
+  check(ingest_samples(dsrc, n, scratch_, sv, vv, &numVol, c.stream), "ingest");
   vol.n += numVol;
   surf.n += n - numVol;
-  pending_.clear();
 }
 
 std::vector<PGLSampleRecord> Storage::download(bool volume) {
@@ -444,7 +468,13 @@ void SubField::renumber(uint32_t oldNodes, uint32_t oldRegions) {
 void SubField::update(SampleSide &in) {
   Context &c = Context::get();
   const uint32_t n = uint32_t(in.n);
-  if (n == 0) return;
+  if (n == 0) {
+    timings = UpdateTimings{};
+    lastReports.clear();
+    lastProfiles.clear();
+    lastReportRegion.clear();
+    return;
+  }
   cudaEvent_t ev[5];
   for (auto &e : ev) check(cudaEventCreate(&e), "event");
   check(cudaEventRecord(ev[0], c.stream), "event");
@@ -562,29 +592,36 @@ void SubField::update(SampleSide &in) {
   std::stable_sort(tasks.begin(), tasks.end(), [](const LeafTask &a, const LeafTask &b) { return a.count > b.count; });
   tasks_.reserve(R);
   reports_.reserve(R);
+  profiles_.reserve(R);
   queue_.reserve(1);
   check(cudaMemcpyAsync(tasks_.p, tasks.data(), R * sizeof(LeafTask), cudaMemcpyHostToDevice, c.stream), "tasks");
   check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), c.stream), "queue");
   ensureUniformDirs();
+  check(cudaEventRecord(ev[4], c.stream), "event");
   if (cfg.fitRegions) {
-    int blocks = std::min<int>(int(R), c.numSMs * 2);
-    check(launch_em(tasks_.p, R, queue_.p, dRegions.p, sP_.p, sD_.p, sPdf_.p, dist_.p, cfg, dUniformDirs.p, reports_.p,
+    int blocks = std::min<int>(int(R), c.numSMs);  // one persistent block per SM (shared memory bound)
+    check(launch_em(tasks_.p, R, queue_.p, dRegions.p, sP_.p, sD_.p, sPdf_.p, dist_.p, cfg, dUniformDirs.p, reports_.p, profiles_.p,
                     std::max(blocks, 1), c.stream),
           "em");
   }
   check(cudaEventRecord(ev[3], c.stream), "event");
   lastReports.resize(R);
+  lastProfiles.resize(R);
+  check(cudaMemcpyAsync(lastProfiles.data(), profiles_.p, R * sizeof(LeafProfile), cudaMemcpyDeviceToHost, c.stream),
+        "profiles");
   check(cudaMemcpyAsync(lastReports.data(), reports_.p, R * sizeof(LeafReport), cudaMemcpyDeviceToHost, c.stream),
         "reports");
   check(cudaStreamSynchronize(c.stream), "update");
   lastReportRegion.resize(R);
   for (uint32_t k = 0; k < R; ++k) lastReportRegion[k] = tasks[k].region;
-  float ms[4];
+  float ms[6];
   check(cudaEventElapsedTime(&ms[0], ev[0], ev[3]), "timing");
   check(cudaEventElapsedTime(&ms[1], ev[0], ev[1]), "timing");
   check(cudaEventElapsedTime(&ms[2], ev[1], ev[2]), "timing");
   check(cudaEventElapsedTime(&ms[3], ev[2], ev[3]), "timing");
-  timings = UpdateTimings{ms[0], ms[1], ms[2], ms[3]};
+  check(cudaEventElapsedTime(&ms[4], ev[2], ev[4]), "timing");
+  check(cudaEventElapsedTime(&ms[5], ev[4], ev[3]), "timing");
+  timings = UpdateTimings{ms[0], ms[1], ms[2], ms[3], ms[4], ms[5], uint64_t(n), R};
   for (auto &e : ev) cudaEventDestroy(e);
   for (RegionHost &h : regions) {
     h.splitFlag = false;

@@ -55,6 +55,9 @@ class Storage {
   SampleSide surf, vol;
   void add(const PGLSampleRecord *s, size_t n);
   void flush();
+  void ingest(const PGLSampleRecord *src, size_t count);
+  void ingestDevice(const PGLSampleRecord *dsrc, size_t count);
+  void flushIfPending();
   void reserve(size_t ns, size_t nv);
   void clearSurface() { flush(); surf.n = 0; }
   void clearVolume() { flush(); vol.n = 0; }
@@ -81,6 +84,8 @@ struct RegionHost {
 // Per-phase timings of the last Update (FieldStatistics, Field.h:153-216).
 struct UpdateTimings {
   float total = 0, copy = 0, spatial = 0, directional = 0;
+  float gather = 0, emKernel = 0;  // the two parts of `directional`
+  uint64_t samples = 0, regions = 0;
 };
 
 class SubField {
@@ -95,6 +100,7 @@ class SubField {
   std::vector<RegionHost> regions;
   UpdateTimings timings;
   std::vector<LeafReport> lastReports;
+  std::vector<LeafProfile> lastProfiles;
   std::vector<uint32_t> lastReportRegion;
 
   DevArray<RegionDir> dRegions;
@@ -122,6 +128,7 @@ class SubField {
   DevArray<IStatsAcc> acc_;
   DevArray<LeafTask> tasks_;
   DevArray<LeafReport> reports_;
+  DevArray<LeafProfile> profiles_;
   DevArray<float4> means_;
   DevArray<unsigned int> queue_;
   DevArray<uint32_t> bounds6_;

@@ -24,6 +24,11 @@ struct SoAView {
   uint64_t base;   // append offset
 };
 
+// Number of this library's own kernels launched so far in the process (CUB's
+// scan and sort kernels not included).
+unsigned long long kernel_launches();
+void count_launch();
+
 cudaError_t em_upload_tables();
 cudaError_t spatial_upload_tables();
 cudaError_t query_upload_tables();
@@ -55,7 +60,7 @@ cudaError_t build_knn(const float4 *means, uint32_t R, Neighbours *out, cudaStre
 size_t em_shared_bytes();
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
                       float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
-                      LeafReport *reports, int numBlocks, cudaStream_t stream);
+                      LeafReport *reports, LeafProfile *profiles, int numBlocks, cudaStream_t stream);
 
 cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s);
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,

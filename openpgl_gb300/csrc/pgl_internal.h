@@ -90,6 +90,16 @@ constexpr uint32_t kTaskFit = 1u, kTaskDecay = 2u;
 struct LeafReport {
   uint32_t emIterations, splits, merges, K;
 };
+// Where the EM kernel spent its time on one region: passes over the leaf's
+// samples by kind and SM clock cycles (clock64 of thread 0) per phase.
+struct LeafProfile {
+  uint32_t count;                      // samples of the leaf
+  uint32_t estepPasses, distPasses, splitPasses;
+  uint64_t cycEstep, cycDist, cycSplit, cycMerge, cycMstep, cycTotal;
+  // inside the passes: cycles thread 0 spent producing, and cycles of the
+  // slowest consumer role (E-step: lobe chain 0; split: chi-square chain 0)
+  uint64_t cycProdE, cycConsE, cycProdS, cycConsS;
+};
 
 // Integer position statistics of one kd child (IntegerSampleStatistics).
 struct IStatsAcc {

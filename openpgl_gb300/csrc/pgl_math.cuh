@@ -190,6 +190,27 @@ PGL_HD void lib_sincosf(float x, float *s, float *c) {
 #endif
 }
 
+// a / b, correctly rounded, from y = RN(1/b) (Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990): with y within half an ulp of 1/b and q0 = RN(a y)
+// within one ulp of a/b, the residual r = a - b q0 is exact under FMA and
+// RN(q0 + r y) = RN(a / b).  The theorem assumes that nothing underflows or
+// overflows, so operands and quotient outside [1e-30, 1e30] in magnitude
+// (zeros, infinities and NaNs included) take the division instead.
+PGL_HD float div_rcp(float a, float b, float y) {
+  float q0 = a * y;
+  float r = fmaf_(-q0, b, a);
+  float q = fmaf_(r, y, q0);
+  const float aa = a < 0.0f ? -a : a, aq = q < 0.0f ? -q : q;
+  if (!(aa >= 1e-30f && aa <= 1e30f && aq >= 1e-30f && aq <= 1e30f)) q = a / b;
+  return q;
+}
+// y = RN(1/b) for 1e-30 <= |b| <= 1e30, else 0 (div_rcp then divides).
+PGL_HD float rcp_for_div(float b) {
+  const float ab = b < 0.0f ? -b : b;
+  return (ab >= 1e-30f && ab <= 1e30f) ? 1.0f / b : 0.0f;
+}
+
 // fastapprox::exp
 PGL_HD float fexp(float v) {
   const float ln2Part1 = float(0.6931457519), ln2Part2 = float(1.4286067653e-6);

@@ -264,23 +264,28 @@ cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out,
   const unsigned threads = 256;
   const uint64_t warps = n;
   unsigned blocks = unsigned((warps * 32 + threads - 1) / threads);
+  count_launch();
   query_kernel<<<blocks, threads, 0, s>>>(p, in, out, n);
   return cudaGetLastError();
 }
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,
                             cudaStream_t s) {
+  count_launch();
   ssd_init_kernel<<<1, 32, 0, s>>>(f, px, py, pz, s1d, st, res);
   return cudaGetLastError();
 }
 cudaError_t launch_ssd_cosine(SSDState *st, float nx, float ny, float nz, float ck, float cn, cudaStream_t s) {
+  count_launch();
   ssd_cosine_kernel<<<1, 32, 0, s>>>(st, nx, ny, nz, ck, cn);
   return cudaGetLastError();
 }
 cudaError_t launch_ssd_sample(const SSDState *st, float ux, float uy, int withPdf, SSDResult *res, cudaStream_t s) {
+  count_launch();
   ssd_sample_kernel<<<1, 32, 0, s>>>(st, ux, uy, withPdf, res);
   return cudaGetLastError();
 }
 cudaError_t launch_ssd_pdf(const SSDState *st, float dx, float dy, float dz, int li, SSDResult *res, cudaStream_t s) {
+  count_launch();
   ssd_pdf_kernel<<<1, 32, 0, s>>>(st, dx, dy, dz, li, res);
   return cudaGetLastError();
 }

@@ -11,6 +11,7 @@
 // memory; because segments are contiguous a block touches few children.  The
 // integer sums are order-free, so the split decisions made from them on the
 // host are bit-identical to the reference's.
+#include <atomic>
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
 
@@ -18,6 +19,11 @@
 #include "pgl_internal.h"
 
 namespace pgl {
+
+static std::atomic<unsigned long long> g_kernel_launches{0};
+unsigned long long kernel_launches() { return g_kernel_launches.load(std::memory_order_relaxed); }
+void count_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
+
 
 
 // ------------------------------------------------------------------ ingest
@@ -406,8 +412,10 @@ cudaError_t ingest_samples(const PGLSampleRecord *in, uint32_t n, Scratch &scrat
   uint32_t *isVol = reinterpret_cast<uint32_t *>(scratch.ptr);
   uint32_t *rank = isVol + (n + 1);
   void *temp = static_cast<char *>(scratch.ptr) + off;
+  count_launch();
   ingest_flag_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in, n, isVol);
   cub::DeviceScan::ExclusiveSum(temp, tempBytes, isVol, rank, int(n), s);
+  count_launch();
   ingest_scatter_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in, n, rank, surf.P, surf.D, surf.pdf, surf.flags, surf.base,
                                                           vol.P, vol.D, vol.pdf, vol.flags, vol.base);
   uint32_t last[2];
@@ -422,6 +430,7 @@ cudaError_t ingest_samples(const PGLSampleRecord *in, uint32_t n, Scratch &scrat
 cudaError_t export_samples(const float4 *P, const float4 *D, const float *pdf, const uint32_t *flags, uint64_t n,
                            PGLSampleRecord *out, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   export_kernel<<<blocks_for(n, 256), 256, 0, s>>>(P, D, pdf, flags, n, out);
   return cudaGetLastError();
 }
@@ -432,6 +441,7 @@ cudaError_t scene_bounds(const float4 *P, uint64_t n, uint32_t *d6, cudaStream_t
   if (e != cudaSuccess || n == 0) return e;
   unsigned b = blocks_for(n, 256);
   if (b > 4096) b = 4096;
+  count_launch();
   bounds_kernel<<<b, 256, 0, s>>>(P, n, d6);
   return cudaGetLastError();
 }
@@ -444,6 +454,7 @@ __global__ void init_posidx_kernel(const float4 *P, uint32_t n, float4 *posIdx) 
 }
 cudaError_t init_posidx(const float4 *P, uint32_t n, float4 *posIdx, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   init_posidx_kernel<<<blocks_for(n, 256), 256, 0, s>>>(P, n, posIdx);
   return cudaGetLastError();
 }
@@ -458,6 +469,7 @@ __global__ void init_acc_kernel(IStatsAcc *acc, uint32_t count) {
 }
 cudaError_t init_acc(IStatsAcc *acc, uint32_t count, cudaStream_t s) {
   if (count == 0) return cudaSuccess;
+  count_launch();
   init_acc_kernel<<<blocks_for(count, 128), 128, 0, s>>>(acc, count);
   return cudaGetLastError();
 }
@@ -466,12 +478,14 @@ cudaError_t kd_root_stats(const float4 *pos, uint32_t n, const KdJob &job, IStat
   unsigned b = blocks_for(n, kKdThreads * 8);
   if (b < 1) b = 1;
   if (b > 2048) b = 2048;
+  count_launch();
   kd_root_stats_kernel<<<b, kKdThreads, 0, s>>>(pos, n, job, acc);
   return cudaGetLastError();
 }
 
 cudaError_t kd_job_of(const uint32_t *node, uint32_t n, const uint32_t *nodeToJob, uint32_t *jobOf, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   kd_job_of_kernel<<<blocks_for(n, 256), 256, 0, s>>>(node, n, nodeToJob, jobOf);
   return cudaGetLastError();
 }
@@ -480,12 +494,14 @@ cudaError_t kd_level(const float4 *pos, const uint32_t *jobOf, uint32_t n, const
                      uint32_t *scanLeft, IStatsAcc *acc, float4 *posOut, uint32_t *nodeOut, Scratch &scratch,
                      cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   kd_classify_kernel<<<blocks_for(n, kKdTile), kKdThreads, 0, s>>>(pos, jobOf, n, jobs, isLeft, acc);
   size_t tempBytes = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, tempBytes, isLeft, scanLeft, int(n), s);
   cudaError_t e = scratch_reserve(scratch, tempBytes);
   if (e != cudaSuccess) return e;
   cub::DeviceScan::ExclusiveSum(scratch.ptr, tempBytes, isLeft, scanLeft, int(n), s);
+  count_launch();
   kd_scatter_kernel<<<blocks_for(n, 256), 256, 0, s>>>(pos, jobOf, isLeft, scanLeft, n, jobs, posOut, nodeOut);
   return cudaGetLastError();
 }
@@ -496,9 +512,11 @@ cudaError_t gather_and_order(const float4 *posIdx, uint32_t n, const float4 *P, 
                              float4 *oP, float4 *oD, float *oPdf, Scratch &scratch, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   if (!sorted) {
+    count_launch();
     gather_kernel<<<blocks_for(n, 256), 256, 0, s>>>(posIdx, n, P, D, pdf, oP, oD, oPdf, keys, vals);
     return cudaGetLastError();
   }
+  count_launch();
   gather_kernel<<<blocks_for(n, 256), 256, 0, s>>>(posIdx, n, P, D, pdf, tmpP, tmpD, tmpPdf, keys, vals);
   // segment offsets: begin[i] and begin[i] + count[i]
   uint32_t *keysOut = keys + n;
@@ -512,18 +530,21 @@ cudaError_t gather_and_order(const float4 *posIdx, uint32_t n, const float4 *P, 
   if (e != cudaSuccess) return e;
   cub::DeviceSegmentedSort::StableSortPairs(scratch.ptr, tempBytes, keys, keysOut, vals, valsOut, int(n),
                                             int(numLeaves), leafBegin, ends, s);
+  count_launch();
   order_kernel<<<numLeaves, 128, 0, s>>>(valsOut, leafBegin, leafCount, numLeaves, tmpP, tmpD, tmpPdf, oP, oD, oPdf);
   return cudaGetLastError();
 }
 
 cudaError_t copy_regions(RegionDir *regions, const uint32_t *dst, const uint32_t *src, uint32_t n, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   copy_region_kernel<<<n, 256, 0, s>>>(regions, dst, src, n);
   return cudaGetLastError();
 }
 
 cudaError_t build_knn(const float4 *means, uint32_t R, Neighbours *out, cudaStream_t s) {
   if (R == 0) return cudaSuccess;
+  count_launch();
   knn_kernel<<<blocks_for(R, 128), 128, 0, s>>>(means, R, out);
   return cudaGetLastError();
 }
