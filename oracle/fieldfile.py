@@ -80,8 +80,10 @@ def _read_field(r: _Reader, width: int, kmax: int = 32):
     f["deterministic"] = bool(r.u8())
     f["fitRegions"] = bool(r.u8())
     f["isSceneBoundsSet"] = bool(r.u8())
+    f["_sceneBounds_offset"] = r.o
     f["sceneBounds"] = r.farr(6)
     f["initialized"] = bool(r.u8())
+    f["_timings_offset"] = r.o
     f["timings"] = r.farr(4)
     cfg = {}
     cfg["initK"] = r.u64()
@@ -104,6 +106,7 @@ def _read_field(r: _Reader, width: int, kmax: int = 32):
     f["factory"] = cfg
     f["kd_settings"] = (r.u64(), r.u64(), r.u64())
     f["kd_isInit"] = bool(r.u8())
+    f["_kd_bounds_offset"] = r.o
     f["kd_bounds"] = r.farr(6)
     nn = r.u64()
     raw = np.frombuffer(r.take(8 * nn), dtype=np.dtype([("split", "<f4"), ("bits", "<u4")])).copy()
@@ -260,3 +263,23 @@ def leaf_of_positions(field, pos):
         cur[active] = left + (p >= split[cur[active]]).astype(np.int64)
         active = (bits[cur] >> 30) != 3
     return (bits[cur] & 0x3FFFFFFF).astype(np.int64)
+
+
+def strip_timings(buf):
+    """The field file with the bytes that do not describe the field set to
+    zero, so that two files of the same field compare equal byte for byte:
+    the per-field update timings (wall-clock values, Field.h:240-267) and, of
+    a sub-field that was never initialised (no samples of its kind yet), the
+    scene and kd-tree bounds, which the reference writes without having set
+    them."""
+    b = bytearray(buf)
+    parsed = read_field_file(bytes(b))
+    for side in ("surface", "volume"):
+        f = parsed[side]
+        o = f["_timings_offset"]
+        b[o:o + 16] = bytes(16)
+        if not f["initialized"]:
+            for key in ("_sceneBounds_offset", "_kd_bounds_offset"):
+                o = f[key]
+                b[o:o + 24] = bytes(24)
+    return bytes(b)

@@ -1,0 +1,86 @@
+#!/usr/bin/env python3
+"""Generates the golden fixtures of this directory by running the reference
+Open PGL library itself (compiled from the reference sources by
+oracle/Makefile.ref into oracle/_ref/, CPU_8 device, deterministic field,
+serial scheduling) on seeded synthetic inputs.
+
+Each case stores:
+  <case>.field.gz   the reference's field file after the last frame
+                    (pglFieldStoreToFile layout, update timings zeroed)
+  <case>.queries.npz  "surface": guided surface queries (Init + cosine
+                    product + SamplePDF + IncomingRadiancePDF per query),
+                    "volume": guided volume queries (Init + SamplePDF +
+                    IncomingRadiancePDF)
+and manifest.json records the generator calls and the SHA-256 of every
+generated input, so a test can check that the generators still produce the
+same inputs before it compares outputs.
+
+Run from the repository root on a machine that has the reference sources:
+    make -C oracle -f Makefile.ref REF=/path/to/openpgl
+    python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import gzip
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle")]
+
+# case name -> (generator, per-frame arguments, queries, maxSamplesPerLeaf)
+CASES = {
+    "cube_single": dict(gen="cube_face_samples", frames=[dict(n=65536, seed=101)],
+                        queries=dict(n=4096, seed=102), leaf=8000),
+    "cube_multiframe_volume": dict(gen="cube_face_samples",
+                                   frames=[dict(n=32768, seed=110 + i, volume_fraction=0.25) for i in range(3)],
+                                   queries=dict(n=4096, seed=113), leaf=4000),
+    "clusters": dict(gen="cluster_samples", frames=[dict(n=60000, seed=120 + i, num_clusters=64) for i in range(2)],
+                     queries=dict(n=4096, seed=122, model_seed=1234), leaf=2000),
+}
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def build_inputs(case):
+    from openpgl_gb300 import synthetic as syn
+
+    gen = getattr(syn, case["gen"])
+    frames = [gen(**kw) for kw in case["frames"]]
+    queries = syn.queries(**case["queries"])
+    return frames, queries
+
+
+def main():
+    import fieldfile
+    import pyoracle
+
+    if not pyoracle.reference_available():
+        sys.exit("oracle/_ref/ref_harness is missing: build it with oracle/Makefile.ref first")
+    manifest = {"generator": "openpgl_gb300.synthetic", "reference": "Open PGL 0.6.0, CPU_8, deterministic, serial",
+                "cases": {}}
+    for name, case in CASES.items():
+        frames, queries = build_inputs(case)
+        field, _, sq, vq = pyoracle.run_reference(frames, queries, max_samples_per_leaf=case["leaf"],
+                                                  deterministic=True, threads=1, device=8)
+        field = fieldfile.strip_timings(field)
+        with gzip.open(os.path.join(HERE, f"{name}.field.gz"), "wb", compresslevel=9) as f:
+            f.write(field)
+        np.savez_compressed(os.path.join(HERE, f"{name}.queries.npz"), surface=sq, volume=vq)
+        manifest["cases"][name] = dict(case, frame_sha256=[sha(f) for f in frames], queries_sha256=sha(queries),
+                                       field_sha256=hashlib.sha256(field).hexdigest())
+        print(name, len(field), "bytes,", len(fieldfile.read_field_file(field)["surface"]["regions"]), "surface regions")
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

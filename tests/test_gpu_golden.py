@@ -1,0 +1,83 @@
+"""The GB300 library against golden outputs of the reference library itself
+(tests/golden).  kd-tree (split dimensions and planes, canonical structure),
+leaf sample statistics and region bounds bit-exact; per leaf the relative PDF
+error on a 64x64 direction grid at most 1e-3; guided queries pick the same
+region with the same rescaled sample1D, pdf within 1e-3 relative."""
+
+import gzip
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from helpers import compare_fields
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
+CASES = sorted(MANIFEST["cases"])
+PDF_TOL = 1e-3
+
+
+@pytest.fixture(scope="module")
+def pgl():
+    import openpgl_gb300
+
+    openpgl_gb300.load()
+    return openpgl_gb300
+
+
+def run_case(pgl, name):
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+
+    case = MANIFEST["cases"][name]
+    frames, queries = make_golden.build_inputs(case)
+    dev = pgl.Device()
+    field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=case["leaf"]))
+    storage = pgl.SampleStorage()
+    for f in frames:
+        storage.add_samples(f)
+        field.update(storage)
+        storage.clear()
+    return field, queries
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_field_matches_reference(pgl, name):
+    field, _ = run_case(pgl, name)
+    ref = gzip.open(os.path.join(GOLDEN, f"{name}.field.gz")).read()
+    for side in ("surface", "volume"):
+        r = compare_fields(field.field_bytes(), ref, side)
+        assert r["tree_equal"], (side, r)
+        assert r["numbering_equal"], (side, r)
+        if r["regions"] == 0:
+            continue
+        assert r["stats_equal"], (side, r)
+        assert r["worst_pdf_rel"] <= PDF_TOL, (side, r)
+        print(side, "regions", r["regions"], "bit-exact", r["bit_exact_regions"], "K flips", r["k_differs"],
+              "worst pdf rel %.2e" % r["worst_pdf_rel"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_queries_match_reference(pgl, name):
+    field, queries = run_case(pgl, name)
+    g = np.load(os.path.join(GOLDEN, f"{name}.queries.npz"))
+    for volume, key in ((False, "surface"), (True, "volume")):
+        out = field.sample_batch(queries, volume=volume, cosine=not volume)
+        ref = g[key]
+        assert np.array_equal(out["ok"], ref["ok"]), key
+        ok = ref["ok"] == 1
+        if not ok.any():
+            continue
+        assert np.array_equal(out["id"][ok], ref["id"][ok]), key
+        assert np.array_equal(out["sample1d"][ok].view(np.uint32), ref["sample1d"][ok].view(np.uint32)), key
+        rel = np.abs(out["pdf"][ok] - ref["pdf"][ok]) / ref["pdf"][ok]
+        assert rel.max() <= PDF_TOL, (key, np.quantile(rel, [0.5, 0.99, 1.0]))
+        assert np.abs(out["dir"][ok] - ref["dir"][ok]).max() <= 1e-3, key
+        print(key, "queries", int(ok.sum()), "bit-exact pdf fraction",
+              float(np.mean(out["pdf"][ok].view(np.uint32) == ref["pdf"][ok].view(np.uint32))))

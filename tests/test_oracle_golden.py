@@ -1,0 +1,110 @@
+"""The oracle (CPU restatement of the reference's field path, oracle/) against
+golden outputs of the reference library itself (tests/golden, made by
+tests/golden/make_golden.py from the compiled reference sources).  Bit-exact:
+the same field file (tree, regions, mixtures, statistics) and the same guided
+query results.  CPU only."""
+
+import gzip
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import fieldfile
+import pyoracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
+CASES = sorted(MANIFEST["cases"])
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def inputs(name):
+    import make_golden
+
+    case = MANIFEST["cases"][name]
+    return make_golden.build_inputs(case), case
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _golden_path():
+    import sys
+
+    sys.path.insert(0, GOLDEN)
+    yield
+
+
+def golden(name):
+    field = gzip.open(os.path.join(GOLDEN, f"{name}.field.gz")).read()
+    q = np.load(os.path.join(GOLDEN, f"{name}.queries.npz"))
+    return field, q["surface"], q["volume"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_generators_reproduce_golden_inputs(name):
+    (frames, queries), case = inputs(name)
+    assert [sha(f) for f in frames] == case["frame_sha256"]
+    assert sha(queries) == case["queries_sha256"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_field_is_the_reference_field(name):
+    (frames, queries), case = inputs(name)
+    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4)
+    for f in frames:
+        orc.update(f)
+    mine = fieldfile.strip_timings(orc.field_bytes())
+    ref, _, _ = golden(name)
+    assert hashlib.sha256(ref).hexdigest() == case["field_sha256"]
+    assert mine == ref
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_queries_are_the_reference_queries(name):
+    (frames, queries), case = inputs(name)
+    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4)
+    for f in frames:
+        orc.update(f)
+    _, rs, rv = golden(name)
+    s = orc.query(queries, volume=False, cosine=True)
+    v = orc.query(queries, volume=True, cosine=False)
+    assert s.tobytes() == rs.tobytes()
+    assert v.tobytes() == rv.tobytes()
+
+
+def test_golden_field_structure():
+    """The parsed reference file is self-consistent: leaves index regions,
+    every region's sample statistics count matches the leaf histogram of its
+    frame, and the canonical tree has one leaf per region."""
+    ref, _, _ = golden("cube_single")
+    f = fieldfile.read_field_file(ref)["surface"]
+    canon = fieldfile.canonical_tree(f)
+    assert canon["leaf"].sum() == len(f["regions"])
+    assert sorted(canon["region"].tolist()) == list(range(len(f["regions"])))
+    (frames, _), _ = inputs("cube_single")
+    pos = np.stack([frames[0]["position"][:, i] for i in range(3)], axis=1)
+    leaf = fieldfile.leaf_of_positions(f, pos)
+    hist = np.bincount(leaf, minlength=len(f["regions"]))
+    n = np.array([r["stats"]["n"] for r in f["regions"]])
+    assert np.array_equal(hist.astype(np.float32), n)
+
+
+@pytest.mark.skipif(not pyoracle.reference_available(), reason="reference library not built here")
+def test_oracle_matches_live_reference_on_fresh_seed():
+    from openpgl_gb300 import synthetic as syn
+
+    frames = [syn.cube_face_samples(20000, 777 + i, volume_fraction=0.3) for i in range(2)]
+    q = syn.queries(1024, 779)
+    field, _, rs, rv = pyoracle.run_reference(frames, q, max_samples_per_leaf=3000)
+    orc = pyoracle.OracleField(3000, deterministic=True, threads=2)
+    for f in frames:
+        orc.update(f)
+    assert fieldfile.strip_timings(orc.field_bytes()) == fieldfile.strip_timings(field)
+    assert orc.query(q).tobytes() == rs.tobytes()
+    assert orc.query(q, volume=True, cosine=False).tobytes() == rv.tobytes()
