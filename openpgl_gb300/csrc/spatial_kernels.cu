@@ -12,6 +12,7 @@
 // integer sums are order-free, so the split decisions made from them on the
 // host are bit-identical to the reference's.
 #include <atomic>
+#include <climits>
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
 
@@ -121,6 +122,19 @@ __device__ __forceinline__ void acc_global(IStatsAcc *a, const long long q[3], c
 // Classifies the samples of every job at this level: side flag (1 = left),
 // child statistics into acc[2*job + side].  jobOf[i] is the job of sample i
 // (or ~0 when the sample already sits in a finished leaf).
+// Adds one sample's integer statistics (or a warp's reduced ones) to an
+// accumulator in shared or global memory.
+__device__ __forceinline__ void acc_add(IStatsAcc *a, const long long m[3], const long long v[3], const long long lo[3],
+                                        const long long hi[3], unsigned long long n) {
+  for (int d = 0; d < 3; ++d) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(&a->m[d]), (unsigned long long)m[d]);
+    atomicAdd(reinterpret_cast<unsigned long long *>(&a->v[d]), (unsigned long long)v[d]);
+    atomicMin(&a->lo[d], lo[d]);
+    atomicMax(&a->hi[d], hi[d]);
+  }
+  atomicAdd(&a->n, n);
+}
+
 __global__ void __launch_bounds__(kKdThreads)
 kd_classify_kernel(const float4 *pos, const uint32_t *jobOf, uint32_t n, const KdJob *jobs, uint32_t *isLeft,
                    IStatsAcc *acc) {
@@ -130,19 +144,8 @@ kd_classify_kernel(const float4 *pos, const uint32_t *jobOf, uint32_t n, const K
   if (tileBegin >= n) return;
   const uint32_t tileEnd = min(n, tileBegin + kKdTile);
   if (threadIdx.x == 0) {
-    // jobs are sorted by segment and samples of a job are contiguous, so the
-    // tile's jobs form a range; finished samples (~0) are skipped
-    uint32_t f = ~0u, l = 0;
-    for (uint32_t i = tileBegin; i < tileEnd; ++i) {
-      uint32_t j = jobOf[i];
-      if (j != ~0u) { f = j; break; }
-    }
-    for (uint32_t i = tileEnd; i > tileBegin; --i) {
-      uint32_t j = jobOf[i - 1];
-      if (j != ~0u) { l = j; break; }
-    }
-    firstJob = f;
-    lastJob = l;
+    firstJob = ~0u;
+    lastJob = 0;
   }
   for (int s = threadIdx.x; s < 2 * kKdLocal; s += blockDim.x) {
     IStatsAcc &a = local[s];
@@ -150,33 +153,83 @@ kd_classify_kernel(const float4 *pos, const uint32_t *jobOf, uint32_t n, const K
     a.n = 0;
   }
   __syncthreads();
-  const bool useLocal = firstJob != ~0u && (lastJob - firstJob) < uint32_t(kKdLocal);
-  for (uint32_t i = tileBegin + threadIdx.x; i < tileEnd; i += blockDim.x) {
-    uint32_t jid = jobOf[i];
-    if (jid == ~0u) { isLeft[i] = 0; continue; }
-    const KdJob j = jobs[jid];
-    float4 p = pos[i];
-    float coord = j.dim == 0 ? p.x : (j.dim == 1 ? p.y : p.z);
-    uint32_t left = coord < j.pos ? 1u : 0u;
-    isLeft[i] = left;
-    uint32_t side = left ? 0u : 1u;
-    if (j.needStats) {
-      long long q[3], qv[3];
-      quantize(j, p, q, qv);
-      if (useLocal) {
-        IStatsAcc *a = &local[2 * (jid - firstJob) + side];
-        for (int d = 0; d < 3; ++d) {
-          atomicAdd(reinterpret_cast<unsigned long long *>(&a->m[d]), (unsigned long long)q[d]);
-          atomicAdd(reinterpret_cast<unsigned long long *>(&a->v[d]), (unsigned long long)qv[d]);
-          atomicMin(&a->lo[d], q[d]);
-          atomicMax(&a->hi[d], q[d]);
-        }
-        atomicAdd(&a->n, 1ull);
-      } else {
-        acc_global(&acc[2 * jid + side], q, qv);
+  // jobs are sorted by segment and samples of a job are contiguous, so the
+  // tile's jobs form the range [min, max] of its job ids (~0: finished sample)
+  {
+    uint32_t f = ~0u, l = 0;
+    for (uint32_t i = tileBegin + threadIdx.x; i < tileEnd; i += blockDim.x) {
+      const uint32_t j = jobOf[i];
+      if (j != ~0u) {
+        f = min(f, j);
+        l = max(l, j);
       }
-    } else {
-      atomicAdd(&acc[2 * jid + side].n, 1ull);
+    }
+    if (f != ~0u) {
+      atomicMin(&firstJob, f);
+      atomicMax(&lastJob, l);
+    }
+  }
+  __syncthreads();
+  const bool useLocal = firstJob != ~0u && (lastJob - firstJob) < uint32_t(kKdLocal);
+  const unsigned full = 0xFFFFFFFFu;
+  const int lane = threadIdx.x & 31;
+  for (uint32_t base = tileBegin; base < tileEnd; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t jid = i < tileEnd ? jobOf[i] : ~0u;
+    KdJob j;
+    uint32_t left = 0;
+    long long q[3] = {0, 0, 0}, qv[3] = {0, 0, 0};
+    bool stats = false;
+    if (jid != ~0u) {
+      j = jobs[jid];
+      const float4 p = pos[i];
+      const float coord = j.dim == 0 ? p.x : (j.dim == 1 ? p.y : p.z);
+      left = coord < j.pos ? 1u : 0u;
+      stats = j.needStats != 0;
+      if (stats) quantize(j, p, q, qv);
+    }
+    if (i < tileEnd) isLeft[i] = left;
+    // one job for the whole warp and 32-bit-safe values: reduce per side
+    // with warp reductions, one set of atomics per side
+    const unsigned act = __ballot_sync(full, jid != ~0u);
+    if (act == 0) continue;
+    const uint32_t j0 = __shfl_sync(full, jid, __ffs(act) - 1);
+    bool small = true;
+    for (int d = 0; d < 3; ++d) small &= (q[d] >= -(1LL << 24) && q[d] <= (1LL << 24) && qv[d] >= 0 && qv[d] <= (1LL << 24));
+    const bool uniform = __all_sync(full, (jid == ~0u || jid == j0) && small);
+    if (uniform) {
+      for (uint32_t side = 0; side < 2; ++side) {
+        const bool mine = jid != ~0u && (left ? 0u : 1u) == side;
+        const unsigned m = __ballot_sync(full, mine);
+        if (m == 0) continue;
+        long long sm[3], sv[3], lo[3], hi[3];
+        const bool needStats = __shfl_sync(full, stats ? 1 : 0, __ffs(m) - 1) != 0;
+        if (needStats) {
+          for (int d = 0; d < 3; ++d) {
+            sm[d] = __reduce_add_sync(full, mine ? int(q[d]) : 0);
+            sv[d] = __reduce_add_sync(full, mine ? int(qv[d]) : 0);
+            lo[d] = __reduce_min_sync(full, mine ? int(q[d]) : INT_MAX);
+            hi[d] = __reduce_max_sync(full, mine ? int(q[d]) : INT_MIN);
+          }
+        }
+        if (lane == __ffs(m) - 1) {
+          const uint32_t slot = 2 * j0 + side;
+          if (needStats) {
+            IStatsAcc *a = useLocal ? &local[slot - 2 * firstJob] : &acc[slot];
+            acc_add(a, sm, sv, lo, hi, (unsigned long long)__popc(m));
+          } else {
+            atomicAdd(&acc[slot].n, (unsigned long long)__popc(m));
+          }
+        }
+      }
+    } else if (jid != ~0u) {
+      const uint32_t side = left ? 0u : 1u;
+      if (stats) {
+        IStatsAcc *a = useLocal ? &local[2 * (jid - firstJob) + side] : &acc[2 * jid + side];
+        acc_add(a, q, qv, q, q, 1ull);
+      } else {
+        atomicAdd(&acc[2 * jid + side].n, 1ull);
+      }
     }
   }
   __syncthreads();
@@ -184,14 +237,7 @@ kd_classify_kernel(const float4 *pos, const uint32_t *jobOf, uint32_t n, const K
     for (int s = threadIdx.x; s < 2 * kKdLocal; s += blockDim.x) {
       const IStatsAcc &a = local[s];
       if (a.n == 0) continue;
-      IStatsAcc *g = &acc[2 * firstJob + s];
-      for (int d = 0; d < 3; ++d) {
-        atomicAdd(reinterpret_cast<unsigned long long *>(&g->m[d]), (unsigned long long)a.m[d]);
-        atomicAdd(reinterpret_cast<unsigned long long *>(&g->v[d]), (unsigned long long)a.v[d]);
-        atomicMin(&g->lo[d], a.lo[d]);
-        atomicMax(&g->hi[d], a.hi[d]);
-      }
-      atomicAdd(&g->n, a.n);
+      acc_add(&acc[2 * firstJob + s], a.m, a.v, a.lo, a.hi, a.n);
     }
   }
 }
@@ -301,8 +347,15 @@ __global__ void order_kernel(const uint32_t *sortedVal, const uint32_t *leafBegi
     oD[b + i] = D[s];
     oPdf[b + i] = pdf[s];
   }
+  __shared__ int anyTie;
+  if (threadIdx.x == 0) anyTie = 0;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  // equal weight keys are rare: look for adjacent equal keys in parallel and
+  // order the runs by the full comparison only when there is one
+  for (uint32_t i = threadIdx.x; i + 1 < c; i += blockDim.x)
+    if (oD[b + i].w == oD[b + i + 1].w) anyTie = 1;
+  __syncthreads();
+  if (anyTie && threadIdx.x == 0) {
     uint32_t i = 0;
     while (i < c) {
       uint32_t j = i + 1;
