@@ -17,6 +17,7 @@
 // summation order (sequential over samples within each SIMD lane), so every
 // accumulator gets the reference's bits.  Scalar per-leaf logic (M step,
 // split/merge bookkeeping) runs on thread 0 between passes.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -29,6 +30,18 @@ namespace pgl {
 constexpr int kEmThreads = 512;
 constexpr int kStageFloats = 19200;  // floats per pipeline stage (two stages, 150 KB)
 constexpr int kMaxPairs = kMaxK * (kMaxK - 1) / 2;
+
+// A pass as the home block of a cluster publishes it to its helper blocks.
+enum PassCmdKind { kCmdEStep = 0, kCmdDistance = 1, kCmdSplit = 2, kCmdExit = 3 };
+struct PassCmd {
+  int kind;
+  int cnt;  // lobe vectors (K rounded up to 8, divided by 8)
+  const float4 *dirw;
+  const float *pdf;
+  const float *dist;
+  uint32_t count;
+  float mcEstimate;
+};
 
 struct Unassigned {
   float sw, dx, dy, dz;
@@ -61,6 +74,7 @@ struct EmShared {
   int iterations;
   LeafReport report;
   LeafProfile prof;
+  PassCmd cmd;
 };
 static_assert(offsetof(EmShared, pbuf) % 16 == 0 &&
                   offsetof(EmShared, lobeA) % 16 == 0,
@@ -688,7 +702,6 @@ __device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cn
     X[4 * C + s] = un ? d.z * w : 0.0f;
   } else if constexpr (kind == kPassDistance) {
     // rows k: wts * rcp(distance); rows Kp + k: wts
-    const VMMState &vm = S.vmm;
     const float sd = valid ? rcp_avx2_tab(in.x, S.rcpTab) : 0.0f;
 #pragma unroll
     for (int k = 0; k < kMaxK; ++k) {
@@ -696,7 +709,7 @@ __device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cn
         float wts = 0.0f;
         if (valid) {
           float a = T.t[k] * T.inv;
-          wts = (w * a) * div_rcp(a * T.pdf, vm.w[k], S.lobeWInv[k]);
+          wts = (w * a) * div_rcp(a * T.pdf, S.lobeB[k].y, S.lobeWInv[k]);
         }
         B[k * R + s] = wts * sd;
         B[(Kp + k) * R + s] = wts;
@@ -746,18 +759,33 @@ __device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cn
 
 __device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
-// Sum of one row (the terms of one accumulator) in sample order; loads run a
-// group of 4 samples ahead of the additions.
+// Sum of one row (the terms of one accumulator) in sample order; loads run 8
+// samples ahead of the additions.
 __device__ __forceinline__ void row_chain(const float *row, int n4, float &acc) {
-  float4 v = ld4(row);
-  for (int s = 0; s < n4; s += 4) {
-    const int sn = s + 4 < n4 ? s + 4 : s;
-    const float4 v1 = ld4(row + sn);
+  int s = 0;
+  if (n4 >= 8) {
+    float4 a = ld4(row), b = ld4(row + 4);
+    for (; s + 8 <= n4; s += 8) {
+      const int sn = s + 16 <= n4 ? s + 8 : s;
+      const float4 a1 = ld4(row + sn), b1 = ld4(row + sn + 4);
+      acc += a.x;
+      acc += a.y;
+      acc += a.z;
+      acc += a.w;
+      acc += b.x;
+      acc += b.y;
+      acc += b.z;
+      acc += b.w;
+      a = a1;
+      b = b1;
+    }
+  }
+  if (s < n4) {
+    const float4 v = ld4(row + s);
     acc += v.x;
     acc += v.y;
     acc += v.z;
     acc += v.w;
-    v = v1;
   }
 }
 
@@ -780,13 +808,11 @@ __device__ __forceinline__ void distance_chain(const float *B, const PassShape &
   if (c < 2 * Kp) row_chain(B + c * sh.R, n4, acc);
 }
 
-// One step of chi2 += (x - chi2) / n with y = RN(1/n); `bad` records a step
-// outside the range where div_rcp's FMA steps are exact.
+// One step of chi2 += (x - chi2) / n with y ~ 1/n (div_faithful_fix); `bad`
+// records a step outside the range where that division is exact.
 __device__ __forceinline__ float chi_step(float acc, float x, float n, float y, float v, bool &bad) {
   const float num = x - acc;
-  const float q0 = num * y;
-  const float r = fmaf_(-q0, n, num);
-  const float q = fmaf_(r, y, q0);
+  const float q = div_faithful_fix(num, n, y);
   const float an = fabsf(num), aq = fabsf(q);
   bad |= (v != 0.0f) && !(an >= 1e-30f && an <= 1e30f && aq >= 1e-30f && aq <= 1e30f) && (num != 0.0f);
   return v != 0.0f ? acc + q : acc;
@@ -815,7 +841,7 @@ __device__ __forceinline__ void split_chain(const float *B, const PassShape &sh,
       const int sn = s + 4 < n4 ? s + 4 : s;
       const float4 x1 = ld4(cr + sn), v1 = ld4(Vr + sn);
       const float n1 = accN + v.x, n2 = n1 + v.y, n3 = n2 + v.z, n4v = n3 + v.w;
-      const float y1 = __frcp_rn(n1), y2 = __frcp_rn(n2), y3 = __frcp_rn(n3), y4 = __frcp_rn(n4v);
+      const float y1 = rcp_approx(n1), y2 = rcp_approx(n2), y3 = rcp_approx(n3), y4 = rcp_approx(n4v);
       const float acc0 = acc;
       bool bad = false;
       acc = chi_step(acc, x.x, n1, y1, v.x, bad);
@@ -836,41 +862,64 @@ __device__ __forceinline__ void split_chain(const float *B, const PassShape &sh,
   }
 }
 
-// Runs one pass over the leaf's samples.  `acc`/`accN` are the consumer's
-// accumulators (initialised by the caller); the producer side is driven here.
+// Cluster barrier when the region is shared by several blocks, else the
+// block barrier.
+__device__ __forceinline__ void round_sync(unsigned G) {
+  if (G > 1) cooperative_groups::this_cluster().sync();
+  else __syncthreads();
+}
+
+// Runs one pass over the leaf's samples in the home block (cluster rank 0).
+// Chunk c is produced by cluster rank c % G into its stage ((c / G) & 1); the
+// home block's consumers read the G chunks of a round in chunk order, from
+// the helper blocks' shared memory for ranks > 0.  `acc`/`accN` are the
+// consumer's accumulators (initialised by the caller).  With G > 1 the pass
+// is first published to the helpers (PassCmd); home and helpers then run the
+// same number of rounds, each ending at a cluster barrier.
 template <PassKind kind>
 __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const PassShape &sh, int cnt, float &acc,
                                       float &accN) {
+  namespace cg = cooperative_groups;
   const int tid = threadIdx.x;
   const int Kp = cnt * kLanes;
   const int C = sh.C;
+  const unsigned G = cg::this_cluster().num_blocks();
+  if (G > 1) {
+    if (tid == 0) S.cmd = PassCmd{int(kind), cnt, L.dirw, L.pdf, L.dist, L.count, S.mcEstimate};
+    cg::this_cluster().sync();
+  }
   const uint32_t numChunks = (L.count + C - 1) / C;
+  const uint32_t rounds = (numChunks + G - 1) / G;
   const bool producer = tid < C;
   const bool consumer = tid >= sh.P;
   const int c = tid - sh.P;
   SampleIn next;
   if (producer) next = load_sample<kind>(L, uint32_t(tid));
   long long cycP = 0, cycC = 0;
-  for (uint32_t it = 0; it <= numChunks; ++it) {
-    if (producer && it < numChunks) {
+  for (uint32_t it = 0; it <= rounds; ++it) {
+    if (producer && it < rounds) {
       const long long t0 = clock64();
       const SampleIn cur = next;
-      if (it + 1 < numChunks) next = load_sample<kind>(L, (it + 1) * C + tid);
+      if (it + 1 < rounds) next = load_sample<kind>(L, (it + 1) * G * C + tid);
       produce<kind>(S, sh, cnt, Kp, tid, cur, S.pbuf + (it & 1) * sh.stage);
       cycP += clock64() - t0;
     }
     if (consumer && it >= 1) {
       const long long t0 = clock64();
-      const uint32_t prev = it - 1;
-      const int n = int(min(uint32_t(C), L.count - prev * C));
-      const int n4 = (n + 3) & ~3;
-      const float *B = S.pbuf + (prev & 1) * sh.stage;
-      if constexpr (kind == kPassEStep) estep_chain(B, sh, c, Kp, n4, acc);
-      else if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
-      else split_chain(B, sh, c, Kp, n4, acc, accN);
+      for (unsigned r = 0; r < G; ++r) {
+        const uint32_t chunk = (it - 1) * G + r;
+        if (chunk >= numChunks) break;
+        const int n = int(min(uint32_t(C), L.count - chunk * C));
+        const int n4 = (n + 3) & ~3;
+        const float *local = S.pbuf + ((it - 1) & 1) * sh.stage;
+        const float *B = r == 0 ? local : cg::this_cluster().map_shared_rank(local, r);
+        if constexpr (kind == kPassEStep) estep_chain(B, sh, c, Kp, n4, acc);
+        else if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
+        else split_chain(B, sh, c, Kp, n4, acc, accN);
+      }
       cycC += clock64() - t0;
     }
-    __syncthreads();
+    round_sync(G);
   }
   const int probe = kind == kPassSplit ? split_chi_base(Kp) : 0;
   if (tid == 0) {
@@ -880,6 +929,60 @@ __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const P
   if (c == probe) {
     if (kind == kPassSplit) S.prof.cycConsS += uint64_t(cycC);
     else if (kind == kPassEStep) S.prof.cycConsE += uint64_t(cycC);
+  }
+}
+
+// The producer side of one pass in a helper block (cluster rank r > 0): the
+// same rounds as the home block's run_pass, producing chunks it * G + r.
+template <PassKind kind>
+__device__ __noinline__ void helper_pass(EmShared &S, const PassCmd &cmd, unsigned rank, unsigned G) {
+  const int tid = threadIdx.x;
+  const int Kp = cmd.cnt * kLanes;
+  const PassShape sh = pass_shape<kind>(Kp);
+  const int C = sh.C;
+  const LeafSamples L{cmd.dirw, cmd.pdf, cmd.dist, cmd.count};
+  const uint32_t numChunks = (L.count + C - 1) / C;
+  const uint32_t rounds = (numChunks + G - 1) / G;
+  const bool producer = tid < C;
+  SampleIn next;
+  if (producer) next = load_sample<kind>(L, rank * C + tid);
+  for (uint32_t it = 0; it <= rounds; ++it) {
+    if (producer && it < rounds && it * G + rank < numChunks) {
+      const SampleIn cur = next;
+      if (it + 1 < rounds) next = load_sample<kind>(L, ((it + 1) * G + rank) * C + tid);
+      produce<kind>(S, sh, cmd.cnt, Kp, tid, cur, S.pbuf + (it & 1) * sh.stage);
+    }
+    cooperative_groups::this_cluster().sync();
+  }
+}
+
+// Helper blocks serve the home block's passes until it publishes kCmdExit.
+// Every command costs both sides one cluster barrier to publish, then the
+// pass's rounds; the exit costs a second barrier so that the home block's
+// shared memory outlives the helpers' read of the command.
+__device__ void helper_loop(EmShared &S, unsigned rank, unsigned G) {
+  namespace cg = cooperative_groups;
+  const int tid = threadIdx.x;
+  EmShared *home = cg::this_cluster().map_shared_rank(&S, 0u);
+  for (;;) {
+    cg::this_cluster().sync();
+    const PassCmd cmd = home->cmd;
+    if (cmd.kind == kCmdExit) {
+      cg::this_cluster().sync();
+      return;
+    }
+    const int Kp = cmd.cnt * kLanes;
+    if (tid < Kp) {
+      S.lobeA[tid] = home->lobeA[tid];
+      S.lobeB[tid] = home->lobeB[tid];
+      S.lobeWInv[tid] = home->lobeWInv[tid];
+      S.invFrame[tid] = home->invFrame[tid];
+    }
+    if (tid == 0) S.mcEstimate = cmd.mcEstimate;
+    __syncthreads();
+    if (cmd.kind == kCmdEStep) helper_pass<kPassEStep>(S, cmd, rank, G);
+    else if (cmd.kind == kCmdDistance) helper_pass<kPassDistance>(S, cmd, rank, G);
+    else helper_pass<kPassSplit>(S, cmd, rank, G);
   }
 }
 
@@ -1295,10 +1398,19 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
   __shared__ uint32_t taskId;
   __shared__ uint64_t afterSplit, afterMerge;
   for (int i = threadIdx.x; i < 2048; i += blockDim.x) S.rcpTab[i] = rcp_seed(uint32_t(i));
+  // a cluster of G blocks shares each region: rank 0 (home) owns it, the
+  // others produce chunks of its passes (helper_loop)
+  const unsigned G = cooperative_groups::this_cluster().num_blocks();
+  const unsigned rank = cooperative_groups::this_cluster().block_rank();
+  if (rank != 0) {
+    __syncthreads();
+    helper_loop(S, rank, G);
+    return;
+  }
   for (;;) {
     if (threadIdx.x == 0) taskId = atomicAdd(queue, 1u);
     __syncthreads();
-    if (taskId >= numTasks) return;
+    if (taskId >= numTasks) break;
     const LeafTask t = tasks[taskId];
     RegionDir &R = regions[t.region];
     // load the region's directional state
@@ -1378,6 +1490,11 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
     }
     __syncthreads();
   }
+  if (G > 1) {  // release the helpers (see helper_loop)
+    if (threadIdx.x == 0) S.cmd.kind = kCmdExit;
+    cooperative_groups::this_cluster().sync();
+    cooperative_groups::this_cluster().sync();
+  }
 }
 
 PGL_DEFINE_TABLE_UPLOAD(em_upload_tables)
@@ -1386,7 +1503,7 @@ size_t em_shared_bytes() { return sizeof(EmShared); }
 
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
                       float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
-                      LeafReport *reports, LeafProfile *profiles, int numBlocks, cudaStream_t stream) {
+                      LeafReport *reports, LeafProfile *profiles, int numSMs, int clusterSize, cudaStream_t stream) {
   static bool attrSet = false;
   const size_t smem = sizeof(EmShared);
   if (!attrSet) {
@@ -1394,10 +1511,37 @@ cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *qu
     if (e != cudaSuccess) return e;
     attrSet = true;
   }
+  if (numTasks == 0) return cudaSuccess;
+  cudaLaunchConfig_t config = {};
+  config.blockDim = dim3(kEmThreads);
+  config.dynamicSmemBytes = smem;
+  config.stream = stream;
+  cudaLaunchAttribute attr[1];
+  int G = clusterSize < 1 ? 1 : clusterSize;
+  int clusters = 0;
+  if (G > 1) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = unsigned(G);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    config.attrs = attr;
+    config.numAttrs = 1;
+    config.gridDim = dim3(unsigned(G) * unsigned(numSMs / G));
+    if (cudaOccupancyMaxActiveClusters(&clusters, em_leaf_kernel, &config) != cudaSuccess || clusters < 1) {
+      cudaGetLastError();
+      G = 1;  // this cluster shape does not fit: one block per region
+    }
+  }
+  if (G == 1) {
+    config.attrs = nullptr;
+    config.numAttrs = 0;
+    clusters = numSMs;
+  }
+  const unsigned used = unsigned(clusters) < numTasks ? unsigned(clusters) : numTasks;
+  config.gridDim = dim3(used * unsigned(G));
   count_launch();
-  em_leaf_kernel<<<numBlocks, kEmThreads, smem, stream>>>(tasks, numTasks, queue, regions, pd, dirw, pdf, dist, cfg,
-                                                          uniformDirs, reports, profiles);
-  return cudaGetLastError();
+  return cudaLaunchKernelEx(&config, em_leaf_kernel, tasks, numTasks, queue, regions, pd, dirw, pdf, dist, cfg,
+                            uniformDirs, reports, profiles);
 }
 
 }  // namespace pgl

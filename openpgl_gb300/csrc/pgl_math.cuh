@@ -211,6 +211,50 @@ PGL_HD float rcp_for_div(float b) {
   return (ab >= 1e-30f && ab <= 1e30f) ? 1.0f / b : 0.0f;
 }
 
+// a / b rounded to nearest from an approximate reciprocal y (relative error
+// a few 2^-24): q1 = q0 + (a - b q0) y with q0 = a y is a faithful quotient
+// (one of the two floats around a/b); the remainder a - b q of a faithful q
+// is exact under FMA; so RN(a/b) is whichever of q1 and its neighbour towards
+// a/b has the smaller remainder (a quotient of floats is never exactly half
+// way between two floats).  Valid for normal b and |a|, |a/b| in
+// [1e-30, 1e30]; the caller checks the range.
+PGL_HD float div_faithful_fix(float a, float b, float y) {
+  const float q0 = a * y;
+  const float r0 = fmaf_(-q0, b, a);
+  const float q1 = fmaf_(r0, y, q0);
+  const float r1 = fmaf_(-q1, b, a);
+  const bool up = (r1 > 0.0f) == (b > 0.0f);  // a/b above q1
+  const uint32_t u = f2u(q1);
+  const float q2 = u2f(((q1 > 0.0f) == up) ? u + 1u : u - 1u);
+  const float r2 = fmaf_(-q2, b, a);
+  const float ar1 = r1 < 0.0f ? -r1 : r1, ar2 = r2 < 0.0f ? -r2 : r2;
+  return (r1 != 0.0f && ar2 < ar1) ? q2 : q1;
+}
+// approximate reciprocal (the hardware's rcp.approx; about one ulp)
+PGL_HD float rcp_approx(float b) {
+#ifdef __CUDA_ARCH__
+  float y;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(y) : "f"(b));
+  return y;
+#else
+  return 1.0f / b;
+#endif
+}
+
+// RN(1/b) for 1e-30 <= |b| <= 1e30 (div_faithful_fix from the approximate
+// reciprocal).
+PGL_HD float rcp_rn(float b) { return div_faithful_fix(1.0f, b, rcp_approx(b)); }
+// The three FMA-unit steps of Markstein's division (div_rcp) without the
+// range check: the caller checks |a| and the result against [1e-30, 1e30].
+PGL_HD float markstein_q(float a, float b, float y) {
+  const float q0 = a * y;
+  return fmaf_(fmaf_(-q0, b, a), y, q0);
+}
+PGL_HD bool in_div_range(float a, float q) {
+  const float aa = a < 0.0f ? -a : a, aq = q < 0.0f ? -q : q;
+  return aa >= 1e-30f && aa <= 1e30f && aq >= 1e-30f && aq <= 1e30f;
+}
+
 // fastapprox::exp
 PGL_HD float fexp(float v) {
   const float ln2Part1 = float(0.6931457519), ln2Part2 = float(1.4286067653e-6);
