@@ -17,7 +17,6 @@
 // summation order (sequential over samples within each SIMD lane), so every
 // accumulator gets the reference's bits.  Scalar per-leaf logic (M step,
 // split/merge bookkeeping) runs on thread 0 between passes.
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -30,18 +29,6 @@ namespace pgl {
 constexpr int kEmThreads = 512;
 constexpr int kStageFloats = 19200;  // floats per pipeline stage (two stages, 150 KB)
 constexpr int kMaxPairs = kMaxK * (kMaxK - 1) / 2;
-
-// A pass as the home block of a cluster publishes it to its helper blocks.
-enum PassCmdKind { kCmdEStep = 0, kCmdDistance = 1, kCmdSplit = 2, kCmdExit = 3 };
-struct PassCmd {
-  int kind;
-  int cnt;  // lobe vectors (K rounded up to 8, divided by 8)
-  const float4 *dirw;
-  const float *pdf;
-  const float *dist;
-  uint32_t count;
-  float mcEstimate;
-};
 
 struct Unassigned {
   float sw, dx, dy, dz;
@@ -74,7 +61,8 @@ struct EmShared {
   int iterations;
   LeafReport report;
   LeafProfile prof;
-  PassCmd cmd;
+  uint32_t validPerWarp[kEmThreads / 32];  // split passes: valid samples per producer warp
+  float splitN0[kMaxK];                     // split passes: chi-square counts at the pass start
 };
 static_assert(offsetof(EmShared, pbuf) % 16 == 0 &&
                   offsetof(EmShared, lobeA) % 16 == 0,
@@ -511,22 +499,22 @@ __device__ void split_merge_stats(SplitState &s, int I, int J, float wI, V3 muI,
 // Every pass over a leaf's samples (E-step, distance pass, split-statistics
 // pass) runs as a two-stage pipeline over chunks of samples, with one
 // __syncthreads per chunk and two shared-memory stages:
-//   producers (threads [0, P)): one sample per thread; all lobe terms of the
-//     sample in registers, its pdf, then the per-(lobe, sample) values of the
-//     pass written to stage (c & 1);
-//   consumers (threads [P, 512)): one thread per accumulator (for example
-//     the x component of lobe 7's weighted direction sum), adding the chunk in
+//   producers (threads [0, C * parts)): `parts` adjacent lanes per sample, one
+//     SIMD vector of 8 lobes each; the lobe terms in registers, the sample pdf
+//     (vfloat8 lane sums carried from part to part in lobe-vector order, then
+//     the 8-lane reduction), then the finished term of every accumulator for
+//     their lobes written to stage (c & 1);
+//   consumers (threads [P, 512)): one thread per accumulator (for example the
+//     x component of lobe 7's weighted direction sum), adding the chunk in
 //     stage ((c - 1) & 1) in sample order.
 // The consumers keep the reference's summation order (sequential over samples
 // within each SIMD lane).  Samples that the reference skips (pdf <= 1e-16)
 // contribute a term of exactly +-0, which leaves an accumulator unchanged:
-// accumulators start at +0 and a round-to-nearest sum that starts at +0
-// never becomes -0.  The producers write each accumulator's finished term,
-// so a consumer lane only loads and adds, and chain warps do not diverge
-// (chi-square lanes have warps of their own).  Each pass
-// gives the consumers only the warps its chains need and the producers the
-// rest; the chunk is one sample per producer thread, bounded by the stage
-// memory.
+// accumulators start at +0 and a round-to-nearest sum that starts at +0 never
+// becomes -0.  Consumer lanes only load and add, so chain warps do not diverge
+// (chi-square lanes have a warp of their own).  Each pass gives the consumers
+// the warps its chains need and the producers the rest; the chunk size
+// follows from the stage memory and the producer threads.
 
 struct LeafSamples {
   const float4 *dirw;  // direction xyz, weight
@@ -539,10 +527,12 @@ enum PassKind { kPassEStep = 0, kPassDistance = 1, kPassSplit = 2 };
 
 // Thread roles and stage layout of one pass (the same in every thread).
 struct PassShape {
-  int P;       // producer threads [0, P); consumers [P, kEmThreads)
-  int C;       // samples per chunk (<= P)
-  int R;       // row stride of the per-(lobe, sample) rows: C + 4 floats
-  int stage;   // floats per stage
+  int P;        // threads [P, kEmThreads) consume
+  int parts;    // producer lanes per sample (lobe vectors, 3 rounded to 4)
+  int C;        // samples per chunk
+  int threads;  // producer threads: C * parts, a multiple of 32
+  int R;        // row stride of the per-(lobe, sample) rows: C + 4 floats
+  int stage;    // floats per stage
 };
 template <PassKind kind>
 __device__ __forceinline__ PassShape pass_shape(int Kp) {
@@ -558,14 +548,21 @@ __device__ __forceinline__ PassShape pass_shape(int Kp) {
     extra = 0;
   } else {  // 5 Kp product chains, then (from a warp boundary) Kp chi-square chains
     consWarps = (5 * Kp + 31) / 32 + 1;
-    rows = 6 * Kp;
-    extra = 1;
+    rows = 7 * Kp;  // a, a w, three covariance terms, chi, 1/n
+    extra = 1;      // validity
   }
   PassShape p;
+  const int cnt = Kp / kLanes;
+  p.parts = cnt == 3 ? 4 : cnt;
   p.P = kEmThreads - 32 * consWarps;
   int c = (kStageFloats - 4 * rows) / (rows + extra);
-  c = c < p.P ? c : p.P;
-  p.C = c & ~31;
+  const int byThreads = p.P / p.parts;
+  c = c < byThreads ? c : byThreads;
+  // C * parts a multiple of 32 (whole warps) and C a multiple of 8 (16-byte
+  // arrays, rows of (C + 4) / 4 odd 16-byte units: conflict-free 128-bit loads)
+  const int mult = 32 / p.parts > 8 ? 32 / p.parts : 8;
+  p.C = c - c % mult;
+  p.threads = p.C * p.parts;
   p.R = p.C + 4;
   p.stage = rows * p.R + extra * p.C;
   return p;
@@ -599,40 +596,53 @@ __device__ void pack_lobes(EmShared &S, int Kp) {
   }
 }
 
-// Producer side of one sample: the E-step terms of all lobes, the sample pdf
-// (vfloat8 lane sums over the lobe vectors, then the 8-lane reduction) and
-// 1/pdf.
-struct SampleTerms {
-  float t[kMaxK];
+// One producer lane's view of a sample: the E-step terms of its 8 lobes
+// (vector v), then the sample pdf and 1/pdf shared by all parts.
+struct PartTerms {
+  float t[kLanes];
   float pdf, inv;
   bool valid;
 };
-__device__ __forceinline__ void sample_terms(const EmShared &S, int cnt, V3 d, SampleTerms &T) {
-  float pv[kLanes];
+__device__ __forceinline__ void part_terms(const EmShared &S, int cnt, int parts, int v, bool have, V3 d,
+                                           PartTerms &T) {
+  const unsigned full = 0xFFFFFFFFu;
+  if (have && v < cnt) {
 #pragma unroll
-  for (int j = 0; j < kLanes; ++j) pv[j] = 0.0f;
+    for (int j = 0; j < kLanes; ++j) {
+      const int k = v * kLanes + j;
+      const float4 A = S.lobeA[k];
+      const float2 B = S.lobeB[k];
+      float ct = dot(d, mk(A.x, A.y, A.z));
+      float cm1 = emin(ct - 1.0f, 0.0f);
+      float ev = B.x * fexp(A.w * cm1);
+      T.t[j] = B.y * ev;
+    }
+  } else {
 #pragma unroll
-  for (int v = 0; v < kMaxK / kLanes; ++v) {
-    if (v < cnt) {
+    for (int j = 0; j < kLanes; ++j) T.t[j] = 0.0f;
+  }
+  // lane sums over the lobe vectors in order: ((t0 + t1) + t2) + t3
+  float p[kLanes];
 #pragma unroll
-      for (int j = 0; j < kLanes; ++j) {
-        const int k = v * kLanes + j;
-        const float4 A = S.lobeA[k];
-        const float2 B = S.lobeB[k];
-        float ct = dot(d, mk(A.x, A.y, A.z));
-        float cm1 = emin(ct - 1.0f, 0.0f);
-        float ev = B.x * fexp(A.w * cm1);
-        T.t[k] = B.y * ev;
-        pv[j] += T.t[k];
-      }
-    } else {
+  for (int j = 0; j < kLanes; ++j) p[j] = T.t[j];
+  for (int step = 1; step < parts; ++step) {
 #pragma unroll
-      for (int j = 0; j < kLanes; ++j) T.t[v * kLanes + j] = 0.0f;
+    for (int j = 0; j < kLanes; ++j) {
+      const float in = __shfl_up_sync(full, p[j], 1);
+      if (v == step) p[j] = in + T.t[j];
     }
   }
-  T.pdf = reduce8(pv);
-  T.valid = T.pdf > 1e-16f;
-  T.inv = T.valid ? rcp_avx2_tab(T.pdf, S.rcpTab) : 0.0f;
+  float pdf = 0.0f, inv = 0.0f;
+  bool valid = false;
+  if (v == parts - 1 && have) {
+    pdf = reduce8(p);
+    valid = pdf > 1e-16f;
+    inv = valid ? rcp_avx2_tab(pdf, S.rcpTab) : 0.0f;
+  }
+  const int last = (int(threadIdx.x & 31) - v) + parts - 1;
+  T.pdf = __shfl_sync(full, pdf, last);
+  T.inv = __shfl_sync(full, inv, last);
+  T.valid = __shfl_sync(full, valid ? 1 : 0, last) != 0;
 }
 
 struct SampleIn {
@@ -654,31 +664,31 @@ __device__ __forceinline__ SampleIn load_sample(const LeafSamples &L, uint32_t i
   return r;
 }
 
-// Producer: fill stage `st` (base pointer B) for the sample in slot s.
+// Producer: lane v of sample slot s fills its lobes' rows of stage B.  In
+// split passes the running count of valid samples (for the chi-square means'
+// 1/n) needs a prefix over the chunk: warp ballots, then a barrier among the
+// producer threads only (named barrier 1), then `base` (valid samples of the
+// earlier chunks) moves on by the chunk's total.
 template <PassKind kind>
-__device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cnt, int Kp, int s, const SampleIn &in,
-                                        float *B) {
-  SampleTerms T;
+__device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cnt, int Kp, int s, int v,
+                                        const SampleIn &in, float *B, uint32_t &base) {
+  PartTerms T;
   const V3 d = mk(in.dw.x, in.dw.y, in.dw.z);
   const float w = in.dw.w;
-  if (in.have) {
-    sample_terms(S, cnt, d, T);
-  } else {
-    T.valid = false;
-    T.pdf = 0.0f;
-    T.inv = 0.0f;
-  }
+  part_terms(S, cnt, sh.parts, v, in.have, d, T);
   const bool valid = in.have && T.valid;
   const int R = sh.R, C = sh.C;
+  const bool mine = v < cnt;  // this lane has lobes
   if constexpr (kind == kPassEStep) {
     // rows q Kp + k: (dx a) w, (dy a) w, (dz a) w, a w; then LL and the
     // unassigned sums per sample
+    if (mine) {
 #pragma unroll
-    for (int k = 0; k < kMaxK; ++k) {
-      if (k < Kp) {
+      for (int j = 0; j < kLanes; ++j) {
+        const int k = v * kLanes + j;
         float px = 0.0f, py = 0.0f, pz = 0.0f, pw = 0.0f;
         if (valid) {
-          const float a = T.t[k] * T.inv;
+          const float a = T.t[j] * T.inv;
           px = (d.x * a) * w;
           py = (d.y * a) * w;
           pz = (d.z * a) * w;
@@ -690,25 +700,28 @@ __device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cn
         B[(3 * Kp + k) * R + s] = pw;
       }
     }
-    float *X = B + 4 * Kp * R;
-    // the log-likelihood only drives the convergence test (its relative
-    // change against 0.005); it is not stored, so the single-precision logf
-    // (<= 1 ulp) stands in for the C library's here
-    X[s] = valid ? w * logf(T.pdf) : 0.0f;
-    const bool un = in.have && !T.valid;
-    X[C + s] = un ? w : 0.0f;
-    X[2 * C + s] = un ? d.x * w : 0.0f;
-    X[3 * C + s] = un ? d.y * w : 0.0f;
-    X[4 * C + s] = un ? d.z * w : 0.0f;
+    if (v == 0) {
+      float *X = B + 4 * Kp * R;
+      // the log-likelihood only drives the convergence test (its relative
+      // change against 0.005); it is not stored, so the single-precision logf
+      // (<= 1 ulp) stands in for the C library's here
+      X[s] = valid ? w * logf(T.pdf) : 0.0f;
+      const bool un = in.have && !T.valid;
+      X[C + s] = un ? w : 0.0f;
+      X[2 * C + s] = un ? d.x * w : 0.0f;
+      X[3 * C + s] = un ? d.y * w : 0.0f;
+      X[4 * C + s] = un ? d.z * w : 0.0f;
+    }
   } else if constexpr (kind == kPassDistance) {
     // rows k: wts * rcp(distance); rows Kp + k: wts
-    const float sd = valid ? rcp_avx2_tab(in.x, S.rcpTab) : 0.0f;
+    if (mine) {
+      const float sd = valid ? rcp_avx2_tab(in.x, S.rcpTab) : 0.0f;
 #pragma unroll
-    for (int k = 0; k < kMaxK; ++k) {
-      if (k < Kp) {
+      for (int j = 0; j < kLanes; ++j) {
+        const int k = v * kLanes + j;
         float wts = 0.0f;
         if (valid) {
-          float a = T.t[k] * T.inv;
+          const float a = T.t[j] * T.inv;
           wts = (w * a) * div_rcp(a * T.pdf, S.lobeB[k].y, S.lobeWInv[k]);
         }
         B[k * R + s] = wts * sd;
@@ -716,20 +729,35 @@ __device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cn
       }
     }
   } else {
-    // rows r Kp + k: a, a w, (a w)(lx lx), (a w)(ly ly), (a w)(lx ly), chi;
-    // then the validity per sample
+    // count of valid samples up to and including this one
+    const unsigned full = 0xFFFFFFFFu;
+    const int lane = int(threadIdx.x & 31), warp = int(threadIdx.x >> 5);
+    const unsigned b = __ballot_sync(full, v == 0 && valid);
+    if (lane == 0) S.validPerWarp[warp] = uint32_t(__popc(b));
+    asm volatile("bar.sync 1, %0;" ::"r"(sh.threads) : "memory");
+    uint32_t before = 0, total = 0;
+    for (int q = 0; q < sh.threads / 32; ++q) {
+      const uint32_t n = S.validPerWarp[q];
+      before += q < warp ? n : 0u;
+      total += n;
+    }
+    const uint32_t count = base + before + uint32_t(__popc(b & ((1u << (lane - v)) - 1u))) + 1u;
+    base += total;
+    // rows r Kp + k: a, a w, (a w)(lx lx), (a w)(ly ly), (a w)(lx ly), chi,
+    // RN(1 / n) with n = n0_k + count; then the validity per sample
     const float spdfv = in.x;
     const float value = w * spdfv;
     const float mcEst = S.mcEstimate;
     // the three divisors are per sample: one reciprocal each, then Markstein
     const float den1 = mcEst * T.pdf, den2 = ((mcEst * mcEst) * T.pdf) * T.pdf;
     const float y1 = rcp_for_div(den1), y2 = rcp_for_div(den2), y3 = rcp_for_div(spdfv);
+    if (mine) {
 #pragma unroll
-    for (int k = 0; k < kMaxK; ++k) {
-      if (k < Kp) {
-        float a = 0.0f, aw = 0.0f, cxx = 0.0f, cyy = 0.0f, cxy = 0.0f, chi = 0.0f;
+      for (int j = 0; j < kLanes; ++j) {
+        const int k = v * kLanes + j;
+        float a = 0.0f, aw = 0.0f, cxx = 0.0f, cyy = 0.0f, cxy = 0.0f, chi = 0.0f, yn = 0.0f;
         if (valid) {
-          a = T.t[k] * T.inv;
+          a = T.t[j] * T.inv;
           float vmf = a * T.pdf;
           float pvp = vmf * value;
           pvp = div_rcp(pvp, den1, y1);
@@ -744,6 +772,8 @@ __device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cn
           cxx = aw * (ld.x * ld.x);
           cyy = aw * (ld.y * ld.y);
           cxy = aw * (ld.x * ld.y);
+          const float n = S.splitN0[k] + float(count);
+          yn = (n >= 1e-30f && n <= 1e30f) ? rcp_rn(n) : 0.0f;
         }
         B[k * R + s] = a;
         B[(Kp + k) * R + s] = aw;
@@ -751,9 +781,10 @@ __device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cn
         B[(3 * Kp + k) * R + s] = cyy;
         B[(4 * Kp + k) * R + s] = cxy;
         B[(5 * Kp + k) * R + s] = chi;
+        B[(6 * Kp + k) * R + s] = yn;
       }
     }
-    B[6 * Kp * R + s] = valid ? 1.0f : 0.0f;
+    if (v == 0) B[7 * Kp * R + s] = valid ? 1.0f : 0.0f;
   }
 }
 
@@ -808,47 +839,51 @@ __device__ __forceinline__ void distance_chain(const float *B, const PassShape &
   if (c < 2 * Kp) row_chain(B + c * sh.R, n4, acc);
 }
 
-// One step of chi2 += (x - chi2) / n with y ~ 1/n (div_faithful_fix); `bad`
-// records a step outside the range where that division is exact.
-__device__ __forceinline__ float chi_step(float acc, float x, float n, float y, float v, bool &bad) {
-  const float num = x - acc;
-  const float q = div_faithful_fix(num, n, y);
-  const float an = fabsf(num), aq = fabsf(q);
-  bad |= (v != 0.0f) && !(an >= 1e-30f && an <= 1e30f && aq >= 1e-30f && aq <= 1e30f) && (num != 0.0f);
-  return v != 0.0f ? acc + q : acc;
-}
-
 // Split-statistics pass (Splitter.h:439-523).  Lanes c < 5 Kp sum row c
 // (r = c / Kp: sumAssignedSamples a, sumWeights a w, then the 2D covariance
 // sums (a w)(lx lx), (a w)(ly ly), (a w)(lx ly)).  Chi-square lanes start at
 // the next warp: the running mean chi2 += (chi - chi2) / n over the valid
-// samples.
+// samples, n counting from n0.  The producers' y = RN(1 / (n0 + count)) holds
+// when that sum equals the lane's own running count n (the usual case);
+// Markstein's steps then give (chi - chi2) / n exactly, and a skipped sample
+// (y = 0) adds +-0.  A group of 4 samples where a count differs or an operand
+// leaves Markstein's range is redone with the division.
 __device__ __forceinline__ int split_chi_base(int Kp) { return ((5 * Kp + 31) / 32) * 32; }
-__device__ __forceinline__ void split_chain(const float *B, const PassShape &sh, int c, int Kp, int n4, float &acc,
-                                            float &accN) {
+__device__ __forceinline__ void split_chain(const float *B, const PassShape &sh, int c, int Kp, int n4, float n0,
+                                            float &acc, float &accN, float &cnt) {
   const int R = sh.R;
   const int chiBase = split_chi_base(Kp);
-  const float *Vr = B + 6 * Kp * R;
   if (c < 5 * Kp) {
     row_chain(B + c * R, n4, acc);
   } else if (c >= chiBase && c < chiBase + Kp) {
-    // the counts and their reciprocals do not depend on chi2: only the
-    // subtract, three FMA-unit operations and the add stay on the chain
     const int k = c - chiBase;
-    const float *cr = B + (5 * Kp + k) * R;
-    float4 x = ld4(cr), v = ld4(Vr);
+    const float *xr = B + (5 * Kp + k) * R, *yr = B + (6 * Kp + k) * R, *vr = B + 7 * Kp * R;
+    float4 x = ld4(xr), y = ld4(yr), v = ld4(vr);
     for (int s = 0; s < n4; s += 4) {
       const int sn = s + 4 < n4 ? s + 4 : s;
-      const float4 x1 = ld4(cr + sn), v1 = ld4(Vr + sn);
+      const float4 x1 = ld4(xr + sn), y1 = ld4(yr + sn), v1 = ld4(vr + sn);
       const float n1 = accN + v.x, n2 = n1 + v.y, n3 = n2 + v.z, n4v = n3 + v.w;
-      const float y1 = rcp_approx(n1), y2 = rcp_approx(n2), y3 = rcp_approx(n3), y4 = rcp_approx(n4v);
+      const float c1 = cnt + v.x, c2 = c1 + v.y, c3 = c2 + v.z, c4 = c3 + v.w;
+      const bool same = (v.x == 0.0f || n1 == n0 + c1) & (v.y == 0.0f || n2 == n0 + c2) &
+                        (v.z == 0.0f || n3 == n0 + c3) & (v.w == 0.0f || n4v == n0 + c4);
       const float acc0 = acc;
-      bool bad = false;
-      acc = chi_step(acc, x.x, n1, y1, v.x, bad);
-      acc = chi_step(acc, x.y, n2, y2, v.y, bad);
-      acc = chi_step(acc, x.z, n3, y3, v.z, bad);
-      acc = chi_step(acc, x.w, n4v, y4, v.w, bad);
-      if (bad) {  // out of the exact range: redo the group with the division
+      const float d1 = x.x - acc;
+      const float q1 = markstein_q(d1, n1, y.x);
+      acc = acc + q1;
+      const float d2 = x.y - acc;
+      const float q2 = markstein_q(d2, n2, y.y);
+      acc = acc + q2;
+      const float d3 = x.z - acc;
+      const float q3 = markstein_q(d3, n3, y.z);
+      acc = acc + q3;
+      const float d4 = x.w - acc;
+      const float q4 = markstein_q(d4, n4v, y.w);
+      acc = acc + q4;
+      const bool bad = !same | (v.x != 0.0f && d1 != 0.0f && !in_div_range(d1, q1)) |
+                       (v.y != 0.0f && d2 != 0.0f && !in_div_range(d2, q2)) |
+                       (v.z != 0.0f && d3 != 0.0f && !in_div_range(d3, q3)) |
+                       (v.w != 0.0f && d4 != 0.0f && !in_div_range(d4, q4));
+      if (bad) {
         acc = acc0;
         if (v.x != 0.0f) acc += (x.x - acc) / n1;
         if (v.y != 0.0f) acc += (x.y - acc) / n2;
@@ -856,70 +891,54 @@ __device__ __forceinline__ void split_chain(const float *B, const PassShape &sh,
         if (v.w != 0.0f) acc += (x.w - acc) / n4v;
       }
       accN = n4v;
+      cnt = c4;
       x = x1;
+      y = y1;
       v = v1;
     }
   }
 }
 
-// Cluster barrier when the region is shared by several blocks, else the
-// block barrier.
-__device__ __forceinline__ void round_sync(unsigned G) {
-  if (G > 1) cooperative_groups::this_cluster().sync();
-  else __syncthreads();
-}
-
-// Runs one pass over the leaf's samples in the home block (cluster rank 0).
-// Chunk c is produced by cluster rank c % G into its stage ((c / G) & 1); the
-// home block's consumers read the G chunks of a round in chunk order, from
-// the helper blocks' shared memory for ranks > 0.  `acc`/`accN` are the
-// consumer's accumulators (initialised by the caller).  With G > 1 the pass
-// is first published to the helpers (PassCmd); home and helpers then run the
-// same number of rounds, each ending at a cluster barrier.
+// Runs one pass over the leaf's samples.  `acc`/`accN` are the consumer's
+// accumulators (initialised by the caller); the producer side is driven here.
 template <PassKind kind>
 __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const PassShape &sh, int cnt, float &acc,
                                       float &accN) {
-  namespace cg = cooperative_groups;
   const int tid = threadIdx.x;
   const int Kp = cnt * kLanes;
   const int C = sh.C;
-  const unsigned G = cg::this_cluster().num_blocks();
-  if (G > 1) {
-    if (tid == 0) S.cmd = PassCmd{int(kind), cnt, L.dirw, L.pdf, L.dist, L.count, S.mcEstimate};
-    cg::this_cluster().sync();
-  }
   const uint32_t numChunks = (L.count + C - 1) / C;
-  const uint32_t rounds = (numChunks + G - 1) / G;
-  const bool producer = tid < C;
+  const bool producer = tid < sh.threads;
+  const int s = tid / sh.parts, v = tid % sh.parts;
   const bool consumer = tid >= sh.P;
   const int c = tid - sh.P;
+  const int chiK = kind == kPassSplit ? c - split_chi_base(Kp) : -1;
+  const float n0 = (chiK >= 0 && chiK < Kp) ? S.splitN0[chiK] : 0.0f;
+  float count = 0.0f;
+  uint32_t base = 0;
   SampleIn next;
-  if (producer) next = load_sample<kind>(L, uint32_t(tid));
+  if (producer) next = load_sample<kind>(L, uint32_t(s));
   long long cycP = 0, cycC = 0;
-  for (uint32_t it = 0; it <= rounds; ++it) {
-    if (producer && it < rounds) {
+  for (uint32_t it = 0; it <= numChunks; ++it) {
+    if (producer && it < numChunks) {
       const long long t0 = clock64();
       const SampleIn cur = next;
-      if (it + 1 < rounds) next = load_sample<kind>(L, (it + 1) * G * C + tid);
-      produce<kind>(S, sh, cnt, Kp, tid, cur, S.pbuf + (it & 1) * sh.stage);
+      if (it + 1 < numChunks) next = load_sample<kind>(L, (it + 1) * C + s);
+      produce<kind>(S, sh, cnt, Kp, s, v, cur, S.pbuf + (it & 1) * sh.stage, base);
       cycP += clock64() - t0;
     }
     if (consumer && it >= 1) {
       const long long t0 = clock64();
-      for (unsigned r = 0; r < G; ++r) {
-        const uint32_t chunk = (it - 1) * G + r;
-        if (chunk >= numChunks) break;
-        const int n = int(min(uint32_t(C), L.count - chunk * C));
-        const int n4 = (n + 3) & ~3;
-        const float *local = S.pbuf + ((it - 1) & 1) * sh.stage;
-        const float *B = r == 0 ? local : cg::this_cluster().map_shared_rank(local, r);
-        if constexpr (kind == kPassEStep) estep_chain(B, sh, c, Kp, n4, acc);
-        else if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
-        else split_chain(B, sh, c, Kp, n4, acc, accN);
-      }
+      const uint32_t prev = it - 1;
+      const int n = int(min(uint32_t(C), L.count - prev * C));
+      const int n4 = (n + 3) & ~3;
+      const float *B = S.pbuf + (prev & 1) * sh.stage;
+      if constexpr (kind == kPassEStep) estep_chain(B, sh, c, Kp, n4, acc);
+      else if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
+      else split_chain(B, sh, c, Kp, n4, n0, acc, accN, count);
       cycC += clock64() - t0;
     }
-    round_sync(G);
+    __syncthreads();
   }
   const int probe = kind == kPassSplit ? split_chi_base(Kp) : 0;
   if (tid == 0) {
@@ -929,60 +948,6 @@ __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const P
   if (c == probe) {
     if (kind == kPassSplit) S.prof.cycConsS += uint64_t(cycC);
     else if (kind == kPassEStep) S.prof.cycConsE += uint64_t(cycC);
-  }
-}
-
-// The producer side of one pass in a helper block (cluster rank r > 0): the
-// same rounds as the home block's run_pass, producing chunks it * G + r.
-template <PassKind kind>
-__device__ __noinline__ void helper_pass(EmShared &S, const PassCmd &cmd, unsigned rank, unsigned G) {
-  const int tid = threadIdx.x;
-  const int Kp = cmd.cnt * kLanes;
-  const PassShape sh = pass_shape<kind>(Kp);
-  const int C = sh.C;
-  const LeafSamples L{cmd.dirw, cmd.pdf, cmd.dist, cmd.count};
-  const uint32_t numChunks = (L.count + C - 1) / C;
-  const uint32_t rounds = (numChunks + G - 1) / G;
-  const bool producer = tid < C;
-  SampleIn next;
-  if (producer) next = load_sample<kind>(L, rank * C + tid);
-  for (uint32_t it = 0; it <= rounds; ++it) {
-    if (producer && it < rounds && it * G + rank < numChunks) {
-      const SampleIn cur = next;
-      if (it + 1 < rounds) next = load_sample<kind>(L, ((it + 1) * G + rank) * C + tid);
-      produce<kind>(S, sh, cmd.cnt, Kp, tid, cur, S.pbuf + (it & 1) * sh.stage);
-    }
-    cooperative_groups::this_cluster().sync();
-  }
-}
-
-// Helper blocks serve the home block's passes until it publishes kCmdExit.
-// Every command costs both sides one cluster barrier to publish, then the
-// pass's rounds; the exit costs a second barrier so that the home block's
-// shared memory outlives the helpers' read of the command.
-__device__ void helper_loop(EmShared &S, unsigned rank, unsigned G) {
-  namespace cg = cooperative_groups;
-  const int tid = threadIdx.x;
-  EmShared *home = cg::this_cluster().map_shared_rank(&S, 0u);
-  for (;;) {
-    cg::this_cluster().sync();
-    const PassCmd cmd = home->cmd;
-    if (cmd.kind == kCmdExit) {
-      cg::this_cluster().sync();
-      return;
-    }
-    const int Kp = cmd.cnt * kLanes;
-    if (tid < Kp) {
-      S.lobeA[tid] = home->lobeA[tid];
-      S.lobeB[tid] = home->lobeB[tid];
-      S.lobeWInv[tid] = home->lobeWInv[tid];
-      S.invFrame[tid] = home->invFrame[tid];
-    }
-    if (tid == 0) S.mcEstimate = cmd.mcEstimate;
-    __syncthreads();
-    if (cmd.kind == kCmdEStep) helper_pass<kPassEStep>(S, cmd, rank, G);
-    else if (cmd.kind == kCmdDistance) helper_pass<kPassDistance>(S, cmd, rank, G);
-    else helper_pass<kPassSplit>(S, cmd, rank, G);
   }
 }
 
@@ -1064,7 +1029,10 @@ __device__ void pass_split_stats(EmShared &S, const LeafSamples &L, SplitState &
   const int cnt = vec_count(int(sp.K));
   const int Kp = cnt * kLanes;
   const PassShape sh = pass_shape<kPassSplit>(Kp);
-  if (tid < Kp) S.invFrame[tid] = inverse_of(frame_of(mk(S.vmm.mx[tid], S.vmm.my[tid], S.vmm.mz[tid]), true));
+  if (tid < Kp) {
+    S.invFrame[tid] = inverse_of(frame_of(mk(S.vmm.mx[tid], S.vmm.my[tid], S.vmm.mz[tid]), true));
+    S.splitN0[tid] = sp.n[tid];
+  }
   pack_lobes(S, Kp);
   __syncthreads();
   const int c = tid - sh.P;
@@ -1398,15 +1366,6 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
   __shared__ uint32_t taskId;
   __shared__ uint64_t afterSplit, afterMerge;
   for (int i = threadIdx.x; i < 2048; i += blockDim.x) S.rcpTab[i] = rcp_seed(uint32_t(i));
-  // a cluster of G blocks shares each region: rank 0 (home) owns it, the
-  // others produce chunks of its passes (helper_loop)
-  const unsigned G = cooperative_groups::this_cluster().num_blocks();
-  const unsigned rank = cooperative_groups::this_cluster().block_rank();
-  if (rank != 0) {
-    __syncthreads();
-    helper_loop(S, rank, G);
-    return;
-  }
   for (;;) {
     if (threadIdx.x == 0) taskId = atomicAdd(queue, 1u);
     __syncthreads();
@@ -1490,11 +1449,6 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
     }
     __syncthreads();
   }
-  if (G > 1) {  // release the helpers (see helper_loop)
-    if (threadIdx.x == 0) S.cmd.kind = kCmdExit;
-    cooperative_groups::this_cluster().sync();
-    cooperative_groups::this_cluster().sync();
-  }
 }
 
 PGL_DEFINE_TABLE_UPLOAD(em_upload_tables)
@@ -1503,7 +1457,7 @@ size_t em_shared_bytes() { return sizeof(EmShared); }
 
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
                       float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
-                      LeafReport *reports, LeafProfile *profiles, int numSMs, int clusterSize, cudaStream_t stream) {
+                      LeafReport *reports, LeafProfile *profiles, int numSMs, cudaStream_t stream) {
   static bool attrSet = false;
   const size_t smem = sizeof(EmShared);
   if (!attrSet) {
@@ -1512,36 +1466,12 @@ cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *qu
     attrSet = true;
   }
   if (numTasks == 0) return cudaSuccess;
-  cudaLaunchConfig_t config = {};
-  config.blockDim = dim3(kEmThreads);
-  config.dynamicSmemBytes = smem;
-  config.stream = stream;
-  cudaLaunchAttribute attr[1];
-  int G = clusterSize < 1 ? 1 : clusterSize;
-  int clusters = 0;
-  if (G > 1) {
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = unsigned(G);
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    config.attrs = attr;
-    config.numAttrs = 1;
-    config.gridDim = dim3(unsigned(G) * unsigned(numSMs / G));
-    if (cudaOccupancyMaxActiveClusters(&clusters, em_leaf_kernel, &config) != cudaSuccess || clusters < 1) {
-      cudaGetLastError();
-      G = 1;  // this cluster shape does not fit: one block per region
-    }
-  }
-  if (G == 1) {
-    config.attrs = nullptr;
-    config.numAttrs = 0;
-    clusters = numSMs;
-  }
-  const unsigned used = unsigned(clusters) < numTasks ? unsigned(clusters) : numTasks;
-  config.gridDim = dim3(used * unsigned(G));
+  // one persistent block per SM (shared memory bound), regions from the queue
+  const unsigned blocks = unsigned(numSMs) < numTasks ? unsigned(numSMs) : numTasks;
   count_launch();
-  return cudaLaunchKernelEx(&config, em_leaf_kernel, tasks, numTasks, queue, regions, pd, dirw, pdf, dist, cfg,
-                            uniformDirs, reports, profiles);
+  em_leaf_kernel<<<blocks, kEmThreads, smem, stream>>>(tasks, numTasks, queue, regions, pd, dirw, pdf, dist, cfg,
+                                                       uniformDirs, reports, profiles);
+  return cudaGetLastError();
 }
 
 }  // namespace pgl

@@ -466,20 +466,6 @@ void SubField::renumber(uint32_t oldNodes, uint32_t oldRegions) {
   regionOrigin_.swap(no);
 }
 
-// Blocks per region of the EM launch (a thread-block cluster shares the
-// region's sample passes).  One by default: helper blocks pay off only when
-// their chunks reach the home block faster than it sums them.
-// PGL_EM_CLUSTER=1,2,4,8 fixes the size (tuning and tests).
-int em_cluster_size(uint32_t regions, int numSMs) {
-  (void)regions;
-  (void)numSMs;
-  if (const char *env = std::getenv("PGL_EM_CLUSTER")) {
-    const int g = std::atoi(env);
-    if (g == 1 || g == 2 || g == 4 || g == 8) return g;
-  }
-  return 1;
-}
-
 void SubField::update(SampleSide &in) {
   Context &c = Context::get();
   const uint32_t n = uint32_t(in.n);
@@ -615,7 +601,7 @@ void SubField::update(SampleSide &in) {
   check(cudaEventRecord(ev[4], c.stream), "event");
   if (cfg.fitRegions) {
     check(launch_em(tasks_.p, R, queue_.p, dRegions.p, sP_.p, sD_.p, sPdf_.p, dist_.p, cfg, dUniformDirs.p, reports_.p,
-                    profiles_.p, c.numSMs, em_cluster_size(R, c.numSMs), c.stream),
+                    profiles_.p, c.numSMs, c.stream),
           "em");
   }
   check(cudaEventRecord(ev[3], c.stream), "event");

@@ -60,8 +60,7 @@ cudaError_t build_knn(const float4 *means, uint32_t R, Neighbours *out, cudaStre
 size_t em_shared_bytes();
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
                       float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
-                      LeafReport *reports, LeafProfile *profiles, int numSMs, int clusterSize,
-                      cudaStream_t stream);
+                      LeafReport *reports, LeafProfile *profiles, int numSMs, cudaStream_t stream);
 
 cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s);
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,
