@@ -43,7 +43,7 @@ struct EmShared {
   SplitState lsplit;  // split statistics used by the recursive splitting
   Frame invFrame[kMaxK];
   __align__(16) float pbuf[2 * kStageFloats];  // the two pipeline stages
-  __align__(16) float4 lobeA[kMaxK];  // mean direction, kappa
+  __align__(16) float4 lobeA[kMaxK + kMaxK / kLanes];  // mean direction, kappa (entry k + k / 8)
   float2 lobeB[kMaxK];                // normalisation, weight
   float lobeWInv[kMaxK];              // RN(1 / weight) for div_rcp
   float xch[2][kMaxK];
@@ -531,7 +531,7 @@ struct PassShape {
   int parts;    // producer lanes per sample (lobe vectors, 3 rounded to 4)
   int C;        // samples per chunk
   int threads;  // producer threads: C * parts, a multiple of 32
-  int R;        // row stride of the per-(lobe, sample) rows: C + 4 floats
+  int R;        // row stride of the per-(lobe, sample) rows: C + 2 floats
   int stage;    // floats per stage
 };
 template <PassKind kind>
@@ -555,15 +555,17 @@ __device__ __forceinline__ PassShape pass_shape(int Kp) {
   const int cnt = Kp / kLanes;
   p.parts = cnt == 3 ? 4 : cnt;
   p.P = kEmThreads - 32 * consWarps;
-  int c = (kStageFloats - 4 * rows) / (rows + extra);
+  int c = (kStageFloats - 2 * rows) / (rows + extra);
   const int byThreads = p.P / p.parts;
   c = c < byThreads ? c : byThreads;
-  // C * parts a multiple of 32 (whole warps) and C a multiple of 8 (16-byte
-  // arrays, rows of (C + 4) / 4 odd 16-byte units: conflict-free 128-bit loads)
+  // C * parts a multiple of 32 (whole warps) and C a multiple of 8.  Rows of
+  // C + 2 floats: (C + 2) / 2 is odd, so the consumers' 64-bit loads of
+  // consecutive rows fall in distinct banks, and rows 8 apart are 16 banks
+  // apart, so two parts of a sample store to distinct banks.
   const int mult = 32 / p.parts > 8 ? 32 / p.parts : 8;
   p.C = c - c % mult;
   p.threads = p.C * p.parts;
-  p.R = p.C + 4;
+  p.R = p.C + 2;
   p.stage = rows * p.R + extra * p.C;
   return p;
 }
@@ -590,7 +592,8 @@ __device__ void pack_lobes(EmShared &S, int Kp) {
   const int tid = threadIdx.x;
   if (tid < Kp) {
     const VMMState &v = S.vmm;
-    S.lobeA[tid] = make_float4(v.mx[tid], v.my[tid], v.mz[tid], v.kappa[tid]);
+    // entry k + k / 8: the parts of a sample read lobes k and k + 8 at once
+    S.lobeA[tid + (tid >> 3)] = make_float4(v.mx[tid], v.my[tid], v.mz[tid], v.kappa[tid]);
     S.lobeB[tid] = make_float2(v.norm[tid], v.w[tid]);
     S.lobeWInv[tid] = rcp_for_div(v.w[tid]);
   }
@@ -610,7 +613,7 @@ __device__ __forceinline__ void part_terms(const EmShared &S, int cnt, int parts
 #pragma unroll
     for (int j = 0; j < kLanes; ++j) {
       const int k = v * kLanes + j;
-      const float4 A = S.lobeA[k];
+      const float4 A = S.lobeA[k + v];
       const float2 B = S.lobeB[k];
       float ct = dot(d, mk(A.x, A.y, A.z));
       float cm1 = emin(ct - 1.0f, 0.0f);
@@ -788,7 +791,11 @@ __device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cn
   }
 }
 
-__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ float4 ld4(const float *p) {  // two 64-bit loads (rows are 8-byte aligned)
+  const float2 a = ld2(p), b = ld2(p + 2);
+  return make_float4(a.x, a.y, b.x, b.y);
+}
 
 // Sum of one row (the terms of one accumulator) in sample order; loads run 8
 // samples ahead of the additions.
