@@ -1465,13 +1465,12 @@ size_t em_shared_bytes() { return sizeof(EmShared); }
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
                       float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
                       LeafReport *reports, LeafProfile *profiles, int numSMs, cudaStream_t stream) {
-  static bool attrSet = false;
   const size_t smem = sizeof(EmShared);
-  if (!attrSet) {
-    cudaError_t e = cudaFuncSetAttribute(em_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    attrSet = true;
-  }
+  // once per process (thread-safe static initialisation: the surface and
+  // volume fields may launch concurrently)
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(em_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (attr != cudaSuccess) return attr;
   if (numTasks == 0) return cudaSuccess;
   // one persistent block per SM (shared memory bound), regions from the queue
   const unsigned blocks = unsigned(numSMs) < numTasks ? unsigned(numSMs) : numTasks;

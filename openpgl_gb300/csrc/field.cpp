@@ -8,7 +8,9 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <numeric>
+#include <thread>
 
 namespace pgl {
 
@@ -17,17 +19,17 @@ void check(cudaError_t e, const char *what) {
 }
 
 Context &Context::get() {
-  static Context c;
-  static bool init = false;
-  if (!init) {
-    check(cudaGetDevice(&c.device), "cudaGetDevice");
-    check(cudaDeviceGetAttribute(&c.numSMs, cudaDevAttrMultiProcessorCount, c.device), "SM count");
-    check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
+  // thread-safe one-time set-up (C++ static initialisation)
+  static Context c = [] {
+    Context x;
+    check(cudaGetDevice(&x.device), "cudaGetDevice");
+    check(cudaDeviceGetAttribute(&x.numSMs, cudaDevAttrMultiProcessorCount, x.device), "SM count");
+    check(cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking), "stream");
     check(em_upload_tables(), "tables (em)");
     check(spatial_upload_tables(), "tables (spatial)");
     check(query_upload_tables(), "tables (query)");
-    init = true;
-  }
+    return x;
+  }();
   return c;
 }
 
@@ -297,7 +299,6 @@ static inline bool is_leaf(const KDNode &n) { return (n.bits >> 30) == 3u; }
 static inline uint32_t child_of(const KDNode &n) { return n.bits & 0x3FFFFFFFu; }
 
 void SubField::buildTree(uint32_t n, const float4 *P) {
-  Context &c = Context::get();
   struct Front {
     uint32_t node, depth;
     float b[6];
@@ -310,17 +311,17 @@ void SubField::buildTree(uint32_t n, const float4 *P) {
     KdJob j{};
     quant_frame(kdBounds, j.c, j.inv);
     acc_.reserve(1);
-    check(init_acc(acc_.p, 1, c.stream), "init acc");
-    check(kd_root_stats(posA_.p, n, j, acc_.p, c.stream), "root stats");
+    check(init_acc(acc_.p, 1, stream()), "init acc");
+    check(kd_root_stats(posA_.p, n, j, acc_.p, stream()), "root stats");
     IStatsAcc a;
-    check(cudaMemcpyAsync(&a, acc_.p, sizeof(a), cudaMemcpyDeviceToHost, c.stream), "D2H");
-    check(cudaStreamSynchronize(c.stream), "sync");
+    check(cudaMemcpyAsync(&a, acc_.p, sizeof(a), cudaMemcpyDeviceToHost, stream()), "D2H");
+    check(cudaStreamSynchronize(stream()), "sync");
     rootStats = stats_from_acc(a, kdBounds);
   }
   Front root{0, 1, {}, 0, n, rootStats};
   std::memcpy(root.b, kdBounds, 24);
   front.push_back(root);
-  check(cudaMemsetAsync(node_.p, 0, size_t(n) * 4, c.stream), "node ids");
+  check(cudaMemsetAsync(node_.p, 0, size_t(n) * 4, stream()), "node ids");
 
   std::vector<KdJob> jobs;
   std::vector<const Front *> jobFront;
@@ -383,22 +384,22 @@ void SubField::buildTree(uint32_t n, const float4 *P) {
     jobs_.reserve(jobs.size());
     nodeToJob_.reserve(nodeToJob.size());
     acc_.reserve(2 * jobs.size());
-    check(cudaMemcpyAsync(jobs_.p, jobs.data(), jobs.size() * sizeof(KdJob), cudaMemcpyHostToDevice, c.stream), "jobs");
-    check(cudaMemcpyAsync(nodeToJob_.p, nodeToJob.data(), nodeToJob.size() * 4, cudaMemcpyHostToDevice, c.stream),
+    check(cudaMemcpyAsync(jobs_.p, jobs.data(), jobs.size() * sizeof(KdJob), cudaMemcpyHostToDevice, stream()), "jobs");
+    check(cudaMemcpyAsync(nodeToJob_.p, nodeToJob.data(), nodeToJob.size() * 4, cudaMemcpyHostToDevice, stream()),
           "node map");
-    check(kd_job_of(node_.p, n, nodeToJob_.p, jobOf_.p, c.stream), "job of");
-    check(init_acc(acc_.p, uint32_t(2 * jobs.size()), c.stream), "init acc");
+    check(kd_job_of(node_.p, n, nodeToJob_.p, jobOf_.p, stream()), "job of");
+    check(init_acc(acc_.p, uint32_t(2 * jobs.size()), stream()), "init acc");
     check(kd_level(posA_.p, jobOf_.p, n, jobs_.p, isLeft_.p, scanLeft_.p, acc_.p, posB_.p, nodeB_.p, scratch_,
-                   c.stream),
+                   stream()),
           "kd level");
     std::swap(posA_.p, posB_.p);
     std::swap(posA_.cap, posB_.cap);
     std::swap(node_.p, nodeB_.p);
     std::swap(node_.cap, nodeB_.cap);
     acc.resize(2 * jobs.size());
-    check(cudaMemcpyAsync(acc.data(), acc_.p, acc.size() * sizeof(IStatsAcc), cudaMemcpyDeviceToHost, c.stream),
+    check(cudaMemcpyAsync(acc.data(), acc_.p, acc.size() * sizeof(IStatsAcc), cudaMemcpyDeviceToHost, stream()),
           "D2H acc");
-    check(cudaStreamSynchronize(c.stream), "sync");
+    check(cudaStreamSynchronize(stream()), "sync");
     std::vector<Front> next;
     next.reserve(2 * jobs.size());
     for (size_t k = 0; k < jobs.size(); ++k) {
@@ -478,7 +479,7 @@ void SubField::update(SampleSide &in) {
   }
   cudaEvent_t ev[5];
   for (auto &e : ev) check(cudaEventCreate(&e), "event");
-  check(cudaEventRecord(ev[0], c.stream), "event");
+  check(cudaEventRecord(ev[0], stream()), "event");
   const bool first = !initialized;
   if (first) {
     iteration = 0;
@@ -489,16 +490,16 @@ void SubField::update(SampleSide &in) {
   for (DevArray<uint32_t> *a : {&node_, &nodeB_, &jobOf_, &isLeft_, &scanLeft_}) a->reserve(n);
   keys_.reserve(2 * size_t(n));
   vals_.reserve(2 * size_t(n));
-  check(init_posidx(in.P.p, n, posA_.p, c.stream), "copy samples");
-  check(cudaEventRecord(ev[1], c.stream), "event");
+  check(init_posidx(in.P.p, n, posA_.p, stream()), "copy samples");
+  check(cudaEventRecord(ev[1], stream()), "event");
 
   if (first) {
     if (!boundsSet) {  // Field.h:326-344
       bounds6_.reserve(6);
-      check(scene_bounds(in.P.p, n - 1, bounds6_.p, c.stream), "bounds");
+      check(scene_bounds(in.P.p, n - 1, bounds6_.p, stream()), "bounds");
       uint32_t o[6];
-      check(cudaMemcpyAsync(o, bounds6_.p, sizeof(o), cudaMemcpyDeviceToHost, c.stream), "D2H");
-      check(cudaStreamSynchronize(c.stream), "sync");
+      check(cudaMemcpyAsync(o, bounds6_.p, sizeof(o), cudaMemcpyDeviceToHost, stream()), "D2H");
+      check(cudaStreamSynchronize(stream()), "sync");
       float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {FLT_MIN, FLT_MIN, FLT_MIN};
       if (n > 1)
         for (int d = 0; d < 3; ++d) {
@@ -524,7 +525,7 @@ void SubField::update(SampleSide &in) {
     regions.assign(1, RegionHost());
     std::memcpy(regions[0].bounds, sceneBounds, 24);
     dRegions.reserve(1);
-    check(cudaMemsetAsync(dRegions.p, 0, sizeof(RegionDir), c.stream), "region 0");
+    check(cudaMemsetAsync(dRegions.p, 0, sizeof(RegionDir), stream()), "region 0");
   }
   const uint32_t oldNodes = uint32_t(nodes.size()), oldRegions = uint32_t(regions.size());
   splitNodes_.clear();
@@ -540,8 +541,8 @@ void SubField::update(SampleSide &in) {
       idx[(R - oldRegions) + k] = regionOrigin_[k];
     }
     copyIdx_.reserve(idx.size());
-    check(cudaMemcpyAsync(copyIdx_.p, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, c.stream), "copy idx");
-    check(copy_regions(dRegions.p, copyIdx_.p, copyIdx_.p + (R - oldRegions), R - oldRegions, c.stream), "copy");
+    check(cudaMemcpyAsync(copyIdx_.p, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, stream()), "copy idx");
+    check(copy_regions(dRegions.p, copyIdx_.p, copyIdx_.p + (R - oldRegions), R - oldRegions, stream()), "copy");
   }
   if (cfg.knn) {  // Field.h:362-387 -> KNN.h:189-266
     std::vector<float4> m(R);
@@ -549,13 +550,13 @@ void SubField::update(SampleSide &in) {
                                                         regions[r].stats.mean[2], 0.0f);
     means_.reserve(R);
     dNbrs.reserve(R);
-    check(cudaMemcpyAsync(means_.p, m.data(), R * sizeof(float4), cudaMemcpyHostToDevice, c.stream), "means");
-    check(build_knn(means_.p, R, dNbrs.p, c.stream), "knn");
+    check(cudaMemcpyAsync(means_.p, m.data(), R * sizeof(float4), cudaMemcpyHostToDevice, stream()), "means");
+    check(build_knn(means_.p, R, dNbrs.p, stream()), "knn");
   }
   dNodes.reserve(nodes.size());
-  check(cudaMemcpyAsync(dNodes.p, nodes.data(), nodes.size() * sizeof(KDNode), cudaMemcpyHostToDevice, c.stream),
+  check(cudaMemcpyAsync(dNodes.p, nodes.data(), nodes.size() * sizeof(KDNode), cudaMemcpyHostToDevice, stream()),
         "nodes");
-  check(cudaEventRecord(ev[2], c.stream), "event");
+  check(cudaEventRecord(ev[2], stream()), "event");
 
   // leaves in sample order, then the per-leaf deterministic order
   std::vector<uint32_t> leafRegions;
@@ -571,9 +572,9 @@ void SubField::update(SampleSide &in) {
     seg[2 * L + k] = uint32_t(regions[leafRegions[k]].re - regions[leafRegions[k]].rb);
   }
   leafSeg_.reserve(seg.size());
-  check(cudaMemcpyAsync(leafSeg_.p, seg.data(), seg.size() * 4, cudaMemcpyHostToDevice, c.stream), "segments");
+  check(cudaMemcpyAsync(leafSeg_.p, seg.data(), seg.size() * 4, cudaMemcpyHostToDevice, stream()), "segments");
   check(gather_and_order(posA_.p, n, in.P.p, in.D.p, in.pdf.p, leafSeg_.p, leafSeg_.p + 2 * L, L, cfg.deterministic,
-                         tmpP_.p, tmpD_.p, tmpPdf_.p, keys_.p, vals_.p, sP_.p, sD_.p, sPdf_.p, scratch_, c.stream),
+                         tmpP_.p, tmpD_.p, tmpPdf_.p, keys_.p, vals_.p, sP_.p, sD_.p, sPdf_.p, scratch_, stream()),
         "gather");
 
   // directional fit / update of every region (Field.h:389-511)
@@ -595,23 +596,23 @@ void SubField::update(SampleSide &in) {
   reports_.reserve(R);
   profiles_.reserve(R);
   queue_.reserve(1);
-  check(cudaMemcpyAsync(tasks_.p, tasks.data(), R * sizeof(LeafTask), cudaMemcpyHostToDevice, c.stream), "tasks");
-  check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), c.stream), "queue");
+  check(cudaMemcpyAsync(tasks_.p, tasks.data(), R * sizeof(LeafTask), cudaMemcpyHostToDevice, stream()), "tasks");
+  check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), stream()), "queue");
   ensureUniformDirs();
-  check(cudaEventRecord(ev[4], c.stream), "event");
+  check(cudaEventRecord(ev[4], stream()), "event");
   if (cfg.fitRegions) {
     check(launch_em(tasks_.p, R, queue_.p, dRegions.p, sP_.p, sD_.p, sPdf_.p, dist_.p, cfg, dUniformDirs.p, reports_.p,
-                    profiles_.p, c.numSMs, c.stream),
+                    profiles_.p, c.numSMs, stream()),
           "em");
   }
-  check(cudaEventRecord(ev[3], c.stream), "event");
+  check(cudaEventRecord(ev[3], stream()), "event");
   lastReports.resize(R);
   lastProfiles.resize(R);
-  check(cudaMemcpyAsync(lastProfiles.data(), profiles_.p, R * sizeof(LeafProfile), cudaMemcpyDeviceToHost, c.stream),
+  check(cudaMemcpyAsync(lastProfiles.data(), profiles_.p, R * sizeof(LeafProfile), cudaMemcpyDeviceToHost, stream()),
         "profiles");
-  check(cudaMemcpyAsync(lastReports.data(), reports_.p, R * sizeof(LeafReport), cudaMemcpyDeviceToHost, c.stream),
+  check(cudaMemcpyAsync(lastReports.data(), reports_.p, R * sizeof(LeafReport), cudaMemcpyDeviceToHost, stream()),
         "reports");
-  check(cudaStreamSynchronize(c.stream), "update");
+  check(cudaStreamSynchronize(stream()), "update");
   lastReportRegion.resize(R);
   for (uint32_t k = 0; k < R; ++k) lastReportRegion[k] = tasks[k].region;
   float ms[6];
@@ -684,8 +685,31 @@ GpuField::GpuField(const FieldConfig &cfg) {
 
 void GpuField::update(Storage &s, bool doSurface, bool doVolume) {  // SurfaceVolumeField.h:102-148
   s.flush();
-  if (doSurface && s.surf.n > 0) surface.update(s.surf);
-  if (doVolume && s.vol.n > 0) volume.update(s.vol);
+  const bool surf = doSurface && s.surf.n > 0, vol = doVolume && s.vol.n > 0;
+  if (surf && vol) {
+    // the two fields are independent: each runs on its own stream from its
+    // own host thread, so their kernels overlap on the GPU
+    std::exception_ptr err;
+    std::thread t([&] {
+      try {
+        volume.update(s.vol);
+      } catch (...) {
+        err = std::current_exception();
+      }
+    });
+    try {
+      surface.update(s.surf);
+    } catch (...) {
+      t.join();
+      throw;
+    }
+    t.join();
+    if (err) std::rethrow_exception(err);
+  } else if (surf) {
+    surface.update(s.surf);
+  } else if (vol) {
+    volume.update(s.vol);
+  }
   iteration++;
 }
 

@@ -90,6 +90,17 @@ struct UpdateTimings {
 
 class SubField {
  public:
+  // The stream this field's Update runs on (created on first use).
+  cudaStream_t stream() {
+    if (!stream_) check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "field stream");
+    return stream_;
+  }
+  ~SubField() {
+    if (stream_) cudaStreamDestroy(stream_);
+  }
+  SubField() = default;
+  SubField(const SubField &) = delete;
+  SubField &operator=(const SubField &) = delete;
   FieldConfig cfg;
   bool isSurface = true;
   uint64_t iteration = 0, totalSPP = 0;
@@ -101,6 +112,7 @@ class SubField {
   UpdateTimings timings;
   std::vector<LeafReport> lastReports;
   std::vector<LeafProfile> lastProfiles;
+  cudaStream_t stream_ = nullptr;
   std::vector<uint32_t> lastReportRegion;
 
   DevArray<RegionDir> dRegions;
