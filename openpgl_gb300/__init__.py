@@ -280,6 +280,15 @@ class Field:
         self.h = self.lib.pglDeviceNewField(device.h, config.args)
         _check(self.h, "pglDeviceNewField")
 
+    @classmethod
+    def from_file(cls, device, path):
+        """pglDeviceNewFieldFromFile: a field from a file in the reference's layout."""
+        f = cls.__new__(cls)
+        f.lib = load()
+        f.h = f.lib.pglDeviceNewFieldFromFile(device.h, os.fsencode(path))
+        _check(f.h, "pglDeviceNewFieldFromFile")
+        return f
+
     def update(self, storage):
         self.lib.pglFieldUpdate(self.h, storage.h)
         err = last_error()

@@ -9,6 +9,8 @@
 #include <cstring>
 #include <fstream>
 #include <iostream>
+#include <iterator>
+#include <memory>
 #include <sstream>
 #include <string>
 
@@ -166,9 +168,23 @@ OPENPGL_CORE_INTERFACE PGLField pglDeviceNewField(PGLDevice device, PGLFieldArgu
   return reinterpret_cast<PGLField>(new GpuField(config_from(args)));
   PGL_CATCH(nullptr)
 }
-OPENPGL_CORE_INTERFACE PGLField pglDeviceNewFieldFromFile(PGLDevice, const char *) {
+// Device::newFieldFromFile (Device.h:217-260): the reference's file layout
+// (VecSize 8 lanes), kd-tree fields with parallax-aware VMMs.
+OPENPGL_CORE_INTERFACE PGLField pglDeviceNewFieldFromFile(PGLDevice device, const char *fieldFileName) {
   PGL_TRY
-  throw std::runtime_error("loading a field from a file is not supported by the GPU library yet");
+  if (!device) throw std::runtime_error("null handle provided to pglDeviceNewFieldFromFile");
+  if (!fieldFileName) throw std::runtime_error("null string provided to pglDeviceNewFieldFromFile");
+  std::ifstream in(fieldFileName, std::ios::binary);
+  if (!in) throw std::runtime_error("error: couldn't open file");
+  std::string bytes((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+  // settings the file does not hold keep the defaults of a new field
+  FieldConfig c;
+  c.maxKappaSplit = 32000.0f;
+  c.maxMeanCosineSplit = kappa_to_mean_cosine(32000.0f);
+  c.laneWidth = 8;
+  std::unique_ptr<GpuField> f(new GpuField(c));
+  f->deserialize(bytes);
+  return reinterpret_cast<PGLField>(f.release());
   PGL_CATCH(nullptr)
 }
 

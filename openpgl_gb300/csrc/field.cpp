@@ -663,6 +663,25 @@ std::vector<RegionDir> SubField::downloadRegions() const {
   return r;
 }
 
+// Device copies of the tree and the region neighbours after a load.
+void SubField::uploadTree() {
+  cudaStream_t st = stream();
+  dNodes.reserve(std::max<size_t>(nodes.size(), 1));
+  if (!nodes.empty())
+    check(cudaMemcpyAsync(dNodes.p, nodes.data(), nodes.size() * sizeof(KDNode), cudaMemcpyHostToDevice, st), "nodes");
+  const uint32_t R = uint32_t(regions.size());
+  if (cfg.knn && R > 0) {
+    std::vector<float4> m(R);
+    for (uint32_t i = 0; i < R; ++i)
+      m[i] = make_float4(regions[i].stats.mean[0], regions[i].stats.mean[1], regions[i].stats.mean[2], 0.0f);
+    means_.reserve(R);
+    dNbrs.reserve(R);
+    check(cudaMemcpyAsync(means_.p, m.data(), R * sizeof(float4), cudaMemcpyHostToDevice, st), "means");
+    check(build_knn(means_.p, R, dNbrs.p, st), "knn");
+  }
+  check(cudaStreamSynchronize(st), "load");
+}
+
 void SubField::uploadRegions(const std::vector<RegionDir> &r) {
   if (r.empty()) return;
   dRegions.reserve(r.size());
@@ -854,6 +873,137 @@ void write_sub(Writer &w, const SubField &f) {  // Field::serialize (Field.h:240
     }
   }
 }
+// Reader of the same layout; a short or malformed file throws.
+struct Reader {
+  const std::string &b;
+  size_t o = 0;
+  explicit Reader(const std::string &buf) : b(buf) {}
+  void raw(void *p, size_t n) {
+    if (o + n > b.size()) throw std::runtime_error("field file is truncated");
+    std::memcpy(p, b.data() + o, n);
+    o += n;
+  }
+  template <typename T>
+  T get() {
+    T v;
+    raw(&v, sizeof(T));
+    return v;
+  }
+  void lanes(float *a, int v) { raw(a + v * kLanes, sizeof(float) * kLanes); }
+};
+void read_sub(Reader &r, SubField &f) {  // Field::deserialize (Field.h:269-301), CPU_8 lane layout
+  FieldConfig &c = f.cfg;
+  f.isSurface = r.get<uint8_t>() != 0;
+  c.decayOnSpatialSplit = r.get<float>();
+  f.iteration = r.get<uint64_t>();
+  f.totalSPP = r.get<uint64_t>();
+  c.deterministic = r.get<uint8_t>() != 0;
+  c.fitRegions = r.get<uint8_t>() != 0;
+  f.boundsSet = r.get<uint8_t>() != 0;
+  r.raw(f.sceneBounds, 24);
+  f.initialized = r.get<uint8_t>() != 0;
+  float t[4];
+  r.raw(t, 16);  // timings of the last update
+  c.initK = uint32_t(r.get<uint64_t>());
+  c.initKappa = r.get<float>();
+  c.maxK = uint32_t(r.get<uint64_t>());
+  c.maxIter = uint32_t(r.get<uint64_t>());
+  c.maxKappa = r.get<float>();
+  c.maxMeanCosine = r.get<float>();
+  c.convergence = r.get<float>();
+  c.weightPrior = r.get<float>();
+  c.mcPriorStrength = r.get<float>();
+  c.mcPrior = r.get<float>();
+  c.splitThreshold = r.get<float>();
+  c.mergeThreshold = r.get<float>();
+  c.partialReFit = r.get<uint8_t>() != 0;
+  c.maxSplitItr = r.get<int32_t>();
+  c.minSplit = r.get<int32_t>();
+  c.minMerge = r.get<int32_t>();
+  c.minRefit = r.get<int32_t>();
+  c.minSamples = r.get<uint64_t>();
+  c.maxSamples = r.get<uint64_t>();
+  c.maxDepth = r.get<uint64_t>();
+  f.kdInit = r.get<uint8_t>() != 0;
+  r.raw(f.kdBounds, 24);
+  const uint64_t numNodes = r.get<uint64_t>();
+  if (numNodes > (uint64_t(1) << 30)) throw std::runtime_error("field file: bad node count");
+  f.nodes.resize(numNodes);
+  for (KDNode &n : f.nodes) {
+    n.split = r.get<float>();
+    n.bits = r.get<uint32_t>();
+  }
+  const uint64_t numRegions = r.get<uint64_t>();
+  if (numRegions > (uint64_t(1) << 30)) throw std::runtime_error("field file: bad region count");
+  std::vector<RegionDir> dir(numRegions);
+  f.regions.assign(numRegions, RegionHost());
+  for (size_t i = 0; i < numRegions; ++i) {
+    RegionDir &d = dir[i];
+    std::memset(static_cast<void *>(&d), 0, sizeof(RegionDir));
+    RegionHost &h = f.regions[i];
+    d.valid = r.get<uint8_t>() != 0;
+    for (int v = 0; v < kMaxK / kLanes; ++v) {
+      r.lanes(d.vmm.w, v);
+      r.lanes(d.vmm.kappa, v);
+      r.lanes(d.vmm.mx, v);
+      r.lanes(d.vmm.my, v);
+      r.lanes(d.vmm.mz, v);
+      r.lanes(d.vmm.norm, v);
+      r.lanes(d.vmm.e2k, v);
+      r.lanes(d.vmm.mc, v);
+      r.lanes(d.vmm.dist, v);
+    }
+    d.vmm.K = uint32_t(r.get<uint64_t>());
+    r.raw(d.vmm.pivot, 12);
+    r.raw(h.bounds, 24);
+    for (int v = 0; v < kMaxK / kLanes; ++v) {
+      r.lanes(d.suff.dx, v);
+      r.lanes(d.suff.dy, v);
+      r.lanes(d.suff.dz, v);
+      r.lanes(d.suff.w, v);
+      r.lanes(d.suff.dw, v);
+    }
+    d.suff.sumWeights = r.get<float>();
+    d.suff.numSamples = r.get<float>();
+    d.suff.overallNumSamples = r.get<float>();
+    d.suff.K = uint32_t(r.get<uint64_t>());
+    d.suff.normalized = r.get<uint8_t>() != 0;
+    for (int v = 0; v < kMaxK / kLanes; ++v) {
+      r.lanes(d.split.chi2, v);
+      r.lanes(d.split.mx, v);
+      r.lanes(d.split.my, v);
+      r.lanes(d.split.cx, v);
+      r.lanes(d.split.cy, v);
+      r.lanes(d.split.cz, v);
+      r.lanes(d.split.n, v);
+      r.lanes(d.split.sw, v);
+      r.lanes(d.split.sa, v);
+    }
+    d.split.K = uint32_t(r.get<uint64_t>());
+    d.afterSplit = r.get<uint64_t>();
+    d.afterMerge = r.get<uint64_t>();
+    r.raw(h.stats.mean, 12);
+    r.raw(h.stats.var, 12);
+    h.stats.n = r.get<float>();
+    r.raw(h.stats.lo, 12);
+    r.raw(h.stats.hi, 12);
+    h.splitFlag = r.get<uint8_t>() != 0;
+    h.rb = r.get<uint64_t>();
+    h.re = r.get<uint64_t>();
+    if (d.vmm.K > uint32_t(kMaxK) || d.suff.K > uint32_t(kMaxK) || d.split.K > uint32_t(kMaxK))
+      throw std::runtime_error("field file: more than 32 lobes");
+  }
+  for (const KDNode &n : f.nodes)
+    if (child_of(n) >= (is_leaf(n) ? numRegions : numNodes)) throw std::runtime_error("field file: bad tree");
+  c.knn = r.get<uint8_t>() != 0;
+  if (r.get<uint8_t>() != 0) {  // KNN points (the region means), rebuilt below
+    const uint32_t np = r.get<uint32_t>();
+    std::vector<float> pts(size_t(np) * 4);
+    r.raw(pts.data(), pts.size() * sizeof(float));
+  }
+  f.uploadRegions(dir);
+  f.uploadTree();
+}
 }  // namespace
 
 std::string GpuField::serialize() const {  // SurfaceVolumeField::storeToFile (SurfaceVolumeField.h:171-214)
@@ -867,6 +1017,21 @@ std::string GpuField::serialize() const {  // SurfaceVolumeField::storeToFile (S
   write_sub(w, surface);
   write_sub(w, volume);
   return w.b;
+}
+
+void GpuField::deserialize(const std::string &bytes) {  // Device::newFieldFromFile (Device.h:217-260)
+  Reader r(bytes);
+  char hdr[sizeof("OPENPGL_0.6.0_FIELD")];
+  r.raw(hdr, sizeof(hdr));
+  if (std::memcmp(hdr, "OPENPGL_0.6.0_FIELD", sizeof(hdr)) != 0) throw std::runtime_error("not an Open PGL 0.6.0 field file");
+  const int32_t spatial = r.get<int32_t>(), directional = r.get<int32_t>();
+  if (spatial != 0 || directional != 0)
+    throw std::runtime_error("field file: only kd-tree fields with parallax-aware VMMs are supported");
+  iteration = r.get<uint64_t>();
+  totalSPP = r.get<uint64_t>();
+  read_sub(r, surface);
+  read_sub(r, volume);
+  if (r.o != bytes.size()) throw std::runtime_error("field file has trailing bytes");
 }
 
 // Field::operator== (Field.h:552-601): exact comparison after the canonical

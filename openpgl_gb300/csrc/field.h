@@ -125,6 +125,7 @@ class SubField {
   FieldView view() const;
   std::vector<RegionDir> downloadRegions() const;
   void uploadRegions(const std::vector<RegionDir> &r);
+  void uploadTree();
   bool valid() const;
 
  private:
@@ -159,6 +160,7 @@ class GpuField {
   void sceneBounds(float out[6]) const;
   void reset();
   std::string serialize() const;  // byte layout of pglFieldStoreToFile (CPU_8 lanes)
+  void deserialize(const std::string &bytes);  // the same layout (pglDeviceNewFieldFromFile)
   bool equals(const GpuField &o) const;
 };
 
