@@ -72,6 +72,25 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int v
 // capacity >= 15 x count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int volume, uint64_t *out,
                                                            size_t capacity);
+// Splits numSamples sample records that live in device memory into the
+// surface records and the inside-volume records (flags & EInsideVolume), each
+// kind in its original order, written to dSurface and dVolume (device
+// buffers with room for numSamples records each); the two counts go to
+// dCounts[0] (surface) and dCounts[1] (volume) in device memory.  Work is
+// enqueued on cudaStream (null: the legacy default stream) and not waited for.
+// No reference counterpart.  Unlike pglSampleStorageAddSamplesDevice it
+// allocates nothing, neither device memory nor library scratch: for callers
+// that must not allocate, such as a renderer that reserves all of its device
+// memory up front, or one that cannot afford the device-wide synchronisation
+// that cudaFree implies in the middle of a frame.
+// Its scratch is one fixed array in device memory: at most 67,108,864 records
+// per call (larger batches are rejected with an error), and calls that may
+// overlap in time (other threads or streams) must be serialised by the caller.
+// The first call on each device looks the array up (cudaGetSymbolAddress);
+// make it before any stream capture.
+OPENPGL_CORE_INTERFACE bool pglSplitSamplesDeviceNoAlloc(const PGLSampleData *dSamples, size_t numSamples,
+                                                         PGLSampleData *dSurface, PGLSampleData *dVolume,
+                                                         uint32_t *dCounts, void *cudaStream);
 // Message of the error raised by the last library call on this thread ("" if
 // that call succeeded).
 OPENPGL_CORE_INTERFACE const char *pglGetLastError();

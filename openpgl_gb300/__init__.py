@@ -146,6 +146,8 @@ C_API = {
                                                       ctypes.c_size_t]),
     "pglDeviceGetCudaStream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "pglGetKernelLaunchCount": (ctypes.c_uint64, []),
+    "pglSplitSamplesDeviceNoAlloc": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_void_p, ctypes.c_void_p]),
     "pglFieldGetLastUpdateProfile": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
 }
 
@@ -174,6 +176,13 @@ def load(build_if_missing=True):
 def kernel_launch_count():
     """Kernels of this library launched so far by the process."""
     return int(load().pglGetKernelLaunchCount())
+
+
+def split_samples_device_noalloc(d_samples, n, d_surface, d_volume, d_counts, stream=None):
+    """pglSplitSamplesDeviceNoAlloc: stable split of n device records into
+    surface and volume records without allocating (pointers are integers)."""
+    ok = load().pglSplitSamplesDeviceNoAlloc(d_samples, n, d_surface, d_volume, d_counts, stream)
+    _check(ok, "pglSplitSamplesDeviceNoAlloc")
 
 
 def last_error():

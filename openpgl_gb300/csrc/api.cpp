@@ -729,6 +729,22 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdatePhases(PGLField field, int vo
   return 8;
   PGL_CATCH(0)
 }
+OPENPGL_CORE_INTERFACE bool pglSplitSamplesDeviceNoAlloc(const PGLSampleData *dSamples, size_t numSamples,
+                                                         PGLSampleData *dSurface, PGLSampleData *dVolume,
+                                                         uint32_t *dCounts, void *cudaStream) {
+  PGL_TRY
+  if (numSamples > split_max_records())
+    throw std::runtime_error("pglSplitSamplesDeviceNoAlloc: at most 67108864 samples per call, got " +
+                             std::to_string(numSamples));
+  if (!dCounts || (numSamples > 0 && (!dSamples || !dSurface || !dVolume)))
+    throw std::runtime_error("pglSplitSamplesDeviceNoAlloc: null device pointer");
+  check(split_samples_noalloc(reinterpret_cast<const PGLSampleRecord *>(dSamples), numSamples,
+                              reinterpret_cast<PGLSampleRecord *>(dSurface), reinterpret_cast<PGLSampleRecord *>(dVolume),
+                              dCounts, static_cast<cudaStream_t>(cudaStream)),
+        "pglSplitSamplesDeviceNoAlloc");
+  return true;
+  PGL_CATCH(false)
+}
 OPENPGL_CORE_INTERFACE uint64_t pglGetKernelLaunchCount() { return kernel_launches(); }
 OPENPGL_CORE_INTERFACE void *pglDeviceGetCudaStream(PGLDevice device) {
   PGL_TRY

@@ -29,6 +29,12 @@ struct SoAView {
 unsigned long long kernel_launches();
 void count_launch();
 
+// Stable split of a device batch into caller buffers with a fixed device
+// scratch array (noalloc.cu); at most split_max_records() records per call.
+size_t split_max_records();
+cudaError_t split_samples_noalloc(const PGLSampleRecord *in, size_t n, PGLSampleRecord *surf, PGLSampleRecord *vol,
+                                  uint32_t *counts, cudaStream_t s);
+
 cudaError_t em_upload_tables();
 cudaError_t spatial_upload_tables();
 cudaError_t query_upload_tables();
