@@ -91,6 +91,40 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
 OPENPGL_CORE_INTERFACE bool pglSplitSamplesDeviceNoAlloc(const PGLSampleData *dSamples, size_t numSamples,
                                                          PGLSampleData *dSurface, PGLSampleData *dVolume,
                                                          uint32_t *dCounts, void *cudaStream);
+// ---- Serving a field (no reference counterpart).  A server answers guided
+// queries against a resident field while it keeps training it: requests of
+// any size from any thread are batched continuously into kernel launches on
+// the server's stream, against a snapshot of the field; an Update runs in the
+// background on the field's own streams and its result replaces the snapshot
+// when it is done (two snapshots: requests already started finish on the one
+// they started on).  While a server serves a field, use the field only through
+// the server; release the server before the field.
+#ifdef __cplusplus
+struct GuidingServer;
+#endif
+typedef struct GuidingServer *PGLGuidingServer;
+// hbmBudgetBytes bounds the device memory of queries in flight (68 bytes per
+// query); larger requests run in several launches.
+OPENPGL_CORE_INTERFACE PGLGuidingServer pglNewGuidingServer(PGLField field, size_t hbmBudgetBytes);
+OPENPGL_CORE_INTERFACE void pglReleaseGuidingServer(PGLGuidingServer server);
+// Queues n queries; `queries` and `results` (host memory) must stay valid until
+// the request is waited for.  Returns a ticket (0 on error).
+OPENPGL_CORE_INTERFACE uint64_t pglGuidingServerSubmit(PGLGuidingServer server, const PGLGuidedQuery *queries,
+                                                       size_t n, PGLGuidedQueryResult *results, bool volume,
+                                                       bool cosineProduct);
+// Blocks until the request is done; reports its latency (submit to results)
+// and the field iteration its results come from.
+OPENPGL_CORE_INTERFACE bool pglGuidingServerWait(PGLGuidingServer server, uint64_t ticket, double *latencyMs,
+                                                 uint64_t *fieldVersion);
+// Training samples for the next Update (copied).
+OPENPGL_CORE_INTERFACE bool pglGuidingServerAddSamples(PGLGuidingServer server, const PGLSampleData *samples,
+                                                       size_t n);
+// Starts an Update with the samples added so far; returns a ticket.
+OPENPGL_CORE_INTERFACE uint64_t pglGuidingServerUpdate(PGLGuidingServer server);
+OPENPGL_CORE_INTERFACE bool pglGuidingServerWaitUpdate(PGLGuidingServer server, uint64_t ticket);
+// queries served, requests done, latency p50 / p99 / p99.9 (ms), launches,
+// updates done, field iteration being served
+OPENPGL_CORE_INTERFACE bool pglGuidingServerStats(PGLGuidingServer server, double out8[8]);
 // Message of the error raised by the last library call on this thread ("" if
 // that call succeeded).
 OPENPGL_CORE_INTERFACE const char *pglGetLastError();

@@ -146,6 +146,16 @@ C_API = {
                                                       ctypes.c_size_t]),
     "pglDeviceGetCudaStream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "pglGetKernelLaunchCount": (ctypes.c_uint64, []),
+    "pglNewGuidingServer": (ctypes.c_void_p, [ctypes.c_void_p, ctypes.c_size_t]),
+    "pglReleaseGuidingServer": (None, [ctypes.c_void_p]),
+    "pglGuidingServerSubmit": (ctypes.c_uint64, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                                 ctypes.c_bool, ctypes.c_bool]),
+    "pglGuidingServerWait": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
+                                             ctypes.POINTER(ctypes.c_uint64)]),
+    "pglGuidingServerAddSamples": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "pglGuidingServerUpdate": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "pglGuidingServerWaitUpdate": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_uint64]),
+    "pglGuidingServerStats": (ctypes.c_bool, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "pglSplitSamplesDeviceNoAlloc": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
                                                      ctypes.c_void_p, ctypes.c_void_p]),
     "pglFieldGetLastUpdateProfile": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
@@ -445,3 +455,56 @@ class SurfaceSamplingDistribution:
 
 class VolumeSamplingDistribution(SurfaceSamplingDistribution):
     volume = True
+
+
+class GuidingServer:
+    """A field served while it trains (pglNewGuidingServer): submit guided
+    queries from any thread, add samples, start Updates in the background."""
+
+    def __init__(self, field, hbm_budget_bytes=1 << 30):
+        self.lib = load()
+        self.field = field
+        self.h = self.lib.pglNewGuidingServer(field.h, hbm_budget_bytes)
+        _check(self.h, "pglNewGuidingServer")
+        self._keep = {}
+
+    def submit(self, queries, volume=False, cosine=True):
+        """Queue a batch; returns (ticket, result array filled when done)."""
+        q = np.ascontiguousarray(queries, dtype=PGL_QUERY_DTYPE)
+        out = np.zeros(len(q), dtype=QUERY_RESULT_DTYPE)
+        t = self.lib.pglGuidingServerSubmit(self.h, q.ctypes.data, len(q), out.ctypes.data, volume, cosine)
+        _check(t != 0, "pglGuidingServerSubmit")
+        self._keep[t] = (q, out)
+        return t, out
+
+    def wait(self, ticket):
+        """(latency ms, field iteration of the results)"""
+        lat = ctypes.c_double()
+        ver = ctypes.c_uint64()
+        ok = self.lib.pglGuidingServerWait(self.h, ticket, ctypes.byref(lat), ctypes.byref(ver))
+        self._keep.pop(ticket, None)
+        _check(ok, "pglGuidingServerWait")
+        return lat.value, ver.value
+
+    def add_samples(self, samples):
+        s = np.ascontiguousarray(samples, dtype=PGL_SAMPLE_DTYPE)
+        _check(self.lib.pglGuidingServerAddSamples(self.h, s.ctypes.data, len(s)), "pglGuidingServerAddSamples")
+
+    def update(self):
+        t = self.lib.pglGuidingServerUpdate(self.h)
+        _check(t != 0, "pglGuidingServerUpdate")
+        return t
+
+    def wait_update(self, ticket):
+        _check(self.lib.pglGuidingServerWaitUpdate(self.h, ticket), "pglGuidingServerWaitUpdate")
+
+    def stats(self):
+        out = (ctypes.c_double * 8)()
+        _check(self.lib.pglGuidingServerStats(self.h, out), "pglGuidingServerStats")
+        keys = ("queries", "requests", "p50_ms", "p99_ms", "p999_ms", "launches", "updates", "iteration")
+        return dict(zip(keys, list(out)))
+
+    def release(self):
+        if self.h:
+            self.lib.pglReleaseGuidingServer(self.h)
+            self.h = None

@@ -20,7 +20,7 @@ LIB = os.path.join(OUT, "libopenpgl_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 CUDA_SOURCES = ["em_kernel.cu", "spatial_kernels.cu", "query_kernels.cu", "noalloc.cu"]
-HOST_SOURCES = ["field.cpp", "api.cpp"]
+HOST_SOURCES = ["field.cpp", "api.cpp", "serve.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -16,6 +16,7 @@
 
 #include "../../include/openpgl_gb300.h"
 #include "field.h"
+#include "serve.h"
 
 using namespace pgl;
 
@@ -742,6 +743,64 @@ OPENPGL_CORE_INTERFACE bool pglSplitSamplesDeviceNoAlloc(const PGLSampleData *dS
                               reinterpret_cast<PGLSampleRecord *>(dSurface), reinterpret_cast<PGLSampleRecord *>(dVolume),
                               dCounts, static_cast<cudaStream_t>(cudaStream)),
         "pglSplitSamplesDeviceNoAlloc");
+  return true;
+  PGL_CATCH(false)
+}
+// ---- serving a field (appended; no reference counterpart)
+OPENPGL_CORE_INTERFACE PGLGuidingServer pglNewGuidingServer(PGLField field, size_t hbmBudgetBytes) {
+  PGL_TRY
+  if (!field) throw std::runtime_error("null field provided to pglNewGuidingServer");
+  return reinterpret_cast<PGLGuidingServer>(new pgl::GuidingServer(F(field), hbmBudgetBytes));
+  PGL_CATCH(nullptr)
+}
+OPENPGL_CORE_INTERFACE void pglReleaseGuidingServer(PGLGuidingServer server) {
+  PGL_TRY
+  delete reinterpret_cast<pgl::GuidingServer *>(server);
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE uint64_t pglGuidingServerSubmit(PGLGuidingServer server, const PGLGuidedQuery *queries,
+                                                       size_t n, PGLGuidedQueryResult *results, bool volume,
+                                                       bool cosineProduct) {
+  PGL_TRY
+  if (!server || (n > 0 && (!queries || !results))) throw std::runtime_error("null pointer");
+  return reinterpret_cast<pgl::GuidingServer *>(server)->submit(reinterpret_cast<const QueryIn *>(queries),
+                                                           reinterpret_cast<QueryOut *>(results), n, volume,
+                                                           cosineProduct);
+  PGL_CATCH(0)
+}
+OPENPGL_CORE_INTERFACE bool pglGuidingServerWait(PGLGuidingServer server, uint64_t ticket, double *latencyMs,
+                                                 uint64_t *fieldVersion) {
+  PGL_TRY
+  if (!server) throw std::runtime_error("null server");
+  reinterpret_cast<pgl::GuidingServer *>(server)->wait(ticket, latencyMs, fieldVersion);
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglGuidingServerAddSamples(PGLGuidingServer server, const PGLSampleData *samples,
+                                                       size_t n) {
+  PGL_TRY
+  if (!server || (n > 0 && !samples)) throw std::runtime_error("null pointer");
+  reinterpret_cast<pgl::GuidingServer *>(server)->addSamples(reinterpret_cast<const PGLSampleRecord *>(samples), n);
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE uint64_t pglGuidingServerUpdate(PGLGuidingServer server) {
+  PGL_TRY
+  if (!server) throw std::runtime_error("null server");
+  return reinterpret_cast<pgl::GuidingServer *>(server)->update();
+  PGL_CATCH(0)
+}
+OPENPGL_CORE_INTERFACE bool pglGuidingServerWaitUpdate(PGLGuidingServer server, uint64_t ticket) {
+  PGL_TRY
+  if (!server) throw std::runtime_error("null server");
+  reinterpret_cast<pgl::GuidingServer *>(server)->waitUpdate(ticket);
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglGuidingServerStats(PGLGuidingServer server, double out8[8]) {
+  PGL_TRY
+  if (!server || !out8) throw std::runtime_error("null pointer");
+  reinterpret_cast<pgl::GuidingServer *>(server)->stats(out8);
   return true;
   PGL_CATCH(false)
 }

@@ -709,8 +709,11 @@ void GpuField::update(Storage &s, bool doSurface, bool doVolume) {  // SurfaceVo
     // the two fields are independent: each runs on its own stream from its
     // own host thread, so their kernels overlap on the GPU
     std::exception_ptr err;
+    int device = 0;
+    check(cudaGetDevice(&device), "cudaGetDevice");
     std::thread t([&] {
       try {
+        check(cudaSetDevice(device), "cudaSetDevice");
         volume.update(s.vol);
       } catch (...) {
         err = std::current_exception();
