@@ -172,6 +172,69 @@ def cpu_queries(frames, queries, threads=None, n=131072):
     return n / dt
 
 
+# ----------------------------------------------------------------- serving
+def run_serving(pgl, field, frames, queries, seconds=6.0, submitters=8, update_every=100):
+    """Guided queries through the guiding server (continuous batching over a
+    double-buffered field) from `submitters` threads, each sending batches of
+    log-uniform size in [1024, 262144] back to back (closed loop: the load is
+    the saturating one), while a 2M-sample Update runs in the background every
+    `update_every` batches.  Beside it the plain drop-in: the per-object API
+    (one Init + cosine product + SamplePDF launch chain per query)."""
+    import threading
+
+    rng = np.random.default_rng(99)
+    sizes = np.exp(rng.uniform(np.log(1024), np.log(262144), size=4096)).astype(int)
+    server = pgl.GuidingServer(field, hbm_budget_bytes=4 << 30)
+    lock = threading.Lock()
+    state = {"next": 0, "batches": 0, "stop": False, "tickets": []}
+    t_end = time.perf_counter() + seconds
+
+    def submitter():
+        while time.perf_counter() < t_end:
+            with lock:
+                i = state["next"]
+                state["next"] += 1
+                state["batches"] += 1
+                upd = state["batches"] % update_every == 0
+            n = int(sizes[i % len(sizes)])
+            off = (i * 7919) % (len(queries) - n)
+            t, out = server.submit(queries[off:off + n])
+            server.wait(t)
+            if upd:
+                server.add_samples(frames[i % len(frames)])
+                state["tickets"].append(server.update())
+
+    t0 = time.perf_counter()
+    threads = [threading.Thread(target=submitter) for _ in range(submitters)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    wall = time.perf_counter() - t0
+    for t in state["tickets"]:
+        server.wait_update(t)
+    st = server.stats()
+    server.release()
+
+    # plain drop-in: per-object calls
+    n_plain = 2000
+    ssd = pgl.SurfaceSamplingDistribution(field)
+    q = queries[:n_plain]
+    t0 = time.perf_counter()
+    for i in range(n_plain):
+        ok, _ = ssd.init(tuple(q["position"][i]), float(q["sample1d"][i]))
+        if ok:
+            ssd.apply_cosine_product(tuple(q["normal"][i]))
+            ssd.sample_pdf(tuple(q["u"][i]))
+    plain_qps = n_plain / (time.perf_counter() - t0)
+    ssd.release()
+    return {"queries_per_s": round(st["queries"] / wall), "p50_ms": round(st["p50_ms"], 3),
+            "p99_ms": round(st["p99_ms"], 3), "p999_ms": round(st["p999_ms"], 3), "requests": int(st["requests"]),
+            "launches": int(st["launches"]), "background_updates": int(st["updates"]), "submitters": submitters,
+            "batch_sizes": "log-uniform 1024-262144", "plain_per_object_queries_per_s": round(plain_qps),
+            "served_vs_plain": round(st["queries"] / wall / plain_qps, 1)}
+
+
 # ----------------------------------------------------------------- GPU arm
 def run_gpu(args, rank, world, local_rank):
     import torch
@@ -251,6 +314,9 @@ def run_gpu(args, rank, world, local_rank):
         field.sample_batch(queries)
     q_e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
 
+    # ---- served guided queries (continuous batching, background updates)
+    serving = run_serving(pgl, field, frames[:2], queries, seconds=args.serve_seconds) if args.serve_seconds > 0 else None
+
     # ---- end to end: host (pinned) sample records through the C API
     pinned = [torch.from_numpy(f.view(np.uint8)).pin_memory() for f in frames]
     host_views = [p.numpy().view(frames[0].dtype) for p in pinned]
@@ -323,6 +389,7 @@ def run_gpu(args, rank, world, local_rank):
                     "p50_ms": round(statistics.median(lat_ms), 3),
                     "p99_ms": round(lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))], 3),
                     "e2e_queries_per_s": round(QUERIES / (q_e2e_ms * 1e-3))},
+        "serving": serving,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -386,6 +453,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--serve-seconds", type=float, default=6.0)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
