@@ -17,6 +17,7 @@
 // summation order (sequential over samples within each SIMD lane), so every
 // accumulator gets the reference's bits.  Scalar per-leaf logic (M step,
 // split/merge bookkeeping) runs on thread 0 between passes.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -29,6 +30,17 @@ namespace pgl {
 constexpr int kEmThreads = 512;
 constexpr int kStageFloats = 19200;  // floats per pipeline stage (two stages, 150 KB)
 constexpr int kMaxPairs = kMaxK * (kMaxK - 1) / 2;
+
+// An E-step or distance pass as the home block of a cluster publishes it.
+enum PassCmdKind { kCmdEStep = 0, kCmdDistance = 1, kCmdExit = 3 };
+struct PassCmd {
+  int kind;
+  int cnt;  // lobe vectors
+  const float4 *dirw;
+  const float *pdf;
+  const float *dist;
+  uint32_t count;
+};
 
 struct Unassigned {
   float sw, dx, dy, dz;
@@ -61,6 +73,10 @@ struct EmShared {
   int iterations;
   LeafReport report;
   LeafProfile prof;
+  PassCmd cmd;         // the pass the home block publishes to its helper blocks
+  int clusterBlocks;   // blocks sharing each region (a thread-block cluster)
+  int producers;       // blocks that produce chunks of E-step and distance passes
+  int homeProduces;    // whether the home block (rank 0) is one of them
   uint32_t validPerWarp[kEmThreads / 32];  // split passes: valid samples per producer warp
   float splitN0[kMaxK];                     // split passes: chi-square counts at the pass start
 };
@@ -535,7 +551,7 @@ struct PassShape {
   int stage;    // floats per stage
 };
 template <PassKind kind>
-__device__ __forceinline__ PassShape pass_shape(int Kp) {
+__device__ __forceinline__ PassShape pass_shape(int Kp, int budget = kStageFloats) {
   // rows: one per (accumulator, lobe); extra: per-sample arrays
   int consWarps, rows, extra;
   if (kind == kPassEStep) {  // 4 Kp lobe chains, then LL and 4 unassigned sums
@@ -555,7 +571,7 @@ __device__ __forceinline__ PassShape pass_shape(int Kp) {
   const int cnt = Kp / kLanes;
   p.parts = cnt == 3 ? 4 : cnt;
   p.P = kEmThreads - 32 * consWarps;
-  int c = (kStageFloats - 2 * rows) / (rows + extra);
+  int c = (budget - 2 * rows) / (rows + extra);
   const int byThreads = p.P / p.parts;
   c = c < byThreads ? c : byThreads;
   // C * parts a multiple of 32 (whole warps) and C a multiple of 8.  Rows of
@@ -906,16 +922,39 @@ __device__ __forceinline__ void split_chain(const float *B, const PassShape &sh,
   }
 }
 
-// Runs one pass over the leaf's samples.  `acc`/`accN` are the consumer's
-// accumulators (initialised by the caller); the producer side is driven here.
+// Stage floats of one producing block's chunk: the home block's two slots
+// are shared by the blocks that produce E-step and distance passes.
+__device__ __forceinline__ int chunk_budget(const EmShared &S, PassKind kind) {
+  if (kind == kPassSplit || S.clusterBlocks <= 1) return kStageFloats;
+  return (kStageFloats / S.producers) & ~7;
+}
+
+// Runs one pass over the leaf's samples in the home block.  `acc`/`accN` are
+// the consumer's accumulators (initialised by the caller).  Chunk c is made by
+// producing block c % producers into sub-stage (c % producers) of the home
+// block's slot ((c / producers) & 1); the home block's consumers add the
+// chunks of a round in chunk order.  With helper blocks (E-step and distance
+// passes in a cluster) the pass is first published (PassCmd); home and
+// helpers then run the same number of rounds, each ending at a cluster
+// barrier.  Split-statistics passes always run in the home block alone.
 template <PassKind kind>
 __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const PassShape &sh, int cnt, float &acc,
                                       float &accN) {
+  namespace cg = cooperative_groups;
   const int tid = threadIdx.x;
   const int Kp = cnt * kLanes;
   const int C = sh.C;
+  const bool cluster = kind != kPassSplit && S.clusterBlocks > 1;
+  const uint32_t PG = cluster ? uint32_t(S.producers) : 1u;
+  const bool homeMakes = !cluster || S.homeProduces;
+  const int sub = chunk_budget(S, kind);
+  if (cluster) {
+    if (tid == 0) S.cmd = PassCmd{int(kind), cnt, L.dirw, L.pdf, L.dist, L.count};
+    cg::this_cluster().sync();
+  }
   const uint32_t numChunks = (L.count + C - 1) / C;
-  const bool producer = tid < sh.threads;
+  const uint32_t rounds = (numChunks + PG - 1) / PG;
+  const bool producer = homeMakes && tid < sh.threads;
   const int s = tid / sh.parts, v = tid % sh.parts;
   const bool consumer = tid >= sh.P;
   const int c = tid - sh.P;
@@ -926,26 +965,30 @@ __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const P
   SampleIn next;
   if (producer) next = load_sample<kind>(L, uint32_t(s));
   long long cycP = 0, cycC = 0;
-  for (uint32_t it = 0; it <= numChunks; ++it) {
-    if (producer && it < numChunks) {
+  for (uint32_t it = 0; it <= rounds; ++it) {
+    if (producer && it < rounds) {
       const long long t0 = clock64();
       const SampleIn cur = next;
-      if (it + 1 < numChunks) next = load_sample<kind>(L, (it + 1) * C + s);
-      produce<kind>(S, sh, cnt, Kp, s, v, cur, S.pbuf + (it & 1) * sh.stage, base);
+      if (it + 1 < rounds) next = load_sample<kind>(L, (it + 1) * PG * C + s);
+      produce<kind>(S, sh, cnt, Kp, s, v, cur, S.pbuf + (it & 1) * kStageFloats, base);
       cycP += clock64() - t0;
     }
     if (consumer && it >= 1) {
       const long long t0 = clock64();
-      const uint32_t prev = it - 1;
-      const int n = int(min(uint32_t(C), L.count - prev * C));
-      const int n4 = (n + 3) & ~3;
-      const float *B = S.pbuf + (prev & 1) * sh.stage;
-      if constexpr (kind == kPassEStep) estep_chain(B, sh, c, Kp, n4, acc);
-      else if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
-      else split_chain(B, sh, c, Kp, n4, n0, acc, accN, count);
+      for (uint32_t r = 0; r < PG; ++r) {
+        const uint32_t chunk = (it - 1) * PG + r;
+        if (chunk >= numChunks) break;
+        const int n = int(min(uint32_t(C), L.count - chunk * C));
+        const int n4 = (n + 3) & ~3;
+        const float *B = S.pbuf + ((it - 1) & 1) * kStageFloats + r * sub;
+        if constexpr (kind == kPassEStep) estep_chain(B, sh, c, Kp, n4, acc);
+        else if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
+        else split_chain(B, sh, c, Kp, n4, n0, acc, accN, count);
+      }
       cycC += clock64() - t0;
     }
-    __syncthreads();
+    if (cluster) cg::this_cluster().sync();
+    else __syncthreads();
   }
   const int probe = kind == kPassSplit ? split_chi_base(Kp) : 0;
   if (tid == 0) {
@@ -958,12 +1001,71 @@ __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const P
   }
 }
 
+// The producer side of a published pass in a helper block (cluster rank
+// r > 0): the home block's rounds, making chunks it * producers + index into
+// the home block's shared memory (distributed shared memory stores).
+template <PassKind kind>
+__device__ __noinline__ void helper_pass(EmShared &S, const PassCmd &cmd, unsigned rank) {
+  namespace cg = cooperative_groups;
+  const int tid = threadIdx.x;
+  const int Kp = cmd.cnt * kLanes;
+  const int sub = chunk_budget(S, kind);
+  const PassShape sh = pass_shape<kind>(Kp, sub);
+  const int C = sh.C;
+  const uint32_t PG = uint32_t(S.producers);
+  const uint32_t index = S.homeProduces ? rank : rank - 1;
+  const LeafSamples L{cmd.dirw, cmd.pdf, cmd.dist, cmd.count};
+  const uint32_t numChunks = (L.count + C - 1) / C;
+  const uint32_t rounds = (numChunks + PG - 1) / PG;
+  const bool producer = tid < sh.threads;
+  const int s = tid / sh.parts, v = tid % sh.parts;
+  uint32_t base = 0;
+  SampleIn next;
+  if (producer) next = load_sample<kind>(L, index * C + s);
+  for (uint32_t it = 0; it <= rounds; ++it) {
+    if (producer && it < rounds && it * PG + index < numChunks) {
+      const SampleIn cur = next;
+      if (it + 1 < rounds) next = load_sample<kind>(L, ((it + 1) * PG + index) * C + s);
+      float *local = S.pbuf + (it & 1) * kStageFloats + index * sub;
+      produce<kind>(S, sh, cmd.cnt, Kp, s, v, cur, cg::this_cluster().map_shared_rank(local, 0u), base);
+    }
+    cg::this_cluster().sync();
+  }
+}
+
+// Helper blocks serve the home block's published passes until kCmdExit.  A
+// command costs both sides one cluster barrier to publish, then the pass's
+// rounds; the exit costs a second barrier so that the home block's shared
+// memory outlives the helpers' read of the command.
+__device__ void helper_loop(EmShared &S, unsigned rank) {
+  namespace cg = cooperative_groups;
+  const int tid = threadIdx.x;
+  EmShared *home = cg::this_cluster().map_shared_rank(&S, 0u);
+  for (;;) {
+    cg::this_cluster().sync();
+    const PassCmd cmd = home->cmd;
+    if (cmd.kind == kCmdExit) {
+      cg::this_cluster().sync();
+      return;
+    }
+    const int Kp = cmd.cnt * kLanes;
+    if (tid < Kp + Kp / kLanes) S.lobeA[tid] = home->lobeA[tid];
+    if (tid < Kp) {
+      S.lobeB[tid] = home->lobeB[tid];
+      S.lobeWInv[tid] = home->lobeWInv[tid];
+    }
+    __syncthreads();
+    if (cmd.kind == kCmdEStep) helper_pass<kPassEStep>(S, cmd, rank);
+    else helper_pass<kPassDistance>(S, cmd, rank);
+  }
+}
+
 // E-step over all samples into S.cur, S.ll and S.un.
 __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
   const int tid = threadIdx.x;
   const int cnt = vec_count(int(S.vmm.K));
   const int Kp = cnt * kLanes;
-  const PassShape sh = pass_shape<kPassEStep>(Kp);
+  const PassShape sh = pass_shape<kPassEStep>(Kp, chunk_budget(S, kPassEStep));
   if (tid == 0) {
     S.un = Unassigned{0.f, 0.f, 0.f, 0.f};
     suff_clear(S.cur, S.vmm.K);
@@ -999,7 +1101,7 @@ __device__ void pass_distances(EmShared &S, const LeafSamples &L, bool init) {
   const int tid = threadIdx.x;
   const int cnt = vec_count(int(S.vmm.K));
   const int Kp = cnt * kLanes;
-  const PassShape sh = pass_shape<kPassDistance>(Kp);
+  const PassShape sh = pass_shape<kPassDistance>(Kp, chunk_budget(S, kPassDistance));
   pack_lobes(S, Kp);
   __syncthreads();
   float acc = 0.0f, accN = 0.0f;
@@ -1373,6 +1475,21 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
   __shared__ uint32_t taskId;
   __shared__ uint64_t afterSplit, afterMerge;
   for (int i = threadIdx.x; i < 2048; i += blockDim.x) S.rcpTab[i] = rcp_seed(uint32_t(i));
+  // a cluster of G blocks shares each region: rank 0 (home) owns it; with 2
+  // blocks both produce E-step and distance chunks, with more the home block
+  // only sums and the others produce (helper_loop)
+  const unsigned G = cooperative_groups::this_cluster().num_blocks();
+  const unsigned rank = cooperative_groups::this_cluster().block_rank();
+  if (threadIdx.x == 0) {
+    S.clusterBlocks = int(G);
+    S.homeProduces = G <= 2 ? 1 : 0;
+    S.producers = G <= 2 ? int(G) : int(G) - 1;
+  }
+  __syncthreads();
+  if (rank != 0) {
+    helper_loop(S, rank);
+    return;
+  }
   for (;;) {
     if (threadIdx.x == 0) taskId = atomicAdd(queue, 1u);
     __syncthreads();
@@ -1456,6 +1573,11 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
     }
     __syncthreads();
   }
+  if (G > 1) {  // release the helpers (helper_loop)
+    if (threadIdx.x == 0) S.cmd.kind = kCmdExit;
+    cooperative_groups::this_cluster().sync();
+    cooperative_groups::this_cluster().sync();
+  }
 }
 
 PGL_DEFINE_TABLE_UPLOAD(em_upload_tables)
@@ -1464,7 +1586,7 @@ size_t em_shared_bytes() { return sizeof(EmShared); }
 
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
                       float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
-                      LeafReport *reports, LeafProfile *profiles, int numSMs, cudaStream_t stream) {
+                      LeafReport *reports, LeafProfile *profiles, int numSMs, int clusterSize, cudaStream_t stream) {
   const size_t smem = sizeof(EmShared);
   // once per process (thread-safe static initialisation: the surface and
   // volume fields may launch concurrently)
@@ -1472,12 +1594,35 @@ cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *qu
       cudaFuncSetAttribute(em_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (attr != cudaSuccess) return attr;
   if (numTasks == 0) return cudaSuccess;
-  // one persistent block per SM (shared memory bound), regions from the queue
-  const unsigned blocks = unsigned(numSMs) < numTasks ? unsigned(numSMs) : numTasks;
+  cudaLaunchConfig_t config = {};
+  config.blockDim = dim3(kEmThreads);
+  config.dynamicSmemBytes = smem;
+  config.stream = stream;
+  cudaLaunchAttribute la[1];
+  int G = clusterSize == 2 || clusterSize == 4 || clusterSize == 8 ? clusterSize : 1;
+  int clusters = numSMs;
+  if (G > 1) {
+    la[0].id = cudaLaunchAttributeClusterDimension;
+    la[0].val.clusterDim.x = unsigned(G);
+    la[0].val.clusterDim.y = 1;
+    la[0].val.clusterDim.z = 1;
+    config.attrs = la;
+    config.numAttrs = 1;
+    config.gridDim = dim3(unsigned(G) * unsigned(numSMs / G));
+    if (cudaOccupancyMaxActiveClusters(&clusters, em_leaf_kernel, &config) != cudaSuccess || clusters < 1) {
+      cudaGetLastError();
+      G = 1;  // this cluster shape does not fit: one block per region
+      clusters = numSMs;
+      config.attrs = nullptr;
+      config.numAttrs = 0;
+    }
+  }
+  // persistent blocks (one per SM; shared memory bound) take regions from the queue
+  const unsigned used = unsigned(clusters) < numTasks ? unsigned(clusters) : numTasks;
+  config.gridDim = dim3(used * unsigned(G));
   count_launch();
-  em_leaf_kernel<<<blocks, kEmThreads, smem, stream>>>(tasks, numTasks, queue, regions, pd, dirw, pdf, dist, cfg,
-                                                       uniformDirs, reports, profiles);
-  return cudaGetLastError();
+  return cudaLaunchKernelEx(&config, em_leaf_kernel, tasks, numTasks, queue, regions, pd, dirw, pdf, dist, cfg,
+                            uniformDirs, reports, profiles);
 }
 
 }  // namespace pgl

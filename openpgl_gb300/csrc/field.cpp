@@ -64,6 +64,7 @@ template struct DevArray<LeafProfile>;
 template struct DevArray<IStatsAcc>;
 template struct DevArray<QueryIn>;
 template struct DevArray<QueryOut>;
+template struct DevArray<unsigned long long>;
 
 // ------------------------------------------------------------------ statistics (host)
 // IntegerSampleStatistics frame (SampleStatistics.h:227-241), SSE rcp form.
@@ -467,6 +468,22 @@ void SubField::renumber(uint32_t oldNodes, uint32_t oldRegions) {
   regionOrigin_.swap(no);
 }
 
+// Blocks per region of the EM launch (a thread-block cluster: with 2 blocks
+// both produce E-step and distance chunks, with more the home block only sums
+// and the others produce).  One by default: the cluster barrier that ends
+// every round of a shared pass costs more than the helpers' chunks save
+// (measured on the multi-frame workload).  PGL_EM_CLUSTER=1, 2, 4 or 8 fixes
+// the size.
+int em_cluster_size(uint32_t regions, int numSMs) {
+  (void)regions;
+  (void)numSMs;
+  if (const char *env = std::getenv("PGL_EM_CLUSTER")) {
+    const int g = std::atoi(env);
+    if (g == 1 || g == 2 || g == 4 || g == 8) return g;
+  }
+  return 1;
+}
+
 void SubField::update(SampleSide &in) {
   Context &c = Context::get();
   const uint32_t n = uint32_t(in.n);
@@ -490,6 +507,7 @@ void SubField::update(SampleSide &in) {
   for (DevArray<uint32_t> *a : {&node_, &nodeB_, &jobOf_, &isLeft_, &scanLeft_}) a->reserve(n);
   keys_.reserve(2 * size_t(n));
   vals_.reserve(2 * size_t(n));
+  keys64_.reserve(2 * size_t(n));
   check(init_posidx(in.P.p, n, posA_.p, stream()), "copy samples");
   check(cudaEventRecord(ev[1], stream()), "event");
 
@@ -574,7 +592,8 @@ void SubField::update(SampleSide &in) {
   leafSeg_.reserve(seg.size());
   check(cudaMemcpyAsync(leafSeg_.p, seg.data(), seg.size() * 4, cudaMemcpyHostToDevice, stream()), "segments");
   check(gather_and_order(posA_.p, n, in.P.p, in.D.p, in.pdf.p, leafSeg_.p, leafSeg_.p + 2 * L, L, cfg.deterministic,
-                         tmpP_.p, tmpD_.p, tmpPdf_.p, keys_.p, vals_.p, sP_.p, sD_.p, sPdf_.p, scratch_, stream()),
+                         tmpP_.p, tmpD_.p, tmpPdf_.p, keys_.p, vals_.p, keys64_.p, sP_.p, sD_.p, sPdf_.p, scratch_,
+                         stream()),
         "gather");
 
   // directional fit / update of every region (Field.h:389-511)
@@ -602,7 +621,7 @@ void SubField::update(SampleSide &in) {
   check(cudaEventRecord(ev[4], stream()), "event");
   if (cfg.fitRegions) {
     check(launch_em(tasks_.p, R, queue_.p, dRegions.p, sP_.p, sD_.p, sPdf_.p, dist_.p, cfg, dUniformDirs.p, reports_.p,
-                    profiles_.p, c.numSMs, stream()),
+                    profiles_.p, c.numSMs, em_cluster_size(R, c.numSMs), stream()),
           "em");
   }
   check(cudaEventRecord(ev[3], stream()), "event");

@@ -59,14 +59,16 @@ cudaError_t kd_level(const float4 *pos, const uint32_t *jobOf, uint32_t n, const
 cudaError_t gather_and_order(const float4 *posIdx, uint32_t n, const float4 *P, const float4 *D, const float *pdf,
                              const uint32_t *leafBegin, const uint32_t *leafCount, uint32_t numLeaves, bool sorted,
                              float4 *tmpP, float4 *tmpD, float *tmpPdf, uint32_t *keys, uint32_t *vals,
-                             float4 *oP, float4 *oD, float *oPdf, Scratch &scratch, cudaStream_t s);
+                             unsigned long long *keys64, float4 *oP, float4 *oD, float *oPdf, Scratch &scratch,
+                             cudaStream_t s);
 cudaError_t copy_regions(RegionDir *regions, const uint32_t *dst, const uint32_t *src, uint32_t n, cudaStream_t s);
 cudaError_t build_knn(const float4 *means, uint32_t R, Neighbours *out, cudaStream_t s);
 
 size_t em_shared_bytes();
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
                       float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
-                      LeafReport *reports, LeafProfile *profiles, int numSMs, cudaStream_t stream);
+                      LeafReport *reports, LeafProfile *profiles, int numSMs, int clusterSize,
+                      cudaStream_t stream);
 
 cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s);
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,

@@ -333,51 +333,41 @@ __device__ __forceinline__ bool sample_less(float4 pa, float4 da, float fa, floa
   if (da.y != db.y) return da.y < db.y;
   return da.z < db.z;
 }
-// Permutes samples by the weight-sorted order and finishes ties of equal
-// weight with the full comparator (one thread per leaf; ties are rare).
-__global__ void order_kernel(const uint32_t *sortedVal, const uint32_t *leafBegin, const uint32_t *leafCount,
-                             uint32_t numLeaves, const float4 *P, const float4 *D, const float *pdf, float4 *oP,
-                             float4 *oD, float *oPdf) {
-  uint32_t leaf = blockIdx.x;
-  if (leaf >= numLeaves) return;
-  uint32_t b = leafBegin[leaf], c = leafCount[leaf];
-  for (uint32_t i = threadIdx.x; i < c; i += blockDim.x) {
-    uint32_t s = sortedVal[b + i];
-    oP[b + i] = P[s];
-    oD[b + i] = D[s];
-    oPdf[b + i] = pdf[s];
-  }
-  __shared__ int anyTie;
-  if (threadIdx.x == 0) anyTie = 0;
-  __syncthreads();
-  // equal weight keys are rare: look for adjacent equal keys in parallel and
-  // order the runs by the full comparison only when there is one
-  for (uint32_t i = threadIdx.x; i + 1 < c; i += blockDim.x)
-    if (oD[b + i].w == oD[b + i + 1].w) anyTie = 1;
-  __syncthreads();
-  if (anyTie && threadIdx.x == 0) {
-    uint32_t i = 0;
-    while (i < c) {
-      uint32_t j = i + 1;
-      while (j < c && oD[b + j].w == oD[b + i].w) ++j;
-      if (j - i > 1) {  // insertion sort of the run [i, j)
-        for (uint32_t x = i + 1; x < j; ++x) {
-          float4 kp = oP[b + x], kd = oD[b + x];
-          float kf = oPdf[b + x];
-          uint32_t y = x;
-          while (y > i && sample_less(kp, kd, kf, oP[b + y - 1], oD[b + y - 1], oPdf[b + y - 1])) {
-            oP[b + y] = oP[b + y - 1];
-            oD[b + y] = oD[b + y - 1];
-            oPdf[b + y] = oPdf[b + y - 1];
-            --y;
-          }
-          oP[b + y] = kp;
-          oD[b + y] = kd;
-          oPdf[b + y] = kf;
-        }
-      }
-      i = j;
+// Permutes the samples into the sorted order (all samples, one thread each).
+__global__ void permute_kernel(const uint32_t *sortedVal, uint32_t n, const float4 *P, const float4 *D,
+                               const float *pdf, float4 *oP, float4 *oD, float *oPdf) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t s = sortedVal[i];
+  oP[i] = P[s];
+  oD[i] = D[s];
+  oPdf[i] = pdf[s];
+}
+// Ties of equal weight within a leaf (equal adjacent 64-bit keys: same leaf,
+// same weight) are ordered by the full comparator.  Float weights collide by
+// chance (a few percent of the samples of a 2M batch), in runs of a handful,
+// so every run is sorted by the thread at its first sample, all runs at once.
+__global__ void fix_ties_kernel(const unsigned long long *sortedKey, uint32_t n, float4 *oP, float4 *oD,
+                                float *oPdf) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i + 1 >= n) return;
+  const unsigned long long k = sortedKey[i];
+  if (sortedKey[i + 1] != k || (i > 0 && sortedKey[i - 1] == k)) return;  // not the start of a run
+  uint32_t j = i + 2;
+  while (j < n && sortedKey[j] == k) ++j;
+  for (uint32_t x = i + 1; x < j; ++x) {  // insertion sort of the run [i, j)
+    float4 kp = oP[x], kd = oD[x];
+    float kf = oPdf[x];
+    uint32_t y = x;
+    while (y > i && sample_less(kp, kd, kf, oP[y - 1], oD[y - 1], oPdf[y - 1])) {
+      oP[y] = oP[y - 1];
+      oD[y] = oD[y - 1];
+      oPdf[y] = oPdf[y - 1];
+      --y;
     }
+    oP[y] = kp;
+    oD[y] = kd;
+    oPdf[y] = kf;
   }
 }
 
@@ -559,10 +549,20 @@ cudaError_t kd_level(const float4 *pos, const uint32_t *jobOf, uint32_t n, const
   return cudaGetLastError();
 }
 
+// 64-bit sort keys: the leaf's ordinal above the 32-bit weight key.
+__global__ void leaf_key_kernel(const uint32_t *leafBegin, const uint32_t *leafEnd, uint32_t numLeaves,
+                                const uint32_t *key, unsigned long long *key64) {
+  const uint32_t leaf = blockIdx.x;
+  if (leaf >= numLeaves) return;
+  const unsigned long long hi = (unsigned long long)leaf << 32;
+  for (uint32_t i = leafBegin[leaf] + threadIdx.x; i < leafEnd[leaf]; i += blockDim.x) key64[i] = hi | key[i];
+}
+
 cudaError_t gather_and_order(const float4 *posIdx, uint32_t n, const float4 *P, const float4 *D, const float *pdf,
                              const uint32_t *leafBegin, const uint32_t *leafCount, uint32_t numLeaves, bool sorted,
                              float4 *tmpP, float4 *tmpD, float *tmpPdf, uint32_t *keys, uint32_t *vals,
-                             float4 *oP, float4 *oD, float *oPdf, Scratch &scratch, cudaStream_t s) {
+                             unsigned long long *keys64, float4 *oP, float4 *oD, float *oPdf, Scratch &scratch,
+                             cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   if (!sorted) {
     count_launch();
@@ -571,20 +571,26 @@ cudaError_t gather_and_order(const float4 *posIdx, uint32_t n, const float4 *P, 
   }
   count_launch();
   gather_kernel<<<blocks_for(n, 256), 256, 0, s>>>(posIdx, n, P, D, pdf, tmpP, tmpD, tmpPdf, keys, vals);
-  // segment offsets: begin[i] and begin[i] + count[i]
-  uint32_t *keysOut = keys + n;
+  // stable order by (leaf, weight key): one LSD radix sort over the bits in
+  // use (the leaves' sample ranges are disjoint and cover [0, n))
   uint32_t *valsOut = vals + n;
-  size_t tempBytes = 0;
+  unsigned long long *keys64Out = keys64 + n;
   const uint32_t *ends = leafBegin + numLeaves;  // caller stores ends after begins
-  (void)leafCount;
-  cub::DeviceSegmentedSort::StableSortPairs(nullptr, tempBytes, keys, keysOut, vals, valsOut, int(n), int(numLeaves),
-                                            leafBegin, ends, s);
+  count_launch();
+  leaf_key_kernel<<<numLeaves, 256, 0, s>>>(leafBegin, ends, numLeaves, keys, keys64);
+  int leafBits = 1;
+  while (leafBits < 32 && (1u << leafBits) < numLeaves) ++leafBits;
+  size_t tempBytes = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tempBytes, keys64, keys64Out, vals, valsOut, int(n), 0, 32 + leafBits, s);
   cudaError_t e = scratch_reserve(scratch, tempBytes);
   if (e != cudaSuccess) return e;
-  cub::DeviceSegmentedSort::StableSortPairs(scratch.ptr, tempBytes, keys, keysOut, vals, valsOut, int(n),
-                                            int(numLeaves), leafBegin, ends, s);
+  cub::DeviceRadixSort::SortPairs(scratch.ptr, tempBytes, keys64, keys64Out, vals, valsOut, int(n), 0, 32 + leafBits,
+                                  s);
   count_launch();
-  order_kernel<<<numLeaves, 128, 0, s>>>(valsOut, leafBegin, leafCount, numLeaves, tmpP, tmpD, tmpPdf, oP, oD, oPdf);
+  permute_kernel<<<blocks_for(n, 256), 256, 0, s>>>(valsOut, n, tmpP, tmpD, tmpPdf, oP, oD, oPdf);
+  count_launch();
+  fix_ties_kernel<<<blocks_for(n, 256), 256, 0, s>>>(keys64Out, n, oP, oD, oPdf);
+  (void)leafCount;
   return cudaGetLastError();
 }
 
