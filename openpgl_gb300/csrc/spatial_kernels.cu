@@ -109,19 +109,7 @@ __device__ __forceinline__ void quantize(const KdJob &j, float4 p, long long q[3
     qv[d] = (long long)tv;
   }
 }
-__device__ __forceinline__ void acc_global(IStatsAcc *a, const long long q[3], const long long qv[3]) {
-  for (int d = 0; d < 3; ++d) {
-    atomicAdd(reinterpret_cast<unsigned long long *>(&a->m[d]), (unsigned long long)q[d]);
-    atomicAdd(reinterpret_cast<unsigned long long *>(&a->v[d]), (unsigned long long)qv[d]);
-    atomicMin(&a->lo[d], q[d]);
-    atomicMax(&a->hi[d], q[d]);
-  }
-  atomicAdd(&a->n, 1ull);
-}
 
-// Classifies the samples of every job at this level: side flag (1 = left),
-// child statistics into acc[2*job + side].  jobOf[i] is the job of sample i
-// (or ~0 when the sample already sits in a finished leaf).
 // Adds one sample's integer statistics (or a warp's reduced ones) to an
 // accumulator in shared or global memory.
 __device__ __forceinline__ void acc_add(IStatsAcc *a, const long long m[3], const long long v[3], const long long lo[3],
@@ -135,6 +123,9 @@ __device__ __forceinline__ void acc_add(IStatsAcc *a, const long long m[3], cons
   atomicAdd(&a->n, n);
 }
 
+// Classifies the samples of every job at this level: side flag (1 = left),
+// child statistics into acc[2*job + side].  jobOf[i] is the job of sample i
+// (or ~0 when the sample already sits in a finished leaf).
 __global__ void __launch_bounds__(kKdThreads)
 kd_classify_kernel(const float4 *pos, const uint32_t *jobOf, uint32_t n, const KdJob *jobs, uint32_t *isLeft,
                    IStatsAcc *acc) {
@@ -264,7 +255,7 @@ kd_root_stats_kernel(const float4 *pos, uint32_t n, KdJob job, IStatsAcc *acc) {
     }
     cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, off);
   }
-  if ((threadIdx.x & 31) == 0 && cnt > 0) acc_global(acc, m, v), atomicAdd(&acc->n, cnt - 1ull);
+  if ((threadIdx.x & 31) == 0 && cnt > 0) acc_add(acc, m, v, lo, hi, cnt);
 }
 
 // Stable partition inside each job's segment using the exclusive scan of the

@@ -129,6 +129,21 @@ def test_field_compare_and_determinism(pgl):
     assert fields[0].field_bytes() == fields[1].field_bytes()
 
 
+def test_one_leaf_fields(pgl):
+    """Fields whose root never splits (one surface and one volume region over
+    several frames): the region's sample statistics, bounds included, and its
+    mixture match the oracle bit for bit."""
+    from openpgl_gb300 import synthetic as syn
+
+    frames = [syn.cube_face_samples(50000, 90 + i, volume_fraction=0.25) for i in range(3)]
+    dev, field, orc = _train(pgl, frames, 1000000)
+    for side in ("surface", "volume"):
+        r = compare_fields(field.field_bytes(), orc.field_bytes(), side)
+        assert r["regions"] == 1, (side, r)
+        assert r["tree_equal"] and r["stats_equal"], (side, r)
+        assert r["bit_exact_regions"] == 1, (side, r)
+
+
 @pytest.mark.parametrize("blocks", ["2", "4", "8"])
 def test_cluster_shared_regions_match_oracle(pgl, blocks, monkeypatch):
     """The EM passes shared by a thread-block cluster (PGL_EM_CLUSTER) give the
