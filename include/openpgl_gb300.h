@@ -63,13 +63,15 @@ OPENPGL_CORE_INTERFACE uint64_t pglGetKernelLaunchCount();
 // Per-region counters of the last Update: region, EM iterations, splits,
 // merges, components (5 x u32 per region); returns the region count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int volume, uint32_t *out, size_t capacity);
-// Where the EM kernel spent the last Update, per region (15 x u64 each):
+// Where the EM kernel spent the last Update, per region (18 x u64 each):
 // region, samples, E-step passes, distance passes, split-statistics passes,
 // then SM clock cycles in E-steps, distance passes, split-statistics passes,
 // merging, M-steps and in total, then inside the passes the cycles of the
 // producing threads and of the slowest summing thread, for E-steps and for
-// split-statistics passes.  Returns the region count; writes when
-// capacity >= 15 x count.
+// split-statistics passes, then the E-step chunks of the region, those made
+// by its own block (the others by blocks that had no region left), and the
+// cycles a summing thread waited for chunks.  Returns the region count;
+// writes when capacity >= 18 x count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int volume, uint64_t *out,
                                                            size_t capacity);
 // Splits numSamples sample records that live in device memory into the

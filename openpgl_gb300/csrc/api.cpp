@@ -815,10 +815,10 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
   PGL_TRY
   const SubField &sf = volume ? F(field)->volume : F(field)->surface;
   size_t n = sf.lastProfiles.size();
-  if (out && cap >= n)
+  if (out && cap >= 18 * n)
     for (size_t i = 0; i < n; ++i) {
       const LeafProfile &p = sf.lastProfiles[i];
-      uint64_t *o = out + 15 * i;
+      uint64_t *o = out + 18 * i;
       o[0] = sf.lastReportRegion[i];
       o[1] = p.count;
       o[2] = p.estepPasses;
@@ -834,6 +834,9 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
       o[12] = p.cycConsE;
       o[13] = p.cycProdS;
       o[14] = p.cycConsS;
+      o[15] = p.chunks;
+      o[16] = p.chunksOwn;
+      o[17] = p.cycWaitE;
     }
   return n;
   PGL_CATCH(0)

@@ -17,7 +17,6 @@
 // summation order (sequential over samples within each SIMD lane), so every
 // accumulator gets the reference's bits.  Scalar per-leaf logic (M step,
 // split/merge bookkeeping) runs on thread 0 between passes.
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -31,15 +30,38 @@ constexpr int kEmThreads = 512;
 constexpr int kStageFloats = 19200;  // floats per pipeline stage (two stages, 150 KB)
 constexpr int kMaxPairs = kMaxK * (kMaxK - 1) / 2;
 
-// An E-step or distance pass as the home block of a cluster publishes it.
-enum PassCmdKind { kCmdEStep = 0, kCmdDistance = 1, kCmdExit = 3 };
-struct PassCmd {
-  int kind;
-  int cnt;  // lobe vectors
+// E-step passes shared between blocks.  Every block owns a board and a ring of
+// chunk slots in global memory.  For each E-step pass the home block publishes
+// the pass on its board (lobe parameters, sample range, chunk shape).  Its own
+// producer warps take chunks from the board's grab word and write them
+// straight into its shared-memory stages; a block that has run out of leaves
+// (a helper) takes chunks from the same grab word and writes them into the
+// ring, from where the home block's loader warp copies them into the stages
+// with bulk copies.  The consumer warps add the chunks in chunk order.
+constexpr int kMaxStages = 8;                          // consumer pipeline stages
+constexpr uint32_t kRingFloats = 65536;                // ring per block (256 KB)
+constexpr uint32_t kRingMaxSlots = 64;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // longest wait before the launch fails
+constexpr uint32_t kGrabIdxBits = 22;                  // grab word: generation | chunks | next chunk
+constexpr uint32_t kGrabMask = (1u << kGrabIdxBits) - 1u;
+constexpr uint32_t kGrabGenMask = (1u << 20) - 1u;
+constexpr uint32_t kMaxSharedChunks = kGrabMask - 4096u;
+
+enum EmError { kErrNone = 0, kErrChunkWait = 1, kErrSlotWait = 2, kErrCopyWait = 3, kErrLeafTooLarge = 4 };
+
+struct __align__(16) BoardParams {  // one pass as its home block publishes it
+  float4 lobeA[kMaxK + kMaxK / kLanes];
+  float2 lobeB[kMaxK];
   const float4 *dirw;
-  const float *pdf;
-  const float *dist;
-  uint32_t count;
+  uint32_t count, seqBase, cnt, pad;
+};
+struct __align__(128) Board {
+  unsigned long long grab;     // generation (bits 44..63), chunks (22..43), next chunk (0..21)
+  uint32_t pad0[30];
+  uint32_t consumed;           // chunks (sequence numbers) whose ring slots are free again
+  uint32_t pad1[31];
+  uint32_t ready[kRingMaxSlots];  // per ring slot: sequence number of the chunk it holds
+  BoardParams params[2];          // by generation parity
 };
 
 struct Unassigned {
@@ -73,15 +95,24 @@ struct EmShared {
   int iterations;
   LeafReport report;
   LeafProfile prof;
-  PassCmd cmd;         // the pass the home block publishes to its helper blocks
-  int clusterBlocks;   // blocks sharing each region (a thread-block cluster)
-  int producers;       // blocks that produce chunks of E-step and distance passes
-  int homeProduces;    // whether the home block (rank 0) is one of them
+  unsigned long long full[kMaxStages];  // stage holds its chunk (bulk copy or own producers)
+  uint32_t stageUses[kMaxStages];       // completed phases of a stage's barrier
+  uint32_t warpDone[kEmThreads / 32];   // chunks of the pass each consumer warp has added
+  uint32_t own[64];    // sequence numbers of chunks this block's producers took
+  BoardParams hp;      // a helper's copy of the pass it produces for
+  Board *board;        // this block's board and ring
+  float *ring;
+  int *err;            // EmError of the launch
+  uint32_t gen, seqBase, abortAt;
+  int hgrab[2], grabbed, helpBoard, helpExit;
+  uint32_t grabGen;
+  uint32_t scanRem[kEmThreads / 32];
+  int scanIdx[kEmThreads / 32];
   uint32_t validPerWarp[kEmThreads / 32];  // split passes: valid samples per producer warp
   float splitN0[kMaxK];                     // split passes: chi-square counts at the pass start
 };
-static_assert(offsetof(EmShared, pbuf) % 16 == 0 &&
-                  offsetof(EmShared, lobeA) % 16 == 0,
+static_assert(offsetof(EmShared, pbuf) % 16 == 0 && offsetof(EmShared, lobeA) % 16 == 0 &&
+                  offsetof(EmShared, hp) % 16 == 0 && offsetof(EmShared, full) % 8 == 0,
               "128-bit shared loads");
 
 // cycle accounting of thread 0 (LeafProfile)
@@ -512,9 +543,9 @@ __device__ void split_merge_stats(SplitState &s, int I, int J, float wI, V3 muI,
 
 // ---------------------------------------------------------------- sample passes
 //
-// Every pass over a leaf's samples (E-step, distance pass, split-statistics
-// pass) runs as a two-stage pipeline over chunks of samples, with one
-// __syncthreads per chunk and two shared-memory stages:
+// Distance and split-statistics passes run in the home block as a two-stage
+// pipeline over chunks of samples, with one __syncthreads per chunk and two
+// shared-memory stages:
 //   producers (threads [0, C * parts)): `parts` adjacent lanes per sample, one
 //     SIMD vector of 8 lobes each; the lobe terms in registers, the sample pdf
 //     (vfloat8 lane sums carried from part to part in lobe-vector order, then
@@ -530,7 +561,9 @@ __device__ void split_merge_stats(SplitState &s, int I, int J, float wI, V3 muI,
 // becomes -0.  Consumer lanes only load and add, so chain warps do not diverge
 // (chi-square lanes have a warp of their own).  Each pass gives the consumers
 // the warps its chains need and the producers the rest; the chunk size
-// follows from the stage memory and the producer threads.
+// follows from the stage memory and the producer threads.  E-step passes
+// (most of the work) use the same roles, with a loader warp besides, and can
+// take chunks made by other blocks (below).
 
 struct LeafSamples {
   const float4 *dirw;  // direction xyz, weight
@@ -539,7 +572,7 @@ struct LeafSamples {
   uint32_t count;
 };
 
-enum PassKind { kPassEStep = 0, kPassDistance = 1, kPassSplit = 2 };
+enum PassKind { kPassDistance = 1, kPassSplit = 2 };  // in-block passes
 
 // Thread roles and stage layout of one pass (the same in every thread).
 struct PassShape {
@@ -554,11 +587,7 @@ template <PassKind kind>
 __device__ __forceinline__ PassShape pass_shape(int Kp, int budget = kStageFloats) {
   // rows: one per (accumulator, lobe); extra: per-sample arrays
   int consWarps, rows, extra;
-  if (kind == kPassEStep) {  // 4 Kp lobe chains, then LL and 4 unassigned sums
-    consWarps = Kp / 8 + 1;
-    rows = 4 * Kp;
-    extra = 5;
-  } else if (kind == kPassDistance) {  // 2 Kp chains
+  if (kind == kPassDistance) {  // 2 Kp chains
     consWarps = (2 * Kp + 31) / 32;
     rows = 2 * Kp;
     extra = 0;
@@ -696,42 +725,9 @@ __device__ __forceinline__ void produce(EmShared &S, const PassShape &sh, int cn
   const float w = in.dw.w;
   part_terms(S, cnt, sh.parts, v, in.have, d, T);
   const bool valid = in.have && T.valid;
-  const int R = sh.R, C = sh.C;
+  const int R = sh.R;
   const bool mine = v < cnt;  // this lane has lobes
-  if constexpr (kind == kPassEStep) {
-    // rows q Kp + k: (dx a) w, (dy a) w, (dz a) w, a w; then LL and the
-    // unassigned sums per sample
-    if (mine) {
-#pragma unroll
-      for (int j = 0; j < kLanes; ++j) {
-        const int k = v * kLanes + j;
-        float px = 0.0f, py = 0.0f, pz = 0.0f, pw = 0.0f;
-        if (valid) {
-          const float a = T.t[j] * T.inv;
-          px = (d.x * a) * w;
-          py = (d.y * a) * w;
-          pz = (d.z * a) * w;
-          pw = a * w;
-        }
-        B[k * R + s] = px;
-        B[(Kp + k) * R + s] = py;
-        B[(2 * Kp + k) * R + s] = pz;
-        B[(3 * Kp + k) * R + s] = pw;
-      }
-    }
-    if (v == 0) {
-      float *X = B + 4 * Kp * R;
-      // the log-likelihood only drives the convergence test (its relative
-      // change against 0.005); it is not stored, so the single-precision logf
-      // (<= 1 ulp) stands in for the C library's here
-      X[s] = valid ? w * logf(T.pdf) : 0.0f;
-      const bool un = in.have && !T.valid;
-      X[C + s] = un ? w : 0.0f;
-      X[2 * C + s] = un ? d.x * w : 0.0f;
-      X[3 * C + s] = un ? d.y * w : 0.0f;
-      X[4 * C + s] = un ? d.z * w : 0.0f;
-    }
-  } else if constexpr (kind == kPassDistance) {
+  if constexpr (kind == kPassDistance) {
     // rows k: wts * rcp(distance); rows Kp + k: wts
     if (mine) {
       const float sd = valid ? rcp_avx2_tab(in.x, S.rcpTab) : 0.0f;
@@ -843,18 +839,6 @@ __device__ __forceinline__ void row_chain(const float *row, int n4, float &acc) 
   }
 }
 
-// E-step (WEMFactory.h:847-892): lanes c < 4 Kp sum row c ((d_q a_k) w for
-// q = c / Kp < 3, a_k w for q = 3), then the log-likelihood and the four
-// unassigned-sample sums.
-__device__ __forceinline__ void estep_chain(const float *B, const PassShape &sh, int c, int Kp, int n4, float &acc) {
-  if (c < 4 * Kp) {
-    row_chain(B + c * sh.R, n4, acc);
-  } else {
-    const int e = c - 4 * Kp;
-    if (e < 5) row_chain(B + 4 * Kp * sh.R + e * sh.C, n4, acc);
-  }
-}
-
 // Distance pass (WEMFactory.h:1199-1326): lanes c < Kp sum wts * rcp(distance),
 // lanes Kp <= c < 2 Kp sum wts.
 __device__ __forceinline__ void distance_chain(const float *B, const PassShape &sh, int c, int Kp, int n4,
@@ -922,39 +906,19 @@ __device__ __forceinline__ void split_chain(const float *B, const PassShape &sh,
   }
 }
 
-// Stage floats of one producing block's chunk: the home block's two slots
-// are shared by the blocks that produce E-step and distance passes.
-__device__ __forceinline__ int chunk_budget(const EmShared &S, PassKind kind) {
-  if (kind == kPassSplit || S.clusterBlocks <= 1) return kStageFloats;
-  return (kStageFloats / S.producers) & ~7;
-}
-
-// Runs one pass over the leaf's samples in the home block.  `acc`/`accN` are
-// the consumer's accumulators (initialised by the caller).  Chunk c is made by
-// producing block c % producers into sub-stage (c % producers) of the home
-// block's slot ((c / producers) & 1); the home block's consumers add the
-// chunks of a round in chunk order.  With helper blocks (E-step and distance
-// passes in a cluster) the pass is first published (PassCmd); home and
-// helpers then run the same number of rounds, each ending at a cluster
-// barrier.  Split-statistics passes always run in the home block alone.
+// Runs one distance or split-statistics pass over the leaf's samples in the
+// home block.  `acc`/`accN` are the consumer's accumulators (initialised by
+// the caller); chunk c is made into stage (c & 1) while the consumers add
+// chunk c - 1.
 template <PassKind kind>
-__device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const PassShape &sh, int cnt, float &acc,
-                                      float &accN) {
-  namespace cg = cooperative_groups;
+__device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const PassShape &sh, int cnt, float &accOut,
+                                      float &accNOut) {
   const int tid = threadIdx.x;
+  float acc = accOut, accN = accNOut;  // the chains run on registers
   const int Kp = cnt * kLanes;
   const int C = sh.C;
-  const bool cluster = kind != kPassSplit && S.clusterBlocks > 1;
-  const uint32_t PG = cluster ? uint32_t(S.producers) : 1u;
-  const bool homeMakes = !cluster || S.homeProduces;
-  const int sub = chunk_budget(S, kind);
-  if (cluster) {
-    if (tid == 0) S.cmd = PassCmd{int(kind), cnt, L.dirw, L.pdf, L.dist, L.count};
-    cg::this_cluster().sync();
-  }
-  const uint32_t numChunks = (L.count + C - 1) / C;
-  const uint32_t rounds = (numChunks + PG - 1) / PG;
-  const bool producer = homeMakes && tid < sh.threads;
+  const uint32_t rounds = (L.count + C - 1) / C;
+  const bool producer = tid < sh.threads;
   const int s = tid / sh.parts, v = tid % sh.parts;
   const bool consumer = tid >= sh.P;
   const int c = tid - sh.P;
@@ -969,131 +933,708 @@ __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const P
     if (producer && it < rounds) {
       const long long t0 = clock64();
       const SampleIn cur = next;
-      if (it + 1 < rounds) next = load_sample<kind>(L, (it + 1) * PG * C + s);
+      if (it + 1 < rounds) next = load_sample<kind>(L, (it + 1) * C + s);
       produce<kind>(S, sh, cnt, Kp, s, v, cur, S.pbuf + (it & 1) * kStageFloats, base);
       cycP += clock64() - t0;
     }
     if (consumer && it >= 1) {
       const long long t0 = clock64();
-      for (uint32_t r = 0; r < PG; ++r) {
-        const uint32_t chunk = (it - 1) * PG + r;
-        if (chunk >= numChunks) break;
-        const int n = int(min(uint32_t(C), L.count - chunk * C));
-        const int n4 = (n + 3) & ~3;
-        const float *B = S.pbuf + ((it - 1) & 1) * kStageFloats + r * sub;
-        if constexpr (kind == kPassEStep) estep_chain(B, sh, c, Kp, n4, acc);
-        else if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
-        else split_chain(B, sh, c, Kp, n4, n0, acc, accN, count);
-      }
+      const uint32_t chunk = it - 1;
+      const int n = int(min(uint32_t(C), L.count - chunk * C));
+      const int n4 = (n + 3) & ~3;
+      const float *B = S.pbuf + (chunk & 1) * kStageFloats;
+      if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
+      else split_chain(B, sh, c, Kp, n4, n0, acc, accN, count);
       cycC += clock64() - t0;
     }
-    if (cluster) cg::this_cluster().sync();
-    else __syncthreads();
-  }
-  const int probe = kind == kPassSplit ? split_chi_base(Kp) : 0;
-  if (tid == 0) {
-    if (kind == kPassSplit) S.prof.cycProdS += uint64_t(cycP);
-    else if (kind == kPassEStep) S.prof.cycProdE += uint64_t(cycP);
-  }
-  if (c == probe) {
-    if (kind == kPassSplit) S.prof.cycConsS += uint64_t(cycC);
-    else if (kind == kPassEStep) S.prof.cycConsE += uint64_t(cycC);
-  }
-}
-
-// The producer side of a published pass in a helper block (cluster rank
-// r > 0): the home block's rounds, making chunks it * producers + index into
-// the home block's shared memory (distributed shared memory stores).
-template <PassKind kind>
-__device__ __noinline__ void helper_pass(EmShared &S, const PassCmd &cmd, unsigned rank) {
-  namespace cg = cooperative_groups;
-  const int tid = threadIdx.x;
-  const int Kp = cmd.cnt * kLanes;
-  const int sub = chunk_budget(S, kind);
-  const PassShape sh = pass_shape<kind>(Kp, sub);
-  const int C = sh.C;
-  const uint32_t PG = uint32_t(S.producers);
-  const uint32_t index = S.homeProduces ? rank : rank - 1;
-  const LeafSamples L{cmd.dirw, cmd.pdf, cmd.dist, cmd.count};
-  const uint32_t numChunks = (L.count + C - 1) / C;
-  const uint32_t rounds = (numChunks + PG - 1) / PG;
-  const bool producer = tid < sh.threads;
-  const int s = tid / sh.parts, v = tid % sh.parts;
-  uint32_t base = 0;
-  SampleIn next;
-  if (producer) next = load_sample<kind>(L, index * C + s);
-  for (uint32_t it = 0; it <= rounds; ++it) {
-    if (producer && it < rounds && it * PG + index < numChunks) {
-      const SampleIn cur = next;
-      if (it + 1 < rounds) next = load_sample<kind>(L, ((it + 1) * PG + index) * C + s);
-      float *local = S.pbuf + (it & 1) * kStageFloats + index * sub;
-      produce<kind>(S, sh, cmd.cnt, Kp, s, v, cur, cg::this_cluster().map_shared_rank(local, 0u), base);
-    }
-    cg::this_cluster().sync();
-  }
-}
-
-// Helper blocks serve the home block's published passes until kCmdExit.  A
-// command costs both sides one cluster barrier to publish, then the pass's
-// rounds; the exit costs a second barrier so that the home block's shared
-// memory outlives the helpers' read of the command.
-__device__ void helper_loop(EmShared &S, unsigned rank) {
-  namespace cg = cooperative_groups;
-  const int tid = threadIdx.x;
-  EmShared *home = cg::this_cluster().map_shared_rank(&S, 0u);
-  for (;;) {
-    cg::this_cluster().sync();
-    const PassCmd cmd = home->cmd;
-    if (cmd.kind == kCmdExit) {
-      cg::this_cluster().sync();
-      return;
-    }
-    const int Kp = cmd.cnt * kLanes;
-    if (tid < Kp + Kp / kLanes) S.lobeA[tid] = home->lobeA[tid];
-    if (tid < Kp) {
-      S.lobeB[tid] = home->lobeB[tid];
-      S.lobeWInv[tid] = home->lobeWInv[tid];
-    }
     __syncthreads();
-    if (cmd.kind == kCmdEStep) helper_pass<kPassEStep>(S, cmd, rank);
-    else helper_pass<kPassDistance>(S, cmd, rank);
+  }
+  accOut = acc;
+  accNOut = accN;
+  const int probe = kind == kPassSplit ? split_chi_base(Kp) : 0;
+  if (tid == 0 && kind == kPassSplit) S.prof.cycProdS += uint64_t(cycP);
+  if (c == probe && kind == kPassSplit) S.prof.cycConsS += uint64_t(cycC);
+}
+
+// ---------------------------------------------------------------- shared E-step passes
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return uint32_t(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(unsigned long long *m, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *m, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *m) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *m, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(m)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// global -> shared bulk copy (16-byte aligned, a multiple of 16 bytes)
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, unsigned long long *m) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(m))
+               : "memory");
+}
+// orders this thread's generic-proxy global accesses with bulk copies
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+__device__ __forceinline__ void bar_named(int id, int threads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+__device__ __forceinline__ void set_error(int *err, int code) { atomicCAS(err, 0, code); }
+__device__ __forceinline__ bool has_error(const int *err) { return *reinterpret_cast<const volatile int *>(err) != 0; }
+
+// Spins until *p >= want (true) or the launch failed / the wait ran out.
+__device__ bool wait_at_least(const uint32_t *p, uint32_t want, int *err) {
+  unsigned long long t0 = 0;
+  unsigned sleep = 64;
+  for (uint32_t it = 0;; ++it) {
+    if (ld_acquire(p) >= want) return true;
+    if ((it & 31) == 31) {
+      if (has_error(err)) return false;
+      const unsigned long long now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kWaitNs) {
+        set_error(err, kErrSlotWait);
+        return false;
+      }
+    }
+    __nanosleep(sleep);
+    sleep = sleep < 1024 ? 2 * sleep : sleep;
+  }
+}
+// Waits for phase `parity` of a stage barrier.  Consumers give up on chunks
+// from *abortAt on (the loader gave up on them: nothing will arrive); every
+// waiter gives up after kWaitNs.
+__device__ bool mbar_wait(unsigned long long *m, uint32_t parity, const volatile uint32_t *abortAt, uint32_t k,
+                          int *err) {
+  unsigned long long t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try_wait(m, parity)) return true;
+    if (abortAt && k >= *abortAt) return false;
+    if ((it & 15) == 15) {
+      const unsigned long long now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kWaitNs) {
+        set_error(err, kErrCopyWait);
+        return false;
+      }
+    }
   }
 }
 
-// E-step over all samples into S.cur, S.ll and S.un.
+__device__ __forceinline__ unsigned long long grab_word(uint32_t gen, uint32_t chunks, uint32_t next) {
+  return (static_cast<unsigned long long>(gen) << (2 * kGrabIdxBits)) |
+         (static_cast<unsigned long long>(chunks) << kGrabIdxBits) | next;
+}
+__device__ __forceinline__ uint32_t grab_gen(unsigned long long w) { return uint32_t(w >> (2 * kGrabIdxBits)); }
+__device__ __forceinline__ uint32_t grab_chunks(unsigned long long w) { return uint32_t(w >> kGrabIdxBits) & kGrabMask; }
+__device__ __forceinline__ uint32_t grab_next(unsigned long long w) { return uint32_t(w) & kGrabMask; }
+// Chunk shape of an E-step pass with `cnt` lobe vectors: consumers need
+// 4 Kp + 5 chains in warps of one kind each (chain_role), one warp loads
+// chunks made by other blocks, producers get
+// the remaining warps (P threads, one chunk of C = P / parts samples).  A
+// chunk holds rows of RS = C + 4 floats (RS / 4 odd, so the consumers'
+// 128-bit loads of 8 consecutive rows hit distinct banks): a_k for k < Kp
+// (the soft assignment t_k / pdf of valid samples, 0 otherwise), the
+// direction x, y, z, the weight of valid samples, then w log(pdf) and the
+// four unassigned-sample terms.
+struct EStepShape {
+  int cnt, Kp, parts, P, cons0, consWarps, C, RS, stageFloats, stages, slots;
+};
+__device__ __forceinline__ EStepShape estep_shape(int cnt) {
+  EStepShape e;
+  e.cnt = cnt;
+  e.Kp = cnt * kLanes;
+  e.parts = cnt == 3 ? 4 : cnt;
+  e.consWarps = 2 + (3 * e.Kp + 31) / 32;  // a w | (d a) w | per-sample rows
+  e.cons0 = kEmThreads - 32 * e.consWarps;  // consumers: threads [cons0, 512)
+  e.P = e.cons0 - 32;                       // producers [0, P), then the loader warp
+  e.C = (e.P / e.parts) & ~7;
+  e.RS = e.C + 4;
+  e.stageFloats = (e.Kp + 9) * e.RS;
+  e.stages = min(kMaxStages, 2 * kStageFloats / e.stageFloats);
+  e.slots = min(int(kRingMaxSlots), int(kRingFloats) / e.stageFloats);
+  return e;
+}
+
+// Producers: `nthreads` threads (index t) fill chunk `chunk` into G (a stage
+// or a ring slot).  A sample's `parts` lanes are adjacent, so every warp holds
+// whole samples; rounds of nthreads / parts samples cover the chunk.
+template <bool kRing>
+__device__ void produce_estep_chunk(const EmShared &S, const EStepShape &e, const float4 *dirw, uint32_t count,
+                                    uint32_t chunk, float *G, int t, int nthreads) {
+  const int per = nthreads / e.parts;
+  const int v = t % e.parts;
+  const int RS = e.RS, Kp = e.Kp;
+  for (int base = 0; base < e.C; base += per) {
+    const int s = base + t / e.parts;
+    const uint32_t idx = chunk * uint32_t(e.C) + uint32_t(s);
+    const bool have = s < e.C && idx < count;
+    const float4 dw = have ? __ldcg(dirw + idx) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const V3 d = mk(dw.x, dw.y, dw.z);
+    PartTerms T;
+    part_terms(S, e.cnt, e.parts, v, have, d, T);
+    if (s < e.C) {
+      const bool valid = have && T.valid;
+      if (v < e.cnt) {
+#pragma unroll
+        for (int j = 0; j < kLanes; ++j) G[(v * kLanes + j) * RS + s] = valid ? T.t[j] * T.inv : 0.0f;
+      }
+      if (v == 0) {
+        const float w = dw.w;
+        const bool un = have && !T.valid;
+        float *X = G + Kp * RS + s;
+        X[0] = d.x;
+        X[RS] = d.y;
+        X[2 * RS] = d.z;
+        X[3 * RS] = valid ? w : 0.0f;
+        // the log-likelihood only drives the convergence test (its relative
+        // change against 0.005); it is not stored, so the single-precision
+        // logf (<= 1 ulp) stands in for the C library's here
+        X[4 * RS] = valid ? w * logf(T.pdf) : 0.0f;
+        X[5 * RS] = un ? w : 0.0f;
+        X[6 * RS] = un ? d.x * w : 0.0f;
+        X[7 * RS] = un ? d.y * w : 0.0f;
+        X[8 * RS] = un ? d.z * w : 0.0f;
+      }
+    }
+  }
+  if (kRing) fence_proxy_async();  // the ring is read by bulk copies
+}
+
+// A helper's chunk of board `b` (taken when its ring slot was free, so the
+// slot wait rarely waits): fill the slot, then publish its sequence number.
+__device__ void produce_for(EmShared &S, Board &b, float *ring, const EStepShape &e, const float4 *dirw,
+                            uint32_t count, uint32_t seqBase, uint32_t chunk) {
+  const int t = threadIdx.x;
+  const uint32_t seq = seqBase + chunk + 1u, slot = (seqBase + chunk) % uint32_t(e.slots);
+  // the slot's previous chunk (sequence number seq - slots) must have been copied out
+  if (t == 0 && seq > uint32_t(e.slots)) wait_at_least(&b.consumed, seq - uint32_t(e.slots), S.err);
+  __syncthreads();
+  produce_estep_chunk<true>(S, e, dirw, count, chunk, ring + size_t(slot) * e.stageFloats, t, kEmThreads);
+  __syncthreads();
+  if (t == 0) {
+    __threadfence();
+    st_release(&b.ready[slot], seq);
+  }
+}
+
+// Consumer side of the sum: a_k w, (d_q a_k) w or a per-sample row, in
+// sample order (the products are those of the reference's E-step).
+// Each chain keeps three groups of four samples in registers: the loads of a
+// group are issued two groups before it is added (a warp issues in order, so
+// loads placed after the dependent adds would wait for them).  The products
+// of two samples share one packed multiply (each component rounded as its
+// own multiply).  The loop runs in a function of its own (its registers are
+// not shared with the rest of the kernel) on 32-bit shared-memory addresses.
+__device__ __forceinline__ float4 lds4(uint32_t a) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+  return v;
+}
+template <int kKind>  // 0: a w, 1: (d a) w, 2: the value itself
+__device__ __forceinline__ void add_group(float &acc, float4 a, float4 d, float4 w) {
+  if (kKind == 2) {
+    acc += a.x;
+    acc += a.y;
+    acc += a.z;
+    acc += a.w;
+  } else {
+    float2 p0 = make_float2(a.x, a.y), p1 = make_float2(a.z, a.w);
+    if (kKind == 1) {
+      p0 = __fmul2_rn(make_float2(d.x, d.y), p0);
+      p1 = __fmul2_rn(make_float2(d.z, d.w), p1);
+    }
+    p0 = __fmul2_rn(p0, make_float2(w.x, w.y));
+    p1 = __fmul2_rn(p1, make_float2(w.z, w.w));
+    acc += p0.x;
+    acc += p0.y;
+    acc += p1.x;
+    acc += p1.y;
+  }
+}
+template <int kKind>
+__device__ __forceinline__ float4 lds_if(uint32_t a) {
+  return kKind ? lds4(a) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+// Rows start at 32-bit shared addresses A, D, W (bytes); n4 samples.
+template <int kKind>
+__device__ __noinline__ float chain_rows(uint32_t A, uint32_t D, uint32_t W, int n4, float acc) {
+  constexpr int kD = kKind == 1, kW = kKind != 2;
+  // rows hold C + 4 >= 12 floats: the first two groups can be read even
+  // when n4 is smaller
+  float4 a0 = lds4(A), d0 = lds_if<kD>(D), w0 = lds_if<kW>(W);
+  float4 a1 = lds4(A + 16), d1 = lds_if<kD>(D + 16), w1 = lds_if<kW>(W + 16);
+  int s = 0;
+  for (; s + 12 <= n4; s += 12) {
+    const uint32_t o2 = uint32_t(s + 8) * 4u;
+    const float4 a2 = lds4(A + o2), d2 = lds_if<kD>(D + o2), w2 = lds_if<kW>(W + o2);
+    add_group<kKind>(acc, a0, d0, w0);
+    const uint32_t o3 = uint32_t(s + 12 < n4 ? s + 12 : 0) * 4u;
+    a0 = lds4(A + o3);
+    d0 = lds_if<kD>(D + o3);
+    w0 = lds_if<kW>(W + o3);
+    add_group<kKind>(acc, a1, d1, w1);
+    const uint32_t o4 = uint32_t(s + 16 < n4 ? s + 16 : 0) * 4u;
+    a1 = lds4(A + o4);
+    d1 = lds_if<kD>(D + o4);
+    w1 = lds_if<kW>(W + o4);
+    add_group<kKind>(acc, a2, d2, w2);
+  }
+  if (s < n4) add_group<kKind>(acc, a0, d0, w0);
+  if (s + 4 < n4) add_group<kKind>(acc, a1, d1, w1);
+  if (s + 8 < n4) {
+    const uint32_t o2 = uint32_t(s + 8) * 4u;
+    add_group<kKind>(acc, lds4(A + o2), lds_if<kD>(D + o2), lds_if<kW>(W + o2));
+  }
+  return acc;
+}
+// The chain of consumer thread c.  Warps hold one kind of chain each, so no
+// warp runs two loops one after the other: the first warp sums a_k w (k =
+// lane), the next ceil(3 Kp / 32) warps sum (d_q a_k) w, the last warp the
+// five per-sample rows; other lanes are idle (kind -1).
+struct ChainRole {
+  int kind, k, q;
+};
+__device__ __forceinline__ ChainRole chain_role(const EStepShape &e, int c) {
+  const int heavyWarps = e.consWarps - 2;
+  const int cw = c >> 5, lane = c & 31;
+  ChainRole r{-1, 0, 0};
+  if (cw == 0) {
+    if (lane < e.Kp) r = ChainRole{0, lane, 3};
+  } else if (cw <= heavyWarps) {
+    const int h = (cw - 1) * 32 + lane;
+    if (h < 3 * e.Kp) r = ChainRole{1, h % e.Kp, h / e.Kp};
+  } else if (lane < 5) {
+    r = ChainRole{2, lane, 0};
+  }
+  return r;
+}
+__device__ __forceinline__ void estep_chunk_chain(const float *B, const EStepShape &e, const ChainRole &role, int n4,
+                                                  float &acc) {
+  const int Kp = e.Kp;
+  const uint32_t base = smem_u32(B), row = uint32_t(e.RS) * 4u;
+  const uint32_t W = base + uint32_t(Kp + 3) * row;
+  if (role.kind == 0) {
+    acc = chain_rows<0>(base + uint32_t(role.k) * row, W, W, n4, acc);
+  } else if (role.kind == 1) {
+    acc = chain_rows<1>(base + uint32_t(role.k) * row, base + uint32_t(Kp + role.q) * row, W, n4, acc);
+  } else if (role.kind == 2) {
+    const uint32_t X = base + uint32_t(Kp + 4 + role.k) * row;
+    acc = chain_rows<2>(X, X, X, n4, acc);
+  }
+}
+
+// Barrier phase of chunk k: use k / stages of stage k % stages.
+__device__ __forceinline__ uint32_t use_parity(const EmShared &S, const EStepShape &e, uint32_t k) {
+  return (S.stageUses[k % uint32_t(e.stages)] + k / uint32_t(e.stages)) & 1u;
+}
+// Chunks that every consumer warp has added (they are added in order).
+__device__ __forceinline__ uint32_t chunks_done(const EmShared &S, const EStepShape &e) {
+  const volatile uint32_t *d = S.warpDone;
+  uint32_t m = d[0];
+  for (int w = 1; w < e.consWarps; ++w) m = min(m, d[w]);
+  return m;
+}
+
+// Consumer warps (threads [cons0, 512)): chunk k is added once stage
+// k % stages is full; each warp then records its progress.
+__device__ __forceinline__ float consume_estep(EmShared &S, const EStepShape &e, uint32_t N, uint32_t count) {
+  const int r = int(threadIdx.x) - e.cons0;
+  const ChainRole role = chain_role(e, r);
+  float acc = 0.0f;
+  const int lane = int(threadIdx.x & 31);
+  long long waited = 0;
+  for (uint32_t k = 0; k < N; ++k) {
+    const int st = int(k % uint32_t(e.stages));
+    const long long w0 = clock64();
+    if (!mbar_wait(&S.full[st], use_parity(S, e, k), &S.abortAt, k, S.err)) break;
+    waited += clock64() - w0;
+    const int n = int(min(uint32_t(e.C), count - k * uint32_t(e.C)));
+    estep_chunk_chain(S.pbuf + st * e.stageFloats, e, role, (n + 3) & ~3, acc);
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();  // this warp's reads of the stage come first
+      reinterpret_cast<volatile uint32_t *>(S.warpDone)[r >> 5] = k + 1u;
+    }
+  }
+  if (r == 32) S.prof.cycWaitE += uint64_t(waited);
+  return acc;
+}
+
+// Waits until the consumers are done with chunk `need - 1` (bounded).
+__device__ void wait_done(const EmShared &S, const EStepShape &e, uint32_t need) {
+  unsigned long long t0 = 0;
+  for (uint32_t it = 0; chunks_done(S, e) < need; ++it) {
+    __nanosleep(64);
+    if ((it & 31) == 31) {
+      if (has_error(S.err)) return;
+      const unsigned long long now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kWaitNs) {
+        set_error(S.err, kErrSlotWait);
+        return;
+      }
+    }
+  }
+  __threadfence_block();
+}
+
+// Loader warp: the chunks of the pass in order, 32 at a time.  A chunk is
+// settled when this block's producers took it (they fill its stage) or when
+// its ring slot holds it and its stage is free (then a bulk copy brings it
+// in).  Ring slots are handed back as the consumers finish chunks (all of
+// them at the end of the pass).
+__device__ void load_chunks(EmShared &S, const EStepShape &e, uint32_t N, uint32_t seqBase) {
+  Board &b = *S.board;
+  const int lane = int(threadIdx.x & 31);
+  const uint32_t bytes = uint32_t(e.stageFloats) * 4u;
+  const uint32_t stages = uint32_t(e.stages);
+  uint32_t issued = 0, released = 0;
+  unsigned long long t0 = 0;
+  while (issued < N) {
+    const uint32_t done = chunks_done(S, e);
+    if (done > released) {
+      if (lane == 0) st_release(&b.consumed, seqBase + done);
+      released = done;
+    }
+    const uint32_t j = issued + uint32_t(lane);
+    bool ok = false, copy = false;
+    if (j < N && j < done + stages) {  // stage j % stages is free
+      const uint32_t seq = seqBase + j + 1u;
+      if (reinterpret_cast<volatile uint32_t *>(S.own)[j & 63u] == seq) ok = true;
+      else if (ld_relaxed(&b.ready[(seqBase + j) % uint32_t(e.slots)]) == seq) ok = copy = true;
+    }
+    const unsigned okMask = __ballot_sync(0xFFFFFFFFu, ok);
+    const uint32_t prefix = okMask == 0xFFFFFFFFu ? 32u : uint32_t(__ffs(~okMask)) - 1u;  // settled from `issued` on
+    if (copy && uint32_t(lane) < prefix) {
+      // the relaxed read saw the producer's release: acquire before the copy
+      fence_acquire();
+      fence_proxy_async();
+      const int st = int(j % stages);
+      mbar_expect_tx(&S.full[st], bytes);
+      bulk_load(S.pbuf + st * e.stageFloats, S.ring + size_t((seqBase + j) % uint32_t(e.slots)) * e.stageFloats,
+                bytes, &S.full[st]);
+    }
+    issued += prefix;
+    if (prefix == 0) {
+      if (has_error(S.err)) {
+        if (lane == 0) S.abortAt = issued;
+        return;
+      }
+      const unsigned long long now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kWaitNs) {
+        if (lane == 0) {
+          set_error(S.err, kErrChunkWait);
+          S.abortAt = issued;
+        }
+        return;
+      }
+      __nanosleep(200);
+    } else {
+      t0 = 0;
+    }
+    __syncwarp();
+  }
+}
+
+// This block's producers (threads [0, P)): take chunks from their own board,
+// write each into its stage once the consumers are done with the stage's
+// previous chunk, and complete the stage's full barrier.  Producing a sample
+// costs the SM several times the issue slots of adding it, so the producers
+// step back while helpers supply the consumers: when the chunks they take
+// are not consecutive (other blocks are taking chunks too), they take the
+// next one only once the board's next free chunk is within `stages` of the
+// consumers; while they are alone, the next grab overlaps the current
+// chunk's production.
+__device__ int take_own_chunk(EmShared &S, const EStepShape &e, Board &b, uint32_t gen) {
+  unsigned long long t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    if (has_error(S.err)) return -1;
+    const unsigned long long w = ld_relaxed64(&b.grab);
+    if (grab_gen(w) != gen || grab_next(w) >= grab_chunks(w)) return -1;  // none left
+    if (grab_next(w) < chunks_done(S, e) + uint32_t(e.stages)) {
+      const unsigned long long w2 = atomicAdd(&b.grab, 1ull);
+      return (grab_gen(w2) == gen && grab_next(w2) < grab_chunks(w2)) ? int(grab_next(w2)) : -1;
+    }
+    __nanosleep(256);
+    if ((it & 15) == 15) {
+      const unsigned long long now = global_ns();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kWaitNs) {
+        set_error(S.err, kErrChunkWait);
+        return -1;
+      }
+    }
+  }
+}
+__device__ void produce_own(EmShared &S, const EStepShape &e, const LeafSamples &L, uint32_t seqBase) {
+  Board &b = *S.board;
+  const int t = threadIdx.x;
+  const uint32_t gen = S.gen;  // read by thread 0 only, which wrote it
+  bool alone = true;           // thread 0: the last two chunks taken were consecutive
+  if (t == 0) {
+    const unsigned long long w = atomicAdd(&b.grab, 1ull);
+    S.hgrab[0] = (!has_error(S.err) && grab_gen(w) == gen && grab_next(w) < grab_chunks(w)) ? int(grab_next(w)) : -1;
+  }
+  uint32_t made = 0;
+  for (uint32_t i = 0;; ++i) {
+    if (t == 0) {
+      const int c0 = S.hgrab[i & 1u];
+      if (c0 >= 0) {
+        // mark the chunk as this block's only once its stage is free: it is
+        // then within `stages` chunks of the consumers, so the marker's slot
+        // (chunk - 64) has been settled and consumed long ago
+        const uint32_t k = uint32_t(c0);
+        if (k >= uint32_t(e.stages)) wait_done(S, e, k - uint32_t(e.stages) + 1u);
+        reinterpret_cast<volatile uint32_t *>(S.own)[k & 63u] = seqBase + k + 1u;
+      }
+    }
+    bar_named(3, e.P);
+    const int chunk = S.hgrab[i & 1u];
+    if (chunk < 0) break;
+    ++made;
+    const uint32_t k = uint32_t(chunk);
+    const int st = int(k % uint32_t(e.stages));
+    unsigned long long w = 0;
+    const bool early = t == 0 && alone && !has_error(S.err);
+    if (early) w = atomicAdd(&b.grab, 1ull);
+    produce_estep_chunk<false>(S, e, L.dirw, L.count, k, S.pbuf + st * e.stageFloats, t, e.P);
+    bar_named(3, e.P);
+    if (t == 0) {
+      mbar_arrive(&S.full[st]);
+      int nextChunk;
+      if (early) {
+        nextChunk = (grab_gen(w) == gen && grab_next(w) < grab_chunks(w)) ? int(grab_next(w)) : -1;
+        alone = nextChunk == chunk + 1;
+      } else {
+        nextChunk = take_own_chunk(S, e, b, gen);
+      }
+      S.hgrab[(i + 1u) & 1u] = nextChunk;
+    }
+  }
+  if (t == 0) S.prof.chunksOwn += made;
+}
+
+// E-step over all samples into S.cur, S.ll and S.un (WEMFactory.h:847-892).
 __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
   const int tid = threadIdx.x;
   const int cnt = vec_count(int(S.vmm.K));
-  const int Kp = cnt * kLanes;
-  const PassShape sh = pass_shape<kPassEStep>(Kp, chunk_budget(S, kPassEStep));
+  const EStepShape e = estep_shape(cnt);
+  const int Kp = e.Kp;
+  uint32_t N = (L.count + uint32_t(e.C) - 1u) / uint32_t(e.C);
+  if (N > kMaxSharedChunks) {
+    if (tid == 0) set_error(S.err, kErrLeafTooLarge);
+    N = 0;
+  }
   if (tid == 0) {
     S.un = Unassigned{0.f, 0.f, 0.f, 0.f};
     suff_clear(S.cur, S.vmm.K);
     S.cur.K = S.vmm.K;
     S.cur.numSamples = float(L.count);
+    S.abortAt = has_error(S.err) ? 0u : 0xFFFFFFFFu;
   }
+  if (tid < kEmThreads / 32) S.warpDone[tid] = 0;
   pack_lobes(S, Kp);
   __syncthreads();
-  float acc = 0.0f, accN = 0.0f;
-  run_pass<kPassEStep>(S, L, sh, cnt, acc, accN);
-  const int c = tid - sh.P;
-  if (c >= 0) {
-    if (c < 4 * Kp) {
-      const int q = c / Kp, k = c % Kp;
-      if (q == 0) S.cur.dx[k] = acc;
-      else if (q == 1) S.cur.dy[k] = acc;
-      else if (q == 2) S.cur.dz[k] = acc;
-      else S.cur.w[k] = acc;
-    } else {
-      const int e = c - 4 * Kp;
-      if (e == 0) S.ll = acc;
-      else if (e == 1) S.un.sw = acc;
-      else if (e == 2) S.un.dx = acc;
-      else if (e == 3) S.un.dy = acc;
-      else if (e == 4) S.un.dz = acc;
+  const uint32_t seqBase = S.seqBase;
+  if (tid == 0) {  // publish the pass on the board
+    Board &b = *S.board;
+    const uint32_t gen = S.gen % kGrabGenMask + 1u;
+    S.gen = gen;
+    BoardParams &bp = b.params[gen & 1u];
+    for (int i = 0; i < Kp + Kp / kLanes; ++i) bp.lobeA[i] = S.lobeA[i];
+    for (int i = 0; i < Kp; ++i) bp.lobeB[i] = S.lobeB[i];
+    bp.dirw = L.dirw;
+    bp.count = L.count;
+    bp.seqBase = seqBase;
+    bp.cnt = uint32_t(cnt);
+    __threadfence();
+    atomicExch(&b.grab, grab_word(gen, N, 0));
+  }
+  float acc = 0.0f;
+  const long long t0 = clock64();
+  if (tid < e.P) produce_own(S, e, L, seqBase);
+  else if (tid < e.cons0) load_chunks(S, e, N, seqBase);
+  else acc = consume_estep(S, e, N, L.count);
+  const long long cyc = clock64() - t0;
+  if (tid == 0) S.prof.cycProdE += uint64_t(cyc);
+  if (tid == e.cons0 + 32) S.prof.cycConsE += uint64_t(cyc);
+  __syncthreads();
+  if (tid >= e.cons0) {
+    const ChainRole role = chain_role(e, tid - e.cons0);
+    if (role.kind == 0) {
+      S.cur.w[role.k] = acc;
+    } else if (role.kind == 1) {
+      if (role.q == 0) S.cur.dx[role.k] = acc;
+      else if (role.q == 1) S.cur.dy[role.k] = acc;
+      else S.cur.dz[role.k] = acc;
+    } else if (role.kind == 2) {
+      const int x = role.k;
+      if (x == 0) S.ll = acc;
+      else if (x == 1) S.un.sw = acc;
+      else if (x == 2) S.un.dx = acc;
+      else if (x == 3) S.un.dy = acc;
+      else S.un.dz = acc;
     }
   }
+  if (tid == 0) {
+    S.prof.chunks += N;
+    for (int st = 0; st < e.stages; ++st)
+      S.stageUses[st] += N > uint32_t(st) ? (N - uint32_t(st) + uint32_t(e.stages) - 1u) / uint32_t(e.stages) : 0u;
+    S.seqBase = seqBase + N;
+    st_release(&S.board->consumed, seqBase + N);
+  }
   __syncthreads();
+}
+
+// A block without leaves produces chunks for other blocks' E-step passes:
+// it picks the board with the most chunks left and takes chunks from it while
+// it has any (loading the pass parameters when the generation changes).  It
+// leaves once every leaf of the launch is finished (or the launch failed).
+__device__ void help_others(EmShared &S, Board *boards, float *rings, const uint32_t *finished, uint32_t numTasks) {
+  const int tid = threadIdx.x;
+  const int nb = int(gridDim.x);
+  int cachedBoard = -1;
+  uint32_t cachedGen = 0;
+  for (;;) {
+    // scan: the board with the most chunks left
+    uint32_t bestRem = 0;
+    int best = -1;
+    for (int i = tid; i < nb; i += kEmThreads) {
+      const unsigned long long w = ld_relaxed64(&boards[i].grab);
+      const uint32_t n = grab_chunks(w), nx = grab_next(w);
+      const uint32_t rem = (grab_gen(w) != 0 && nx < n) ? n - nx : 0u;
+      if (rem > bestRem) {
+        bestRem = rem;
+        best = i;
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const uint32_t r = __shfl_down_sync(0xFFFFFFFFu, bestRem, off);
+      const int i = __shfl_down_sync(0xFFFFFFFFu, best, off);
+      if (r > bestRem) {
+        bestRem = r;
+        best = i;
+      }
+    }
+    if ((tid & 31) == 0) {
+      S.scanRem[tid >> 5] = bestRem;
+      S.scanIdx[tid >> 5] = best;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t r = 0;
+      int bi = -1;
+      for (int w = 0; w < kEmThreads / 32; ++w)
+        if (S.scanRem[w] > r) {
+          r = S.scanRem[w];
+          bi = S.scanIdx[w];
+        }
+      S.helpBoard = bi;
+      S.helpExit = has_error(S.err) || (bi < 0 && ld_acquire(finished) >= numTasks);
+    }
+    __syncthreads();
+    if (S.helpExit) return;
+    const int bi = S.helpBoard;
+    if (bi < 0) {
+      __nanosleep(1000);
+      continue;
+    }
+    Board &b = boards[bi];
+    for (int tries = 0;;) {
+      if (tid == 0) {
+        // take the board's next chunk only when its ring slot is free (the
+        // pass's sequence numbers are known once its parameters are loaded);
+        // a chunk of a pass not loaded yet is taken, and loaded below
+        const unsigned long long w = ld_relaxed64(&b.grab);
+        const uint32_t consumed = ld_relaxed(&b.consumed);
+        int ch = -1;
+        uint32_t g = 0;
+        bool room = true;
+        if (has_error(S.err) || grab_gen(w) == 0 || grab_next(w) >= grab_chunks(w)) {
+          ch = -1;
+        } else {
+          if (bi == cachedBoard && grab_gen(w) == cachedGen)
+            room = S.hp.seqBase + grab_next(w) + 1u <= consumed + uint32_t(estep_shape(int(S.hp.cnt)).slots);
+          if (room) {
+            const unsigned long long w2 = atomicAdd(&b.grab, 1ull);
+            if (grab_gen(w2) != 0 && grab_next(w2) < grab_chunks(w2)) {
+              ch = int(grab_next(w2));
+              g = grab_gen(w2);
+            }
+          }
+        }
+        S.grabbed = room ? ch : -2;  // -2: the ring is full for now
+        S.grabGen = g;
+      }
+      __syncthreads();
+      const int chunk = S.grabbed;
+      const uint32_t gen = S.grabGen;
+      if (chunk == -2) {
+        __syncthreads();  // everyone has read S.grabbed before thread 0 rewrites it
+        if (++tries > 64) break;  // look at the other boards again
+        __nanosleep(200);
+        continue;
+      }
+      if (chunk < 0) break;
+      tries = 0;
+      if (bi != cachedBoard || gen != cachedGen) {
+        // the generation was published (atomic exchange) after its parameters
+        if (tid == 0) __threadfence();
+        __syncthreads();
+        const BoardParams &src = b.params[gen & 1u];
+        for (int i = tid; i < kMaxK + kMaxK / kLanes; i += kEmThreads) S.lobeA[i] = __ldcg(&src.lobeA[i]);
+        for (int i = tid; i < kMaxK; i += kEmThreads) S.lobeB[i] = __ldcg(&src.lobeB[i]);
+        if (tid == 0) {
+          S.hp.dirw = reinterpret_cast<const float4 *>(__ldcg(reinterpret_cast<const unsigned long long *>(&src.dirw)));
+          S.hp.count = __ldcg(&src.count);
+          S.hp.seqBase = __ldcg(&src.seqBase);
+          S.hp.cnt = __ldcg(&src.cnt);
+        }
+        __syncthreads();
+        cachedBoard = bi;
+        cachedGen = gen;
+      }
+      const EStepShape e = estep_shape(int(S.hp.cnt));
+      produce_for(S, b, rings + size_t(bi) * kRingFloats, e, S.hp.dirw, S.hp.count, S.hp.seqBase, uint32_t(chunk));
+      __syncthreads();
+    }
+  }
 }
 
 // init/updateComponentDistances (WEMFactory.h:1199-1326)
@@ -1101,7 +1642,7 @@ __device__ void pass_distances(EmShared &S, const LeafSamples &L, bool init) {
   const int tid = threadIdx.x;
   const int cnt = vec_count(int(S.vmm.K));
   const int Kp = cnt * kLanes;
-  const PassShape sh = pass_shape<kPassDistance>(Kp, chunk_budget(S, kPassDistance));
+  const PassShape sh = pass_shape<kPassDistance>(Kp);
   pack_lobes(S, Kp);
   __syncthreads();
   float acc = 0.0f, accN = 0.0f;
@@ -1467,35 +2008,36 @@ __device__ void reproject_leaf(const LeafTask &t, float4 *pd, float4 *dirw, floa
 }
 
 __global__ void __launch_bounds__(kEmThreads)
-em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
-               float4 *dirw, const float *pdf, float *dist, FieldConfig cfg, const float *uniformDirs,
-               LeafReport *reports, LeafProfile *profiles) {
+em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, EmSides sides, LeafReport *reports,
+               LeafProfile *profiles, Board *boards, float *rings, int *err, uint32_t *finished) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EmShared &S = *reinterpret_cast<EmShared *>(smem_raw);
   __shared__ uint32_t taskId;
   __shared__ uint64_t afterSplit, afterMerge;
   for (int i = threadIdx.x; i < 2048; i += blockDim.x) S.rcpTab[i] = rcp_seed(uint32_t(i));
-  // a cluster of G blocks shares each region: rank 0 (home) owns it; with 2
-  // blocks both produce E-step and distance chunks, with more the home block
-  // only sums and the others produce (helper_loop)
-  const unsigned G = cooperative_groups::this_cluster().num_blocks();
-  const unsigned rank = cooperative_groups::this_cluster().block_rank();
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) S.own[i] = 0;
   if (threadIdx.x == 0) {
-    S.clusterBlocks = int(G);
-    S.homeProduces = G <= 2 ? 1 : 0;
-    S.producers = G <= 2 ? int(G) : int(G) - 1;
+    S.board = boards + blockIdx.x;
+    S.ring = rings + size_t(blockIdx.x) * kRingFloats;
+    S.err = err;
+    S.gen = 0;
+    S.seqBase = 0;
+    for (int i = 0; i < kMaxStages; ++i) {
+      mbar_init(&S.full[i], 1);
+      S.stageUses[i] = 0;
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
-  if (rank != 0) {
-    helper_loop(S, rank);
-    return;
-  }
   for (;;) {
     if (threadIdx.x == 0) taskId = atomicAdd(queue, 1u);
     __syncthreads();
     if (taskId >= numTasks) break;
     const LeafTask t = tasks[taskId];
-    RegionDir &R = regions[t.region];
+    const EmSide &E = sides.side[(t.flags & kTaskVolume) ? 1 : 0];
+    const FieldConfig &cfg = E.cfg;
+    RegionDir &R = E.regions[t.region];
     // load the region's directional state
     {
       const uint32_t *src = reinterpret_cast<const uint32_t *>(&R.vmm);
@@ -1510,12 +2052,12 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
     }
     const long long leafStart = clock64();
     if (threadIdx.x == 0) {
-      S.prof = LeafProfile{t.count, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      S.prof = LeafProfile{t.count, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
       afterSplit = R.afterSplit;
       afterMerge = R.afterMerge;
       S.report = LeafReport{0, 0, 0, 0};
     }
-    reproject_leaf(t, pd, dirw, dist);
+    reproject_leaf(t, E.pd, E.dirw, E.dist);
     __syncthreads();
     const bool fit = (t.flags & kTaskFit) != 0;
     if (!fit && (t.flags & kTaskDecay) && threadIdx.x == 0) {  // Field.h:457-461
@@ -1525,9 +2067,9 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
     __syncthreads();
     uint32_t valid = R.valid;
     if (t.count > 0) {
-      LeafSamples L{dirw + t.begin, pdf + t.begin, dist + t.begin, t.count};
+      LeafSamples L{E.dirw + t.begin, E.pdf + t.begin, E.dist + t.begin, t.count};
       if (fit) {
-        asm_fit(S, L, cfg, uniformDirs);
+        asm_fit(S, L, cfg, E.uniformDirs);
         if (threadIdx.x == 0) {
           S.vmm.pivot[0] = t.mean[0]; S.vmm.pivot[1] = t.mean[1]; S.vmm.pivot[2] = t.mean[2];
           valid = vmm_is_valid(S.vmm) ? 1u : 0u;
@@ -1570,59 +2112,49 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Re
         S.prof.cycTotal = uint64_t(clock64() - leafStart);
         profiles[taskId] = S.prof;
       }
+      atomicAdd(finished, 1u);
     }
     __syncthreads();
   }
-  if (G > 1) {  // release the helpers (helper_loop)
-    if (threadIdx.x == 0) S.cmd.kind = kCmdExit;
-    cooperative_groups::this_cluster().sync();
-    cooperative_groups::this_cluster().sync();
-  }
+  // no leaves left: produce for the blocks still working on theirs
+  help_others(S, boards, rings, finished, numTasks);
 }
 
 PGL_DEFINE_TABLE_UPLOAD(em_upload_tables)
 
 size_t em_shared_bytes() { return sizeof(EmShared); }
 
-cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
-                      float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
-                      LeafReport *reports, LeafProfile *profiles, int numSMs, int clusterSize, cudaStream_t stream) {
+// Shared-pass memory of a launch with `blocks` blocks: the boards, the error
+// word and the finished-leaf counter, then one chunk ring per block.
+static size_t share_header_bytes(int blocks) {
+  return (size_t(blocks) * sizeof(Board) + 2 * sizeof(int) + 255) & ~size_t(255);
+}
+size_t em_share_bytes(int blocks) { return share_header_bytes(blocks) + size_t(blocks) * kRingFloats * sizeof(float); }
+size_t em_share_error_offset(int blocks) { return size_t(blocks) * sizeof(Board); }
+
+cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, const EmSides &sides,
+                      LeafReport *reports, LeafProfile *profiles, void *share, int blocks, cudaStream_t stream) {
   const size_t smem = sizeof(EmShared);
-  // once per process (thread-safe static initialisation: the surface and
-  // volume fields may launch concurrently)
+  // once per process (thread-safe static initialisation)
   static const cudaError_t attr =
       cudaFuncSetAttribute(em_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (attr != cudaSuccess) return attr;
   if (numTasks == 0) return cudaSuccess;
-  cudaLaunchConfig_t config = {};
-  config.blockDim = dim3(kEmThreads);
-  config.dynamicSmemBytes = smem;
-  config.stream = stream;
-  cudaLaunchAttribute la[1];
-  int G = clusterSize == 2 || clusterSize == 4 || clusterSize == 8 ? clusterSize : 1;
-  int clusters = numSMs;
-  if (G > 1) {
-    la[0].id = cudaLaunchAttributeClusterDimension;
-    la[0].val.clusterDim.x = unsigned(G);
-    la[0].val.clusterDim.y = 1;
-    la[0].val.clusterDim.z = 1;
-    config.attrs = la;
-    config.numAttrs = 1;
-    config.gridDim = dim3(unsigned(G) * unsigned(numSMs / G));
-    if (cudaOccupancyMaxActiveClusters(&clusters, em_leaf_kernel, &config) != cudaSuccess || clusters < 1) {
-      cudaGetLastError();
-      G = 1;  // this cluster shape does not fit: one block per region
-      clusters = numSMs;
-      config.attrs = nullptr;
-      config.numAttrs = 0;
-    }
-  }
-  // persistent blocks (one per SM; shared memory bound) take regions from the queue
-  const unsigned used = unsigned(clusters) < numTasks ? unsigned(clusters) : numTasks;
-  config.gridDim = dim3(used * unsigned(G));
+  if (blocks < 1 || share == nullptr) return cudaErrorInvalidValue;
+  // boards start empty (generation 0, no chunk ready); error word and counter 0
+  unsigned char *base = static_cast<unsigned char *>(share);
+  cudaError_t e = cudaMemsetAsync(base, 0, share_header_bytes(blocks), stream);
+  if (e != cudaSuccess) return e;
+  Board *boards = reinterpret_cast<Board *>(base);
+  int *err = reinterpret_cast<int *>(base + em_share_error_offset(blocks));
+  uint32_t *finished = reinterpret_cast<uint32_t *>(base + em_share_error_offset(blocks) + sizeof(int));
+  float *rings = reinterpret_cast<float *>(base + share_header_bytes(blocks));
+  // persistent blocks (one per SM: shared memory bound) take leaves from the
+  // queue; blocks without a leaf help the others' E-step passes
   count_launch();
-  return cudaLaunchKernelEx(&config, em_leaf_kernel, tasks, numTasks, queue, regions, pd, dirw, pdf, dist, cfg,
-                            uniformDirs, reports, profiles);
+  em_leaf_kernel<<<unsigned(blocks), kEmThreads, smem, stream>>>(tasks, numTasks, queue, sides, reports, profiles,
+                                                                 boards, rings, err, finished);
+  return cudaGetLastError();
 }
 
 }  // namespace pgl

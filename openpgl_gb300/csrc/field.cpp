@@ -65,6 +65,7 @@ template struct DevArray<IStatsAcc>;
 template struct DevArray<QueryIn>;
 template struct DevArray<QueryOut>;
 template struct DevArray<unsigned long long>;
+template struct DevArray<unsigned char>;
 
 // ------------------------------------------------------------------ statistics (host)
 // IntegerSampleStatistics frame (SampleStatistics.h:227-241), SSE rcp form.
@@ -468,34 +469,19 @@ void SubField::renumber(uint32_t oldNodes, uint32_t oldRegions) {
   regionOrigin_.swap(no);
 }
 
-// Blocks per region of the EM launch (a thread-block cluster: with 2 blocks
-// both produce E-step and distance chunks, with more the home block only sums
-// and the others produce).  One by default: the cluster barrier that ends
-// every round of a shared pass costs more than the helpers' chunks save
-// (measured on the multi-frame workload).  PGL_EM_CLUSTER=1, 2, 4 or 8 fixes
-// the size.
-int em_cluster_size(uint32_t regions, int numSMs) {
-  (void)regions;
-  (void)numSMs;
-  if (const char *env = std::getenv("PGL_EM_CLUSTER")) {
-    const int g = std::atoi(env);
-    if (g == 1 || g == 2 || g == 4 || g == 8) return g;
-  }
-  return 1;
-}
-
-void SubField::update(SampleSide &in) {
-  Context &c = Context::get();
+bool SubField::prepare(SampleSide &in) {
   const uint32_t n = uint32_t(in.n);
+  pending.clear();
   if (n == 0) {
     timings = UpdateTimings{};
     lastReports.clear();
     lastProfiles.clear();
     lastReportRegion.clear();
-    return;
+    return false;
   }
-  cudaEvent_t ev[5];
-  for (auto &e : ev) check(cudaEventCreate(&e), "event");
+  cudaEvent_t *ev = events;
+  for (int k = 0; k < 4; ++k)
+    if (!ev[k]) check(cudaEventCreate(&ev[k]), "event");
   check(cudaEventRecord(ev[0], stream()), "event");
   const bool first = !initialized;
   if (first) {
@@ -610,43 +596,34 @@ void SubField::update(SampleSide &in) {
       t.varOverN[d] = h.stats.var[d] / h.stats.n;
     }
   }
-  std::stable_sort(tasks.begin(), tasks.end(), [](const LeafTask &a, const LeafTask &b) { return a.count > b.count; });
-  tasks_.reserve(R);
-  reports_.reserve(R);
-  profiles_.reserve(R);
-  queue_.reserve(1);
-  check(cudaMemcpyAsync(tasks_.p, tasks.data(), R * sizeof(LeafTask), cudaMemcpyHostToDevice, stream()), "tasks");
-  check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), stream()), "queue");
+  pending = std::move(tasks);
   ensureUniformDirs();
-  check(cudaEventRecord(ev[4], stream()), "event");
-  if (cfg.fitRegions) {
-    check(launch_em(tasks_.p, R, queue_.p, dRegions.p, sP_.p, sD_.p, sPdf_.p, dist_.p, cfg, dUniformDirs.p, reports_.p,
-                    profiles_.p, c.numSMs, em_cluster_size(R, c.numSMs), stream()),
-          "em");
-  }
   check(cudaEventRecord(ev[3], stream()), "event");
-  lastReports.resize(R);
-  lastProfiles.resize(R);
-  check(cudaMemcpyAsync(lastProfiles.data(), profiles_.p, R * sizeof(LeafProfile), cudaMemcpyDeviceToHost, stream()),
-        "profiles");
-  check(cudaMemcpyAsync(lastReports.data(), reports_.p, R * sizeof(LeafReport), cudaMemcpyDeviceToHost, stream()),
-        "reports");
-  check(cudaStreamSynchronize(stream()), "update");
-  lastReportRegion.resize(R);
-  for (uint32_t k = 0; k < R; ++k) lastReportRegion[k] = tasks[k].region;
+  pendingSamples_ = n;
+  return true;
+}
+
+EmSide SubField::emSide() { return EmSide{dRegions.p, sP_.p, sD_.p, sPdf_.p, dist_.p, dUniformDirs.p, cfg}; }
+
+void SubField::finish(std::vector<LeafReport> reports, std::vector<LeafProfile> profiles,
+                      std::vector<uint32_t> regionOf, cudaEvent_t emStart, cudaEvent_t emEnd) {
+  const uint32_t R = uint32_t(regions.size());
+  lastReports = std::move(reports);
+  lastProfiles = std::move(profiles);
+  lastReportRegion = std::move(regionOf);
   float ms[6];
-  check(cudaEventElapsedTime(&ms[0], ev[0], ev[3]), "timing");
-  check(cudaEventElapsedTime(&ms[1], ev[0], ev[1]), "timing");
-  check(cudaEventElapsedTime(&ms[2], ev[1], ev[2]), "timing");
-  check(cudaEventElapsedTime(&ms[3], ev[2], ev[3]), "timing");
-  check(cudaEventElapsedTime(&ms[4], ev[2], ev[4]), "timing");
-  check(cudaEventElapsedTime(&ms[5], ev[4], ev[3]), "timing");
-  timings = UpdateTimings{ms[0], ms[1], ms[2], ms[3], ms[4], ms[5], uint64_t(n), R};
-  for (auto &e : ev) cudaEventDestroy(e);
+  check(cudaEventElapsedTime(&ms[0], events[0], emEnd), "timing");
+  check(cudaEventElapsedTime(&ms[1], events[0], events[1]), "timing");
+  check(cudaEventElapsedTime(&ms[2], events[1], events[2]), "timing");
+  check(cudaEventElapsedTime(&ms[3], events[2], emEnd), "timing");
+  check(cudaEventElapsedTime(&ms[4], events[2], events[3]), "timing");
+  check(cudaEventElapsedTime(&ms[5], emStart, emEnd), "timing");
+  timings = UpdateTimings{ms[0], ms[1], ms[2], ms[3], ms[4], ms[5], uint64_t(pendingSamples_), R};
   for (RegionHost &h : regions) {
     h.splitFlag = false;
     h.rb = h.re = 0;
   }
+  pending.clear();
   initialized = true;
   iteration++;
 }
@@ -724,34 +701,112 @@ GpuField::GpuField(const FieldConfig &cfg) {
 void GpuField::update(Storage &s, bool doSurface, bool doVolume) {  // SurfaceVolumeField.h:102-148
   s.flush();
   const bool surf = doSurface && s.surf.n > 0, vol = doVolume && s.vol.n > 0;
+  if (doSurface && !surf) surface.prepare(s.surf);  // clears the last update's counters
+  if (doVolume && !vol) volume.prepare(s.vol);
+  SubField *sides[2];
+  int count = 0;
   if (surf && vol) {
-    // the two fields are independent: each runs on its own stream from its
-    // own host thread, so their kernels overlap on the GPU
+    // the two trees are independent: each is built on its own stream from
+    // its own host thread, so their kernels overlap on the GPU
     std::exception_ptr err;
     int device = 0;
     check(cudaGetDevice(&device), "cudaGetDevice");
     std::thread t([&] {
       try {
         check(cudaSetDevice(device), "cudaSetDevice");
-        volume.update(s.vol);
+        volume.prepare(s.vol);
       } catch (...) {
         err = std::current_exception();
       }
     });
     try {
-      surface.update(s.surf);
+      surface.prepare(s.surf);
     } catch (...) {
       t.join();
       throw;
     }
     t.join();
     if (err) std::rethrow_exception(err);
+    sides[count++] = &surface;
+    sides[count++] = &volume;
   } else if (surf) {
-    surface.update(s.surf);
+    if (surface.prepare(s.surf)) sides[count++] = &surface;
   } else if (vol) {
-    volume.update(s.vol);
+    if (volume.prepare(s.vol)) sides[count++] = &volume;
   }
+  if (count > 0) runEm(sides, count);
   iteration++;
+}
+
+// Directional fit / update of every region of the prepared sub-fields
+// (Field.h:389-511) in one launch: the leaves of both, largest first, share
+// one queue, and blocks without a leaf help the remaining leaves' E-steps.
+void GpuField::runEm(SubField *const *sides, int count) {
+  Context &c = Context::get();
+  cudaStream_t s = sides[0]->stream();
+  std::vector<LeafTask> all;
+  EmSides es{};
+  for (int i = 0; i < count; ++i) {
+    SubField &f = *sides[i];
+    es.side[f.isSurface ? 0 : 1] = f.emSide();
+    if (i > 0) check(cudaStreamWaitEvent(s, f.events[3], 0), "wait for the other tree");
+    if (!f.cfg.fitRegions) continue;
+    for (LeafTask t : f.pending) {
+      if (!f.isSurface) t.flags |= kTaskVolume;
+      all.push_back(t);
+    }
+  }
+  std::stable_sort(all.begin(), all.end(), [](const LeafTask &a, const LeafTask &b) { return a.count > b.count; });
+  const uint32_t T = uint32_t(all.size());
+  cudaEvent_t emStart, emEnd;
+  check(cudaEventCreate(&emStart), "event");
+  check(cudaEventCreate(&emEnd), "event");
+  std::vector<LeafReport> reports(T);
+  std::vector<LeafProfile> profiles(T);
+  int emError = 0;
+  if (T > 0) {
+    tasks_.reserve(T);
+    reports_.reserve(T);
+    profiles_.reserve(T);
+    queue_.reserve(1);
+    emShare_.reserve(em_share_bytes(c.numSMs));
+    check(cudaMemcpyAsync(tasks_.p, all.data(), T * sizeof(LeafTask), cudaMemcpyHostToDevice, s), "tasks");
+    check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), s), "queue");
+  }
+  check(cudaEventRecord(emStart, s), "event");
+  if (T > 0) check(launch_em(tasks_.p, T, queue_.p, es, reports_.p, profiles_.p, emShare_.p, c.numSMs, s), "em");
+  check(cudaEventRecord(emEnd, s), "event");
+  if (T > 0) {
+    check(cudaMemcpyAsync(profiles.data(), profiles_.p, T * sizeof(LeafProfile), cudaMemcpyDeviceToHost, s),
+          "profiles");
+    check(cudaMemcpyAsync(reports.data(), reports_.p, T * sizeof(LeafReport), cudaMemcpyDeviceToHost, s), "reports");
+    check(cudaMemcpyAsync(&emError, emShare_.p + em_share_error_offset(c.numSMs), sizeof(int),
+                          cudaMemcpyDeviceToHost, s),
+          "EM status");
+  }
+  check(cudaStreamSynchronize(s), "update");
+  if (emError != 0) {
+    cudaEventDestroy(emStart);
+    cudaEventDestroy(emEnd);
+    throw std::runtime_error("directional fit failed: a wait between EM blocks ran out (code " +
+                             std::to_string(emError) + ")");
+  }
+  for (int i = 0; i < count; ++i) {
+    SubField &f = *sides[i];
+    const uint32_t side = f.isSurface ? 0u : kTaskVolume;
+    std::vector<LeafReport> r;
+    std::vector<LeafProfile> p;
+    std::vector<uint32_t> region;
+    for (uint32_t k = 0; k < T; ++k)
+      if ((all[k].flags & kTaskVolume) == side) {
+        r.push_back(reports[k]);
+        p.push_back(profiles[k]);
+        region.push_back(all[k].region);
+      }
+    f.finish(std::move(r), std::move(p), std::move(region), emStart, emEnd);
+  }
+  cudaEventDestroy(emStart);
+  cudaEventDestroy(emEnd);
 }
 
 void GpuField::setSceneBounds(const float b[6]) {  // SurfaceVolumeField.h:87-93

@@ -96,6 +96,8 @@ class SubField {
     return stream_;
   }
   ~SubField() {
+    for (cudaEvent_t e : events)
+      if (e) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
   }
   SubField() = default;
@@ -120,7 +122,16 @@ class SubField {
   DevArray<Neighbours> dNbrs;
   DevArray<float> dUniformDirs;
 
-  void update(SampleSide &in);
+  // An Update runs in three steps so that one EM launch serves both
+  // sub-fields: prepare() builds the tree, gathers the samples in leaf order
+  // and lists the leaf tasks (false when there are no samples); the EM launch
+  // (GpuField::runEm); finish() keeps the per-leaf counters and timings.
+  bool prepare(SampleSide &in);
+  EmSide emSide();
+  void finish(std::vector<LeafReport> reports, std::vector<LeafProfile> profiles, std::vector<uint32_t> regionOf,
+              cudaEvent_t emStart, cudaEvent_t emEnd);
+  std::vector<LeafTask> pending;  // leaf tasks of the prepared update, by region
+  cudaEvent_t events[4] = {};     // start, samples copied, tree built, tasks ready
   void reset();
   FieldView view() const;
   std::vector<RegionDir> downloadRegions() const;
@@ -132,6 +143,7 @@ class SubField {
   void buildTree(uint32_t n, const float4 *P);
   void renumber(uint32_t oldNodes, uint32_t oldRegions);
   void ensureUniformDirs();
+  uint32_t pendingSamples_ = 0;
 
   // working buffers (sized to the largest update seen)
   DevArray<float4> posA_, posB_, sP_, sD_, tmpP_, tmpD_;
@@ -140,11 +152,7 @@ class SubField {
   DevArray<unsigned long long> keys64_;
   DevArray<KdJob> jobs_;
   DevArray<IStatsAcc> acc_;
-  DevArray<LeafTask> tasks_;
-  DevArray<LeafReport> reports_;
-  DevArray<LeafProfile> profiles_;
   DevArray<float4> means_;
-  DevArray<unsigned int> queue_;
   DevArray<uint32_t> bounds6_;
   Scratch scratch_;
   std::vector<uint32_t> splitNodes_;        // nodes split in this update (creation order)
@@ -163,6 +171,16 @@ class GpuField {
   std::string serialize() const;  // byte layout of pglFieldStoreToFile (CPU_8 lanes)
   void deserialize(const std::string &bytes);  // the same layout (pglDeviceNewFieldFromFile)
   bool equals(const GpuField &o) const;
+
+ private:
+  void runEm(SubField *const *sides, int count);
+  // the EM launch of both sub-fields: leaf tasks, per-leaf counters, queue,
+  // boards and chunk rings
+  DevArray<LeafTask> tasks_;
+  DevArray<LeafReport> reports_;
+  DevArray<LeafProfile> profiles_;
+  DevArray<unsigned int> queue_;
+  DevArray<unsigned char> emShare_;
 };
 
 // Per-object sampling distribution (plain drop-in path).

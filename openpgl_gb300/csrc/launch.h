@@ -65,10 +65,30 @@ cudaError_t copy_regions(RegionDir *regions, const uint32_t *dst, const uint32_t
 cudaError_t build_knn(const float4 *means, uint32_t R, Neighbours *out, cudaStream_t s);
 
 size_t em_shared_bytes();
-cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, RegionDir *regions, float4 *pd,
-                      float4 *dirw, const float *pdf, float *dist, const FieldConfig &cfg, const float *uniformDirs,
-                      LeafReport *reports, LeafProfile *profiles, int numSMs, int clusterSize,
-                      cudaStream_t stream);
+// One sub-field (surface or volume) of an EM launch: its regions, its
+// samples in leaf order (position and distance, direction and weight, pdf,
+// reprojected distance), the uniform directions of first fits and its
+// configuration.  Tasks flagged kTaskVolume belong to side[1].
+struct EmSide {
+  RegionDir *regions;
+  float4 *pd;
+  float4 *dirw;
+  const float *pdf;
+  float *dist;
+  const float *uniformDirs;
+  FieldConfig cfg;
+};
+struct EmSides {
+  EmSide side[2];
+};
+// Device memory through which the EM launch's blocks share E-step passes
+// (boards, an error word, chunk rings): em_share_bytes(blocks) bytes; after
+// the launch the int at em_share_error_offset(blocks) is non-zero if a wait
+// of the launch ran out (its results are then not valid).
+size_t em_share_bytes(int blocks);
+size_t em_share_error_offset(int blocks);
+cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, const EmSides &sides,
+                      LeafReport *reports, LeafProfile *profiles, void *share, int blocks, cudaStream_t stream);
 
 cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s);
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,

@@ -79,11 +79,11 @@ struct LeafTask {
   uint32_t region;
   uint32_t begin;
   uint32_t count;
-  uint32_t flags;      // kTaskFit | kTaskDecay
+  uint32_t flags;      // kTaskFit | kTaskDecay | kTaskVolume
   float mean[3];       // region sample mean (reprojection pivot, new VMM pivot)
   float varOverN[3];   // getVariance() (reprojection distance)
 };
-constexpr uint32_t kTaskFit = 1u, kTaskDecay = 2u;
+constexpr uint32_t kTaskFit = 1u, kTaskDecay = 2u, kTaskVolume = 4u;  // kTaskVolume: a volume leaf
 
 // Per-leaf counters written by the EM kernel (fit statistics, for tests and
 // the statistics API).
@@ -99,6 +99,9 @@ struct LeafProfile {
   // inside the passes: cycles thread 0 spent producing, and cycles of the
   // slowest consumer role (E-step: lobe chain 0; split: chi-square chain 0)
   uint64_t cycProdE, cycConsE, cycProdS, cycConsS;
+  // E-step chunks of the leaf, those its own block produced (the rest came
+  // from helper blocks), and the cycles a summing thread waited for chunks
+  uint64_t chunks, chunksOwn, cycWaitE;
 };
 
 // Integer position statistics of one kd child (IntegerSampleStatistics).

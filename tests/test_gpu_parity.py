@@ -142,18 +142,3 @@ def test_one_leaf_fields(pgl):
         assert r["regions"] == 1, (side, r)
         assert r["tree_equal"] and r["stats_equal"], (side, r)
         assert r["bit_exact_regions"] == 1, (side, r)
-
-
-@pytest.mark.parametrize("blocks", ["2", "4", "8"])
-def test_cluster_shared_regions_match_oracle(pgl, blocks, monkeypatch):
-    """The EM passes shared by a thread-block cluster (PGL_EM_CLUSTER) give the
-    same field as one block per region."""
-    from openpgl_gb300 import synthetic as syn
-
-    monkeypatch.setenv("PGL_EM_CLUSTER", blocks)
-    frames = [syn.cube_face_samples(100000, 80 + i, volume_fraction=0.25) for i in range(2)]
-    dev, field, orc = _train(pgl, frames, 6000)
-    for side in ("surface", "volume"):
-        r = compare_fields(field.field_bytes(), orc.field_bytes(), side)
-        assert r["tree_equal"] and r["stats_equal"], (side, r)
-        assert r["worst_pdf_rel"] <= PDF_TOL, (side, r)
