@@ -46,6 +46,7 @@ constexpr uint32_t kGrabIdxBits = 22;                  // grab word: generation 
 constexpr uint32_t kGrabMask = (1u << kGrabIdxBits) - 1u;
 constexpr uint32_t kGrabGenMask = (1u << 20) - 1u;
 constexpr uint32_t kMaxSharedChunks = kGrabMask - 4096u;
+constexpr uint32_t kMaxHelpers = 16;                   // helper blocks per board at a time
 
 enum EmError { kErrNone = 0, kErrChunkWait = 1, kErrSlotWait = 2, kErrCopyWait = 3, kErrLeafTooLarge = 4 };
 
@@ -60,6 +61,8 @@ struct __align__(128) Board {
   uint32_t pad0[30];
   uint32_t consumed;           // chunks (sequence numbers) whose ring slots are free again
   uint32_t pad1[31];
+  uint32_t helpers;            // helper blocks attached to the board (at most kMaxHelpers)
+  uint32_t pad2[31];
   uint32_t ready[kRingMaxSlots];  // per ring slot: sequence number of the chunk it holds
   BoardParams params[2];          // by generation parity
 };
@@ -1001,6 +1004,16 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *m, uint32_t pa
       : "memory");
   return ok != 0;
 }
+// whether phase `parity` has completed, without waiting
+__device__ __forceinline__ bool mbar_test_wait(unsigned long long *m, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(m)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
 // global -> shared bulk copy (16-byte aligned, a multiple of 16 bytes)
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, unsigned long long *m) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -1316,8 +1329,8 @@ __device__ void wait_done(const EmShared &S, const EStepShape &e, uint32_t need)
 // Loader warp: the chunks of the pass in order, 32 at a time.  A chunk is
 // settled when this block's producers took it (they fill its stage) or when
 // its ring slot holds it and its stage is free (then a bulk copy brings it
-// in).  Ring slots are handed back as the consumers finish chunks (all of
-// them at the end of the pass).
+// in).  Ring slots are handed back as the copies land (all of them at the
+// end of the pass).
 __device__ void load_chunks(EmShared &S, const EStepShape &e, uint32_t N, uint32_t seqBase) {
   Board &b = *S.board;
   const int lane = int(threadIdx.x & 31);
@@ -1327,9 +1340,14 @@ __device__ void load_chunks(EmShared &S, const EStepShape &e, uint32_t N, uint32
   unsigned long long t0 = 0;
   while (issued < N) {
     const uint32_t done = chunks_done(S, e);
-    if (done > released) {
-      if (lane == 0) st_release(&b.consumed, seqBase + done);
-      released = done;
+    // a chunk's ring slot is free once its copy has landed (its stage's
+    // barrier phase completed); stages of chunks past `done` are not reused
+    // yet, so their phases are still the ones to test
+    uint32_t rel = released > done ? released : done;
+    while (rel < issued && mbar_test_wait(&S.full[rel % stages], use_parity(S, e, rel))) ++rel;
+    if (rel > released) {
+      if (lane == 0) st_release(&b.consumed, seqBase + rel);
+      released = rel;
     }
     const uint32_t j = issued + uint32_t(lane);
     bool ok = false, copy = false;
@@ -1523,7 +1541,8 @@ __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
 }
 
 // A block without leaves produces chunks for other blocks' E-step passes:
-// it picks the board with the most chunks left and takes chunks from it while
+// it picks the board with the most chunks left (among boards with fewer than
+// kMaxHelpers helpers) and takes chunks from it while
 // it has any (loading the pass parameters when the generation changes).  It
 // leaves once every leaf of the launch is finished (or the launch failed).
 __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint32_t *finished, uint32_t numTasks) {
@@ -1538,7 +1557,8 @@ __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint
     for (int i = tid; i < nb; i += kEmThreads) {
       const unsigned long long w = ld_relaxed64(&boards[i].grab);
       const uint32_t n = grab_chunks(w), nx = grab_next(w);
-      const uint32_t rem = (grab_gen(w) != 0 && nx < n) ? n - nx : 0u;
+      const bool open = ld_relaxed(&boards[i].helpers) < kMaxHelpers;
+      const uint32_t rem = (grab_gen(w) != 0 && nx < n && open) ? n - nx : 0u;
       if (rem > bestRem) {
         bestRem = rem;
         best = i;
@@ -1576,6 +1596,20 @@ __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint
       continue;
     }
     Board &b = boards[bi];
+    // attach to the board while it has fewer than kMaxHelpers helpers: with
+    // at most one chunk held per helper, the chunks taken stay close to the
+    // ring's free slots, and the other helpers stay free for other boards
+    if (tid == 0) {
+      const uint32_t before = atomicAdd(&b.helpers, 1u);
+      S.helpExit = before < kMaxHelpers ? 0 : 1;
+      if (before >= kMaxHelpers) atomicSub(&b.helpers, 1u);
+    }
+    __syncthreads();
+    if (S.helpExit) {
+      __syncthreads();
+      __nanosleep(500);
+      continue;
+    }
     for (int tries = 0;;) {
       if (tid == 0) {
         // take the board's next chunk only when its ring slot is free (the
@@ -1634,6 +1668,7 @@ __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint
       produce_for(S, b, rings + size_t(bi) * kRingFloats, e, S.hp.dirw, S.hp.count, S.hp.seqBase, uint32_t(chunk));
       __syncthreads();
     }
+    if (tid == 0) atomicSub(&b.helpers, 1u);
   }
 }
 
