@@ -46,7 +46,7 @@ constexpr uint32_t kGrabIdxBits = 22;                  // grab word: generation 
 constexpr uint32_t kGrabMask = (1u << kGrabIdxBits) - 1u;
 constexpr uint32_t kGrabGenMask = (1u << 20) - 1u;
 constexpr uint32_t kMaxSharedChunks = kGrabMask - 4096u;
-constexpr uint32_t kMaxHelpers = 16;                   // helper blocks per board at a time
+constexpr uint32_t kMaxHelpers = 4;                    // helper blocks per board at a time
 
 enum EmError { kErrNone = 0, kErrChunkWait = 1, kErrSlotWait = 2, kErrCopyWait = 3, kErrLeafTooLarge = 4 };
 
