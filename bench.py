@@ -52,9 +52,10 @@ WORKLOAD = ("multi-frame: 8 frames x 2,097,152 samples (25% inside-volume, cube 
 # (3008 B) read and written once
 EM_BYTES_PER_SAMPLE = 32
 REGION_STATE_BYTES = 3008
-# DRAM traffic of the EM kernel per sample, from the ncu capture summarised in
-# profiles/em_leaf_kernel_multiframe.md (None until captured)
-EM_TRAFFIC_PER_SAMPLE = None
+# DRAM bytes (read + write) per sample of one EM launch, from the ncu capture summarised in
+# profiles/em_leaf_kernel_multiframe_131k.md (7.70 MB for 131,072 samples); traffic scales with
+# the samples of a launch
+EM_TRAFFIC_PER_SAMPLE = 58.7
 
 
 # the port against the compiled reference (CPU_8, AVX2) on x86, first frame
