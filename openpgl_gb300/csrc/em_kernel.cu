@@ -109,6 +109,9 @@ struct EmShared {
   uint32_t gen, seqBase, abortAt;
   int hgrab[2], grabbed, helpBoard, helpExit;
   uint32_t grabGen;
+  int grabExact;                                  // the chunk taken is the one whose slot was checked
+  int nextGrabbed, nextExact, hasNext;            // a helper's next chunk, taken while producing
+  uint32_t nextGen;
   uint32_t scanRem[kEmThreads / 32];
   int scanIdx[kEmThreads / 32];
   uint32_t validPerWarp[kEmThreads / 32];  // split passes: valid samples per producer warp
@@ -1148,15 +1151,46 @@ __device__ void produce_estep_chunk(const EmShared &S, const EStepShape &e, cons
   if (kRing) fence_proxy_async();  // the ring is read by bulk copies
 }
 
-// A helper's chunk of board `b` (taken when its ring slot was free, so the
-// slot wait rarely waits): fill the slot, then publish its sequence number.
+// A helper takes the next chunk of board `b` (one thread): only when that
+// chunk's ring slot is free (known once the pass's parameters are loaded; a
+// chunk of a pass not loaded yet is taken anyway).  Returns the chunk, -1 when
+// the pass has none left, -2 when the ring is full for now; `exact` says the
+// chunk taken is the one whose slot was checked (others can take chunks
+// between the check and the atomic).
+__device__ int helper_take(EmShared &S, Board &b, bool paramsLoaded, uint32_t paramsGen, uint32_t &gen, int &exact) {
+  const unsigned long long w = ld_relaxed64(&b.grab);
+  const uint32_t consumed = ld_relaxed(&b.consumed);
+  exact = 0;
+  gen = 0;
+  if (has_error(S.err) || grab_gen(w) == 0 || grab_next(w) >= grab_chunks(w)) return -1;
+  const bool known = paramsLoaded && grab_gen(w) == paramsGen;
+  if (known && S.hp.seqBase + grab_next(w) + 1u > consumed + uint32_t(estep_shape(int(S.hp.cnt)).slots)) return -2;
+  const unsigned long long w2 = atomicAdd(&b.grab, 1ull);
+  if (grab_gen(w2) == 0 || grab_next(w2) >= grab_chunks(w2)) return -1;
+  gen = grab_gen(w2);
+  exact = known && w2 == w;
+  return int(grab_next(w2));
+}
+
+// A helper's chunk of board `b`: wait until its ring slot is free (unless
+// its slot was checked), fill the slot, then publish its sequence number.
+// Warp 15 holds no samples of a chunk (C <= 384 samples in lanes 0..479), so
+// its lane 0 takes the helper's next chunk meanwhile.
 __device__ void produce_for(EmShared &S, Board &b, float *ring, const EStepShape &e, const float4 *dirw,
-                            uint32_t count, uint32_t seqBase, uint32_t chunk) {
+                            uint32_t count, uint32_t seqBase, uint32_t chunk, bool exact, uint32_t paramsGen) {
   const int t = threadIdx.x;
   const uint32_t seq = seqBase + chunk + 1u, slot = (seqBase + chunk) % uint32_t(e.slots);
   // the slot's previous chunk (sequence number seq - slots) must have been copied out
-  if (t == 0 && seq > uint32_t(e.slots)) wait_at_least(&b.consumed, seq - uint32_t(e.slots), S.err);
+  if (t == 0 && !exact && seq > uint32_t(e.slots)) wait_at_least(&b.consumed, seq - uint32_t(e.slots), S.err);
   __syncthreads();
+  if (t == kEmThreads - 32) {
+    uint32_t g = 0;
+    int x = 0;
+    S.nextGrabbed = helper_take(S, b, true, paramsGen, g, x);
+    S.nextGen = g;
+    S.nextExact = x;
+    S.hasNext = 1;
+  }
   produce_estep_chunk<true>(S, e, dirw, count, chunk, ring + size_t(slot) * e.stageFloats, t, kEmThreads);
   __syncthreads();
   if (t == 0) {
@@ -1326,10 +1360,10 @@ __device__ void wait_done(const EmShared &S, const EStepShape &e, uint32_t need)
   __threadfence_block();
 }
 
-// Loader warp: the chunks of the pass in order, 32 at a time.  A chunk is
-// settled when this block's producers took it (they fill its stage) or when
-// its ring slot holds it and its stage is free (then a bulk copy brings it
-// in).  Ring slots are handed back as the copies land (all of them at the
+// Loader warp: the chunks of the pass, 32 at a time.  A chunk is settled
+// when this block's producers took it (they fill its stage) or when its ring
+// slot holds it and its stage is free (then a bulk copy brings it in, also
+// ahead of a late chunk); the settled count advances in order.  Ring slots are handed back as the copies land (all of them at the
 // end of the pass).
 __device__ void load_chunks(EmShared &S, const EStepShape &e, uint32_t N, uint32_t seqBase) {
   Board &b = *S.board;
@@ -1337,6 +1371,7 @@ __device__ void load_chunks(EmShared &S, const EStepShape &e, uint32_t N, uint32
   const uint32_t bytes = uint32_t(e.stageFloats) * 4u;
   const uint32_t stages = uint32_t(e.stages);
   uint32_t issued = 0, released = 0;
+  unsigned handled = 0;  // bit i: chunk issued + i is settled (own, or its copy issued)
   unsigned long long t0 = 0;
   while (issued < N) {
     const uint32_t done = chunks_done(S, e);
@@ -1350,15 +1385,17 @@ __device__ void load_chunks(EmShared &S, const EStepShape &e, uint32_t N, uint32
       released = rel;
     }
     const uint32_t j = issued + uint32_t(lane);
-    bool ok = false, copy = false;
-    if (j < N && j < done + stages) {  // stage j % stages is free
+    bool ok = (handled >> lane) & 1u, copy = false;
+    if (!ok && j < N && j < done + stages) {  // stage j % stages is free
       const uint32_t seq = seqBase + j + 1u;
       if (reinterpret_cast<volatile uint32_t *>(S.own)[j & 63u] == seq) ok = true;
       else if (ld_relaxed(&b.ready[(seqBase + j) % uint32_t(e.slots)]) == seq) ok = copy = true;
     }
     const unsigned okMask = __ballot_sync(0xFFFFFFFFu, ok);
     const uint32_t prefix = okMask == 0xFFFFFFFFu ? 32u : uint32_t(__ffs(~okMask)) - 1u;  // settled from `issued` on
-    if (copy && uint32_t(lane) < prefix) {
+    // copies may be issued out of order (only the summing is in order): a
+    // chunk that is ready behind a late one is copied now
+    if (copy) {
       // the relaxed read saw the producer's release: acquire before the copy
       fence_acquire();
       fence_proxy_async();
@@ -1368,6 +1405,7 @@ __device__ void load_chunks(EmShared &S, const EStepShape &e, uint32_t N, uint32
                 bytes, &S.full[st]);
     }
     issued += prefix;
+    handled = prefix >= 32u ? 0u : (okMask >> prefix);
     if (prefix == 0) {
       if (has_error(S.err)) {
         if (lane == 0) S.abortAt = issued;
@@ -1610,31 +1648,21 @@ __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint
       __nanosleep(500);
       continue;
     }
+    if (tid == 0) S.hasNext = 0;
     for (int tries = 0;;) {
       if (tid == 0) {
-        // take the board's next chunk only when its ring slot is free (the
-        // pass's sequence numbers are known once its parameters are loaded);
-        // a chunk of a pass not loaded yet is taken, and loaded below
-        const unsigned long long w = ld_relaxed64(&b.grab);
-        const uint32_t consumed = ld_relaxed(&b.consumed);
-        int ch = -1;
-        uint32_t g = 0;
-        bool room = true;
-        if (has_error(S.err) || grab_gen(w) == 0 || grab_next(w) >= grab_chunks(w)) {
-          ch = -1;
+        if (S.hasNext) {  // taken while the last chunk was produced
+          S.grabbed = S.nextGrabbed;
+          S.grabGen = S.nextGen;
+          S.grabExact = S.nextExact;
+          S.hasNext = 0;
         } else {
-          if (bi == cachedBoard && grab_gen(w) == cachedGen)
-            room = S.hp.seqBase + grab_next(w) + 1u <= consumed + uint32_t(estep_shape(int(S.hp.cnt)).slots);
-          if (room) {
-            const unsigned long long w2 = atomicAdd(&b.grab, 1ull);
-            if (grab_gen(w2) != 0 && grab_next(w2) < grab_chunks(w2)) {
-              ch = int(grab_next(w2));
-              g = grab_gen(w2);
-            }
-          }
+          uint32_t g = 0;
+          int x = 0;
+          S.grabbed = helper_take(S, b, bi == cachedBoard, cachedGen, g, x);
+          if (S.grabbed != -2 && S.grabbed != -1) S.grabGen = g;
+          S.grabExact = x;
         }
-        S.grabbed = room ? ch : -2;  // -2: the ring is full for now
-        S.grabGen = g;
       }
       __syncthreads();
       const int chunk = S.grabbed;
@@ -1665,7 +1693,8 @@ __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint
         cachedGen = gen;
       }
       const EStepShape e = estep_shape(int(S.hp.cnt));
-      produce_for(S, b, rings + size_t(bi) * kRingFloats, e, S.hp.dirw, S.hp.count, S.hp.seqBase, uint32_t(chunk));
+      produce_for(S, b, rings + size_t(bi) * kRingFloats, e, S.hp.dirw, S.hp.count, S.hp.seqBase, uint32_t(chunk),
+                  S.grabExact != 0, cachedGen);
       __syncthreads();
     }
     if (tid == 0) atomicSub(&b.helpers, 1u);
