@@ -398,6 +398,106 @@ __device__ void map_step(VMMState &v, const SuffState &cur, const SuffState &pre
   vmm_calc_norm(v);
 }
 
+// suff_normalize and map_step by one warp, lane k doing lobe k: every lobe's
+// arithmetic is the scalar functions' own; the sums over lobes keep the
+// scalar order (vfloat8 lane sums over k, then the 8-lane reduction) on lane 0.
+__device__ void suff_normalize_warp(SuffState &s, float n) {
+  const unsigned full = 0xFFFFFFFFu;
+  const int k = int(threadIdx.x & 31);
+  const int Kp = vec_count(int(s.K)) * kLanes;
+  float nrm = 0.0f;
+  if (k == 0) {
+    s.numSamples = n;
+    float sv[kLanes] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int j = 0; j < Kp; ++j) sv[j % kLanes] += s.w[j];
+    s.sumWeights = reduce8(sv);
+    nrm = n / s.sumWeights;
+    s.normalized = 1;
+  }
+  nrm = __shfl_sync(full, nrm, 0);  // lane 0 has read every weight
+  if (k < Kp) {
+    s.dx[k] *= nrm;
+    s.dy[k] *= nrm;
+    s.dz[k] *= nrm;
+    s.w[k] *= nrm;
+  }
+  __syncwarp();
+}
+__device__ void map_step_warp(VMMState &v, const SuffState &cur, const SuffState &prev, const FieldConfig &cfg,
+                              const int *mask) {
+  const unsigned full = 0xFFFFFFFFu;
+  const int k = int(threadIdx.x & 31);
+  const int c = vec_count(int(v.K)), Kp = c * kLanes;
+  const bool act = k < Kp;
+  const float K = float(v.K);
+  const float N = cur.numSamples + prev.numSamples;
+  const int rem = int(v.K % kLanes);
+  if (!mask) {
+    if (act) {
+      const float w = cur.w[k] + prev.w[k];
+      v.w[k] = (cfg.weightPrior + w) / ((cfg.weightPrior * K) + N);
+    }
+  } else {
+    float wNew = 0.0f, wOld = 0.0f;
+    int m = 0;
+    if (act) {
+      const float w = cur.w[k] + prev.w[k];
+      wNew = (cfg.weightPrior + w) / ((cfg.weightPrior * K) + N);
+      wOld = v.w[k];
+      m = mask[k];
+    }
+    // lane sums over the lobes in order, on lane 0
+    float sw[kLanes] = {0, 0, 0, 0, 0, 0, 0, 0}, sp[kLanes] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int j = 0; j < Kp; ++j) {
+      const float pj = __shfl_sync(full, m ? wNew : 0.0f, j);
+      const float wj = __shfl_sync(full, m ? 0.0f : wOld, j);
+      sp[j % kLanes] += pj;
+      sw[j % kLanes] += wj;
+    }
+    float inv = 0.0f;
+    if (k == 0) {
+      inv = 1.0f / reduce8(sp);
+      inv *= 1.0f - reduce8(sw);
+    }
+    inv = __shfl_sync(full, inv, 0);
+    if (act) v.w[k] = m ? wNew * inv : wOld;
+  }
+  if (rem > 0 && k >= (c - 1) * kLanes + rem && k < Kp) v.w[k] = 0.0f;
+
+  const float curN = cur.numSamples, prevN = prev.numSamples, NN = curN + prevN;
+  const float overallN = cur.numSamples + prev.overallNumSamples;
+  const float curW = curN / NN, prevW = 1.0f - curW;
+  if (act) {
+    const float partialN = v.w[k] * overallN;
+    const V3 cm = cur.w[k] > 0.0f ? mk(cur.dx[k] / cur.w[k], cur.dy[k] / cur.w[k], cur.dz[k] / cur.w[k]) : mk(0, 0, 0);
+    const V3 pm =
+        prev.w[k] > 0.0f ? mk(prev.dx[k] / prev.w[k], prev.dy[k] / prev.w[k], prev.dz[k] / prev.w[k]) : mk(0, 0, 0);
+    const V3 md = cm * curW + pm * prevW;
+    float mc = length(md);
+    const bool upd = mask ? (mask[k] != 0) : true;
+    if (upd && mc > 0.0f) {
+      v.mx[k] = md.x / mc;
+      v.my[k] = md.y / mc;
+      v.mz[k] = md.z / mc;
+    }
+    mc = (cfg.mcPrior * cfg.mcPriorStrength + mc * partialN) / (cfg.mcPriorStrength + partialN);
+    mc = emin(cfg.maxMeanCosine, mc);
+    if (upd) {
+      v.mc[k] = mc;
+      v.kappa[k] = mean_cosine_to_kappa(mc);
+    }
+    if (rem > 0 && k >= (c - 1) * kLanes + rem) {
+      v.mx[k] = 0.0f; v.my[k] = 0.0f; v.mz[k] = 1.0f; v.mc[k] = 0.0f; v.kappa[k] = 0.0f;
+      if (!mask) { v.norm[k] = kInv4Pi; v.e2k[k] = 1.0f; }
+    }
+    // vmm_calc_norm for lobe k
+    v.e2k[k] = fexp(-2.0f * v.kappa[k]);
+    const float nrm = v.kappa[k] / (kTwoPiF * (1.0f - v.e2k[k]));
+    v.norm[k] = v.kappa[k] > 0.0f ? nrm : kInv4Pi;
+  }
+  __syncwarp();
+}
+
 __device__ void map3d_to_2d(V3 d, float &x, float &y) {  // Splitter.h:161-171
   float alpha = facos(d.z);
   float inv_sinc = alpha / fsin(alpha);
@@ -1793,19 +1893,24 @@ __device__ int em_loop(EmShared &S, const LeafSamples &L, SuffState &prev, bool 
     pass_estep(S, L);
     PGL_PROF_END(t0, cycEstep)
     PGL_PROF_BEGIN(t1)
-    if (tid == 0) {
-      S.prof.estepPasses++;
-      if (S.un.sw > 0.0f && S.cur.K < kMaxK) {  // handleUnassignedSampleStats (WEMFactory.h:731-748)
-        int t = int(S.cur.K);
-        S.cur.K++;
-        S.cur.w[t] = S.un.sw; S.cur.dx[t] = S.un.dx; S.cur.dy[t] = S.un.dy; S.cur.dz[t] = S.un.dz;
-        prev.K++;
-        prev.w[t] = 0.0f; prev.dx[t] = prev.dy[t] = prev.dz[t] = 0.0f;
-        S.vmm.K++;
-        if (partial) S.mask[S.vmm.K - 1] = 1;
+    if (tid < 32) {  // the M-step by warp 0, lane k on lobe k
+      if (tid == 0) {
+        S.prof.estepPasses++;
+        if (S.un.sw > 0.0f && S.cur.K < kMaxK) {  // handleUnassignedSampleStats (WEMFactory.h:731-748)
+          int t = int(S.cur.K);
+          S.cur.K++;
+          S.cur.w[t] = S.un.sw; S.cur.dx[t] = S.un.dx; S.cur.dy[t] = S.un.dy; S.cur.dz[t] = S.un.dz;
+          prev.K++;
+          prev.w[t] = 0.0f; prev.dx[t] = prev.dy[t] = prev.dz[t] = 0.0f;
+          S.vmm.K++;
+          if (partial) S.mask[S.vmm.K - 1] = 1;
+        }
       }
-      suff_normalize(S.cur, S.cur.numSamples);
-      map_step(S.vmm, S.cur, prev, cfg, partial ? S.mask : nullptr);
+      __syncwarp();
+      suff_normalize_warp(S.cur, S.cur.numSamples);
+      map_step_warp(S.vmm, S.cur, prev, cfg, partial ? S.mask : nullptr);
+    }
+    if (tid == 0) {
       S.iterations++;
       bool converged = false;
       if (S.iterations > 1) {
