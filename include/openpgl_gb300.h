@@ -74,6 +74,23 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int v
 // writes when capacity >= 18 x count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int volume, uint64_t *out,
                                                            size_t capacity);
+// Schedule parameters of the field's EM launch (no reference counterpart;
+// they change the Update's speed, never its result), as int[4]: helper
+// blocks that may work on one region at a time (0-64, default 4), the E-step
+// chunk-size divisor (1-4, default 1), the pipeline stages of the summing
+// warps (2-8, default 8), and 1 to queue regions by their previous Update's
+// measured cost instead of by sample count (default 0).  Set returns false
+// (and records the error) for values out of range.
+OPENPGL_CORE_INTERFACE bool pglFieldSetEmTuning(PGLField field, const int *tuning);
+OPENPGL_CORE_INTERFACE bool pglFieldGetEmTuning(PGLField field, int *tuning);
+// The next Update first times candidate schedules (helper blocks 2/4/8 x
+// chunk divisor 1/2, x queue order when costs are known) on its own regions,
+// restoring the state they change after each trial, keeps the fastest and
+// then runs; its result is the same as without tuning.
+OPENPGL_CORE_INTERFACE void pglFieldAutotuneNextUpdate(PGLField field);
+// The trials of the last tuning: int[4] schedule and milliseconds each;
+// returns their count, writes when capacity >= count.
+OPENPGL_CORE_INTERFACE size_t pglFieldGetEmTuningTrials(PGLField field, int *tunings, float *ms, size_t capacity);
 // Splits numSamples sample records that live in device memory into the
 // surface records and the inside-volume records (flags & EInsideVolume), each
 // kind in its original order, written to dSurface and dVolume (device

@@ -159,6 +159,10 @@ C_API = {
     "pglSplitSamplesDeviceNoAlloc": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
                                                      ctypes.c_void_p, ctypes.c_void_p]),
     "pglFieldGetLastUpdateProfile": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
+    "pglFieldSetEmTuning": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pglFieldGetEmTuning": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pglFieldAutotuneNextUpdate": (None, [ctypes.c_void_p]),
+    "pglFieldGetEmTuningTrials": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
 }
 
 _lib = None
@@ -353,6 +357,30 @@ class Field:
         out = (ctypes.c_float * 4)()
         self.lib.pglFieldGetLastUpdateTimings(self.h, int(volume), out)
         return dict(total=out[0], copy=out[1], spatial=out[2], directional=out[3])
+
+    def set_em_tuning(self, max_helpers=4, chunk_div=1, stage_cap=8, order_by_cost=0):
+        """EM schedule parameters (speed only; see pglFieldSetEmTuning)."""
+        t = (ctypes.c_int * 4)(max_helpers, chunk_div, stage_cap, order_by_cost)
+        if not self.lib.pglFieldSetEmTuning(self.h, t):
+            raise ValueError(last_error())
+
+    def em_tuning(self):
+        t = (ctypes.c_int * 4)()
+        self.lib.pglFieldGetEmTuning(self.h, t)
+        return dict(max_helpers=t[0], chunk_div=t[1], stage_cap=t[2], order_by_cost=t[3])
+
+    def autotune_next_update(self):
+        """The next Update times candidate EM schedules first and keeps the fastest."""
+        self.lib.pglFieldAutotuneNextUpdate(self.h)
+
+    def tuning_trials(self):
+        n = self.lib.pglFieldGetEmTuningTrials(self.h, None, None, 0)
+        t = (ctypes.c_int * (4 * n))()
+        ms = (ctypes.c_float * n)()
+        if n:
+            self.lib.pglFieldGetEmTuningTrials(self.h, t, ms, n)
+        return [dict(max_helpers=t[4 * i], chunk_div=t[4 * i + 1], stage_cap=t[4 * i + 2],
+                     order_by_cost=t[4 * i + 3], ms=ms[i]) for i in range(n)]
 
     def profile(self, volume=False):
         """Per-region EM profile of the last Update (see pglFieldGetLastUpdateProfile)."""

@@ -841,6 +841,49 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
   return n;
   PGL_CATCH(0)
 }
+// EM schedule parameters of a field: helper blocks per region, chunk size
+// divisor, pipeline stages, queue order by measured cost (int[4]).
+OPENPGL_CORE_INTERFACE bool pglFieldSetEmTuning(PGLField field, const int *tuning) {
+  PGL_TRY
+  if (!field || !tuning) throw std::runtime_error("null argument");
+  const EmTuning t{tuning[0], tuning[1], tuning[2], tuning[3]};
+  if (!em_tuning_valid(t)) throw std::runtime_error("EM tuning out of range");
+  F(field)->tuning = t;
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglFieldGetEmTuning(PGLField field, int *tuning) {
+  PGL_TRY
+  if (!field || !tuning) throw std::runtime_error("null argument");
+  const EmTuning &t = F(field)->tuning;
+  tuning[0] = t.maxHelpers;
+  tuning[1] = t.chunkDiv;
+  tuning[2] = t.stageCap;
+  tuning[3] = t.orderByCost;
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE void pglFieldAutotuneNextUpdate(PGLField field) {
+  PGL_TRY
+  if (!field) throw std::runtime_error("null field");
+  F(field)->autotuneNext = true;
+  PGL_CATCH_VOID
+}
+OPENPGL_CORE_INTERFACE size_t pglFieldGetEmTuningTrials(PGLField field, int *tunings, float *ms, size_t cap) {
+  PGL_TRY
+  const auto &trials = F(field)->lastTuneTrials;
+  if (tunings && ms && cap >= trials.size())
+    for (size_t i = 0; i < trials.size(); ++i) {
+      const EmTuning &t = trials[i].t;
+      tunings[4 * i] = t.maxHelpers;
+      tunings[4 * i + 1] = t.chunkDiv;
+      tunings[4 * i + 2] = t.stageCap;
+      tunings[4 * i + 3] = t.orderByCost;
+      ms[i] = trials[i].ms;
+    }
+  return trials.size();
+  PGL_CATCH(0)
+}
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int volume, uint32_t *out, size_t cap) {
   PGL_TRY
   const SubField &sf = volume ? F(field)->volume : F(field)->surface;

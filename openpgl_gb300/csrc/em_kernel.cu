@@ -46,7 +46,6 @@ constexpr uint32_t kGrabIdxBits = 22;                  // grab word: generation 
 constexpr uint32_t kGrabMask = (1u << kGrabIdxBits) - 1u;
 constexpr uint32_t kGrabGenMask = (1u << 20) - 1u;
 constexpr uint32_t kMaxSharedChunks = kGrabMask - 4096u;
-constexpr uint32_t kMaxHelpers = 4;                    // helper blocks per board at a time
 
 enum EmError { kErrNone = 0, kErrChunkWait = 1, kErrSlotWait = 2, kErrCopyWait = 3, kErrLeafTooLarge = 4 };
 
@@ -61,7 +60,7 @@ struct __align__(128) Board {
   uint32_t pad0[30];
   uint32_t consumed;           // chunks (sequence numbers) whose ring slots are free again
   uint32_t pad1[31];
-  uint32_t helpers;            // helper blocks attached to the board (at most kMaxHelpers)
+  uint32_t helpers;            // helper blocks attached to the board (at most EmTuning::maxHelpers)
   uint32_t pad2[31];
   uint32_t ready[kRingMaxSlots];  // per ring slot: sequence number of the chunk it holds
   BoardParams params[2];          // by generation parity
@@ -107,6 +106,7 @@ struct EmShared {
   float *ring;
   int *err;            // EmError of the launch
   uint32_t gen, seqBase, abortAt;
+  EmTuning tune;       // the launch's schedule parameters (the same in every block)
   int hgrab[2], grabbed, helpBoard, helpExit;
   uint32_t grabGen;
   int grabExact;                                  // the chunk taken is the one whose slot was checked
@@ -1190,7 +1190,7 @@ __device__ __forceinline__ uint32_t grab_next(unsigned long long w) { return uin
 struct EStepShape {
   int cnt, Kp, parts, P, cons0, consWarps, C, RS, stageFloats, stages, slots;
 };
-__device__ __forceinline__ EStepShape estep_shape(int cnt) {
+__device__ __forceinline__ EStepShape estep_shape(int cnt, const EmTuning &tune) {
   EStepShape e;
   e.cnt = cnt;
   e.Kp = cnt * kLanes;
@@ -1198,10 +1198,10 @@ __device__ __forceinline__ EStepShape estep_shape(int cnt) {
   e.consWarps = 2 + (3 * e.Kp + 31) / 32;  // a w | (d a) w | per-sample rows
   e.cons0 = kEmThreads - 32 * e.consWarps;  // consumers: threads [cons0, 512)
   e.P = e.cons0 - 32;                       // producers [0, P), then the loader warp
-  e.C = (e.P / e.parts) & ~7;
+  e.C = ((e.P / e.parts) / tune.chunkDiv) & ~7;
   e.RS = e.C + 4;
   e.stageFloats = (e.Kp + 9) * e.RS;
-  e.stages = min(kMaxStages, 2 * kStageFloats / e.stageFloats);
+  e.stages = min(min(kMaxStages, tune.stageCap), 2 * kStageFloats / e.stageFloats);
   e.slots = min(int(kRingMaxSlots), int(kRingFloats) / e.stageFloats);
   return e;
 }
@@ -1264,7 +1264,7 @@ __device__ int helper_take(EmShared &S, Board &b, bool paramsLoaded, uint32_t pa
   gen = 0;
   if (has_error(S.err) || grab_gen(w) == 0 || grab_next(w) >= grab_chunks(w)) return -1;
   const bool known = paramsLoaded && grab_gen(w) == paramsGen;
-  if (known && S.hp.seqBase + grab_next(w) + 1u > consumed + uint32_t(estep_shape(int(S.hp.cnt)).slots)) return -2;
+  if (known && S.hp.seqBase + grab_next(w) + 1u > consumed + uint32_t(estep_shape(int(S.hp.cnt), S.tune).slots)) return -2;
   const unsigned long long w2 = atomicAdd(&b.grab, 1ull);
   if (grab_gen(w2) == 0 || grab_next(w2) >= grab_chunks(w2)) return -1;
   gen = grab_gen(w2);
@@ -1610,7 +1610,7 @@ __device__ void produce_own(EmShared &S, const EStepShape &e, const LeafSamples 
 __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
   const int tid = threadIdx.x;
   const int cnt = vec_count(int(S.vmm.K));
-  const EStepShape e = estep_shape(cnt);
+  const EStepShape e = estep_shape(cnt, S.tune);
   const int Kp = e.Kp;
   uint32_t N = (L.count + uint32_t(e.C) - 1u) / uint32_t(e.C);
   if (N > kMaxSharedChunks) {
@@ -1680,7 +1680,7 @@ __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
 
 // A block without leaves produces chunks for other blocks' E-step passes:
 // it picks the board with the most chunks left (among boards with fewer than
-// kMaxHelpers helpers) and takes chunks from it while
+// EmTuning::maxHelpers helpers) and takes chunks from it while
 // it has any (loading the pass parameters when the generation changes).  It
 // leaves once every leaf of the launch is finished (or the launch failed).
 __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint32_t *finished, uint32_t numTasks) {
@@ -1695,7 +1695,7 @@ __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint
     for (int i = tid; i < nb; i += kEmThreads) {
       const unsigned long long w = ld_relaxed64(&boards[i].grab);
       const uint32_t n = grab_chunks(w), nx = grab_next(w);
-      const bool open = ld_relaxed(&boards[i].helpers) < kMaxHelpers;
+      const bool open = ld_relaxed(&boards[i].helpers) < uint32_t(S.tune.maxHelpers);
       const uint32_t rem = (grab_gen(w) != 0 && nx < n && open) ? n - nx : 0u;
       if (rem > bestRem) {
         bestRem = rem;
@@ -1734,13 +1734,13 @@ __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint
       continue;
     }
     Board &b = boards[bi];
-    // attach to the board while it has fewer than kMaxHelpers helpers: with
+    // attach to the board while it has fewer than maxHelpers helpers: with
     // at most one chunk held per helper, the chunks taken stay close to the
     // ring's free slots, and the other helpers stay free for other boards
     if (tid == 0) {
       const uint32_t before = atomicAdd(&b.helpers, 1u);
-      S.helpExit = before < kMaxHelpers ? 0 : 1;
-      if (before >= kMaxHelpers) atomicSub(&b.helpers, 1u);
+      S.helpExit = before < uint32_t(S.tune.maxHelpers) ? 0 : 1;
+      if (before >= uint32_t(S.tune.maxHelpers)) atomicSub(&b.helpers, 1u);
     }
     __syncthreads();
     if (S.helpExit) {
@@ -1792,7 +1792,7 @@ __device__ void help_others(EmShared &S, Board *boards, float *rings, const uint
         cachedBoard = bi;
         cachedGen = gen;
       }
-      const EStepShape e = estep_shape(int(S.hp.cnt));
+      const EStepShape e = estep_shape(int(S.hp.cnt), S.tune);
       produce_for(S, b, rings + size_t(bi) * kRingFloats, e, S.hp.dirw, S.hp.count, S.hp.seqBase, uint32_t(chunk),
                   S.grabExact != 0, cachedGen);
       __syncthreads();
@@ -2178,7 +2178,7 @@ __device__ void reproject_leaf(const LeafTask &t, float4 *pd, float4 *dirw, floa
 
 __global__ void __launch_bounds__(kEmThreads)
 em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, EmSides sides, LeafReport *reports,
-               LeafProfile *profiles, Board *boards, float *rings, int *err, uint32_t *finished) {
+               LeafProfile *profiles, Board *boards, float *rings, int *err, uint32_t *finished, EmTuning tune) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EmShared &S = *reinterpret_cast<EmShared *>(smem_raw);
   __shared__ uint32_t taskId;
@@ -2189,6 +2189,7 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Em
     S.board = boards + blockIdx.x;
     S.ring = rings + size_t(blockIdx.x) * kRingFloats;
     S.err = err;
+    S.tune = tune;
     S.gen = 0;
     S.seqBase = 0;
     for (int i = 0; i < kMaxStages; ++i) {
@@ -2298,18 +2299,23 @@ size_t em_shared_bytes() { return sizeof(EmShared); }
 static size_t share_header_bytes(int blocks) {
   return (size_t(blocks) * sizeof(Board) + 2 * sizeof(int) + 255) & ~size_t(255);
 }
+bool em_tuning_valid(const EmTuning &t) {
+  return t.maxHelpers >= 0 && t.maxHelpers <= 64 && t.chunkDiv >= 1 && t.chunkDiv <= 4 && t.stageCap >= 2 &&
+         t.stageCap <= kMaxStages && (t.orderByCost == 0 || t.orderByCost == 1);
+}
 size_t em_share_bytes(int blocks) { return share_header_bytes(blocks) + size_t(blocks) * kRingFloats * sizeof(float); }
 size_t em_share_error_offset(int blocks) { return size_t(blocks) * sizeof(Board); }
 
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, const EmSides &sides,
-                      LeafReport *reports, LeafProfile *profiles, void *share, int blocks, cudaStream_t stream) {
+                      LeafReport *reports, LeafProfile *profiles, void *share, int blocks, const EmTuning &tune,
+                      cudaStream_t stream) {
   const size_t smem = sizeof(EmShared);
   // once per process (thread-safe static initialisation)
   static const cudaError_t attr =
       cudaFuncSetAttribute(em_leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (attr != cudaSuccess) return attr;
   if (numTasks == 0) return cudaSuccess;
-  if (blocks < 1 || share == nullptr) return cudaErrorInvalidValue;
+  if (blocks < 1 || share == nullptr || !em_tuning_valid(tune)) return cudaErrorInvalidValue;
   // boards start empty (generation 0, no chunk ready); error word and counter 0
   unsigned char *base = static_cast<unsigned char *>(share);
   cudaError_t e = cudaMemsetAsync(base, 0, share_header_bytes(blocks), stream);
@@ -2322,7 +2328,7 @@ cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *qu
   // queue; blocks without a leaf help the others' E-step passes
   count_launch();
   em_leaf_kernel<<<unsigned(blocks), kEmThreads, smem, stream>>>(tasks, numTasks, queue, sides, reports, profiles,
-                                                                 boards, rings, err, finished);
+                                                                 boards, rings, err, finished, tune);
   return cudaGetLastError();
 }
 

@@ -611,6 +611,8 @@ void SubField::finish(std::vector<LeafReport> reports, std::vector<LeafProfile> 
   lastReports = std::move(reports);
   lastProfiles = std::move(profiles);
   lastReportRegion = std::move(regionOf);
+  for (size_t k = 0; k < lastProfiles.size(); ++k)
+    if (lastReportRegion[k] < R) regions[lastReportRegion[k]].lastCost = lastProfiles[k].cycTotal;
   float ms[6];
   check(cudaEventElapsedTime(&ms[0], events[0], emEnd), "timing");
   check(cudaEventElapsedTime(&ms[1], events[0], events[1]), "timing");
@@ -741,22 +743,124 @@ void GpuField::update(Storage &s, bool doSurface, bool doVolume) {  // SurfaceVo
 // Directional fit / update of every region of the prepared sub-fields
 // (Field.h:389-511) in one launch: the leaves of both, largest first, share
 // one queue, and blocks without a leaf help the remaining leaves' E-steps.
+// The leaf tasks of the prepared sub-fields in queue order, largest first:
+// by the previous Update's measured cost of the region (when asked and
+// known), else by sample count.
+std::vector<LeafTask> GpuField::emOrder(SubField *const *sides, int count, bool byCost) const {
+  std::vector<std::pair<uint64_t, LeafTask>> keyed;
+  for (int i = 0; i < count; ++i) {
+    const SubField &f = *sides[i];
+    if (!f.cfg.fitRegions) continue;
+    for (LeafTask t : f.pending) {
+      if (!f.isSurface) t.flags |= kTaskVolume;
+      const uint64_t cost = f.regions[t.region].lastCost;
+      keyed.emplace_back(byCost && cost > 0 ? cost : uint64_t(t.count), t);
+    }
+  }
+  std::stable_sort(keyed.begin(), keyed.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+  std::vector<LeafTask> all;
+  all.reserve(keyed.size());
+  for (const auto &k : keyed) all.push_back(k.second);
+  return all;
+}
+
+// Times every candidate schedule on this Update's leaves: the state an EM
+// launch changes (regions, the samples' reprojected directions and
+// distances) is saved, restored before each trial and after the last, so
+// the Update itself then runs once more with the fastest schedule and gives
+// the same field as without tuning.
+void GpuField::autotuneEm(SubField *const *sides, int count, cudaStream_t s) {
+  Context &c = Context::get();
+  struct Piece {
+    void *dev;
+    size_t bytes;
+  };
+  std::vector<Piece> pieces;
+  for (int i = 0; i < count; ++i) {
+    const EmSide e = sides[i]->emSide();
+    const size_t n = sides[i]->pendingSamples();
+    pieces.push_back({e.regions, sides[i]->regions.size() * sizeof(RegionDir)});
+    pieces.push_back({e.dirw, n * sizeof(float4)});
+    pieces.push_back({e.dist, n * sizeof(float)});
+  }
+  size_t total = 0;
+  for (const Piece &p : pieces) total += (p.bytes + 255) & ~size_t(255);
+  tuneSnap_.reserve(total);
+  auto copyAll = [&](bool save) {
+    size_t off = 0;
+    for (const Piece &p : pieces) {
+      void *snap = tuneSnap_.p + off;
+      check(cudaMemcpyAsync(save ? snap : p.dev, save ? p.dev : snap, p.bytes, cudaMemcpyDeviceToDevice, s),
+            "tuning snapshot");
+      off += (p.bytes + 255) & ~size_t(255);
+    }
+  };
+  copyAll(true);
+  bool costs = false;
+  for (int i = 0; i < count; ++i)
+    for (const RegionHost &h : sides[i]->regions) costs = costs || h.lastCost > 0;
+  EmSides es{};
+  for (int i = 0; i < count; ++i) es.side[sides[i]->isSurface ? 0 : 1] = sides[i]->emSide();
+  lastTuneTrials.clear();
+  cudaEvent_t e0, e1;
+  check(cudaEventCreate(&e0), "event");
+  check(cudaEventCreate(&e1), "event");
+  float bestMs = 0.0f;
+  EmTuning best = tuning;
+  for (int order = 0; order <= (costs ? 1 : 0); ++order) {
+    const std::vector<LeafTask> all = emOrder(sides, count, order != 0);
+    const uint32_t T = uint32_t(all.size());
+    if (T == 0) break;
+    tasks_.reserve(T);
+    reports_.reserve(T);
+    profiles_.reserve(T);
+    queue_.reserve(1);
+    emShare_.reserve(em_share_bytes(c.numSMs));
+    check(cudaMemcpyAsync(tasks_.p, all.data(), T * sizeof(LeafTask), cudaMemcpyHostToDevice, s), "tasks");
+    for (int helpers : {2, 4, 8})
+      for (int div : {1, 2}) {
+        const EmTuning t{helpers, div, 8, order};
+        copyAll(false);
+        check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), s), "queue");
+        check(cudaEventRecord(e0, s), "event");
+        check(launch_em(tasks_.p, T, queue_.p, es, reports_.p, profiles_.p, emShare_.p, c.numSMs, t, s), "em");
+        check(cudaEventRecord(e1, s), "event");
+        int emError = 0;
+        check(cudaMemcpyAsync(&emError, emShare_.p + em_share_error_offset(c.numSMs), sizeof(int),
+                              cudaMemcpyDeviceToHost, s),
+              "EM status");
+        check(cudaStreamSynchronize(s), "tuning trial");
+        if (emError != 0) throw std::runtime_error("directional fit failed in a tuning trial (code " +
+                                                   std::to_string(emError) + ")");
+        float ms = 0.0f;
+        check(cudaEventElapsedTime(&ms, e0, e1), "timing");
+        lastTuneTrials.push_back({t, ms});
+        if (lastTuneTrials.size() == 1 || ms < bestMs) {
+          bestMs = ms;
+          best = t;
+        }
+      }
+  }
+  copyAll(false);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  tuning = best;
+}
+
 void GpuField::runEm(SubField *const *sides, int count) {
   Context &c = Context::get();
   cudaStream_t s = sides[0]->stream();
-  std::vector<LeafTask> all;
   EmSides es{};
   for (int i = 0; i < count; ++i) {
     SubField &f = *sides[i];
     es.side[f.isSurface ? 0 : 1] = f.emSide();
     if (i > 0) check(cudaStreamWaitEvent(s, f.events[3], 0), "wait for the other tree");
-    if (!f.cfg.fitRegions) continue;
-    for (LeafTask t : f.pending) {
-      if (!f.isSurface) t.flags |= kTaskVolume;
-      all.push_back(t);
-    }
   }
-  std::stable_sort(all.begin(), all.end(), [](const LeafTask &a, const LeafTask &b) { return a.count > b.count; });
+  if (autotuneNext) {
+    autotuneNext = false;
+    autotuneEm(sides, count, s);
+  }
+  const std::vector<LeafTask> all = emOrder(sides, count, tuning.orderByCost != 0);
   const uint32_t T = uint32_t(all.size());
   cudaEvent_t emStart, emEnd;
   check(cudaEventCreate(&emStart), "event");
@@ -774,7 +878,8 @@ void GpuField::runEm(SubField *const *sides, int count) {
     check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), s), "queue");
   }
   check(cudaEventRecord(emStart, s), "event");
-  if (T > 0) check(launch_em(tasks_.p, T, queue_.p, es, reports_.p, profiles_.p, emShare_.p, c.numSMs, s), "em");
+  if (T > 0)
+    check(launch_em(tasks_.p, T, queue_.p, es, reports_.p, profiles_.p, emShare_.p, c.numSMs, tuning, s), "em");
   check(cudaEventRecord(emEnd, s), "event");
   if (T > 0) {
     check(cudaMemcpyAsync(profiles.data(), profiles_.p, T * sizeof(LeafProfile), cudaMemcpyDeviceToHost, s),

@@ -79,6 +79,7 @@ struct RegionHost {
   float bounds[6] = {0, 0, 0, 0, 0, 0};
   bool splitFlag = false;
   uint64_t rb = 0, re = 0;
+  uint64_t lastCost = 0;  // SM cycles of the region's last directional update (queue order)
 };
 
 // Per-phase timings of the last Update (FieldStatistics, Field.h:153-216).
@@ -131,6 +132,7 @@ class SubField {
   void finish(std::vector<LeafReport> reports, std::vector<LeafProfile> profiles, std::vector<uint32_t> regionOf,
               cudaEvent_t emStart, cudaEvent_t emEnd);
   std::vector<LeafTask> pending;  // leaf tasks of the prepared update, by region
+  uint32_t pendingSamples() const { return pendingSamples_; }
   cudaEvent_t events[4] = {};     // start, samples copied, tree built, tasks ready
   void reset();
   FieldView view() const;
@@ -172,8 +174,21 @@ class GpuField {
   void deserialize(const std::string &bytes);  // the same layout (pglDeviceNewFieldFromFile)
   bool equals(const GpuField &o) const;
 
+  // EM schedule parameters (never the result): set directly, or chosen by
+  // timing the candidates on the next Update (autotuneNext).
+  EmTuning tuning;
+  bool autotuneNext = false;
+  struct TuneTrial {
+    EmTuning t;
+    float ms;
+  };
+  std::vector<TuneTrial> lastTuneTrials;
+
  private:
   void runEm(SubField *const *sides, int count);
+  std::vector<LeafTask> emOrder(SubField *const *sides, int count, bool byCost) const;
+  void autotuneEm(SubField *const *sides, int count, cudaStream_t s);
+  DevArray<unsigned char> tuneSnap_;  // state an EM launch changes, kept while trials run
   // the EM launch of both sub-fields: leaf tasks, per-leaf counters, queue,
   // boards and chunk rings
   DevArray<LeafTask> tasks_;

@@ -81,6 +81,18 @@ struct EmSide {
 struct EmSides {
   EmSide side[2];
 };
+// Schedule parameters of an EM launch (they change the speed, never the
+// result): helper blocks per region at a time, the E-step chunk size
+// divisor (samples per chunk = the producers' sample slots / chunkDiv), the
+// consumers' pipeline stages, and whether leaves go to the queue by the
+// previous Update's measured cost (else by sample count), largest first.
+struct EmTuning {
+  int maxHelpers = 4;
+  int chunkDiv = 1;
+  int stageCap = 8;
+  int orderByCost = 0;
+};
+bool em_tuning_valid(const EmTuning &t);
 // Device memory through which the EM launch's blocks share E-step passes
 // (boards, an error word, chunk rings): em_share_bytes(blocks) bytes; after
 // the launch the int at em_share_error_offset(blocks) is non-zero if a wait
@@ -88,7 +100,8 @@ struct EmSides {
 size_t em_share_bytes(int blocks);
 size_t em_share_error_offset(int blocks);
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, const EmSides &sides,
-                      LeafReport *reports, LeafProfile *profiles, void *share, int blocks, cudaStream_t stream);
+                      LeafReport *reports, LeafProfile *profiles, void *share, int blocks, const EmTuning &tune,
+                      cudaStream_t stream);
 
 cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s);
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,
