@@ -61,7 +61,8 @@ OPENPGL_CORE_INTERFACE void *pglDeviceGetCudaStream(PGLDevice device);
 // (the scan and sort kernels of CUB that it calls are not counted).
 OPENPGL_CORE_INTERFACE uint64_t pglGetKernelLaunchCount();
 // Per-region counters of the last Update: region, EM iterations, splits,
-// merges, components (5 x u32 per region); returns the region count.
+// merges, components (5 x u32 per region); returns the region count, writes
+// when capacity >= 5 x count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int volume, uint32_t *out, size_t capacity);
 // Where the EM kernel spent the last Update, per region (18 x u64 each):
 // region, samples, E-step passes, distance passes, split-statistics passes,

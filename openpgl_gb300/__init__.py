@@ -399,7 +399,8 @@ class Field:
     def reports(self, volume=False):
         n = self.lib.pglFieldGetLastUpdateReports(self.h, int(volume), None, 0)
         out = np.zeros((n, 5), dtype=np.uint32)
-        self.lib.pglFieldGetLastUpdateReports(self.h, int(volume), out.ctypes.data, n)
+        if n:
+            self.lib.pglFieldGetLastUpdateReports(self.h, int(volume), out.ctypes.data, out.size)
         return out
 
     def statistics_string(self, volume=False):

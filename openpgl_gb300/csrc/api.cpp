@@ -888,7 +888,7 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int v
   PGL_TRY
   const SubField &sf = volume ? F(field)->volume : F(field)->surface;
   size_t n = sf.lastReports.size();
-  if (out && cap >= n)
+  if (out && cap >= 5 * n)
     for (size_t i = 0; i < n; ++i) {
       out[5 * i + 0] = sf.lastReportRegion[i];
       out[5 * i + 1] = sf.lastReports[i].emIterations;
