@@ -16,6 +16,12 @@ pinned memory (pglSampleStorageAddSamples on host records) and the read-back
 of the per-region update reports.  The inputs (16.8M x 40 B = 671 MB) are
 larger than L2 (129 MB), so no flush is needed between steps.
 
+Beside the headline, `clustered` times the clustered workload: one Update of
+a fresh field on 16,777,216 surface samples around 4096 Gaussian clusters
+(Zipf masses, 1-6 lobes each), maxSamplesPerLeaf 32000, with the default EM
+schedule and with the schedule the EM autotuner picks on the Update before
+(the fields are compared byte for byte).
+
 `--impl reference` times the CPU restatement of the reference algorithm (the
 oracle, built with the reference's arithmetic) with all host threads on a
 bounded sample of the same workload.
@@ -130,6 +136,67 @@ class ClockSampler:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- clustered workload
+CLUSTER_SAMPLES = 16_777_216
+CLUSTER_SEED = 77
+
+
+def run_clustered(pgl, dev, stream, steps, warmup):
+    """One Update of a fresh field per step on the clustered samples (already
+    in device memory): default EM schedule, then the schedule the autotuner
+    picks (its sweep runs inside one untimed Update)."""
+    import torch
+
+    from openpgl_gb300 import synthetic as syn
+
+    samples = syn.cluster_samples(CLUSTER_SAMPLES, CLUSTER_SEED)
+    d = torch.from_numpy(samples.view(np.uint8)).to("cuda")
+    storage = pgl.SampleStorage()
+    torch.cuda.synchronize()
+
+    def update(tuning=None, autotune=False):
+        field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF))
+        if tuning:
+            field.set_em_tuning(**tuning)
+        if autotune:
+            field.autotune_next_update()
+        storage.clear()
+        storage.add_samples_device(d.data_ptr(), CLUSTER_SAMPLES)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        field.update(storage)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return field, a.elapsed_time(b)
+
+    def timed(tuning=None):
+        for _ in range(warmup):
+            update(tuning)
+        first, times, ems = None, [], []
+        for _ in range(steps):
+            field, t = update(tuning)
+            times.append(t)
+            ems.append(field.phases(False)["em_kernel"])
+            first = first or field
+        return first, statistics.median(times), statistics.median(ems)
+
+    ref, ms_default, em_default = timed()
+    tuned_field, tune_ms = update(autotune=True)
+    chosen = tuned_field.em_tuning()
+    trials = tuned_field.tuning_trials()
+    same = tuned_field.field_bytes() == ref.field_bytes()
+    field, ms_tuned, em_tuned = timed(chosen)
+    same = same and field.field_bytes() == ref.field_bytes()
+    return {"workload": "clustered: 16,777,216 surface samples around 4096 Gaussian clusters (Zipf(1.1) masses, "
+                        "1-6 vMF lobes each), maxSamplesPerLeaf 32000, deterministic; one Update of a fresh field",
+            "regions": int(ref.phases(False)["regions"]),
+            "update_ms": round(ms_default, 3), "em_kernel_ms": round(em_default, 3),
+            "autotuned": {"update_ms": round(ms_tuned, 3), "em_kernel_ms": round(em_tuned, 3), "schedule": chosen,
+                          "trials": len(trials), "tuning_update_ms": round(tune_ms, 1),
+                          "best_trial_ms": round(min(t["ms"] for t in trials), 3) if trials else None},
+            "same_field": bool(same)}
 
 
 # ----------------------------------------------------------------- CPU baseline
@@ -316,6 +383,9 @@ def run_gpu(args, rank, world, local_rank):
         field.sample_batch(queries)
     q_e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
 
+    # ---- clustered workload, default and autotuned EM schedule
+    clustered = run_clustered(pgl, dev, stream, args.steps, 1) if args.clustered else None
+
     # ---- served guided queries (continuous batching, background updates)
     serving = run_serving(pgl, field, frames[:2], queries, seconds=args.serve_seconds) if args.serve_seconds > 0 else None
 
@@ -392,6 +462,7 @@ def run_gpu(args, rank, world, local_rank):
                     "p99_ms": round(lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))], 3),
                     "e2e_queries_per_s": round(QUERIES / (q_e2e_ms * 1e-3))},
         "serving": serving,
+        "clustered": clustered,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -456,6 +527,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--serve-seconds", type=float, default=6.0)
+    ap.add_argument("--no-clustered", dest="clustered", action="store_false",
+                    help="skip the clustered workload (default and autotuned EM schedule)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
