@@ -956,11 +956,16 @@ __device__ __forceinline__ void distance_chain(const float *B, const PassShape &
 // (r = c / Kp: sumAssignedSamples a, sumWeights a w, then the 2D covariance
 // sums (a w)(lx lx), (a w)(ly ly), (a w)(lx ly)).  Chi-square lanes start at
 // the next warp: the running mean chi2 += (chi - chi2) / n over the valid
-// samples, n counting from n0.  The producers' y = RN(1 / (n0 + count)) holds
-// when that sum equals the lane's own running count n (the usual case);
-// Markstein's steps then give (chi - chi2) / n exactly, and a skipped sample
-// (y = 0) adds +-0.  A group of 4 samples where a count differs or an operand
-// leaves Markstein's range is redone with the division.
+// samples, n counting from n0.  Markstein's steps with the producers'
+// y = RN(1 / (n0 + count)) give (chi - chi2) / n exactly (a skipped sample,
+// y = 0, adds +-0) when y belongs to the lane's own running count n (the
+// usual case: n equals n0 + count) and the difference d and the quotient lie
+// in [1e-30, 1e30] (or d is 0).  The chain checks this per group of four
+// samples beside the additions, not between them: the counts, the largest
+// |d| against 1e30 and the smallest non-zero |d| against 1e-30 times the
+// group's last n (so every quotient of the group is in range).  From the
+// first group that fails (rare) the chunk is summed again with divisions,
+// which give the same bits wherever Markstein's steps were exact.
 __device__ __forceinline__ int split_chi_base(int Kp) { return ((5 * Kp + 31) / 32) * 32; }
 __device__ __forceinline__ void split_chain(const float *B, const PassShape &sh, int c, int Kp, int n4, float n0,
                                             float &acc, float &accN, float &cnt) {
@@ -971,43 +976,54 @@ __device__ __forceinline__ void split_chain(const float *B, const PassShape &sh,
   } else if (c >= chiBase && c < chiBase + Kp) {
     const int k = c - chiBase;
     const float *xr = B + (5 * Kp + k) * R, *yr = B + (6 * Kp + k) * R, *vr = B + 7 * Kp * R;
+    const float accStart = acc, nStart = accN;
+    int redoAt = n4;  // first group that failed the range check
+    float accRedo = 0.0f, nRedo = 0.0f;
     float4 x = ld4(xr), y = ld4(yr), v = ld4(vr);
     for (int s = 0; s < n4; s += 4) {
       const int sn = s + 4 < n4 ? s + 4 : s;
       const float4 x1 = ld4(xr + sn), y1 = ld4(yr + sn), v1 = ld4(vr + sn);
+      const float accG = acc, nG = accN;
       const float n1 = accN + v.x, n2 = n1 + v.y, n3 = n2 + v.z, n4v = n3 + v.w;
       const float c1 = cnt + v.x, c2 = c1 + v.y, c3 = c2 + v.z, c4 = c3 + v.w;
       const bool same = (v.x == 0.0f || n1 == n0 + c1) & (v.y == 0.0f || n2 == n0 + c2) &
                         (v.z == 0.0f || n3 == n0 + c3) & (v.w == 0.0f || n4v == n0 + c4);
-      const float acc0 = acc;
       const float d1 = x.x - acc;
-      const float q1 = markstein_q(d1, n1, y.x);
-      acc = acc + q1;
+      acc = acc + markstein_q(d1, n1, y.x);
       const float d2 = x.y - acc;
-      const float q2 = markstein_q(d2, n2, y.y);
-      acc = acc + q2;
+      acc = acc + markstein_q(d2, n2, y.y);
       const float d3 = x.z - acc;
-      const float q3 = markstein_q(d3, n3, y.z);
-      acc = acc + q3;
+      acc = acc + markstein_q(d3, n3, y.z);
       const float d4 = x.w - acc;
-      const float q4 = markstein_q(d4, n4v, y.w);
-      acc = acc + q4;
-      const bool bad = !same | (v.x != 0.0f && d1 != 0.0f && !in_div_range(d1, q1)) |
-                       (v.y != 0.0f && d2 != 0.0f && !in_div_range(d2, q2)) |
-                       (v.z != 0.0f && d3 != 0.0f && !in_div_range(d3, q3)) |
-                       (v.w != 0.0f && d4 != 0.0f && !in_div_range(d4, q4));
-      if (bad) {
-        acc = acc0;
-        if (v.x != 0.0f) acc += (x.x - acc) / n1;
-        if (v.y != 0.0f) acc += (x.y - acc) / n2;
-        if (v.z != 0.0f) acc += (x.z - acc) / n3;
-        if (v.w != 0.0f) acc += (x.w - acc) / n4v;
+      acc = acc + markstein_q(d4, n4v, y.w);
+      const float a1 = fabsf(d1), a2 = fabsf(d2), a3 = fabsf(d3), a4 = fabsf(d4);
+      const float gMax = fmaxf(fmaxf(a1, a2), fmaxf(a3, a4));
+      const float gMin = fminf(fminf(a1 == 0.0f ? INFINITY : a1, a2 == 0.0f ? INFINITY : a2),
+                               fminf(a3 == 0.0f ? INFINITY : a3, a4 == 0.0f ? INFINITY : a4));
+      if ((!same || !(gMax <= 1e30f) || gMin < 1.0000002e-30f * n4v) && redoAt == n4) {
+        redoAt = s;
+        accRedo = accG;
+        nRedo = nG;
       }
       accN = n4v;
       cnt = c4;
       x = x1;
       y = y1;
       v = v1;
+    }
+    if (acc != acc) {
+      redoAt = 0;
+      accRedo = accStart;
+      nRedo = nStart;
+    }
+    if (redoAt < n4) {
+      acc = accRedo;
+      accN = nRedo;
+      for (int s = redoAt; s < n4; ++s) {
+        const float vv = vr[s];
+        accN += vv;
+        if (vv != 0.0f) acc += (xr[s] - acc) / accN;
+      }
     }
   }
 }
