@@ -44,6 +44,19 @@ void DevArray<T>::reserve(size_t n, bool keep) {
   p = np;
   cap = want;
 }
+void HostPinned::reserve(size_t bytes) {
+  if (bytes <= cap && p) return;
+  const size_t want = std::max<size_t>(bytes + bytes / 4, 4096);
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+  check(cudaMallocHost(reinterpret_cast<void **>(&p), want), "cudaMallocHost");
+  cap = want;
+}
+HostPinned::~HostPinned() {
+  if (p) cudaFreeHost(p);
+}
+
 template <typename T>
 void DevArray<T>::release() {
   if (p) cudaFree(p);
@@ -327,7 +340,6 @@ void SubField::buildTree(uint32_t n, const float4 *P) {
 
   std::vector<KdJob> jobs;
   std::vector<const Front *> jobFront;
-  std::vector<uint32_t> nodeToJob;
   std::vector<IStatsAcc> acc;
   const uint32_t oldRegions = uint32_t(regions.size());
   while (!front.empty()) {
@@ -381,16 +393,25 @@ void SubField::buildTree(uint32_t n, const float4 *P) {
       jobFront.push_back(&f);
     }
     if (jobs.empty()) break;
-    nodeToJob.assign(nodes.size(), ~0u);
-    for (size_t k = 0; k < jobs.size(); ++k) nodeToJob[jobFront[k]->node] = uint32_t(k);
+    // the level's jobs, node map and (coming back) child statistics share one
+    // page-locked block: the copies run asynchronously; the previous level's
+    // copies are done (its statistics were read after a synchronisation)
+    const size_t jobBytes = (jobs.size() * sizeof(KdJob) + 15) & ~size_t(15);
+    const size_t mapBytes = (nodes.size() * 4 + 15) & ~size_t(15);
+    const size_t accBytes = 2 * jobs.size() * sizeof(IStatsAcc);
+    kdStage_.reserve(jobBytes + mapBytes + accBytes);
+    KdJob *hJobs = reinterpret_cast<KdJob *>(kdStage_.p);
+    uint32_t *hMap = reinterpret_cast<uint32_t *>(kdStage_.p + jobBytes);
+    IStatsAcc *hAcc = reinterpret_cast<IStatsAcc *>(kdStage_.p + jobBytes + mapBytes);
+    std::copy(jobs.begin(), jobs.end(), hJobs);
+    std::fill(hMap, hMap + nodes.size(), ~0u);
+    for (size_t k = 0; k < jobs.size(); ++k) hMap[jobFront[k]->node] = uint32_t(k);
     jobs_.reserve(jobs.size());
-    nodeToJob_.reserve(nodeToJob.size());
+    nodeToJob_.reserve(nodes.size());
     acc_.reserve(2 * jobs.size());
-    check(cudaMemcpyAsync(jobs_.p, jobs.data(), jobs.size() * sizeof(KdJob), cudaMemcpyHostToDevice, stream()), "jobs");
-    check(cudaMemcpyAsync(nodeToJob_.p, nodeToJob.data(), nodeToJob.size() * 4, cudaMemcpyHostToDevice, stream()),
-          "node map");
-    check(kd_job_of(node_.p, n, nodeToJob_.p, jobOf_.p, stream()), "job of");
-    check(init_acc(acc_.p, uint32_t(2 * jobs.size()), stream()), "init acc");
+    check(cudaMemcpyAsync(jobs_.p, hJobs, jobs.size() * sizeof(KdJob), cudaMemcpyHostToDevice, stream()), "jobs");
+    check(cudaMemcpyAsync(nodeToJob_.p, hMap, nodes.size() * 4, cudaMemcpyHostToDevice, stream()), "node map");
+    check(kd_job_of(node_.p, n, nodeToJob_.p, jobOf_.p, acc_.p, uint32_t(2 * jobs.size()), stream()), "job of");
     check(kd_level(posA_.p, jobOf_.p, n, jobs_.p, isLeft_.p, scanLeft_.p, acc_.p, posB_.p, nodeB_.p, scratch_,
                    stream()),
           "kd level");
@@ -398,10 +419,9 @@ void SubField::buildTree(uint32_t n, const float4 *P) {
     std::swap(posA_.cap, posB_.cap);
     std::swap(node_.p, nodeB_.p);
     std::swap(node_.cap, nodeB_.cap);
-    acc.resize(2 * jobs.size());
-    check(cudaMemcpyAsync(acc.data(), acc_.p, acc.size() * sizeof(IStatsAcc), cudaMemcpyDeviceToHost, stream()),
-          "D2H acc");
+    check(cudaMemcpyAsync(hAcc, acc_.p, accBytes, cudaMemcpyDeviceToHost, stream()), "D2H acc");
     check(cudaStreamSynchronize(stream()), "sync");
+    acc.assign(hAcc, hAcc + 2 * jobs.size());
     std::vector<Front> next;
     next.reserve(2 * jobs.size());
     for (size_t k = 0; k < jobs.size(); ++k) {

@@ -39,6 +39,18 @@ struct DevArray {
   DevArray &operator=(const DevArray &) = delete;
 };
 
+// Page-locked host memory (grows; the caller makes sure no copy from or to the
+// old block is in flight when it grows).
+struct HostPinned {
+  unsigned char *p = nullptr;
+  size_t cap = 0;
+  void reserve(size_t bytes);
+  ~HostPinned();
+  HostPinned() = default;
+  HostPinned(const HostPinned &) = delete;
+  HostPinned &operator=(const HostPinned &) = delete;
+};
+
 struct SampleSide {
   DevArray<float4> P, D;
   DevArray<float> pdf;
@@ -154,6 +166,7 @@ class SubField {
   DevArray<unsigned long long> keys64_;
   DevArray<KdJob> jobs_;
   DevArray<IStatsAcc> acc_;
+  HostPinned kdStage_;  // a kd level's jobs and node map going up, its child statistics coming back
   DevArray<float4> means_;
   DevArray<uint32_t> bounds6_;
   Scratch scratch_;

@@ -50,7 +50,9 @@ cudaError_t scene_bounds(const float4 *P, uint64_t n, uint32_t *d6, cudaStream_t
 cudaError_t init_posidx(const float4 *P, uint32_t n, float4 *posIdx, cudaStream_t s);
 cudaError_t init_acc(IStatsAcc *acc, uint32_t count, cudaStream_t s);
 cudaError_t kd_root_stats(const float4 *pos, uint32_t n, const KdJob &job, IStatsAcc *acc, cudaStream_t s);
-cudaError_t kd_job_of(const uint32_t *node, uint32_t n, const uint32_t *nodeToJob, uint32_t *jobOf, cudaStream_t s);
+// jobOf[i] = nodeToJob[node[i]] (~0 for finished samples); clears acc[0, accCount)
+cudaError_t kd_job_of(const uint32_t *node, uint32_t n, const uint32_t *nodeToJob, uint32_t *jobOf, IStatsAcc *acc,
+                      uint32_t accCount, cudaStream_t s);
 cudaError_t kd_level(const float4 *pos, const uint32_t *jobOf, uint32_t n, const KdJob *jobs, uint32_t *isLeft,
                      uint32_t *scanLeft, IStatsAcc *acc, float4 *posOut, uint32_t *nodeOut, Scratch &scratch,
                      cudaStream_t s);

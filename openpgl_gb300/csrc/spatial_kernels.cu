@@ -289,8 +289,17 @@ __global__ void kd_scatter_kernel(const float4 *pos, const uint32_t *jobOf, cons
 
 // Maps each sample's node to the job index of the next level (~0 if the node
 // is a finished leaf).
-__global__ void kd_job_of_kernel(const uint32_t *node, uint32_t n, const uint32_t *nodeToJob, uint32_t *jobOf) {
+// The job of every sample of a level (~0 for samples in finished leaves), and
+// the level's child accumulators cleared, in one launch.
+__global__ void kd_job_of_kernel(const uint32_t *node, uint32_t n, const uint32_t *nodeToJob, uint32_t *jobOf,
+                                 IStatsAcc *acc, uint32_t accCount) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < accCount) {
+    IStatsAcc a;
+    for (int d = 0; d < 3; ++d) { a.m[d] = 0; a.v[d] = 0; a.lo[d] = LLONG_MAX; a.hi[d] = LLONG_MIN; }
+    a.n = 0;
+    acc[i] = a;
+  }
   if (i >= n) return;
   uint32_t nd = node[i];
   jobOf[i] = nd == ~0u ? ~0u : nodeToJob[nd];
@@ -517,10 +526,12 @@ cudaError_t kd_root_stats(const float4 *pos, uint32_t n, const KdJob &job, IStat
   return cudaGetLastError();
 }
 
-cudaError_t kd_job_of(const uint32_t *node, uint32_t n, const uint32_t *nodeToJob, uint32_t *jobOf, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
+cudaError_t kd_job_of(const uint32_t *node, uint32_t n, const uint32_t *nodeToJob, uint32_t *jobOf, IStatsAcc *acc,
+                      uint32_t accCount, cudaStream_t s) {
+  const uint32_t m = n > accCount ? n : accCount;
+  if (m == 0) return cudaSuccess;
   count_launch();
-  kd_job_of_kernel<<<blocks_for(n, 256), 256, 0, s>>>(node, n, nodeToJob, jobOf);
+  kd_job_of_kernel<<<blocks_for(m, 256), 256, 0, s>>>(node, n, nodeToJob, jobOf, acc, accCount);
   return cudaGetLastError();
 }
 
