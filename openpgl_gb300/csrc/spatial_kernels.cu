@@ -123,9 +123,65 @@ __device__ __forceinline__ void acc_add(IStatsAcc *a, const long long m[3], cons
   atomicAdd(&a->n, n);
 }
 
+// A warp's running integer statistics of one job's two children, per lane.
+struct WarpSideAcc {
+  long long m[2][3], v[2][3], lo[2][3], hi[2][3];
+  unsigned long long n[2];
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int sd = 0; sd < 2; ++sd) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) { m[sd][d] = 0; v[sd][d] = 0; lo[sd][d] = LLONG_MAX; hi[sd][d] = LLONG_MIN; }
+      n[sd] = 0;
+    }
+  }
+};
+__device__ __forceinline__ long long warp_sum64(long long x) {
+  for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, off);
+  return x;
+}
+__device__ __forceinline__ long long warp_min64(long long x) {
+  for (int off = 16; off > 0; off >>= 1) x = min(x, __shfl_xor_sync(0xFFFFFFFFu, x, off));
+  return x;
+}
+__device__ __forceinline__ long long warp_max64(long long x) {
+  for (int off = 16; off > 0; off >>= 1) x = max(x, __shfl_xor_sync(0xFFFFFFFFu, x, off));
+  return x;
+}
+// Adds a warp's running statistics of job `job` to acc[2 job + side] (or to
+// the block's shared copy) and clears them.
+__device__ __forceinline__ void warp_flush(WarpSideAcc &w, uint32_t job, bool stats, IStatsAcc *acc,
+                                           IStatsAcc *local, bool useLocal, uint32_t firstJob) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int sd = 0; sd < 2; ++sd) {
+    unsigned long long cnt = (unsigned long long)warp_sum64((long long)w.n[sd]);
+    if (cnt == 0) continue;
+    const uint32_t slot = 2 * job + uint32_t(sd);
+    if (stats) {
+      long long sm[3], sv[3], lo[3], hi[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        sm[d] = warp_sum64(w.m[sd][d]);
+        sv[d] = warp_sum64(w.v[sd][d]);
+        lo[d] = warp_min64(w.lo[sd][d]);
+        hi[d] = warp_max64(w.hi[sd][d]);
+      }
+      if (lane == 0) acc_add(useLocal ? &local[slot - 2 * firstJob] : &acc[slot], sm, sv, lo, hi, cnt);
+    } else if (lane == 0) {
+      atomicAdd(&acc[slot].n, cnt);
+    }
+  }
+  w.clear();
+}
+
 // Classifies the samples of every job at this level: side flag (1 = left),
 // child statistics into acc[2*job + side].  jobOf[i] is the job of sample i
-// (or ~0 when the sample already sits in a finished leaf).
+// (or ~0 when the sample already sits in a finished leaf).  Samples of a job
+// are contiguous, so a warp mostly meets one job: each lane keeps running
+// statistics of the warp's current job in registers, and the warp reduces
+// and adds them only when its job changes and at the end; a group of 32
+// samples that mixes jobs adds per sample.
 __global__ void __launch_bounds__(kKdThreads)
 kd_classify_kernel(const float4 *pos, const uint32_t *jobOf, uint32_t n, const KdJob *jobs, uint32_t *isLeft,
                    IStatsAcc *acc) {
@@ -163,7 +219,10 @@ kd_classify_kernel(const float4 *pos, const uint32_t *jobOf, uint32_t n, const K
   __syncthreads();
   const bool useLocal = firstJob != ~0u && (lastJob - firstJob) < uint32_t(kKdLocal);
   const unsigned full = 0xFFFFFFFFu;
-  const int lane = threadIdx.x & 31;
+  WarpSideAcc w;
+  w.clear();
+  uint32_t cur = ~0u;  // the warp's current job
+  bool curStats = false;
   for (uint32_t base = tileBegin; base < tileEnd; base += blockDim.x) {
     const uint32_t i = base + threadIdx.x;
     const uint32_t jid = i < tileEnd ? jobOf[i] : ~0u;
@@ -180,36 +239,27 @@ kd_classify_kernel(const float4 *pos, const uint32_t *jobOf, uint32_t n, const K
       if (stats) quantize(j, p, q, qv);
     }
     if (i < tileEnd) isLeft[i] = left;
-    // one job for the whole warp and 32-bit-safe values: reduce per side
-    // with warp reductions, one set of atomics per side
     const unsigned act = __ballot_sync(full, jid != ~0u);
     if (act == 0) continue;
     const uint32_t j0 = __shfl_sync(full, jid, __ffs(act) - 1);
-    bool small = true;
-    for (int d = 0; d < 3; ++d) small &= (q[d] >= -(1LL << 24) && q[d] <= (1LL << 24) && qv[d] >= 0 && qv[d] <= (1LL << 24));
-    const bool uniform = __all_sync(full, (jid == ~0u || jid == j0) && small);
-    if (uniform) {
-      for (uint32_t side = 0; side < 2; ++side) {
-        const bool mine = jid != ~0u && (left ? 0u : 1u) == side;
-        const unsigned m = __ballot_sync(full, mine);
-        if (m == 0) continue;
-        long long sm[3], sv[3], lo[3], hi[3];
-        const bool needStats = __shfl_sync(full, stats ? 1 : 0, __ffs(m) - 1) != 0;
-        if (needStats) {
+    if (__all_sync(full, jid == ~0u || jid == j0)) {
+      if (j0 != cur) {
+        if (cur != ~0u) warp_flush(w, cur, curStats, acc, local, useLocal, firstJob);
+        cur = j0;
+        curStats = __shfl_sync(full, stats ? 1 : 0, __ffs(act) - 1) != 0;
+      }
+      // both sides with selects (fixed register indices)
+#pragma unroll
+      for (int sd = 0; sd < 2; ++sd) {
+        const bool on = jid != ~0u && (left != 0u) == (sd == 0);
+        w.n[sd] += on ? 1ull : 0ull;
+        if (curStats) {
+#pragma unroll
           for (int d = 0; d < 3; ++d) {
-            sm[d] = __reduce_add_sync(full, mine ? int(q[d]) : 0);
-            sv[d] = __reduce_add_sync(full, mine ? int(qv[d]) : 0);
-            lo[d] = __reduce_min_sync(full, mine ? int(q[d]) : INT_MAX);
-            hi[d] = __reduce_max_sync(full, mine ? int(q[d]) : INT_MIN);
-          }
-        }
-        if (lane == __ffs(m) - 1) {
-          const uint32_t slot = 2 * j0 + side;
-          if (needStats) {
-            IStatsAcc *a = useLocal ? &local[slot - 2 * firstJob] : &acc[slot];
-            acc_add(a, sm, sv, lo, hi, (unsigned long long)__popc(m));
-          } else {
-            atomicAdd(&acc[slot].n, (unsigned long long)__popc(m));
+            w.m[sd][d] += on ? q[d] : 0ll;
+            w.v[sd][d] += on ? qv[d] : 0ll;
+            w.lo[sd][d] = min(w.lo[sd][d], on ? q[d] : LLONG_MAX);
+            w.hi[sd][d] = max(w.hi[sd][d], on ? q[d] : LLONG_MIN);
           }
         }
       }
@@ -223,6 +273,7 @@ kd_classify_kernel(const float4 *pos, const uint32_t *jobOf, uint32_t n, const K
       }
     }
   }
+  if (cur != ~0u) warp_flush(w, cur, curStats, acc, local, useLocal, firstJob);
   __syncthreads();
   if (useLocal) {
     for (int s = threadIdx.x; s < 2 * kKdLocal; s += blockDim.x) {
