@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "x86_approx_tables.h"
+#include "../openpgl_gb300/csrc/hg_table.h"
 
 namespace orc {
 
@@ -1729,6 +1730,64 @@ static void runQuery(const SubField &f, const QueryIn &q, QueryOut &o, bool cosi
   o.pdfLi = vmmPdf(li, d);
 }
 
+// Volume query with the single-lobe Henyey-Greenstein product
+// (VMMVolumeSamplingDistribution.h:54-128, VMMPhaseFunctions.h:45-57): the
+// shifted mixture times each lobe of the phase function's three-lobe fit
+// (lobes of the fit's sign facing dir, else -dir), products weighted by their
+// integrals; a sample picks a product by u.x, then samples it with u.x
+// rescaled; the pdf is the weighted sum of the products' pdfs.
+static void runQueryHG(const SubField &f, const QueryIn &q, float meanCosine, QueryOut &o) {
+  std::memset(&o, 0, sizeof(o));
+  float s1d = q.s1d;
+  o.s1d = s1d;
+  if (!(f.iteration > 0)) return;
+  const float *b = f.kdBounds;
+  for (int d = 0; d < 3; ++d)
+    if (!(q.pos[d] >= b[d] && q.pos[d] <= b[3 + d])) return;
+  uint32_t leaf = uint32_t(f.leafAt(q.pos));
+  uint32_t reg = leaf;
+  if (f.cfg.knn && s1d >= 0.f) reg = f.approximateClosest(leaf, q.pos, &s1d);
+  o.s1d = s1d;
+  const Region &r = f.regions[reg];
+  if (!r.valid) return;
+  VMM li = r.vmm;
+  V3 shift = v3(li.pivot[0] - q.pos[0], li.pivot[1] - q.pos[1], li.pivot[2] - q.pos[2]);
+  vmmParallaxShift(li, shift);
+  const float absG = std::fabs(meanCosine);
+  const float step = (pgl::kHgMaxMeanCosine - pgl::kHgMinMeanCosine) / float(pgl::kHgFits);
+  int idx = int(std::floor((absG - pgl::kHgMinMeanCosine) / step));
+  idx = std::min(idx, pgl::kHgFits - 1);
+  const V3 dir = v3(q.normal[0], q.normal[1], q.normal[2]);
+  VMM g[pgl::kHgLobes];
+  float w[pgl::kHgLobes];
+  float sum = 0.0f;
+  for (int i = 0; i < pgl::kHgLobes; ++i) {
+    const pgl::HgLobeFit &fit = pgl::kHgTable[idx][i];
+    g[i] = li;
+    const V3 out = meanCosine * fit.meanCosine > 0.f ? dir : v3(-dir.x, -dir.y, -dir.z);
+    w[i] = vmmProduct(g[i], fit.weight, out, fit.kappa, fit.normalization);
+    sum += w[i];
+  }
+  for (int i = 0; i < pgl::kHgLobes; ++i) w[i] /= sum;
+  float acc = 0.0f;
+  int i = 0;
+  for (; i < pgl::kHgLobes - 1; ++i) {
+    const float next = acc + w[i];
+    if (next > q.u[0]) break;
+    acc = next;
+  }
+  V3 d = vmmSample(g[i], (q.u[0] - acc) / w[i], q.u[1]);
+  float pdf = 0.0f;
+  for (int k = 0; k < pgl::kHgLobes; ++k) pdf += w[k] * vmmPdf(g[k], d);
+  o.ok = 1;
+  o.id = leaf;
+  o.dir[0] = d.x;
+  o.dir[1] = d.y;
+  o.dir[2] = d.z;
+  o.pdf = pdf;
+  o.pdfLi = vmmPdf(li, d);
+}
+
 // ------------------------------------------------------------------ field file
 struct Writer {
   std::string b;
@@ -1922,6 +1981,13 @@ void orc_field_query(void *h, int volume, int cosine, const QueryIn *q, QueryOut
   Field *f = static_cast<Field *>(h);
   const SubField &s = volume ? f->volume : f->surface;
   for (uint64_t i = 0; i < n; ++i) runQuery(s, q[i], o[i], cosine != 0);
+}
+
+// Volume queries with the Henyey-Greenstein product, query i with mean cosine g[i]
+// and q[i].normal as the direction of the phase function.
+void orc_field_query_hg(void *h, const QueryIn *q, const float *g, QueryOut *o, uint64_t n) {
+  Field *f = static_cast<Field *>(h);
+  for (uint64_t i = 0; i < n; ++i) runQueryHG(f->volume, q[i], g[i], o[i]);
 }
 
 // Region index of each position (kd traversal only) for leaf-assignment checks.

@@ -44,6 +44,7 @@ def load():
         lib.orc_field_store.restype = u64
         lib.orc_field_store.argtypes = [vp, ctypes.c_char_p, u64]
         lib.orc_field_query.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, u64]
+        lib.orc_field_query_hg.argtypes = [vp, vp, vp, vp, u64]
         lib.orc_field_leaf_of.argtypes = [vp, ctypes.c_int, vp, vp, u64]
         lib.orc_field_set_scene_bounds.argtypes = [vp, vp]
         for n in ("orc_fexp", "orc_flog", "orc_rcp", "orc_rsqrt"):
@@ -92,11 +93,27 @@ class OracleField:
         self.lib.orc_field_query(self.h, int(volume), int(cosine), q.ctypes.data, out.ctypes.data, len(q))
         return out
 
+    def query_hg(self, queries, mean_cosines):
+        """Volume queries with the Henyey-Greenstein product (direction = the
+        query's normal)."""
+        q = np.ascontiguousarray(queries)
+        g = np.ascontiguousarray(mean_cosines, dtype=np.float32)
+        out = np.zeros(len(q), dtype=QUERY_OUT_DTYPE)
+        self.lib.orc_field_query_hg(self.h, q.ctypes.data, g.ctypes.data, out.ctypes.data, len(q))
+        return out
+
     def leaf_of(self, positions, volume=False):
         p = np.ascontiguousarray(np.asarray(positions, np.float32).reshape(-1, 3))
         out = np.zeros(len(p), dtype=np.int32)
         self.lib.orc_field_leaf_of(self.h, int(volume), p.ctypes.data, out.ctypes.data, len(p))
         return out
+
+
+def hg_mean_cosines(n):
+    """Mean cosine of the phase function for query i (the reference harness
+    uses the same float arithmetic): -0.99 .. 0.99 in steps of 0.01."""
+    i = np.arange(n, dtype=np.int64) % 199
+    return i.astype(np.float32) * np.float32(0.01) - np.float32(0.99)
 
 
 def reference_available():
@@ -106,7 +123,8 @@ def reference_available():
 def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministic=True, threads=1, device=8):
     """Runs the reference library on ``frames`` (list of sample arrays) and
     returns (field file bytes, per-frame update ms, surface query out, volume
-    query out)."""
+    query out, volume query out with the Henyey-Greenstein product of mean
+    cosine hg_mean_cosines(n))."""
     import sys
 
     sys.path.insert(0, os.path.dirname(HERE))
@@ -128,8 +146,9 @@ def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministi
         subprocess.run(args, check=True, env=env)
         field = open(os.path.join(td, "ref.field"), "rb").read()
         times = [float(x) for x in open(os.path.join(td, "ref.times")).read().split()]
-        sq = vq = None
+        sq = vq = hq = None
         if queries is not None:
             sq = np.fromfile(os.path.join(td, "ref.surfq.bin"), dtype=QUERY_OUT_DTYPE)
             vq = np.fromfile(os.path.join(td, "ref.volq.bin"), dtype=QUERY_OUT_DTYPE)
-        return field, times, sq, vq
+            hq = np.fromfile(os.path.join(td, "ref.volhgq.bin"), dtype=QUERY_OUT_DTYPE)
+        return field, times, sq, vq, hq

@@ -12,6 +12,9 @@
 //              <out_prefix>.surfq.bin  n * {ok u32, id u32, s1d f, dir f3, pdf f,
 //                                           pdfLi f} (surface queries)
 //              <out_prefix>.volq.bin   same for the volume field
+//              <out_prefix>.volhgq.bin same, volume field with the Henyey-Greenstein
+//                                      product: direction = the query's normal,
+//                                      mean cosine of query i = hg_mean_cosine(i)
 #include <openpgl/cpp/OpenPGL.h>
 
 #include <chrono>
@@ -29,6 +32,10 @@ struct QueryOut {
   uint32_t ok, id;
   float s1d, dir[3], pdf, pdfLi;
 };
+
+// Mean cosine of the phase function for query i: -0.99 .. 0.99 in steps of 0.01
+// (float arithmetic; the tests compute the same values).
+float hg_mean_cosine(uint64_t i) { return float(int(i % 199u)) * 0.01f - 0.99f; }
 
 bool readAll(const char *path, std::vector<char> &buf) {
   FILE *f = std::fopen(path, "rb");
@@ -92,7 +99,7 @@ int main(int argc, char **argv) {
     uint64_t nq;
     std::memcpy(&nq, qbuf.data(), 8);
     const Query *q = reinterpret_cast<const Query *>(qbuf.data() + 8);
-    std::vector<QueryOut> surf(nq), vol(nq);
+    std::vector<QueryOut> surf(nq), vol(nq), volhg(nq);
     openpgl::cpp::SurfaceSamplingDistribution ssd(&field);
     openpgl::cpp::VolumeSamplingDistribution vsd(&field);
     for (uint64_t i = 0; i < nq; ++i) {
@@ -124,6 +131,19 @@ int main(int argc, char **argv) {
         v.pdfLi = vsd.IncomingRadiancePDF(d);
         v.id = vsd.GetId();
       }
+      QueryOut &h = volhg[i];
+      std::memset(&h, 0, sizeof(h));
+      float s1dh = q[i].s1d;
+      h.ok = vsd.Init(&field, pos, s1dh) ? 1u : 0u;
+      h.s1d = s1dh;
+      if (h.ok) {
+        vsd.ApplySingleLobeHenyeyGreensteinProduct(nrm, hg_mean_cosine(i));
+        pgl_vec3f d;
+        h.pdf = vsd.SamplePDF(u, d);
+        h.dir[0] = d.x; h.dir[1] = d.y; h.dir[2] = d.z;
+        h.pdfLi = vsd.IncomingRadiancePDF(d);
+        h.id = vsd.GetId();
+      }
     }
     FILE *fs = std::fopen((prefix + ".surfq.bin").c_str(), "wb");
     std::fwrite(surf.data(), sizeof(QueryOut), surf.size(), fs);
@@ -131,6 +151,9 @@ int main(int argc, char **argv) {
     FILE *fv = std::fopen((prefix + ".volq.bin").c_str(), "wb");
     std::fwrite(vol.data(), sizeof(QueryOut), vol.size(), fv);
     std::fclose(fv);
+    FILE *fh = std::fopen((prefix + ".volhgq.bin").c_str(), "wb");
+    std::fwrite(volhg.data(), sizeof(QueryOut), volhg.size(), fh);
+    std::fclose(fh);
   }
   return 0;
 }

@@ -10,7 +10,9 @@ Each case stores:
   <case>.queries.npz  "surface": guided surface queries (Init + cosine
                     product + SamplePDF + IncomingRadiancePDF per query),
                     "volume": guided volume queries (Init + SamplePDF +
-                    IncomingRadiancePDF)
+                    IncomingRadiancePDF), "volume_hg": the same with the
+                    single-lobe Henyey-Greenstein product first (direction =
+                    the query's normal, mean cosine pyoracle.hg_mean_cosines)
 and manifest.json records the generator calls and the SHA-256 of every
 generated input, so a test can check that the generators still produce the
 same inputs before it compares outputs.
@@ -69,12 +71,12 @@ def main():
                 "cases": {}}
     for name, case in CASES.items():
         frames, queries = build_inputs(case)
-        field, _, sq, vq = pyoracle.run_reference(frames, queries, max_samples_per_leaf=case["leaf"],
+        field, _, sq, vq, hq = pyoracle.run_reference(frames, queries, max_samples_per_leaf=case["leaf"],
                                                   deterministic=True, threads=1, device=8)
         field = fieldfile.strip_timings(field)
         with gzip.open(os.path.join(HERE, f"{name}.field.gz"), "wb", compresslevel=9) as f:
             f.write(field)
-        np.savez_compressed(os.path.join(HERE, f"{name}.queries.npz"), surface=sq, volume=vq)
+        np.savez_compressed(os.path.join(HERE, f"{name}.queries.npz"), surface=sq, volume=vq, volume_hg=hq)
         manifest["cases"][name] = dict(case, frame_sha256=[sha(f) for f in frames], queries_sha256=sha(queries),
                                        field_sha256=hashlib.sha256(field).hexdigest())
         print(name, len(field), "bytes,", len(fieldfile.read_field_file(field)["surface"]["regions"]), "surface regions")

@@ -78,6 +78,19 @@ def test_oracle_queries_are_the_reference_queries(name):
     assert v.tobytes() == rv.tobytes()
 
 
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_hg_queries_are_the_reference_queries(name):
+    """Volume queries with the single-lobe Henyey-Greenstein product
+    (VMMVolumeSamplingDistribution.h:54-80) over mean cosines -0.99 .. 0.99."""
+    (frames, queries), case = inputs(name)
+    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4)
+    for f in frames:
+        orc.update(f)
+    rh = np.load(os.path.join(GOLDEN, f"{name}.queries.npz"))["volume_hg"]
+    h = orc.query_hg(queries, pyoracle.hg_mean_cosines(len(queries)))
+    assert h.tobytes() == rh.tobytes()
+
+
 def test_golden_field_structure():
     """The parsed reference file is self-consistent: leaves index regions,
     every region's sample statistics count matches the leaf histogram of its
@@ -101,10 +114,11 @@ def test_oracle_matches_live_reference_on_fresh_seed():
 
     frames = [syn.cube_face_samples(20000, 777 + i, volume_fraction=0.3) for i in range(2)]
     q = syn.queries(1024, 779)
-    field, _, rs, rv = pyoracle.run_reference(frames, q, max_samples_per_leaf=3000)
+    field, _, rs, rv, rh = pyoracle.run_reference(frames, q, max_samples_per_leaf=3000)
     orc = pyoracle.OracleField(3000, deterministic=True, threads=2)
     for f in frames:
         orc.update(f)
     assert fieldfile.strip_timings(orc.field_bytes()) == fieldfile.strip_timings(field)
     assert orc.query(q).tobytes() == rs.tobytes()
     assert orc.query(q, volume=True, cosine=False).tobytes() == rv.tobytes()
+    assert orc.query_hg(q, pyoracle.hg_mean_cosines(len(q))).tobytes() == rh.tobytes()
