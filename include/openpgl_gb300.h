@@ -40,6 +40,19 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatch(PGLField field, const PGLG
 OPENPGL_CORE_INTERFACE bool pglFieldSampleBatchDevice(PGLField field, bool volume, const PGLGuidedQuery *dQueries,
                                                       size_t n, PGLGuidedQueryResult *dResults, bool cosineProduct,
                                                       void *cudaStream);
+// Volume guided queries with the single-lobe Henyey-Greenstein product
+// (what pglVolumeSamplingDistributionApplySingleLobeHenyeyGreensteinProduct
+// does per object): query i's normal is the phase function's direction and
+// meanCosines[i] its mean cosine g; results as the per-object calls (Init +
+// product + SamplePDF + IncomingRadiancePDF).  Host buffers, or device
+// buffers enqueued on `cudaStream` (null: the library's stream; does not
+// synchronise).
+OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHG(PGLField field, const PGLGuidedQuery *queries,
+                                                        const float *meanCosines, size_t n,
+                                                        PGLGuidedQueryResult *results);
+OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHGDevice(PGLField field, const PGLGuidedQuery *dQueries,
+                                                              const float *dMeanCosines, size_t n,
+                                                              PGLGuidedQueryResult *dResults, void *cudaStream);
 // Adds samples that already live in device memory.
 OPENPGL_CORE_INTERFACE void pglSampleStorageAddSamplesDevice(PGLSampleStorage sampleStorage,
                                                              const PGLSampleData *dSamples, size_t numSamples);

@@ -136,6 +136,10 @@ C_API = {
                                                   ctypes.c_void_p]),
     "pglFieldSampleBatchDevice": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_bool, ctypes.c_void_p, ctypes.c_size_t,
                                                   ctypes.c_void_p, ctypes.c_bool, ctypes.c_void_p]),
+    "pglFieldSampleVolumeBatchHG": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                    ctypes.c_void_p]),
+    "pglFieldSampleVolumeBatchHGDevice": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                          ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
     "pglSampleStorageAddSamplesDevice": (None, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "pglFieldStoreToBuffer": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     "pglFieldGetLastUpdateTimings": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
@@ -422,6 +426,18 @@ class Field:
         _check(ok, "pglFieldSampleBatch")
         return out
 
+    def sample_batch_hg(self, queries, mean_cosines):
+        """Volume guided queries with the Henyey-Greenstein product (the query's
+        normal is the phase function's direction)."""
+        q = np.ascontiguousarray(queries, dtype=PGL_QUERY_DTYPE)
+        g = np.ascontiguousarray(mean_cosines, dtype=np.float32)
+        if len(g) != len(q):
+            raise ValueError("one mean cosine per query")
+        out = np.zeros(len(q), dtype=QUERY_RESULT_DTYPE)
+        _check(self.lib.pglFieldSampleVolumeBatchHG(self.h, q.ctypes.data, g.ctypes.data, len(q), out.ctypes.data),
+               "pglFieldSampleVolumeBatchHG")
+        return out
+
     def sample_batch_device(self, q_ptr, n, out_ptr, volume=False, cosine=True, stream=None):
         ok = self.lib.pglFieldSampleBatchDevice(self.h, volume, q_ptr, n, out_ptr, cosine, stream)
         _check(ok, "pglFieldSampleBatchDevice")
@@ -484,6 +500,13 @@ class SurfaceSamplingDistribution:
 
 class VolumeSamplingDistribution(SurfaceSamplingDistribution):
     volume = True
+
+    def apply_hg_product(self, direction, mean_cosine):
+        self.lib.pglVolumeSamplingDistributionApplySingleLobeHenyeyGreensteinProduct(self.h, Vec3(*direction),
+                                                                                     float(mean_cosine))
+
+    def supports_hg_product(self):
+        return bool(self.lib.pglVolumeSamplingDistributionSupportsApplySingleLobeHenyeyGreensteinProduct(self.h))
 
 
 class GuidingServer:

@@ -435,15 +435,20 @@ OPENPGL_CORE_INTERFACE bool pglVolumeSamplingDistributionValidate(PGLVolumeSampl
 OPENPGL_CORE_INTERFACE void pglVolumeSamplingDistributionClear(PGLVolumeSamplingDistribution d) {
   D(d)->numDistributions = 0;
 }
+// VMMVolumeSamplingDistribution::applySingleLobeHenyeyGreensteinProduct
+// (VMMVolumeSamplingDistribution.h:54-80; api.cpp:742-747)
 OPENPGL_CORE_INTERFACE void pglVolumeSamplingDistributionApplySingleLobeHenyeyGreensteinProduct(
-    PGLVolumeSamplingDistribution, pgl_vec3f, const float) {
+    PGLVolumeSamplingDistribution d, pgl_vec3f dir, const float meanCosine) {
   PGL_TRY
-  throw std::runtime_error("the Henyey-Greenstein product is not supported by the GPU library yet");
+  if (D(d)->numDistributions == 0) return;
+  Context &c = Context::get();
+  check(launch_ssd_hg(D(d)->dState, dir.x, dir.y, dir.z, meanCosine, c.stream), "Henyey-Greenstein product");
+  D(d)->numDistributions = kMaxProducts;
   PGL_CATCH_VOID
 }
 OPENPGL_CORE_INTERFACE bool pglVolumeSamplingDistributionSupportsApplySingleLobeHenyeyGreensteinProduct(
     PGLVolumeSamplingDistribution) {
-  return false;
+  return true;
 }
 OPENPGL_CORE_INTERFACE PGLRegion pglVolumeSamplingGetRegion(PGLVolumeSamplingDistribution d) {
   return reinterpret_cast<PGLRegion>(const_cast<void *>(D(d)->regionTag));
@@ -652,11 +657,9 @@ OPENPGL_CORE_INTERFACE void pglPathSegmentStoragePropagateSamples(PGLPathSegment
                                                                   bool) PGL_UNSUPPORTED()
 
 // ------------------------------------------------------------------ appended entry points (openpgl_gb300.h)
-OPENPGL_CORE_INTERFACE bool pglFieldSampleBatchDevice(PGLField field, bool volume, const PGLGuidedQuery *dQueries,
-                                                      size_t n, PGLGuidedQueryResult *dResults, bool cosineProduct,
-                                                      void *cudaStream) {
-  PGL_TRY
-  Context &c = Context::get();
+static void launch_batch(PGLField field, bool volume, const PGLGuidedQuery *dQueries, size_t n,
+                         PGLGuidedQueryResult *dResults, bool cosineProduct, const float *dMeanCosines,
+                         cudaStream_t s) {
   const SubField &sf = volume ? F(field)->volume : F(field)->surface;
   QueryParams p{};
   p.f = sf.view();
@@ -664,10 +667,29 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleBatchDevice(PGLField field, bool volum
   p.cosNorm = cosine_lobe_normalization();
   p.cosine = cosineProduct ? 1 : 0;
   p.samplesPerQuery = 1;
-  cudaStream_t s = cudaStream ? static_cast<cudaStream_t>(cudaStream) : c.stream;
+  p.hgMeanCosine = dMeanCosines;
   check(launch_query(p, reinterpret_cast<const QueryIn *>(dQueries), reinterpret_cast<QueryOut *>(dResults),
                      uint32_t(n), s),
         "query");
+}
+OPENPGL_CORE_INTERFACE bool pglFieldSampleBatchDevice(PGLField field, bool volume, const PGLGuidedQuery *dQueries,
+                                                      size_t n, PGLGuidedQueryResult *dResults, bool cosineProduct,
+                                                      void *cudaStream) {
+  PGL_TRY
+  Context &c = Context::get();
+  launch_batch(field, volume, dQueries, n, dResults, cosineProduct, nullptr,
+               cudaStream ? static_cast<cudaStream_t>(cudaStream) : c.stream);
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHGDevice(PGLField field, const PGLGuidedQuery *dQueries,
+                                                              const float *dMeanCosines, size_t n,
+                                                              PGLGuidedQueryResult *dResults, void *cudaStream) {
+  PGL_TRY
+  if (n > 0 && dMeanCosines == nullptr) throw std::runtime_error("Henyey-Greenstein batch without mean cosines");
+  Context &c = Context::get();
+  launch_batch(field, true, dQueries, n, dResults, false, dMeanCosines,
+               cudaStream ? static_cast<cudaStream_t>(cudaStream) : c.stream);
   return true;
   PGL_CATCH(false)
 }
@@ -696,6 +718,27 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatch(PGLField field, const PGLG
                                                       PGLGuidedQueryResult *results) {
   PGL_TRY
   return sample_batch_host(field, true, queries, n, results, false);
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHG(PGLField field, const PGLGuidedQuery *queries,
+                                                        const float *meanCosines, size_t n,
+                                                        PGLGuidedQueryResult *results) {
+  PGL_TRY
+  if (n > 0 && meanCosines == nullptr) throw std::runtime_error("Henyey-Greenstein batch without mean cosines");
+  Context &c = Context::get();
+  static thread_local DevArray<QueryIn> dq;
+  static thread_local DevArray<QueryOut> dr;
+  static thread_local DevArray<float> dg;
+  dq.reserve(n);
+  dr.reserve(n);
+  dg.reserve(n);
+  check(cudaMemcpyAsync(dq.p, queries, n * sizeof(QueryIn), cudaMemcpyHostToDevice, c.stream), "H2D queries");
+  check(cudaMemcpyAsync(dg.p, meanCosines, n * sizeof(float), cudaMemcpyHostToDevice, c.stream), "H2D mean cosines");
+  launch_batch(field, true, reinterpret_cast<const PGLGuidedQuery *>(dq.p), n,
+               reinterpret_cast<PGLGuidedQueryResult *>(dr.p), false, dg.p, c.stream);
+  check(cudaMemcpyAsync(results, dr.p, n * sizeof(QueryOut), cudaMemcpyDeviceToHost, c.stream), "D2H results");
+  check(cudaStreamSynchronize(c.stream), "queries");
+  return true;
   PGL_CATCH(false)
 }
 OPENPGL_CORE_INTERFACE void pglSampleStorageAddSamplesDevice(PGLSampleStorage s, const PGLSampleData *d, size_t n) {

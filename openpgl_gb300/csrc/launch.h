@@ -109,6 +109,9 @@ cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out,
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,
                             cudaStream_t s);
 cudaError_t launch_ssd_cosine(SSDState *st, float nx, float ny, float nz, float ck, float cn, cudaStream_t s);
+// The single-lobe Henyey-Greenstein product of an initialised distribution
+// (VMMVolumeSamplingDistribution.h:54-80).
+cudaError_t launch_ssd_hg(SSDState *st, float dx, float dy, float dz, float meanCosine, cudaStream_t s);
 cudaError_t launch_ssd_sample(const SSDState *st, float ux, float uy, int withPdf, SSDResult *res, cudaStream_t s);
 cudaError_t launch_ssd_pdf(const SSDState *st, float dx, float dy, float dz, int li, SSDResult *res, cudaStream_t s);
 

@@ -147,10 +147,15 @@ struct Lobe {
   float w, kappa, mx, my, mz, norm, e2k;
 };
 
+// Up to three products (the Henyey-Greenstein fit's lobes) per distribution.
+constexpr int kMaxProducts = 3;
 struct SSDState {
-  Lobe li[kMaxK];
-  Lobe g[kMaxK];
+  Lobe li[kMaxK];                 // the region's mixture shifted to the query point
+  Lobe g[kMaxK];                  // it times the cosine lobe (surface), or li
+  Lobe h[kMaxProducts][kMaxK];    // li times each lobe of the phase function's fit (volume)
+  float hw[kMaxProducts];         // the products' weights (their integrals, normalised)
   uint32_t K;
+  uint32_t numProducts;           // 0: sample and evaluate g; else h[0, numProducts)
 };
 
 struct SSDResult {
@@ -164,6 +169,9 @@ struct QueryParams {
   float cosKappa, cosNorm;
   int cosine;
   int samplesPerQuery;  // SamplePDF calls per query (u re-used per call index)
+  const float *hgMeanCosine;  // volume queries: per-query mean cosine of the
+                              // Henyey-Greenstein product (the query's normal is
+                              // its direction), or null for no product
 };
 
 }  // namespace pgl

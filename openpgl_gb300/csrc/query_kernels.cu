@@ -9,6 +9,7 @@
 // j+24 summed in vector order, then the 8-lane tree).
 #include <cuda_runtime.h>
 
+#include "hg_table.h"
 #include "launch.h"
 #include "pgl_internal.h"
 
@@ -85,9 +86,14 @@ __device__ __forceinline__ Lobe load_shifted(const VMMState &v, int lane, float 
   return L;
 }
 
-// PAVMM::product with a single lobe (the cosine lobe)
-__device__ __forceinline__ Lobe product_lobe(Lobe L, V3 n, float kappa, float normalization, int cnt, int lane,
-                                             float &integral) {
+// the phase function fits (VMMPhaseFunctions.cpp), uploaded with the seed tables
+static_assert(kHgLobes == kMaxProducts, "a distribution holds one product per lobe of the fit");
+static __constant__ HgLobeFit c_hg[kHgFits][kHgLobes];
+
+// PAVMM::product with a single lobe of weight `weight` (the cosine lobe, or a
+// lobe of the phase function's fit); integral = the product's integral
+__device__ __forceinline__ Lobe product_lobe(Lobe L, V3 n, float kappa, float normalization, float weight, int cnt,
+                                             int lane, float &integral) {
   V3 mu = mk(L.mx, L.my, L.mz);
   V3 nm = mu * L.kappa + n * kappa;
   float nk = sqrtf(dot(nm, nm));
@@ -101,7 +107,7 @@ __device__ __forceinline__ Lobe product_lobe(Lobe L, V3 n, float kappa, float no
   float c0 = dot(mu, nm), c1 = dot(n, nm);
   float ev = fexp(L.kappa * (c0 - 1.0f) + kappa * (c1 - 1.0f));
   scale *= ev;
-  scale *= L.w * 1.0f;
+  scale *= L.w * weight;
   Lobe R;
   R.w = scale; R.kappa = nk; R.mx = nm.x; R.my = nm.y; R.mz = nm.z; R.norm = nn; R.e2k = ne;
   integral = lane_sum(lane < cnt * kLanes ? R.w : 0.0f, cnt, lane);
@@ -166,7 +172,50 @@ __device__ V3 mixture_sample(const Lobe &L, int K, float ux, float uy, int lane)
 }
 
 
-// Batched guided query: Init + optional cosine product + SamplePDF (+ pdfLi).
+// The Henyey-Greenstein product (VMMVolumeSamplingDistribution.h:54-80,
+// VMMPhaseFunctions.h:45-57): the fit for |meanCosine|, li times each of its
+// lobes (lobes of the fit's sign facing dir, else -dir); w = the products'
+// integrals over their sum.
+__device__ __forceinline__ void hg_products(const Lobe &li, V3 dir, float meanCosine, int cnt, int lane,
+                                            Lobe h[kHgLobes], float w[kHgLobes]) {
+  const float absG = fabsf(meanCosine);
+  const float step = (kHgMaxMeanCosine - kHgMinMeanCosine) / float(kHgFits);
+  int idx = int(floorf((absG - kHgMinMeanCosine) / step));
+  idx = idx < kHgFits - 1 ? idx : kHgFits - 1;
+  float sum = 0.0f;
+#pragma unroll
+  for (int i = 0; i < kHgLobes; ++i) {
+    const HgLobeFit fit = c_hg[idx][i];
+    const V3 out = meanCosine * fit.meanCosine > 0.f ? dir : mk(-dir.x, -dir.y, -dir.z);
+    h[i] = product_lobe(li, out, fit.kappa, fit.normalization, fit.weight, cnt, lane, w[i]);
+    sum += w[i];
+  }
+#pragma unroll
+  for (int i = 0; i < kHgLobes; ++i) w[i] /= sum;
+}
+// Sample of a weighted set of products: the first product whose running
+// weight passes u.x, sampled with u.x rescaled into it
+// (VMMVolumeSamplingDistribution.h:87-105); pdf = the weighted sum.
+__device__ __forceinline__ V3 products_sample(const Lobe h[kHgLobes], const float w[kHgLobes], int np, int K, float ux,
+                                              float uy, int lane, float &pdf) {
+  float acc = 0.0f;
+  int i = 0;
+  for (; i < np - 1; ++i) {
+    const float next = acc + w[i];
+    if (next > ux) break;
+    acc = next;
+  }
+  const Lobe g = i == 0 ? h[0] : (i == 1 ? h[1] : h[2]);
+  const float wi = i == 0 ? w[0] : (i == 1 ? w[1] : w[2]);
+  const V3 d = mixture_sample(g, K, (ux - acc) / wi, uy, lane);
+  const int cnt = vec_count(K);
+  pdf = 0.0f;
+  for (int k = 0; k < np; ++k) pdf += w[k] * mixture_pdf(h[k], d, cnt, lane);
+  return d;
+}
+
+// Batched guided query: Init + optional cosine product (surface) or
+// Henyey-Greenstein product (volume) + SamplePDF (+ pdfLi).
 __global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, uint32_t n) {
   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -187,16 +236,24 @@ __global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, ui
     if (R.valid) {
       const int K = int(R.vmm.K), cnt = vec_count(K);
       Lobe li = load_shifted(R.vmm, lane, q.px, q.py, q.pz);
-      Lobe g = li;
-      if (P.cosine) {
-        float integral;
-        g = product_lobe(li, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, cnt, lane, integral);
+      V3 d;
+      if (P.hgMeanCosine) {
+        Lobe h[kHgLobes];
+        float w[kHgLobes];
+        hg_products(li, mk(q.nx, q.ny, q.nz), P.hgMeanCosine[gw], cnt, lane, h, w);
+        d = products_sample(h, w, kHgLobes, K, q.ux, q.uy, lane, o.pdf);
+      } else {
+        Lobe g = li;
+        if (P.cosine) {
+          float integral;
+          g = product_lobe(li, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, 1.0f, cnt, lane, integral);
+        }
+        d = mixture_sample(g, K, (q.ux - 0.0f) / 1.0f, q.uy, lane);
+        o.pdf = 0.0f + 1.0f * mixture_pdf(g, d, cnt, lane);
       }
-      V3 d = mixture_sample(g, K, (q.ux - 0.0f) / 1.0f, q.uy, lane);
       o.ok = 1;
       o.id = leaf;
       o.dx = d.x; o.dy = d.y; o.dz = d.z;
-      o.pdf = 0.0f + 1.0f * mixture_pdf(g, d, cnt, lane);
       o.pdfLi = mixture_pdf(li, d, cnt, lane);
     }
   }
@@ -223,7 +280,10 @@ __global__ void ssd_init_kernel(FieldView f, float px, float py, float pz, float
       Lobe li = load_shifted(R.vmm, lane, px, py, pz);
       st->li[lane] = li;
       st->g[lane] = li;
-      if (lane == 0) st->K = R.vmm.K;
+      if (lane == 0) {
+        st->K = R.vmm.K;
+        st->numProducts = 0;
+      }
       r.ok = 1;
       r.id = leaf;
     }
@@ -234,16 +294,42 @@ __global__ void ssd_cosine_kernel(SSDState *st, float nx, float ny, float nz, fl
   const int lane = threadIdx.x & 31;
   const int cnt = vec_count(int(st->K));
   float integral;
-  Lobe g = product_lobe(st->g[lane], mk(nx, ny, nz), cosKappa, cosNorm, cnt, lane, integral);
+  Lobe g = product_lobe(st->g[lane], mk(nx, ny, nz), cosKappa, cosNorm, 1.0f, cnt, lane, integral);
   __syncwarp();
   st->g[lane] = g;
+}
+__global__ void ssd_hg_kernel(SSDState *st, float dx, float dy, float dz, float meanCosine) {
+  const int lane = threadIdx.x & 31;
+  const int cnt = vec_count(int(st->K));
+  Lobe h[kHgLobes];
+  float w[kHgLobes];
+  hg_products(st->li[lane], mk(dx, dy, dz), meanCosine, cnt, lane, h, w);
+#pragma unroll
+  for (int i = 0; i < kHgLobes; ++i) st->h[i][lane] = h[i];
+  if (lane == 0) {
+    for (int i = 0; i < kHgLobes; ++i) st->hw[i] = w[i];
+    st->numProducts = kHgLobes;
+  }
 }
 __global__ void ssd_sample_kernel(const SSDState *st, float ux, float uy, int withPdf, SSDResult *res) {
   const int lane = threadIdx.x & 31;
   const int K = int(st->K), cnt = vec_count(K);
-  Lobe g = st->g[lane];
-  V3 d = mixture_sample(g, K, (ux - 0.0f) / 1.0f, uy, lane);
-  float pdf = withPdf ? 0.0f + 1.0f * mixture_pdf(g, d, cnt, lane) : 0.0f;
+  V3 d;
+  float pdf = 0.0f;
+  if (st->numProducts > 0) {
+    Lobe h[kHgLobes];
+    float w[kHgLobes];
+#pragma unroll
+    for (int i = 0; i < kHgLobes; ++i) {
+      h[i] = st->h[i][lane];
+      w[i] = st->hw[i];
+    }
+    d = products_sample(h, w, int(st->numProducts), K, ux, uy, lane, pdf);
+  } else {
+    Lobe g = st->g[lane];
+    d = mixture_sample(g, K, (ux - 0.0f) / 1.0f, uy, lane);
+    pdf = withPdf ? 0.0f + 1.0f * mixture_pdf(g, d, cnt, lane) : 0.0f;
+  }
   if (lane == 0) {
     res->dx = d.x; res->dy = d.y; res->dz = d.z; res->pdf = pdf;
   }
@@ -251,13 +337,26 @@ __global__ void ssd_sample_kernel(const SSDState *st, float ux, float uy, int wi
 __global__ void ssd_pdf_kernel(const SSDState *st, float dx, float dy, float dz, int li, SSDResult *res) {
   const int lane = threadIdx.x & 31;
   const int cnt = vec_count(int(st->K));
-  Lobe L = li ? st->li[lane] : st->g[lane];
-  float pdf = li ? mixture_pdf(L, mk(dx, dy, dz), cnt, lane) : 0.0f + 1.0f * mixture_pdf(L, mk(dx, dy, dz), cnt, lane);
+  const V3 d = mk(dx, dy, dz);
+  float pdf;
+  if (li) {
+    pdf = mixture_pdf(st->li[lane], d, cnt, lane);
+  } else if (st->numProducts > 0) {
+    pdf = 0.0f;
+    for (uint32_t k = 0; k < st->numProducts; ++k) pdf += st->hw[k] * mixture_pdf(st->h[k][lane], d, cnt, lane);
+  } else {
+    pdf = 0.0f + 1.0f * mixture_pdf(st->g[lane], d, cnt, lane);
+  }
   if (lane == 0) res->pdf = pdf;
 }
 
 // ---------------------------------------------------------------- launchers
-PGL_DEFINE_TABLE_UPLOAD(query_upload_tables)
+PGL_DEFINE_TABLE_UPLOAD(query_upload_seed_tables)
+cudaError_t query_upload_tables() {
+  cudaError_t e = query_upload_seed_tables();
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(c_hg, kHgTable, sizeof(kHgTable));
+}
 
 cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
@@ -277,6 +376,11 @@ cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, fl
 cudaError_t launch_ssd_cosine(SSDState *st, float nx, float ny, float nz, float ck, float cn, cudaStream_t s) {
   count_launch();
   ssd_cosine_kernel<<<1, 32, 0, s>>>(st, nx, ny, nz, ck, cn);
+  return cudaGetLastError();
+}
+cudaError_t launch_ssd_hg(SSDState *st, float dx, float dy, float dz, float meanCosine, cudaStream_t s) {
+  count_launch();
+  ssd_hg_kernel<<<1, 32, 0, s>>>(st, dx, dy, dz, meanCosine);
   return cudaGetLastError();
 }
 cudaError_t launch_ssd_sample(const SSDState *st, float ux, float uy, int withPdf, SSDResult *res, cudaStream_t s) {

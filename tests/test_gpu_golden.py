@@ -67,8 +67,13 @@ def test_field_matches_reference(pgl, name):
 def test_queries_match_reference(pgl, name):
     field, queries = run_case(pgl, name)
     g = np.load(os.path.join(GOLDEN, f"{name}.queries.npz"))
-    for volume, key in ((False, "surface"), (True, "volume")):
-        out = field.sample_batch(queries, volume=volume, cosine=not volume)
+    import pyoracle
+
+    for volume, key in ((False, "surface"), (True, "volume"), (True, "volume_hg")):
+        if key == "volume_hg":  # with the Henyey-Greenstein product, mean cosines -0.99 .. 0.99
+            out = field.sample_batch_hg(queries, pyoracle.hg_mean_cosines(len(queries)))
+        else:
+            out = field.sample_batch(queries, volume=volume, cosine=not volume)
         ref = g[key]
         assert np.array_equal(out["ok"], ref["ok"]), key
         ok = ref["ok"] == 1

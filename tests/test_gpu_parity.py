@@ -142,3 +142,52 @@ def test_one_leaf_fields(pgl):
         assert r["regions"] == 1, (side, r)
         assert r["tree_equal"] and r["stats_equal"], (side, r)
         assert r["bit_exact_regions"] == 1, (side, r)
+
+
+def test_hg_product_matches_oracle_and_per_object(pgl, tmp_path):
+    """Volume queries with the single-lobe Henyey-Greenstein product on the
+    oracle's own field (loaded from its field file, so the regions are the
+    same bits and only the query arithmetic is compared): the batch against
+    the oracle (same region and sample1D, pdfs within 1e-3), and the
+    per-object calls (Init, ApplySingleLobeHenyeyGreensteinProduct, SamplePDF,
+    PDF, IncomingRadiancePDF) against the batch bit for bit.  The fields the
+    GPU trains itself are checked with the product against the reference's
+    golden outputs in test_gpu_golden.py."""
+    import pyoracle
+    from openpgl_gb300 import synthetic as syn
+
+    orc = pyoracle.OracleField(4000, deterministic=True, threads=8)
+    for i in range(2):
+        orc.update(syn.cube_face_samples(131072, 70 + i, volume_fraction=0.5))
+    path = tmp_path / "oracle.field"
+    path.write_bytes(orc.field_bytes())
+    dev = pgl.Device()
+    field = pgl.Field.from_file(dev, str(path))
+    q = syn.queries(8192, 71)
+    g = pyoracle.hg_mean_cosines(len(q))
+    out = field.sample_batch_hg(q, g)
+    ref = orc.query_hg(q, g)
+    assert np.array_equal(out["ok"], ref["ok"])
+    ok = ref["ok"] == 1
+    assert ok.sum() > 1000
+    assert np.array_equal(out["id"][ok], ref["id"][ok])
+    assert np.array_equal(out["sample1d"][ok].view(np.uint32), ref["sample1d"][ok].view(np.uint32))
+    rel = np.abs(out["pdf"][ok] - ref["pdf"][ok]) / ref["pdf"][ok]
+    assert np.quantile(rel, 0.999) <= PDF_TOL, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
+    relli = np.abs(out["pdfLi"][ok] - ref["pdfLi"][ok]) / ref["pdfLi"][ok]
+    assert np.quantile(relli, 0.999) <= PDF_TOL
+    assert np.quantile(np.abs(out["dir"][ok] - ref["dir"][ok]).max(axis=1), 0.999) <= 1e-3
+    vsd = pgl.VolumeSamplingDistribution(field)
+    assert vsd.supports_hg_product()
+    for i in range(0, len(q), 128):
+        ok_i, s1d = vsd.init(tuple(q["position"][i]), float(q["sample1d"][i]))
+        assert ok_i == bool(out["ok"][i])
+        if not ok_i:
+            continue
+        vsd.apply_hg_product(tuple(q["normal"][i]), float(g[i]))
+        d, pdf = vsd.sample_pdf(tuple(q["u"][i]))
+        assert np.float32(pdf) == out["pdf"][i]
+        assert np.array_equal(np.array(d, np.float32), out["dir"][i])
+        assert np.float32(vsd.pdf(d)) == out["pdf"][i]
+        assert np.float32(vsd.incoming_radiance_pdf(d)) == out["pdfLi"][i]
+    vsd.release()
