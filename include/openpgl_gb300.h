@@ -105,6 +105,30 @@ OPENPGL_CORE_INTERFACE void pglFieldAutotuneNextUpdate(PGLField field);
 // The trials of the last tuning: int[4] schedule and milliseconds each;
 // returns their count, writes when capacity >= count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetEmTuningTrials(PGLField field, int *tunings, float *ms, size_t capacity);
+// Training samples from many paths at once on the device (what
+// pglPathSegmentStoragePrepareSamples does for one path in host memory):
+// path p is dSegments[dPathBegin[p], dPathBegin[p + 1]) (numPaths + 1 offsets
+// in device memory).  Writes the samples to dSamples (device memory with room
+// for dPathBegin[numPaths] records, the segment count, which bounds the
+// sample count) in path order, each path's in the reference's order, and
+// path p's first slot to dSampleBegin[p] (numPaths + 1 entries, the last is
+// the total).  Enqueued on cudaStream (null: the library's stream); does not
+// synchronise.
+OPENPGL_CORE_INTERFACE bool pglPathSegmentsPrepareSamplesDevice(const PGLPathSegmentData *dSegments,
+                                                                const uint32_t *dPathBegin, size_t numPaths,
+                                                                float maxDistance, bool useNEEMiWeights,
+                                                                bool guideDirectLight,
+                                                                bool rrAffectsDirectContribution,
+                                                                PGLSampleData *dSamples, uint32_t *dSampleBegin,
+                                                                void *cudaStream);
+// The same for pglPathSegmentStoragePropagateSamples: the paths' samples go
+// into sampleStorage without leaving the device.  Returns their count;
+// synchronises with the library's stream.
+OPENPGL_CORE_INTERFACE size_t pglPathSegmentsPropagateSamplesDevice(const PGLPathSegmentData *dSegments,
+                                                                    const uint32_t *dPathBegin, size_t numPaths,
+                                                                    float maxDistance, PGLSampleStorage sampleStorage,
+                                                                    bool guideDirectLight, bool useNEEMiWeights,
+                                                                    bool rrAffectsDirectContribution);
 // Splits numSamples sample records that live in device memory into the
 // surface records and the inside-volume records (flags & EInsideVolume), each
 // kind in its original order, written to dSurface and dVolume (device

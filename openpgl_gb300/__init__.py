@@ -167,6 +167,29 @@ C_API = {
     "pglFieldGetEmTuning": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p]),
     "pglFieldAutotuneNextUpdate": (None, [ctypes.c_void_p]),
     "pglFieldGetEmTuningTrials": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "pglNewPathSegmentStorage": (ctypes.c_void_p, []),
+    "pglReleasePathSegmentStorage": (None, [ctypes.c_void_p]),
+    "pglPathSegmentStorageReserve": (None, [ctypes.c_void_p, ctypes.c_size_t]),
+    "pglPathSegmentStorageClear": (None, [ctypes.c_void_p]),
+    "pglPathSegmentSetMaxDistance": (None, [ctypes.c_void_p, ctypes.c_float]),
+    "pglPathSegmentGetMaxDistance": (ctypes.c_float, [ctypes.c_void_p]),
+    "pglPathSegmentGetNumSegments": (ctypes.c_int, [ctypes.c_void_p]),
+    "pglPathSegmentGetNumSamples": (ctypes.c_int, [ctypes.c_void_p]),
+    "pglPathSegmentStoragePrepareSamples": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_bool, ctypes.c_bool,
+                                                              ctypes.c_bool]),
+    "pglPathSegmentStorageCalculatePixelEstimate": (Vec3, [ctypes.c_void_p, ctypes.c_bool]),
+    "pglPathSegmentStorageGetSamples": (ctypes.c_void_p, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
+    "pglPathSegmentStorageNextSegment": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "pglPathSegmentStorageValidateSamples": (ctypes.c_bool, [ctypes.c_void_p]),
+    "pglPathSegmentStorageValidateSegments": (ctypes.c_bool, [ctypes.c_void_p]),
+    "pglPathSegmentStoragePropagateSamples": (None, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_bool, ctypes.c_bool,
+                                                     ctypes.c_bool]),
+    "pglPathSegmentsPrepareSamplesDevice": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                            ctypes.c_float, ctypes.c_bool, ctypes.c_bool, ctypes.c_bool,
+                                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pglPathSegmentsPropagateSamplesDevice": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                                ctypes.c_float, ctypes.c_void_p, ctypes.c_bool,
+                                                                ctypes.c_bool, ctypes.c_bool]),
 }
 
 _lib = None
@@ -507,6 +530,91 @@ class VolumeSamplingDistribution(SurfaceSamplingDistribution):
 
     def supports_hg_product(self):
         return bool(self.lib.pglVolumeSamplingDistributionSupportsApplySingleLobeHenyeyGreensteinProduct(self.h))
+
+
+class PathSegmentStorage:
+    """One path's segments and the samples made from them (the reference's
+    PathSegmentStorage, host memory)."""
+
+    def __init__(self, reserve=64):
+        from .synthetic import PGL_SAMPLE_DTYPE
+
+        self.lib = load()
+        self._dtype = PGL_SAMPLE_DTYPE
+        self.h = self.lib.pglNewPathSegmentStorage()
+        _check(self.h, "pglNewPathSegmentStorage")
+        self.lib.pglPathSegmentStorageReserve(self.h, reserve)
+
+    def clear(self):
+        self.lib.pglPathSegmentStorageClear(self.h)
+
+    def set_max_distance(self, d):
+        self.lib.pglPathSegmentSetMaxDistance(self.h, float(d))
+
+    def max_distance(self):
+        return self.lib.pglPathSegmentGetMaxDistance(self.h)
+
+    def num_segments(self):
+        return self.lib.pglPathSegmentGetNumSegments(self.h)
+
+    def num_samples(self):
+        return self.lib.pglPathSegmentGetNumSamples(self.h)
+
+    def add_segments(self, segments):
+        """Appends PGL_PATH_SEGMENT_DTYPE records (NextSegment, then filled)."""
+        seg = np.ascontiguousarray(segments)
+        for i in range(len(seg)):
+            p = self.lib.pglPathSegmentStorageNextSegment(self.h)
+            if not p:
+                raise RuntimeError("path segment storage is full")
+            ctypes.memmove(p, seg[i:i + 1].ctypes.data, seg.dtype.itemsize)
+
+    def prepare_samples(self, use_nee_mi_weights=False, guide_direct_light=False, rr_affects_direct=True):
+        return self.lib.pglPathSegmentStoragePrepareSamples(self.h, use_nee_mi_weights, guide_direct_light,
+                                                            rr_affects_direct)
+
+    def samples(self):
+        n = ctypes.c_size_t(0)
+        p = self.lib.pglPathSegmentStorageGetSamples(self.h, ctypes.byref(n))
+        out = np.zeros(n.value, dtype=self._dtype)
+        if n.value:
+            ctypes.memmove(out.ctypes.data, p, n.value * self._dtype.itemsize)
+        return out
+
+    def pixel_estimate(self, rr_affects_direct=True):
+        c = self.lib.pglPathSegmentStorageCalculatePixelEstimate(self.h, rr_affects_direct)
+        return (c.x, c.y, c.z)
+
+    def validate_segments(self):
+        return bool(self.lib.pglPathSegmentStorageValidateSegments(self.h))
+
+    def validate_samples(self):
+        return bool(self.lib.pglPathSegmentStorageValidateSamples(self.h))
+
+    def propagate(self, storage, guide_direct_light=False, use_nee_mi_weights=False, rr_affects_direct=True):
+        self.lib.pglPathSegmentStoragePropagateSamples(self.h, storage.h, guide_direct_light, use_nee_mi_weights,
+                                                       rr_affects_direct)
+
+    def release(self):
+        if self.h:
+            self.lib.pglReleasePathSegmentStorage(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def path_samples_device(d_segments, d_path_begin, num_paths, max_distance, d_samples, d_sample_begin,
+                        use_nee_mi_weights=False, guide_direct_light=False, rr_affects_direct=True, stream=None):
+    """pglPathSegmentsPrepareSamplesDevice on device pointers."""
+    lib = load()
+    _check(lib.pglPathSegmentsPrepareSamplesDevice(d_segments, d_path_begin, num_paths, float(max_distance),
+                                                   use_nee_mi_weights, guide_direct_light, rr_affects_direct,
+                                                   d_samples, d_sample_begin, stream),
+           "pglPathSegmentsPrepareSamplesDevice")
 
 
 class GuidingServer:

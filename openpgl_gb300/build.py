@@ -19,8 +19,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libopenpgl_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CUDA_SOURCES = ["em_kernel.cu", "spatial_kernels.cu", "query_kernels.cu", "noalloc.cu"]
-HOST_SOURCES = ["field.cpp", "api.cpp", "serve.cpp"]
+CUDA_SOURCES = ["em_kernel.cu", "spatial_kernels.cu", "query_kernels.cu", "noalloc.cu", "path_kernels.cu"]
+HOST_SOURCES = ["field.cpp", "api.cpp", "serve.cpp", "pathsegments.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -47,6 +47,15 @@ void fail(const char *fn, const std::exception &e) {
   g_lastError = std::string(fn) + ": " + e.what();
   std::cout << g_lastError << std::endl;
 }
+}  // namespace
+
+// The error convention of the C API for entry points defined in other files.
+namespace pgl {
+void api_error(const char *fn, const std::exception &e) { fail(fn, e); }
+void api_clear_error() { g_lastError.clear(); }
+}  // namespace pgl
+
+namespace {
 
 GpuField *F(PGLField f) { return reinterpret_cast<GpuField *>(f); }
 Storage *S(PGLSampleStorage s) { return reinterpret_cast<Storage *>(s); }
@@ -623,38 +632,6 @@ OPENPGL_CORE_INTERFACE PGLString pglFieldStatisticsToCSVString(PGLFieldStatistic
   return make_string(ss.str());
 }
 OPENPGL_CORE_INTERFACE void pglReleaseString(PGLString str) { delete[] str.m_str; }
-
-// ------------------------------------------------------------------ path segments: outside the GPU path
-#define PGL_UNSUPPORTED(ret)                                                                          \
-  {                                                                                                   \
-    g_lastError = std::string(__func__) + ": path segment storage is not part of the GPU library"; \
-    return ret;                                                                                       \
-  }
-OPENPGL_CORE_INTERFACE PGLPathSegmentStorage pglNewPathSegmentStorage() PGL_UNSUPPORTED(nullptr)
-OPENPGL_CORE_INTERFACE void pglReleasePathSegmentStorage(PGLPathSegmentStorage) {}
-OPENPGL_CORE_INTERFACE void pglPathSegmentStorageReserve(PGLPathSegmentStorage, size_t) PGL_UNSUPPORTED()
-OPENPGL_CORE_INTERFACE void pglPathSegmentStorageClear(PGLPathSegmentStorage) PGL_UNSUPPORTED()
-OPENPGL_CORE_INTERFACE void pglPathSegmentSetMaxDistance(PGLPathSegmentStorage, float) PGL_UNSUPPORTED()
-OPENPGL_CORE_INTERFACE float pglPathSegmentGetMaxDistance(PGLPathSegmentStorage) PGL_UNSUPPORTED(0.0f)
-OPENPGL_CORE_INTERFACE int pglPathSegmentGetNumSegments(PGLPathSegmentStorage) PGL_UNSUPPORTED(0)
-OPENPGL_CORE_INTERFACE int pglPathSegmentGetNumSamples(PGLPathSegmentStorage) PGL_UNSUPPORTED(0)
-OPENPGL_CORE_INTERFACE size_t pglPathSegmentStoragePrepareSamples(PGLPathSegmentStorage, const bool, const bool,
-                                                                  const bool) PGL_UNSUPPORTED(0)
-OPENPGL_CORE_INTERFACE pgl_vec3f pglPathSegmentStorageCalculatePixelEstimate(PGLPathSegmentStorage, const bool)
-    PGL_UNSUPPORTED(pgl_vec3f{})
-OPENPGL_CORE_INTERFACE const PGLSampleData *pglPathSegmentStorageGetSamples(PGLPathSegmentStorage, size_t &n) {
-  n = 0;
-  PGL_UNSUPPORTED(nullptr)
-}
-OPENPGL_CORE_INTERFACE void pglPathSegmentStorageAddSample(PGLPathSegmentStorage, PGLSampleData) PGL_UNSUPPORTED()
-OPENPGL_CORE_INTERFACE PGLPathSegmentData *pglPathSegmentStorageNextSegment(PGLPathSegmentStorage)
-    PGL_UNSUPPORTED(nullptr)
-OPENPGL_CORE_INTERFACE void pglPathSegmentStorageAddSegment(PGLPathSegmentStorage, PGLPathSegmentData)
-    PGL_UNSUPPORTED()
-OPENPGL_CORE_INTERFACE bool pglPathSegmentStorageValidateSamples(PGLPathSegmentStorage) PGL_UNSUPPORTED(false)
-OPENPGL_CORE_INTERFACE bool pglPathSegmentStorageValidateSegments(PGLPathSegmentStorage) PGL_UNSUPPORTED(false)
-OPENPGL_CORE_INTERFACE void pglPathSegmentStoragePropagateSamples(PGLPathSegmentStorage, PGLSampleStorage, bool, bool,
-                                                                  bool) PGL_UNSUPPORTED()
 
 // ------------------------------------------------------------------ appended entry points (openpgl_gb300.h)
 static void launch_batch(PGLField field, bool volume, const PGLGuidedQuery *dQueries, size_t n,

@@ -106,6 +106,14 @@ cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *qu
                       cudaStream_t stream);
 
 cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s);
+// Samples of numPaths paths (path p = seg[begin[p], begin[p + 1])): offsets
+// (numPaths + 1 entries) gets each path's first sample slot and the total;
+// out needs room for the total (at most begin[numPaths]).
+struct PathSegmentRecord;
+struct PathFlags;
+cudaError_t launch_path_samples(const PathSegmentRecord *seg, const uint32_t *begin, uint32_t numPaths,
+                                float maxDistance, PathFlags fl, PGLSampleRecord *out, uint32_t *offsets,
+                                Scratch &scratch, cudaStream_t s);
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,
                             cudaStream_t s);
 cudaError_t launch_ssd_cosine(SSDState *st, float nx, float ny, float nz, float ck, float cn, cudaStream_t s);

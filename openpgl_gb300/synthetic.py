@@ -226,3 +226,70 @@ def frames_blob(frames):
 
 def queries_blob(q):
     return np.uint64(len(q)).tobytes() + np.ascontiguousarray(q).tobytes()
+
+
+# PGLPathSegmentData (data.h), 136 bytes
+PGL_PATH_SEGMENT_DTYPE = np.dtype(
+    [("position", "<f4", (3,)), ("direction_in", "<f4", (3,)), ("direction_out", "<f4", (3,)),
+     ("normal", "<f4", (3,)), ("volume_scatter", "u1"), ("pad0", "u1", (3,)), ("pdf_direction_in", "<f4"),
+     ("is_delta", "u1"), ("pad1", "u1", (3,)), ("scattering_weight", "<f4", (3,)),
+     ("transmittance_weight", "<f4", (3,)), ("direct_contribution", "<f4", (3,)), ("mi_weight", "<f4"),
+     ("scattered_contribution", "<f4", (3,)), ("rr_probability", "<f4"), ("eta", "<f4"), ("roughness", "<f4"),
+     ("pad2", "<u4"), ("region_ptr", "<u8")])
+assert PGL_PATH_SEGMENT_DTYPE.itemsize == 136
+
+
+def path_segments(num_paths, seed, max_len=12):
+    """Random-walk paths of 1..max_len segments in [0, 10]^3 with the mix of
+    vertex kinds a path tracer records: delta and glossy vertices (roughness
+    spread over [0, 1], a fifth below 0.01), refractive ones (eta != 1),
+    volume scattering, zero and partial Russian roulette, lights hit and
+    next-event contributions.  Returns (segments, begin) with begin[p] the
+    first segment of path p (num_paths + 1 entries)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lens = 1 + np.minimum(np.floor(rng.random(num_paths) * max_len), max_len - 1).astype(np.int64)
+    begin = np.zeros(num_paths + 1, dtype=np.uint64)
+    begin[1:] = np.cumsum(lens)
+    n = int(begin[-1])
+    s = np.zeros(n, dtype=PGL_PATH_SEGMENT_DTYPE)
+    start = rng.random((num_paths, 3)) * 10.0
+    steps = (rng.random((n, 3)) - 0.5) * 3.0
+    pos = np.repeat(start, lens, axis=0)
+    first = np.zeros(n, dtype=bool)
+    first[begin[:-1].astype(np.int64)] = True
+    for p in range(num_paths):  # walk: cumulative steps within each path
+        b, e = int(begin[p]), int(begin[p + 1])
+        pos[b:e] += np.cumsum(np.concatenate([np.zeros((1, 3)), steps[b + 1:e]]), axis=0)
+    s["position"] = pos.astype(np.float32)
+    s["direction_in"] = _unit_sphere(rng, n).astype(np.float32)
+    s["direction_out"] = _unit_sphere(rng, n).astype(np.float32)
+    s["normal"] = _unit_sphere(rng, n).astype(np.float32)
+    s["volume_scatter"] = (rng.random(n) < 0.2).astype(np.uint8)
+    s["pdf_direction_in"] = (0.01 * det_exp(rng.random(n) * det_log(1000.0))).astype(np.float32)
+    s["is_delta"] = (rng.random(n) < 0.1).astype(np.uint8)
+    s["scattering_weight"] = (rng.random((n, 3)) * 1.2).astype(np.float32)
+    s["transmittance_weight"] = (0.5 + 0.5 * rng.random((n, 3))).astype(np.float32)
+    dc = rng.random((n, 3)) * 2.0
+    dc[rng.random(n) < 0.5] = 0.0
+    s["direct_contribution"] = dc.astype(np.float32)
+    s["mi_weight"] = rng.random(n).astype(np.float32)
+    sc = rng.random((n, 3))
+    sc[rng.random(n) < 0.8] = 0.0
+    s["scattered_contribution"] = sc.astype(np.float32)
+    rr = rng.random(n)
+    u = rng.random(n)
+    rr = np.where(u < 0.5, 1.0, np.where(u < 0.6, 0.0, rr))
+    s["rr_probability"] = rr.astype(np.float32)
+    eta = 1.0 + rng.random(n)
+    eta[rng.random(n) < 0.7] = 1.0
+    s["eta"] = eta.astype(np.float32)
+    rough = rng.random(n)
+    rough[rng.random(n) < 0.2] *= 0.01
+    s["roughness"] = rough.astype(np.float32)
+    return s, begin
+
+
+def paths_blob(segments, begin, extra=b""):
+    """u64 numPaths, u64 begin[numPaths + 1], then the segments."""
+    return (np.uint64(len(begin) - 1).tobytes() + np.ascontiguousarray(begin, dtype=np.uint64).tobytes()
+            + np.ascontiguousarray(segments).tobytes())

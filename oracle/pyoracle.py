@@ -15,6 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle_pgl.so")
+REF_PATHS = os.path.join(HERE, "_ref", "ref_paths")
 REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 
 QUERY_OUT_DTYPE = np.dtype(
@@ -114,6 +115,30 @@ def hg_mean_cosines(n):
     uses the same float arithmetic): -0.99 .. 0.99 in steps of 0.01."""
     i = np.arange(n, dtype=np.int64) % 199
     return i.astype(np.float32) * np.float32(0.01) - np.float32(0.99)
+
+
+def run_reference_paths(segments, begin, max_distance):
+    """Runs the reference's path segment storage (oracle/_ref/ref_paths) path
+    by path for the eight flag sets (bit 0 useNEEMiWeights, bit 1
+    guideDirectLight, bit 2 rrAffectsDirectContribution); returns (counts
+    [8, numPaths], samples concatenated flag set by flag set and path by path,
+    pixel estimates [2, numPaths, 3] for rrAffectsDirectContribution false and
+    true)."""
+    import sys
+
+    sys.path.insert(0, os.path.dirname(HERE))
+    from openpgl_gb300 import synthetic
+
+    num_paths = len(begin) - 1
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "paths.bin")
+        with open(path, "wb") as f:
+            f.write(synthetic.paths_blob(segments, begin))
+        subprocess.run([REF_PATHS, path, os.path.join(td, "ref"), repr(float(max_distance))], check=True)
+        counts = np.fromfile(os.path.join(td, "ref.counts.bin"), dtype=np.uint32).reshape(8, num_paths)
+        samples = np.fromfile(os.path.join(td, "ref.samples.bin"), dtype=synthetic.PGL_SAMPLE_DTYPE)
+        pixel = np.fromfile(os.path.join(td, "ref.pixel.bin"), dtype=np.float32).reshape(2, num_paths, 3)
+    return counts, samples, pixel
 
 
 def reference_available():

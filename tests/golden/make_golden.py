@@ -13,8 +13,10 @@ Each case stores:
                     IncomingRadiancePDF), "volume_hg": the same with the
                     single-lobe Henyey-Greenstein product first (direction =
                     the query's normal, mean cosine pyoracle.hg_mean_cosines)
-and manifest.json records the generator calls and the SHA-256 of every
-generated input, so a test can check that the generators still produce the
+and paths.npz the samples and pixel estimates of the reference's path
+segment storage on synthetic paths (counts per flag set and path, samples,
+pixel estimates); manifest.json records the generator calls and the SHA-256
+of every generated input, so a test can check that the generators still produce the
 same inputs before it compares outputs.
 
 Run from the repository root on a machine that has the reference sources:
@@ -61,6 +63,16 @@ def build_inputs(case):
     return frames, queries
 
 
+# path segment case: generator arguments and the storage's max distance
+PATHS = dict(num_paths=1024, seed=5, max_len=12, max_distance=3.0)
+
+
+def build_paths(case):
+    from openpgl_gb300 import synthetic as syn
+
+    return syn.path_segments(case["num_paths"], case["seed"], case["max_len"])
+
+
 def main():
     import fieldfile
     import pyoracle
@@ -80,6 +92,12 @@ def main():
         manifest["cases"][name] = dict(case, frame_sha256=[sha(f) for f in frames], queries_sha256=sha(queries),
                                        field_sha256=hashlib.sha256(field).hexdigest())
         print(name, len(field), "bytes,", len(fieldfile.read_field_file(field)["surface"]["regions"]), "surface regions")
+    # path segments -> samples (PathSegmentDataStorage), all eight flag sets
+    segs, begin = build_paths(PATHS)
+    counts, samples, pixel = pyoracle.run_reference_paths(segs, begin, PATHS["max_distance"])
+    np.savez_compressed(os.path.join(HERE, "paths.npz"), counts=counts, samples=samples, pixel=pixel)
+    manifest["paths"] = dict(PATHS, segments_sha256=sha(segs), begin_sha256=sha(begin))
+    print("paths", len(begin) - 1, "paths,", len(segs), "segments,", len(samples), "samples")
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
 
