@@ -1,6 +1,7 @@
-// Path segment storage (reference: include/openpgl/pathsegmentstorage.h:36-70).
-// Outside the GPU path: every call reports "unsupported" and returns a neutral
-// value, so renderers linking the full C++ wrapper still resolve the symbols.
+// Path segment storage (reference: include/openpgl/pathsegmentstorage.h:36-70):
+// one path's segments in host memory and the training samples made from them
+// (openpgl_gb300/csrc/pathsegments.cpp).  Many paths at once on the device:
+// pglPathSegmentsPrepareSamplesDevice in openpgl_gb300.h.
 #pragma once
 #ifdef __cplusplus
 #include <cstdint>
