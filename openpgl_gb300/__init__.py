@@ -24,6 +24,7 @@ PGL_DEVICE_TYPE_CPU_4, PGL_DEVICE_TYPE_CPU_8, PGL_DEVICE_TYPE_CPU_16, PGL_DEVICE
 PGL_DEVICE_TYPE_GPU_SM103 = 4
 PGL_SPATIAL_STRUCTURE_KDTREE = 0
 PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM = 0
+PGL_DIRECTIONAL_DISTRIBUTION_VMM = 2
 
 QUERY_RESULT_DTYPE = np.dtype(
     [("ok", "<u4"), ("id", "<u4"), ("sample1d", "<f4"), ("dir", "<f4", (3,)), ("pdf", "<f4"), ("pdfLi", "<f4")]
@@ -254,11 +255,11 @@ class Device:
 class FieldConfig:
     """FieldConfig::Init (cpp/FieldConfig.h:62-64)."""
 
-    def __init__(self, deterministic=True, max_samples_per_leaf=32000):
+    def __init__(self, deterministic=True, max_samples_per_leaf=32000, parallax=True):
         self.args = FieldArguments()
-        load().pglFieldArgumentsSetDefaults(ctypes.byref(self.args), PGL_SPATIAL_STRUCTURE_KDTREE,
-                                            PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM, deterministic,
-                                            max_samples_per_leaf)
+        kind = PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM if parallax else PGL_DIRECTIONAL_DISTRIBUTION_VMM
+        load().pglFieldArgumentsSetDefaults(ctypes.byref(self.args), PGL_SPATIAL_STRUCTURE_KDTREE, kind,
+                                            deterministic, max_samples_per_leaf)
 
 
 class SampleStorage:

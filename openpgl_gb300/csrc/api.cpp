@@ -83,9 +83,12 @@ static_assert(sizeof(PGLGuidedQueryResult) == sizeof(QueryOut), "query result la
 
 FieldConfig config_from(const PGLFieldArguments &args) {  // Device.h:99-136
   if (args.spatialStructureType != PGL_SPATIAL_STRUCTURE_KDTREE ||
-      args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM)
-    throw std::runtime_error("only the kd-tree + parallax-aware VMM field runs on the GPU");
+      (args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM &&
+       args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_VMM))
+    throw std::runtime_error("only kd-tree fields with (parallax-aware) VMMs run on the GPU");
   FieldConfig c;
+  // Device.h:139-178: the plain VMM is the same mixture without parallax compensation
+  c.parallax = args.directionalDistributionType == PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM ? 1u : 0u;
   const PGLKDTreeArguments *kd = static_cast<const PGLKDTreeArguments *>(args.spatialSturctureArguments);
   const PGLVMMFactoryArguments *vm = static_cast<const PGLVMMFactoryArguments *>(args.directionalDistributionArguments);
   if (!kd || !vm) throw std::runtime_error("null field arguments");

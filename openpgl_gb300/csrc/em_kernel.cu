@@ -2171,7 +2171,14 @@ __device__ void asm_update(EmShared &S, const LeafSamples &L, const FieldConfig 
 
 // Reprojection of a leaf's samples to the region's sample mean
 // (WEMFactory.h:1151-1196); positions are not needed afterwards.
-__device__ void reproject_leaf(const LeafTask &t, float4 *pd, float4 *dirw, float *dist) {
+// WEMFactory::prepareSamples (WEMFactory.h:1183-1196): parallax-aware
+// mixtures reproject the samples onto the region's mean; plain ones keep them
+// (the distance passes still read each sample's distance).
+__device__ void reproject_leaf(const LeafTask &t, float4 *pd, float4 *dirw, float *dist, bool parallax) {
+  if (!parallax) {
+    for (uint32_t i = threadIdx.x; i < t.count; i += blockDim.x) dist[t.begin + i] = pd[t.begin + i].w;
+    return;
+  }
   V3 var = mk(t.varOverN[0], t.varOverN[1], t.varOverN[2]);
   float minD = length(var);
   minD = 3.f * 3.f * sqrtf(minD);
@@ -2243,7 +2250,7 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Em
       afterMerge = R.afterMerge;
       S.report = LeafReport{0, 0, 0, 0};
     }
-    reproject_leaf(t, E.pd, E.dirw, E.dist);
+    reproject_leaf(t, E.pd, E.dirw, E.dist, cfg.parallax != 0);
     __syncthreads();
     const bool fit = (t.flags & kTaskFit) != 0;
     if (!fit && (t.flags & kTaskDecay) && threadIdx.x == 0) {  // Field.h:457-461
@@ -2263,7 +2270,7 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Em
           afterMerge = 0;
         }
       } else {
-        if (threadIdx.x == 0) {  // Field.h:476-482
+        if (threadIdx.x == 0 && cfg.parallax) {  // Field.h:476-482
           V3 shift = mk(S.vmm.pivot[0] - t.mean[0], S.vmm.pivot[1] - t.mean[1], S.vmm.pivot[2] - t.mean[2]);
           suff_parallax_shift(S.suff, S.vmm, shift);
           vmm_parallax_shift(S.vmm, shift);

@@ -669,6 +669,7 @@ FieldView SubField::view() const {
   v.iteration = (initialized && !nodes.empty()) ? uint32_t(iteration) : 0u;
   v.knn = cfg.knn;
   v.numNodes = uint32_t(nodes.size());
+  v.parallax = cfg.parallax;
   return v;
 }
 
@@ -1208,12 +1209,15 @@ void read_sub(Reader &r, SubField &f) {  // Field::deserialize (Field.h:269-301)
 }
 }  // namespace
 
+// PGL_SPATIAL_STRUCTURE_TYPE / PGL_DIRECTIONAL_DISTRIBUTION_TYPE values (types.h)
+constexpr int32_t kSpatialKdTree = 0, kDirParallaxVmm = 0, kDirVmm = 2;
+
 std::string GpuField::serialize() const {  // SurfaceVolumeField::storeToFile (SurfaceVolumeField.h:171-214)
   Writer w;
   const char hdr[] = "OPENPGL_0.6.0_FIELD";
   w.raw(hdr, sizeof(hdr));
-  w.put<int32_t>(0);
-  w.put<int32_t>(0);
+  w.put<int32_t>(kSpatialKdTree);
+  w.put<int32_t>(surface.cfg.parallax ? kDirParallaxVmm : kDirVmm);
   w.put<uint64_t>(iteration);
   w.put<uint64_t>(totalSPP);
   write_sub(w, surface);
@@ -1227,13 +1231,15 @@ void GpuField::deserialize(const std::string &bytes) {  // Device::newFieldFromF
   r.raw(hdr, sizeof(hdr));
   if (std::memcmp(hdr, "OPENPGL_0.6.0_FIELD", sizeof(hdr)) != 0) throw std::runtime_error("not an Open PGL 0.6.0 field file");
   const int32_t spatial = r.get<int32_t>(), directional = r.get<int32_t>();
-  if (spatial != 0 || directional != 0)
-    throw std::runtime_error("field file: only kd-tree fields with parallax-aware VMMs are supported");
+  if (spatial != kSpatialKdTree || (directional != kDirParallaxVmm && directional != kDirVmm))
+    throw std::runtime_error("field file: only kd-tree fields with (parallax-aware) VMMs are supported");
+  const uint32_t parallax = directional == kDirParallaxVmm ? 1u : 0u;
   iteration = r.get<uint64_t>();
   totalSPP = r.get<uint64_t>();
   read_sub(r, surface);
   read_sub(r, volume);
   if (r.o != bytes.size()) throw std::runtime_error("field file has trailing bytes");
+  surface.cfg.parallax = volume.cfg.parallax = parallax;
 }
 
 // Field::operator== (Field.h:552-601): exact comparison after the canonical

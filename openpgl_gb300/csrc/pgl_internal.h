@@ -26,6 +26,7 @@ struct FieldConfig {
   float maxKappaSplit = 32000.0f;    // OPENPGL_MAX_KAPPA, hard-coded in the splitter
   float maxMeanCosineSplit = 0.0f;   // KappaToMeanCosine(32000)
   uint32_t laneWidth = 8;            // merging stops at K <= lane width (CPU_8)
+  uint32_t parallax = 1;             // PARALLAX_AWARE_VMM (1) or VMM (0): reprojection and shifts
 };
 
 // Parallax-aware vMF mixture, lane-major (lobe k at index k), as
@@ -141,6 +142,7 @@ struct FieldView {
   uint32_t iteration;
   uint32_t knn;
   uint32_t numNodes;
+  uint32_t parallax;  // shift the region's mixture to the query point
 };
 
 struct Lobe {

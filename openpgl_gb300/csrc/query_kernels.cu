@@ -70,8 +70,10 @@ __device__ __forceinline__ float lane_sum(float v, int cnt, int lane) {
   return __shfl_sync(0xFFFFFFFFu, acc, 0);
 }
 
-// Copy of the region's lobe with the parallax shift to the query point.
-__device__ __forceinline__ Lobe load_shifted(const VMMState &v, int lane, float p0, float p1, float p2) {
+// Copy of the region's lobe with the parallax shift to the query point
+// (parallax-aware mixtures only: VMMSurfaceSamplingDistribution.h:41-46).
+__device__ __forceinline__ Lobe load_shifted(const VMMState &v, int lane, float p0, float p1, float p2,
+                                             bool parallax) {
   Lobe L;
   L.w = v.w[lane]; L.kappa = v.kappa[lane]; L.norm = v.norm[lane]; L.e2k = v.e2k[lane];
   float dist = v.dist[lane];
@@ -81,7 +83,7 @@ __device__ __forceinline__ Lobe load_shifted(const VMMState &v, int lane, float 
   float len = length(p);
   p = p / len;
   bool cond = (dist > 0.0f) && (dist >= -FLT_MAX) && (dist <= FLT_MAX);
-  if (cond) mu = p;
+  if (cond && parallax) mu = p;
   L.mx = mu.x; L.my = mu.y; L.mz = mu.z;
   return L;
 }
@@ -235,7 +237,7 @@ __global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, ui
     const RegionDir &R = f.regions[reg];
     if (R.valid) {
       const int K = int(R.vmm.K), cnt = vec_count(K);
-      Lobe li = load_shifted(R.vmm, lane, q.px, q.py, q.pz);
+      Lobe li = load_shifted(R.vmm, lane, q.px, q.py, q.pz, f.parallax != 0);
       V3 d;
       if (P.hgMeanCosine) {
         Lobe h[kHgLobes];
@@ -277,7 +279,7 @@ __global__ void ssd_init_kernel(FieldView f, float px, float py, float pz, float
     r.s1d = s1d;
     const RegionDir &R = f.regions[reg];
     if (R.valid) {
-      Lobe li = load_shifted(R.vmm, lane, px, py, pz);
+      Lobe li = load_shifted(R.vmm, lane, px, py, pz, f.parallax != 0);
       st->li[lane] = li;
       st->g[lane] = li;
       if (lane == 0) {

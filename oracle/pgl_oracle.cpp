@@ -306,6 +306,7 @@ struct Config {  // effective values of FieldConfig::Init (api.cpp:755-787, Devi
   float splitThreshold = 0.5f, mergeThreshold = 0.025f;
   bool useSplitMerge = true, partialReFit = true;
   int maxSplitItr = 1, minSplit = 4000, minRefit = 4000, minMerge = 8000;
+  bool parallax = true;  // PARALLAX_AWARE_VMM; false: VMM (Device.h:139-178)
 };
 
 // ------------------------------------------------------------------ VMM ops
@@ -1558,6 +1559,7 @@ struct SubField {
   }
 
   void prepare(Region &r, size_t b, size_t e) {  // WEMFactory.h:1151-1196
+    if (!cfg.parallax) return;  // WEMFactory.h:1186: plain VMMs keep their samples
     const Stats &st = r.stats;
     V3 var = v3(st.var[0] / st.n, st.var[1] / st.n, st.var[2] / st.n);
     float minD = lengthf(var);
@@ -1616,9 +1618,11 @@ struct SubField {
       std::memcpy(mean, r.stats.mean, 12);
       if (r.re - r.rb > 0) {
         if (cfg.deterministic) std::sort(samples.begin() + r.rb, samples.begin() + r.re, sampleLess);
-        V3 shift = v3(r.vmm.pivot[0] - mean[0], r.vmm.pivot[1] - mean[1], r.vmm.pivot[2] - mean[2]);
-        suffParallaxShift(r.suff, r.vmm, shift);
-        vmmParallaxShift(r.vmm, shift);
+        if (cfg.parallax) {  // Field.h:476-482
+          V3 shift = v3(r.vmm.pivot[0] - mean[0], r.vmm.pivot[1] - mean[1], r.vmm.pivot[2] - mean[2]);
+          suffParallaxShift(r.suff, r.vmm, shift);
+          vmmParallaxShift(r.vmm, shift);
+        }
         prepare(r, r.rb, r.re);
         asmUpdate(r, samples.data() + r.rb, r.re - r.rb, cfg);
         r.valid = vmmIsValid(r.vmm) && suffIsValid(r.suff) && splitIsValid(r.split);
@@ -1713,7 +1717,7 @@ static void runQuery(const SubField &f, const QueryIn &q, QueryOut &o, bool cosi
   if (!r.valid) return;
   VMM li = r.vmm;
   V3 shift = v3(li.pivot[0] - q.pos[0], li.pivot[1] - q.pos[1], li.pivot[2] - q.pos[2]);
-  vmmParallaxShift(li, shift);
+  if (f.cfg.parallax) vmmParallaxShift(li, shift);  // VMMSurfaceSamplingDistribution.h:41-46
   VMM g = li;
   if (cosine) {
     const float ck = 2.18853f;
@@ -1752,7 +1756,7 @@ static void runQueryHG(const SubField &f, const QueryIn &q, float meanCosine, Qu
   if (!r.valid) return;
   VMM li = r.vmm;
   V3 shift = v3(li.pivot[0] - q.pos[0], li.pivot[1] - q.pos[1], li.pivot[2] - q.pos[2]);
-  vmmParallaxShift(li, shift);
+  if (f.cfg.parallax) vmmParallaxShift(li, shift);  // VMMSurfaceSamplingDistribution.h:41-46
   const float absG = std::fabs(meanCosine);
   const float step = (pgl::kHgMaxMeanCosine - pgl::kHgMinMeanCosine) / float(pgl::kHgFits);
   int idx = int(std::floor((absG - pgl::kHgMinMeanCosine) / step));
@@ -1967,8 +1971,8 @@ uint64_t orc_field_store(void *h, char *out, uint64_t cap) {
   Writer w;
   const char hdr[] = "OPENPGL_0.6.0_FIELD";
   w.raw(hdr, sizeof(hdr));
-  w.put<int32_t>(0);
-  w.put<int32_t>(0);
+  w.put<int32_t>(0);                             // kd-tree
+  w.put<int32_t>(f->surface.cfg.parallax ? 0 : 2);  // PARALLAX_AWARE_VMM or VMM (types.h)
   w.put<uint64_t>(f->iteration);
   w.put<uint64_t>(0);
   writeSub(w, f->surface);
@@ -1981,6 +1985,13 @@ void orc_field_query(void *h, int volume, int cosine, const QueryIn *q, QueryOut
   Field *f = static_cast<Field *>(h);
   const SubField &s = volume ? f->volume : f->surface;
   for (uint64_t i = 0; i < n; ++i) runQuery(s, q[i], o[i], cosine != 0);
+}
+
+// The plain VMM field type (PGL_DIRECTIONAL_DISTRIBUTION_VMM) instead of the
+// parallax-aware one; call before the first update.
+void orc_field_set_parallax(void *h, int parallax) {
+  Field *f = static_cast<Field *>(h);
+  f->surface.cfg.parallax = f->volume.cfg.parallax = parallax != 0;
 }
 
 // Volume queries with the Henyey-Greenstein product, query i with mean cosine g[i]

@@ -46,6 +46,7 @@ def load():
         lib.orc_field_store.argtypes = [vp, ctypes.c_char_p, u64]
         lib.orc_field_query.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, u64]
         lib.orc_field_query_hg.argtypes = [vp, vp, vp, vp, u64]
+        lib.orc_field_set_parallax.argtypes = [vp, ctypes.c_int]
         lib.orc_field_leaf_of.argtypes = [vp, ctypes.c_int, vp, vp, u64]
         lib.orc_field_set_scene_bounds.argtypes = [vp, vp]
         for n in ("orc_fexp", "orc_flog", "orc_rcp", "orc_rsqrt"):
@@ -58,9 +59,11 @@ def load():
 class OracleField:
     """Oracle restatement of a kd-tree PA-VMM field (deterministic CPU_8)."""
 
-    def __init__(self, max_samples_per_leaf=32000, deterministic=True, threads=1):
+    def __init__(self, max_samples_per_leaf=32000, deterministic=True, threads=1, parallax=True):
         self.lib = load()
         self.h = self.lib.orc_field_new(int(deterministic), int(max_samples_per_leaf), int(threads))
+        if not parallax:
+            self.lib.orc_field_set_parallax(self.h, 0)
 
     def close(self):
         if self.h:
@@ -145,7 +148,8 @@ def reference_available():
     return os.path.exists(REF_HARNESS)
 
 
-def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministic=True, threads=1, device=8):
+def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministic=True, threads=1, device=8,
+                  parallax=True):
     """Runs the reference library on ``frames`` (list of sample arrays) and
     returns (field file bytes, per-frame update ms, surface query out, volume
     query out, volume query out with the Henyey-Greenstein product of mean
@@ -168,6 +172,7 @@ def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministi
             args.append(qpath)
         env = dict(os.environ)
         env["PGL_ORACLE_THREADS"] = str(threads)
+        env["PGL_REF_PLAIN_VMM"] = "0" if parallax else "1"
         subprocess.run(args, check=True, env=env)
         field = open(os.path.join(td, "ref.field"), "rb").read()
         times = [float(x) for x in open(os.path.join(td, "ref.times")).read().split()]

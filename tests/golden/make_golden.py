@@ -47,6 +47,10 @@ CASES = {
                                    queries=dict(n=4096, seed=113), leaf=4000),
     "clusters": dict(gen="cluster_samples", frames=[dict(n=60000, seed=120 + i, num_clusters=64) for i in range(2)],
                      queries=dict(n=4096, seed=122, model_seed=1234), leaf=2000),
+    # the plain VMM field type (no parallax compensation)
+    "cube_plain_vmm": dict(gen="cube_face_samples",
+                           frames=[dict(n=32768, seed=130 + i, volume_fraction=0.25) for i in range(3)],
+                           queries=dict(n=4096, seed=133), leaf=4000, parallax=False),
 }
 
 
@@ -84,6 +88,7 @@ def main():
     for name, case in CASES.items():
         frames, queries = build_inputs(case)
         field, _, sq, vq, hq = pyoracle.run_reference(frames, queries, max_samples_per_leaf=case["leaf"],
+                                                      parallax=case.get("parallax", True),
                                                   deterministic=True, threads=1, device=8)
         field = fieldfile.strip_timings(field)
         with gzip.open(os.path.join(HERE, f"{name}.field.gz"), "wb", compresslevel=9) as f:

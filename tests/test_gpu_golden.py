@@ -38,7 +38,8 @@ def run_case(pgl, name):
     case = MANIFEST["cases"][name]
     frames, queries = make_golden.build_inputs(case)
     dev = pgl.Device()
-    field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=case["leaf"]))
+    field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=case["leaf"],
+                                           parallax=case.get("parallax", True)))
     storage = pgl.SampleStorage()
     for f in frames:
         storage.add_samples(f)

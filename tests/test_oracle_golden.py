@@ -56,7 +56,7 @@ def test_generators_reproduce_golden_inputs(name):
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_field_is_the_reference_field(name):
     (frames, queries), case = inputs(name)
-    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4)
+    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4, parallax=case.get("parallax", True))
     for f in frames:
         orc.update(f)
     mine = fieldfile.strip_timings(orc.field_bytes())
@@ -68,7 +68,7 @@ def test_oracle_field_is_the_reference_field(name):
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_queries_are_the_reference_queries(name):
     (frames, queries), case = inputs(name)
-    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4)
+    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4, parallax=case.get("parallax", True))
     for f in frames:
         orc.update(f)
     _, rs, rv = golden(name)
@@ -83,7 +83,7 @@ def test_oracle_hg_queries_are_the_reference_queries(name):
     """Volume queries with the single-lobe Henyey-Greenstein product
     (VMMVolumeSamplingDistribution.h:54-80) over mean cosines -0.99 .. 0.99."""
     (frames, queries), case = inputs(name)
-    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4)
+    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4, parallax=case.get("parallax", True))
     for f in frames:
         orc.update(f)
     rh = np.load(os.path.join(GOLDEN, f"{name}.queries.npz"))["volume_hg"]
