@@ -20,7 +20,10 @@ Beside the headline, `clustered` times the clustered workload: one Update of
 a fresh field on 16,777,216 surface samples around 4096 Gaussian clusters
 (Zipf masses, 1-6 lobes each), maxSamplesPerLeaf 32000, with the default EM
 schedule and with the schedule the EM autotuner picks on the Update before
-(the fields are compared byte for byte).
+(the fields are compared byte for byte).  `widened` times the rows built
+beyond the core path: volume guided queries with the Henyey-Greenstein
+product, training samples made from path segments on the device, and the
+multi-frame step with the plain VMM field type.
 
 `--impl reference` times the CPU restatement of the reference algorithm (the
 oracle, built with the reference's arithmetic) with all host threads on a
@@ -197,6 +200,83 @@ def run_clustered(pgl, dev, stream, steps, warmup):
                           "trials": len(trials), "tuning_update_ms": round(tune_ms, 1),
                           "best_trial_ms": round(min(t["ms"] for t in trials), 3) if trials else None},
             "same_field": bool(same)}
+
+
+# ----------------------------------------------------------------- widened rows
+PATHS = 131_072
+
+
+def run_widened(pgl, dev, stream, field, queries, frames, d_frames, steps, warmup):
+    """The rows built beyond the core path, each timed on the device with CUDA
+    events: volume guided queries with the Henyey-Greenstein product (mean
+    cosines uniform in [-0.9, 0.9]), training samples made from 131,072
+    synthetic paths, and one
+    multi-frame step with the plain VMM field type."""
+    import torch
+
+    from openpgl_gb300 import synthetic as syn
+
+    out = {}
+    # HG product queries on the trained field's volume sub-field
+    n = len(queries)
+    g = (np.random.Generator(np.random.PCG64(4343)).random(n) * 1.8 - 0.9).astype(np.float32)
+    qd = torch.from_numpy(queries.view(np.uint8)).to("cuda")
+    gd = torch.from_numpy(g).to("cuda")
+    rd = torch.empty(n * 32, dtype=torch.uint8, device="cuda")
+    for _ in range(max(warmup, 3)):
+        field.sample_batch_hg_device(qd.data_ptr(), gd.data_ptr(), n, rd.data_ptr(), stream=dev.cuda_stream())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(steps, 5)
+    a.record(stream)
+    for _ in range(reps):
+        field.sample_batch_hg_device(qd.data_ptr(), gd.data_ptr(), n, rd.data_ptr(), stream=dev.cuda_stream())
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    out["hg_queries"] = {"queries_per_s": round(n / (ms * 1e-3)), "batch": n, "ms_per_batch": round(ms, 3)}
+    # samples from path segments
+    segs, begin = syn.path_segments(PATHS, 6161)
+    d_segs = torch.from_numpy(segs.view(np.uint8)).to("cuda")
+    d_begin = torch.from_numpy(begin.astype(np.uint32).view(np.int32)).to("cuda")
+    d_out = torch.empty(len(segs) * 40, dtype=torch.uint8, device="cuda")
+    d_off = torch.empty(PATHS + 1, dtype=torch.int32, device="cuda")
+
+    def prep():
+        pgl.path_samples_device(d_segs.data_ptr(), d_begin.data_ptr(), PATHS, 3.0, d_out.data_ptr(), d_off.data_ptr(),
+                                stream=dev.cuda_stream())
+
+    for _ in range(max(warmup, 3)):
+        prep()
+    a.record(stream)
+    for _ in range(reps):
+        prep()
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    made = int(d_off[-1].item())
+    out["path_samples"] = {"paths": PATHS, "segments": len(segs), "samples": made, "ms": round(ms, 3),
+                           "segments_per_s": round(len(segs) / (ms * 1e-3)),
+                           "segment_bytes_gbs": round(len(segs) * 136 / (ms * 1e-3) / 1e9, 1)}
+    # the plain VMM field type on the multi-frame workload (one step after one warm-up)
+    plain = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF,
+                                           parallax=False))
+    storage = pgl.SampleStorage()
+
+    def step():
+        plain.reset()
+        for f, d in zip(frames, d_frames):
+            storage.clear()
+            storage.add_samples_device(d.data_ptr(), len(f))
+            plain.update(storage)
+
+    step()
+    torch.cuda.synchronize()
+    a.record(stream)
+    step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    out["plain_vmm_update"] = {"value": round(a.elapsed_time(b), 3), "unit": UNIT}
+    return out
 
 
 # ----------------------------------------------------------------- CPU baseline
@@ -383,6 +463,9 @@ def run_gpu(args, rank, world, local_rank):
         field.sample_batch(queries)
     q_e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
 
+    # ---- rows beyond the core path: HG queries, path-segment samples, plain VMM
+    widened = run_widened(pgl, dev, stream, field, queries, frames, d_frames, args.steps, args.warmup)
+
     # ---- clustered workload, default and autotuned EM schedule
     clustered = run_clustered(pgl, dev, stream, args.steps, 1) if args.clustered else None
 
@@ -463,6 +546,7 @@ def run_gpu(args, rank, world, local_rank):
                     "e2e_queries_per_s": round(QUERIES / (q_e2e_ms * 1e-3))},
         "serving": serving,
         "clustered": clustered,
+        "widened": widened,
         "gpu_launches": int(launches),
         "clocks": clk,
     }

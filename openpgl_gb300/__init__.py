@@ -462,6 +462,10 @@ class Field:
                "pglFieldSampleVolumeBatchHG")
         return out
 
+    def sample_batch_hg_device(self, q_ptr, g_ptr, n, out_ptr, stream=None):
+        ok = self.lib.pglFieldSampleVolumeBatchHGDevice(self.h, q_ptr, g_ptr, n, out_ptr, stream)
+        _check(ok, "pglFieldSampleVolumeBatchHGDevice")
+
     def sample_batch_device(self, q_ptr, n, out_ptr, volume=False, cosine=True, stream=None):
         ok = self.lib.pglFieldSampleBatchDevice(self.h, volume, q_ptr, n, out_ptr, cosine, stream)
         _check(ok, "pglFieldSampleBatchDevice")

@@ -254,12 +254,12 @@ def path_segments(num_paths, seed, max_len=12):
     s = np.zeros(n, dtype=PGL_PATH_SEGMENT_DTYPE)
     start = rng.random((num_paths, 3)) * 10.0
     steps = (rng.random((n, 3)) - 0.5) * 3.0
-    pos = np.repeat(start, lens, axis=0)
+    # walk: cumulative steps within each path (a path's first vertex is its start)
     first = np.zeros(n, dtype=bool)
     first[begin[:-1].astype(np.int64)] = True
-    for p in range(num_paths):  # walk: cumulative steps within each path
-        b, e = int(begin[p]), int(begin[p + 1])
-        pos[b:e] += np.cumsum(np.concatenate([np.zeros((1, 3)), steps[b + 1:e]]), axis=0)
+    steps[first] = 0.0
+    cs = np.cumsum(steps, axis=0)
+    pos = np.repeat(start, lens, axis=0) + (cs - np.repeat(cs[first], lens, axis=0))
     s["position"] = pos.astype(np.float32)
     s["direction_in"] = _unit_sphere(rng, n).astype(np.float32)
     s["direction_out"] = _unit_sphere(rng, n).astype(np.float32)
