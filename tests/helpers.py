@@ -66,3 +66,43 @@ def compare_fields(gpu_bytes, orc_bytes, side="surface"):
     res.update(bit_exact_regions=bit, k_differs=kdiff, worst_pdf_rel=worst, stats_equal=stats_equal,
                rel_errs=np.array(rel_errs))
     return res
+
+
+def leaf_log_likelihoods(field_bytes, samples, side="surface"):
+    """Per region: the weighted log-likelihood sum_i w_i log pdf(d_i) of the
+    region's samples under its mixture, in FP64, with the samples reprojected
+    onto the region's mean as the parallax-aware fit sees them
+    (WEMFactory.h:1151-1196: distance max(9 sqrt(|variance|), d)).  Meant for
+    the first Update of a field, where a region's sample statistics are those
+    of the samples given.  Returns {region: (LL, sum_i w_i |log pdf(d_i)|)},
+    the second a scale for relative comparisons (LL itself can be near 0)."""
+    f = fieldfile.read_field_file(field_bytes)[side]
+    pos = np.stack([samples["position"][:, i] for i in range(3)], axis=1).astype(np.float64)
+    d = np.stack([samples["direction"][:, i] for i in range(3)], axis=1).astype(np.float64)
+    w = samples["weight"].astype(np.float64)
+    dist = samples["distance"].astype(np.float64)
+    leaf = fieldfile.leaf_of_positions(f, pos.astype(np.float32))
+    out = {}
+    for r, reg in enumerate(f["regions"]):
+        m = leaf == r
+        if not m.any() or not reg["valid"]:
+            continue
+        st = reg["stats"]
+        mean = st["mean"].astype(np.float64)
+        var = st["var"].astype(np.float64) / float(st["n"])
+        min_d = 9.0 * np.sqrt(np.sqrt((var * var).sum()))
+        p, dd, ww, di = pos[m], d[m].copy(), w[m], dist[m]
+        ok = np.isfinite(di) & (di > 0.0)
+        dm = np.maximum(min_d, di[ok])
+        o = p[ok] + dd[ok] * dm[:, None]
+        nd = o - mean
+        dd[ok] = nd / np.sqrt((nd * nd).sum(axis=1))[:, None]
+        v = reg["vmm"]
+        K = int(v["K"])
+        mu = np.stack([v["mx"][:K], v["my"][:K], v["mz"][:K]], axis=1).astype(np.float64)
+        kap, nrm, wk = (v[k][:K].astype(np.float64) for k in ("kappa", "norm", "w"))
+        pdf = (wk[None, :] * nrm[None, :] * np.exp(kap[None, :] * (dd @ mu.T - 1.0))).sum(axis=1)
+        good = pdf > 0
+        t = ww[good] * np.log(pdf[good])
+        out[r] = (float(t.sum()), float(np.abs(t).sum()))
+    return out

@@ -53,6 +53,23 @@ def test_first_build_matches_oracle(pgl, n, leaf):
     print("bit-exact regions", r["bit_exact_regions"], "of", r["regions"])
 
 
+def test_leaf_log_likelihood_matches_oracle(pgl):
+    """Per region, the weighted log-likelihood of its reprojected samples under
+    the GPU's mixture against the same under the oracle's mixture (both
+    evaluated in FP64): within 1e-4 relative."""
+    from helpers import leaf_log_likelihoods
+    from openpgl_gb300 import synthetic as syn
+
+    frame = syn.cube_face_samples(262144, 23)
+    dev, field, orc = _train(pgl, [frame], 8000)
+    a = leaf_log_likelihoods(field.field_bytes(), frame)
+    b = leaf_log_likelihoods(orc.field_bytes(), frame)
+    assert a.keys() == b.keys() and len(a) > 10
+    # relative to the LL's scale (sum of |w log pdf|; the LL itself can be near 0)
+    rel = [abs(a[r][0] - b[r][0]) / max(b[r][1], 1e-30) for r in b]
+    assert max(rel) <= 1e-4, sorted(rel)[-5:]
+
+
 def test_multiframe_surface_and_volume(pgl):
     from openpgl_gb300 import synthetic as syn
 
