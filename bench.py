@@ -22,8 +22,9 @@ a fresh field on 16,777,216 surface samples around 4096 Gaussian clusters
 schedule and with the schedule the EM autotuner picks on the Update before
 (the fields are compared byte for byte).  `widened` times the rows built
 beyond the core path: volume guided queries with the Henyey-Greenstein
-product, training samples made from path segments on the device, and the
-multi-frame step with the plain VMM field type.
+product, training samples made from path segments on the device, the
+multi-frame step with the plain VMM field type, and the multi-frame step in
+the plain drop-in form (one EM launch per region) beside the batched one.
 
 `--impl reference` times the CPU restatement of the reference algorithm (the
 oracle, built with the reference's arithmetic) with all host threads on a
@@ -262,20 +263,30 @@ def run_widened(pgl, dev, stream, field, queries, frames, d_frames, steps, warmu
                                            parallax=False))
     storage = pgl.SampleStorage()
 
-    def step():
-        plain.reset()
+    def step(fld):
+        fld.reset()
         for f, d in zip(frames, d_frames):
             storage.clear()
             storage.add_samples_device(d.data_ptr(), len(f))
-            plain.update(storage)
+            fld.update(storage)
 
-    step()
+    step(plain)
     torch.cuda.synchronize()
     a.record(stream)
-    step()
+    step(plain)
     b.record(stream)
     torch.cuda.synchronize()
     out["plain_vmm_update"] = {"value": round(a.elapsed_time(b), 3), "unit": UNIT}
+    # the plain drop-in form of the Update: one single-block EM launch per region
+    per_region = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF))
+    per_region.set_plain_update(True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    step(per_region)
+    b.record(stream)
+    torch.cuda.synchronize()
+    out["plain_update"] = {"value": round(a.elapsed_time(b), 3), "unit": UNIT,
+                           "form": "one single-block EM launch per region, one after the other"}
     return out
 
 
@@ -463,8 +474,10 @@ def run_gpu(args, rank, world, local_rank):
         field.sample_batch(queries)
     q_e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
 
-    # ---- rows beyond the core path: HG queries, path-segment samples, plain VMM
+    # ---- rows beyond the core path: HG queries, path-segment samples, plain VMM,
+    # and the plain drop-in form of the Update beside the batched one
     widened = run_widened(pgl, dev, stream, field, queries, frames, d_frames, args.steps, args.warmup)
+    widened["plain_update"]["batched_speedup"] = round(widened["plain_update"]["value"] / ms, 2)
 
     # ---- clustered workload, default and autotuned EM schedule
     clustered = run_clustered(pgl, dev, stream, args.steps, 1) if args.clustered else None

@@ -97,6 +97,11 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
 // (and records the error) for values out of range.
 OPENPGL_CORE_INTERFACE bool pglFieldSetEmTuning(PGLField field, const int *tuning);
 OPENPGL_CORE_INTERFACE bool pglFieldGetEmTuning(PGLField field, int *tuning);
+// The plain form of the Update's directional fit (no reference counterpart;
+// for comparisons): one single-block EM launch per region, one after the
+// other, instead of one persistent launch for all regions of both
+// sub-fields with E-step passes shared between blocks.  Same results.
+OPENPGL_CORE_INTERFACE bool pglFieldSetPlainUpdate(PGLField field, bool plain);
 // The next Update first times candidate schedules (helper blocks 2/4/8 x
 // chunk divisor 1/2, x queue order when costs are known) on its own regions,
 // restoring the state they change after each trial, keeps the fastest and

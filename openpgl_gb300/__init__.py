@@ -167,6 +167,7 @@ C_API = {
     "pglFieldSetEmTuning": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p]),
     "pglFieldGetEmTuning": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p]),
     "pglFieldAutotuneNextUpdate": (None, [ctypes.c_void_p]),
+    "pglFieldSetPlainUpdate": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_bool]),
     "pglFieldGetEmTuningTrials": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "pglNewPathSegmentStorage": (ctypes.c_void_p, []),
     "pglReleasePathSegmentStorage": (None, [ctypes.c_void_p]),
@@ -396,6 +397,10 @@ class Field:
         t = (ctypes.c_int * 4)()
         self.lib.pglFieldGetEmTuning(self.h, t)
         return dict(max_helpers=t[0], chunk_div=t[1], stage_cap=t[2], order_by_cost=t[3])
+
+    def set_plain_update(self, plain=True):
+        """The plain form of the directional fit: one launch per region (same results)."""
+        _check(self.lib.pglFieldSetPlainUpdate(self.h, bool(plain)), "pglFieldSetPlainUpdate")
 
     def autotune_next_update(self):
         """The next Update times candidate EM schedules first and keeps the fastest."""

@@ -869,9 +869,17 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
 OPENPGL_CORE_INTERFACE bool pglFieldSetEmTuning(PGLField field, const int *tuning) {
   PGL_TRY
   if (!field || !tuning) throw std::runtime_error("null argument");
-  const EmTuning t{tuning[0], tuning[1], tuning[2], tuning[3]};
+  EmTuning t{tuning[0], tuning[1], tuning[2], tuning[3]};
+  t.plainLaunches = F(field)->tuning.plainLaunches;
   if (!em_tuning_valid(t)) throw std::runtime_error("EM tuning out of range");
   F(field)->tuning = t;
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglFieldSetPlainUpdate(PGLField field, bool plain) {
+  PGL_TRY
+  if (!field) throw std::runtime_error("null field");
+  F(field)->tuning.plainLaunches = plain ? 1 : 0;
   return true;
   PGL_CATCH(false)
 }

@@ -2324,7 +2324,8 @@ static size_t share_header_bytes(int blocks) {
 }
 bool em_tuning_valid(const EmTuning &t) {
   return t.maxHelpers >= 0 && t.maxHelpers <= 64 && t.chunkDiv >= 1 && t.chunkDiv <= 4 && t.stageCap >= 2 &&
-         t.stageCap <= kMaxStages && (t.orderByCost == 0 || t.orderByCost == 1);
+         t.stageCap <= kMaxStages && (t.orderByCost == 0 || t.orderByCost == 1) &&
+         (t.plainLaunches == 0 || t.plainLaunches == 1);
 }
 size_t em_share_bytes(int blocks) { return share_header_bytes(blocks) + size_t(blocks) * kRingFloats * sizeof(float); }
 size_t em_share_error_offset(int blocks) { return size_t(blocks) * sizeof(Board); }

@@ -899,14 +899,28 @@ void GpuField::runEm(SubField *const *sides, int count) {
     check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), s), "queue");
   }
   check(cudaEventRecord(emStart, s), "event");
-  if (T > 0)
-    check(launch_em(tasks_.p, T, queue_.p, es, reports_.p, profiles_.p, emShare_.p, c.numSMs, tuning, s), "em");
+  // the batched form: one persistent launch for every region of both
+  // sub-fields; the plain form: one single-block launch per region, in order
+  // (its launches run one after the other; each sees only its own region)
+  const int blocks = tuning.plainLaunches ? 1 : c.numSMs;
+  if (T > 0 && !tuning.plainLaunches)
+    check(launch_em(tasks_.p, T, queue_.p, es, reports_.p, profiles_.p, emShare_.p, blocks, tuning, s), "em");
+  for (uint32_t k = 0; T > 0 && tuning.plainLaunches && k < T; ++k) {
+    if (k > 0) check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), s), "queue");
+    check(launch_em(tasks_.p + k, 1, queue_.p, es, reports_.p + k, profiles_.p + k, emShare_.p, 1, tuning, s), "em");
+    if ((k & 63u) == 63u) {  // a failed launch stops the chain
+      check(cudaMemcpyAsync(&emError, emShare_.p + em_share_error_offset(1), sizeof(int), cudaMemcpyDeviceToHost, s),
+            "EM status");
+      check(cudaStreamSynchronize(s), "plain EM");
+      if (emError != 0) break;
+    }
+  }
   check(cudaEventRecord(emEnd, s), "event");
   if (T > 0) {
     check(cudaMemcpyAsync(profiles.data(), profiles_.p, T * sizeof(LeafProfile), cudaMemcpyDeviceToHost, s),
           "profiles");
     check(cudaMemcpyAsync(reports.data(), reports_.p, T * sizeof(LeafReport), cudaMemcpyDeviceToHost, s), "reports");
-    check(cudaMemcpyAsync(&emError, emShare_.p + em_share_error_offset(c.numSMs), sizeof(int),
+    check(cudaMemcpyAsync(&emError, emShare_.p + em_share_error_offset(blocks), sizeof(int),
                           cudaMemcpyDeviceToHost, s),
           "EM status");
   }

@@ -93,6 +93,7 @@ struct EmTuning {
   int chunkDiv = 1;
   int stageCap = 8;
   int orderByCost = 0;
+  int plainLaunches = 0;  // 1: one single-block launch per region (the plain form), same results
 };
 bool em_tuning_valid(const EmTuning &t);
 // Device memory through which the EM launch's blocks share E-step passes

@@ -70,3 +70,19 @@ def test_out_of_range_tuning_is_rejected(pgl):
         with pytest.raises(ValueError):
             field.set_em_tuning(**bad)
     assert field.em_tuning() == dict(max_helpers=4, chunk_div=1, stage_cap=8, order_by_cost=0)
+
+
+def test_plain_launches_give_the_same_field(pgl):
+    """The plain form (one single-block EM launch per region) trains the same
+    field as the batched launch."""
+    frames = _frames()[:2]
+    _, ref = _train(pgl, frames)
+    dev = pgl.Device()
+    field = pgl.Field(dev, pgl.FieldConfig(True, 4000))
+    field.set_plain_update(True)
+    st = pgl.SampleStorage()
+    for f in frames:
+        st.add_samples(f)
+        field.update(st)
+        st.clear()
+    assert field.field_bytes() == ref.field_bytes()
