@@ -333,10 +333,115 @@ void SubField::buildTree(uint32_t n, const float4 *P) {
     check(cudaStreamSynchronize(stream()), "sync");
     rootStats = stats_from_acc(a, kdBounds);
   }
-  Front root{0, 1, {}, 0, n, rootStats};
-  std::memcpy(root.b, kdBounds, 24);
-  front.push_back(root);
-  check(cudaMemsetAsync(node_.p, 0, size_t(n) * 4, stream()), "node ids");
+  if (!is_leaf(nodes[0]) && n > 0) {
+    // One pass down the existing tree instead of one level at a time: each
+    // sample goes to the leaf it reaches (the builder's partition rule), the
+    // samples are sorted by leaf (depth-first order), and the leaves' sample
+    // statistics come from one classification launch, each leaf in its
+    // parent's quantisation frame as the level-by-level pass would give them
+    // (integer sums: the order does not matter).  The leaves then form the
+    // first front; only the leaves that split go on level by level.
+    struct Leaf {
+      uint32_t node, depth;
+      float b[6], pb[6];
+    };
+    std::vector<Leaf> leaves;
+    std::vector<Leaf> stack;
+    Leaf r0{0, 1, {}, {}};
+    std::memcpy(r0.b, kdBounds, 24);
+    std::memcpy(r0.pb, kdBounds, 24);
+    stack.push_back(r0);
+    while (!stack.empty()) {  // depth-first, left first
+      const Leaf t = stack.back();
+      stack.pop_back();
+      const KDNode &nd = nodes[t.node];
+      if (is_leaf(nd)) {
+        leaves.push_back(t);
+        continue;
+      }
+      const uint32_t dim = nd.bits >> 30, c = child_of(nd);
+      Leaf l{c, t.depth + 1, {}, {}}, r{c + 1, t.depth + 1, {}, {}};
+      std::memcpy(l.b, t.b, 24);
+      std::memcpy(r.b, t.b, 24);
+      std::memcpy(l.pb, t.b, 24);
+      std::memcpy(r.pb, t.b, 24);
+      l.b[3 + dim] = nd.split;
+      r.b[dim] = nd.split;
+      stack.push_back(r);
+      stack.push_back(l);
+    }
+    const uint32_t L = uint32_t(leaves.size());
+    // page-locked staging: tree, node -> slot, slot -> node, per-leaf jobs, statistics back
+    const size_t treeBytes = (nodes.size() * sizeof(KDNode) + 15) & ~size_t(15);
+    const size_t mapBytes = (nodes.size() * 4 + 15) & ~size_t(15);
+    const size_t slotBytes = (size_t(L) * 4 + 15) & ~size_t(15);
+    const size_t jobBytes = (size_t(L) * sizeof(KdJob) + 15) & ~size_t(15);
+    const size_t accBytes = 2 * size_t(L) * sizeof(IStatsAcc);
+    kdStage_.reserve(treeBytes + mapBytes + slotBytes + jobBytes + accBytes);
+    unsigned char *base = kdStage_.p;
+    KDNode *hTree = reinterpret_cast<KDNode *>(base);
+    uint32_t *hSlot = reinterpret_cast<uint32_t *>(base + treeBytes);
+    uint32_t *hNode = reinterpret_cast<uint32_t *>(base + treeBytes + mapBytes);
+    KdJob *hJobs = reinterpret_cast<KdJob *>(base + treeBytes + mapBytes + slotBytes);
+    IStatsAcc *hAcc = reinterpret_cast<IStatsAcc *>(base + treeBytes + mapBytes + slotBytes + jobBytes);
+    std::copy(nodes.begin(), nodes.end(), hTree);
+    std::fill(hSlot, hSlot + nodes.size(), ~0u);
+    for (uint32_t k = 0; k < L; ++k) {
+      hSlot[leaves[k].node] = k;
+      hNode[k] = leaves[k].node;
+      KdJob j{};
+      j.dim = 0;
+      j.pos = INFINITY;  // every sample on the "left": one accumulator per leaf
+      j.needStats = 1u;
+      quant_frame(leaves[k].pb, j.c, j.inv);
+      hJobs[k] = j;
+    }
+    routeNodes_.reserve(nodes.size());
+    nodeToJob_.reserve(nodes.size());
+    leafSeg_.reserve(L);
+    jobs_.reserve(L);
+    acc_.reserve(2 * size_t(L));
+    keys_.reserve(n);
+    vals_.reserve(n);
+    keysB_.reserve(n);
+    valsB_.reserve(n);
+    check(cudaMemcpyAsync(routeNodes_.p, hTree, nodes.size() * sizeof(KDNode), cudaMemcpyHostToDevice, stream()),
+          "tree");
+    check(cudaMemcpyAsync(nodeToJob_.p, hSlot, nodes.size() * 4, cudaMemcpyHostToDevice, stream()), "node slots");
+    check(cudaMemcpyAsync(leafSeg_.p, hNode, size_t(L) * 4, cudaMemcpyHostToDevice, stream()), "slot nodes");
+    check(cudaMemcpyAsync(jobs_.p, hJobs, size_t(L) * sizeof(KdJob), cudaMemcpyHostToDevice, stream()), "leaf jobs");
+    check(kd_route(posA_.p, n, routeNodes_.p, nodeToJob_.p, L, leafSeg_.p, keys_.p, vals_.p, keysB_.p, valsB_.p,
+                   posB_.p, node_.p, scratch_, stream()),
+          "route");
+    std::swap(posA_.p, posB_.p);
+    std::swap(posA_.cap, posB_.cap);
+    check(kd_job_of(node_.p, n, nodeToJob_.p, jobOf_.p, acc_.p, 2 * L, stream()), "leaf of");
+    check(kd_classify(posA_.p, jobOf_.p, n, jobs_.p, isLeft_.p, acc_.p, stream()), "leaf statistics");
+    check(cudaMemcpyAsync(hAcc, acc_.p, accBytes, cudaMemcpyDeviceToHost, stream()), "D2H leaf statistics");
+    check(cudaStreamSynchronize(stream()), "sync");
+    uint32_t begin = 0;
+    for (uint32_t k = 0; k < L; ++k) {
+      IStatsAcc a = hAcc[2 * k];
+      const IStatsAcc &b = hAcc[2 * k + 1];  // samples with a NaN coordinate
+      for (int d = 0; d < 3; ++d) {
+        a.m[d] += b.m[d];
+        a.v[d] += b.v[d];
+        a.lo[d] = std::min(a.lo[d], b.lo[d]);
+        a.hi[d] = std::max(a.hi[d], b.hi[d]);
+      }
+      a.n += b.n;
+      Front f{leaves[k].node, leaves[k].depth, {}, begin, begin + uint32_t(a.n), stats_from_acc(a, leaves[k].pb)};
+      std::memcpy(f.b, leaves[k].b, 24);
+      front.push_back(f);
+      begin += uint32_t(a.n);
+    }
+    if (begin != n) throw std::runtime_error("kd descent lost samples");
+  } else {
+    Front root{0, 1, {}, 0, n, rootStats};
+    std::memcpy(root.b, kdBounds, 24);
+    front.push_back(root);
+    check(cudaMemsetAsync(node_.p, 0, size_t(n) * 4, stream()), "node ids");
+  }
 
   std::vector<KdJob> jobs;
   std::vector<const Front *> jobFront;

@@ -163,6 +163,8 @@ class SubField {
   DevArray<float4> posA_, posB_, sP_, sD_, tmpP_, tmpD_;
   DevArray<float> sPdf_, tmpPdf_, dist_;
   DevArray<uint32_t> node_, nodeB_, jobOf_, isLeft_, scanLeft_, keys_, vals_, nodeToJob_, leafSeg_, copyIdx_;
+  DevArray<uint32_t> keysB_, valsB_;  // second buffers of the one-pass descent's sort
+  DevArray<KDNode> routeNodes_;       // the tree as it stands at the start of an Update
   DevArray<unsigned long long> keys64_;
   DevArray<KdJob> jobs_;
   DevArray<IStatsAcc> acc_;

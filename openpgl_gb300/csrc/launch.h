@@ -50,6 +50,16 @@ cudaError_t scene_bounds(const float4 *P, uint64_t n, uint32_t *d6, cudaStream_t
 cudaError_t init_posidx(const float4 *P, uint32_t n, float4 *posIdx, cudaStream_t s);
 cudaError_t init_acc(IStatsAcc *acc, uint32_t count, cudaStream_t s);
 cudaError_t kd_root_stats(const float4 *pos, uint32_t n, const KdJob &job, IStatsAcc *acc, cudaStream_t s);
+// One pass down an existing tree (the root is not a leaf): every sample goes
+// to the leaf it reaches; the samples come out in leaf-slot order
+// (nodeSlot: node -> slot, slotNode: slot -> node), positions into posOut and
+// leaf nodes into nodeOut.  keys/vals/keysB/valsB: n entries each.
+cudaError_t kd_route(const float4 *pos, uint32_t n, const KDNode *nodes, const uint32_t *nodeSlot, uint32_t numSlots,
+                     const uint32_t *slotNode, uint32_t *keys, uint32_t *vals, uint32_t *keysB, uint32_t *valsB,
+                     float4 *posOut, uint32_t *nodeOut, Scratch &scratch, cudaStream_t s);
+// The classification and child statistics of one level alone (no partition).
+cudaError_t kd_classify(const float4 *pos, const uint32_t *jobOf, uint32_t n, const KdJob *jobs, uint32_t *isLeft,
+                        IStatsAcc *acc, cudaStream_t s);
 // jobOf[i] = nodeToJob[node[i]] (~0 for finished samples); clears acc[0, accCount)
 cudaError_t kd_job_of(const uint32_t *node, uint32_t n, const uint32_t *nodeToJob, uint32_t *jobOf, IStatsAcc *acc,
                       uint32_t accCount, cudaStream_t s);

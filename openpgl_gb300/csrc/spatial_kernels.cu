@@ -309,6 +309,34 @@ kd_root_stats_kernel(const float4 *pos, uint32_t n, KdJob job, IStatsAcc *acc) {
   if ((threadIdx.x & 31) == 0 && cnt > 0) acc_add(acc, m, v, lo, hi, cnt);
 }
 
+// One pass down an existing tree: the leaf every sample reaches, by the
+// builder's rule (coord < split goes left, KDTreeBuilder.h:193), as the
+// leaf's slot (key) beside the sample's index (val).
+__global__ void kd_route_kernel(const float4 *pos, uint32_t n, const KDNode *nodes, const uint32_t *nodeSlot,
+                                uint32_t *key, uint32_t *val) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pos[i];
+  uint32_t nd = 0;
+  KDNode node = nodes[0];
+  while ((node.bits >> 30) != 3u) {
+    const uint32_t dim = node.bits >> 30;
+    const float c = dim == 0 ? p.x : (dim == 1 ? p.y : p.z);
+    nd = (node.bits & 0x3FFFFFFFu) + (c < node.split ? 0u : 1u);
+    node = nodes[nd];
+  }
+  key[i] = nodeSlot[nd];
+  val[i] = i;
+}
+// Samples in slot order: positions and their leaf nodes.
+__global__ void kd_route_gather_kernel(const float4 *pos, const uint32_t *key, const uint32_t *val, uint32_t n,
+                                       const uint32_t *slotNode, float4 *posOut, uint32_t *nodeOut) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  posOut[j] = pos[val[j]];
+  nodeOut[j] = slotNode[key[j]];
+}
+
 // Stable partition inside each job's segment using the exclusive scan of the
 // left flags; finished samples keep their place.
 __global__ void kd_scatter_kernel(const float4 *pos, const uint32_t *jobOf, const uint32_t *isLeft,
@@ -599,6 +627,37 @@ cudaError_t kd_level(const float4 *pos, const uint32_t *jobOf, uint32_t n, const
   cub::DeviceScan::ExclusiveSum(scratch.ptr, tempBytes, isLeft, scanLeft, int(n), s);
   count_launch();
   kd_scatter_kernel<<<blocks_for(n, 256), 256, 0, s>>>(pos, jobOf, isLeft, scanLeft, n, jobs, posOut, nodeOut);
+  return cudaGetLastError();
+}
+
+cudaError_t kd_route(const float4 *pos, uint32_t n, const KDNode *nodes, const uint32_t *nodeSlot, uint32_t numSlots,
+                     const uint32_t *slotNode, uint32_t *keys, uint32_t *vals, uint32_t *keysB, uint32_t *valsB,
+                     float4 *posOut, uint32_t *nodeOut, Scratch &scratch, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  count_launch();
+  kd_route_kernel<<<blocks_for(n, 256), 256, 0, s>>>(pos, n, nodes, nodeSlot, keys, vals);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  int bits = 1;
+  while (bits < 32 && (1u << bits) < numSlots) ++bits;
+  cub::DoubleBuffer<uint32_t> k(keys, keysB), v(vals, valsB);
+  size_t tempBytes = 0;
+  e = cub::DeviceRadixSort::SortPairs(nullptr, tempBytes, k, v, int(n), 0, bits, s);
+  if (e != cudaSuccess) return e;
+  e = scratch_reserve(scratch, tempBytes);
+  if (e != cudaSuccess) return e;
+  e = cub::DeviceRadixSort::SortPairs(scratch.ptr, tempBytes, k, v, int(n), 0, bits, s);
+  if (e != cudaSuccess) return e;
+  count_launch();
+  kd_route_gather_kernel<<<blocks_for(n, 256), 256, 0, s>>>(pos, k.Current(), v.Current(), n, slotNode, posOut,
+                                                              nodeOut);
+  return cudaGetLastError();
+}
+cudaError_t kd_classify(const float4 *pos, const uint32_t *jobOf, uint32_t n, const KdJob *jobs, uint32_t *isLeft,
+                        IStatsAcc *acc, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  count_launch();
+  kd_classify_kernel<<<blocks_for(n, kKdTile), kKdThreads, 0, s>>>(pos, jobOf, n, jobs, isLeft, acc);
   return cudaGetLastError();
 }
 
