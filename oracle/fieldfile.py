@@ -1,6 +1,8 @@
 """Reader for the reference's binary field file (``pglFieldStoreToFile``) for
-the kd-tree + parallax-aware VMM field at SIMD width 8 (PGL_DEVICE_TYPE_CPU_8)
-or 4.  Test infrastructure: it lets tests compare the reference's tree and
+kd-tree fields with (parallax-aware) VMMs at SIMD width 8
+(PGL_DEVICE_TYPE_CPU_8) or 4, and with directional quadtrees (DQT.h:87-100,
+DQTFactory.h:33-137: factory configuration, per region the quadtree nodes
+and the statistics nodes).  Test infrastructure: it lets tests compare the reference's tree and
 regions with the restatement in this folder and with the GPU library.
 
 Layout (all little endian, packed as written by the stream writes):
@@ -70,7 +72,7 @@ def _lanes(r: _Reader, nvec, width, comps):
     return out
 
 
-def _read_field(r: _Reader, width: int, kmax: int = 32):
+def _read_field(r: _Reader, width: int, kmax: int = 32, dqt: bool = False):
     nvec = (kmax + width - 1) // width
     f = {}
     f["isSurface"] = bool(r.u8())
@@ -85,6 +87,8 @@ def _read_field(r: _Reader, width: int, kmax: int = 32):
     f["initialized"] = bool(r.u8())
     f["_timings_offset"] = r.o
     f["timings"] = r.farr(4)
+    if dqt:
+        return _read_dqt_field(r, f)
     cfg = {}
     cfg["initK"] = r.u64()
     cfg["initKappa"] = r.f32()
@@ -181,6 +185,59 @@ def _read_field(r: _Reader, width: int, kmax: int = 32):
     return f
 
 
+DQT_NODE = np.dtype([("offsetChildren", "<u4"), ("sampleWeight", "<f4")])
+DQT_STATS_NODE = np.dtype([("offsetChildren", "<u4"), ("sampleWeight", "<f4"), ("splitWeight", "<f4"),
+                           ("numSamples", "<f4"), ("firstMoment", "<f4"), ("secondMoment", "<f4")])
+
+
+def _read_kd_and_tail(r: _Reader, f, read_region):
+    f["kd_settings"] = (r.u64(), r.u64(), r.u64())
+    f["kd_isInit"] = bool(r.u8())
+    f["_kd_bounds_offset"] = r.o
+    f["kd_bounds"] = r.farr(6)
+    nn = r.u64()
+    f["nodes"] = np.frombuffer(r.take(8 * nn), dtype=np.dtype([("split", "<f4"), ("bits", "<u4")])).copy()
+    regions = []
+    for _ in range(r.u64()):
+        g = read_region(r)
+        st = {}
+        st["mean"] = r.farr(3)
+        st["var"] = r.farr(3)
+        st["n"] = r.f32()
+        st["bounds"] = r.farr(6)
+        g["stats"] = st
+        g["splitFlag"] = bool(r.u8())
+        g["range"] = (r.u64(), r.u64())
+        regions.append(g)
+    f["regions"] = regions
+    f["useStochasticNN"] = bool(r.u8())
+    built = bool(r.u8())
+    f["knn_built"] = built
+    if built:
+        npnt = r.u32()
+        f["knn_points"] = np.frombuffer(r.take(16 * npnt), dtype="<f4").reshape(npnt, 4)[:, :3].copy()
+    return f
+
+
+def _read_dqt_field(r: _Reader, f):
+    # DirectionalQuadtreeFactory::Configuration, written as the raw struct
+    f["factory"] = dict(leafEstimator=r.i32(), splitMetric=r.i32(), splitThreshold=r.f32(),
+                        footprintFactor=r.f32(), maxLevels=r.u32())
+
+    def region(r):
+        g = {"valid": bool(r.u8())}
+        pivot = r.farr(3)
+        n = r.u64()
+        g["dqt"] = {"pivot": pivot, "nodes": np.frombuffer(r.take(8 * n), dtype=DQT_NODE).copy()}
+        g["bounds"] = r.farr(6)
+        num = r.f32()
+        n = r.u64()
+        g["dqt_stats"] = {"numSamples": num, "nodes": np.frombuffer(r.take(24 * n), dtype=DQT_STATS_NODE).copy()}
+        return g
+
+    return _read_kd_and_tail(r, f, region)
+
+
 def read_field_file(path_or_bytes, width: int = 8):
     buf = path_or_bytes if isinstance(path_or_bytes, (bytes, bytearray)) else open(path_or_bytes, "rb").read()
     r = _Reader(bytes(buf))
@@ -189,8 +246,9 @@ def read_field_file(path_or_bytes, width: int = 8):
     out = {"spatialType": r.i32(), "directionalType": r.i32()}
     out["iteration"] = r.u64()
     out["totalSPP"] = r.u64()
-    out["surface"] = _read_field(r, width)
-    out["volume"] = _read_field(r, width)
+    dqt = out["directionalType"] == 1  # PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE
+    out["surface"] = _read_field(r, width, dqt=dqt)
+    out["volume"] = _read_field(r, width, dqt=dqt)
     if r.o != len(r.b):
         raise ValueError(f"trailing bytes in field file: {len(r.b) - r.o}")
     return out

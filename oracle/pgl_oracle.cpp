@@ -307,6 +307,7 @@ struct Config {  // effective values of FieldConfig::Init (api.cpp:755-787, Devi
   bool useSplitMerge = true, partialReFit = true;
   int maxSplitItr = 1, minSplit = 4000, minRefit = 4000, minMerge = 8000;
   bool parallax = true;  // PARALLAX_AWARE_VMM; false: VMM (Device.h:139-178)
+  bool dqt = false;      // PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE (Device.h:185-210)
 };
 
 // ------------------------------------------------------------------ VMM ops
@@ -1367,6 +1368,260 @@ struct Neighbours {
   uint32_t size;
 };
 
+// ------------------------------------------------------------------ directional quadtree
+// DirectionalQuadtree<SphereToSquareCylindrical> and DirectionalQuadtreeFactory
+// (dqt/DQT.h, DQTFactory.h, Traversal.h, Rect.h, SphereToSquare.h) at the
+// defaults of PGLDQTFactoryArguments (include/openpgl/config.h:95-102):
+// REJECTION_SAMPLING leaf estimator, MEAN split metric, split threshold 0.01,
+// footprint factor 1, 12 levels.  The other estimator / metric combinations
+// are not restated.
+struct DqtConfig {  // DQTFactory.h:33-70, stored as the raw 20-byte struct
+  int32_t leafEstimator = 0, splitMetric = 0;
+  float splitThreshold = 0.01f, footprintFactor = 1.0f;
+  uint32_t maxLevels = 12;
+};
+static_assert(sizeof(DqtConfig) == 20, "DirectionalQuadtreeFactory::Configuration is 20 bytes");
+struct DqtNode {  // DirectionalQuadtreeNode (DQT.h:12-23)
+  uint32_t child = 0;
+  float weight = 0.0f;
+};
+struct DqtStatsNode {  // DirectionalQuadtreeFactory::StatsNode (DQTFactory.h:72-81)
+  uint32_t child = 0;
+  float sampleWeight = 0.0f, splitWeight = 0.0f, numSamples = 0.0f, first = 0.0f, second = 0.0f;
+};
+static_assert(sizeof(DqtStatsNode) == 24, "StatsNode is 24 bytes");
+struct DqtRegion {  // the quadtree of a region and its training statistics
+  float pivot[3] = {0.0f, 0.0f, 0.0f};
+  std::vector<DqtNode> nodes = {DqtNode()};
+  float numSamples = 0.0f;
+  std::vector<DqtStatsNode> stats = {DqtStatsNode()};
+};
+struct Box2 {  // Rect<float> (Rect.h:8-40)
+  float x0, y0, x1, y1;
+  float area() const { return (x1 - x0) * (y1 - y0); }
+  Box2 child(uint32_t c) const {
+    const float mx = (x0 + x1) / 2.0f, my = (y0 + y1) / 2.0f;
+    return {(c & 1) ? mx : x0, (c & 2) ? my : y0, (c & 1) ? x1 : mx, (c & 2) ? y1 : my};
+  }
+  Box2 intersect(const Box2 &o) const {
+    Box2 r{smax(x0, o.x0), smax(y0, o.y0), smin(x1, o.x1), smin(y1, o.y1)};
+    r.x1 = smax(r.x0, r.x1);
+    r.y1 = smax(r.y0, r.y1);
+    return r;
+  }
+};
+static inline float clampf(float v, float lo, float hi) { return emax(lo, emin(v, hi)); }  // embree::clamp
+
+// SphereToSquareCylindrical (SphereToSquare.h:34-61): x = (cos theta + 1) / 2,
+// y = phi / 2pi + 1/2 (phi from libm's atan2f, the division in double).
+static void dqtDirToPoint(V3 d, float &px, float &py) {
+  const float dx = clampf(d.x, -1.f, 1.f), dy = clampf(d.y, -1.f, 1.f), dz = clampf(d.z, -1.f, 1.f);
+  const float phi = std::atan2(dy, dx);
+  px = clampf((dz + 1.0f) / 2.0f, 0.f, 1.f);
+  py = clampf(float(double(phi) / (2.0 * M_PI) + 0.5), 0.f, 1.f);
+}
+static V3 dqtPointToDir(float px, float py) {
+  px = clampf(px, 0.f, 1.f);
+  py = clampf(py, 0.f, 1.f);
+  const float cosTheta = 2.0f * px - 1.0f;
+  const float sinTheta = std::sqrt(1.0f - cosTheta * cosTheta);
+  const float phi = float((double(py) - 0.5) * 2.0 * M_PI);
+  return v3(clampf(sinTheta * std::cos(phi), -1.f, 1.f), clampf(sinTheta * std::sin(phi), -1.f, 1.f),
+            clampf(cosTheta, -1.f, 1.f));
+}
+static const float kDqtJacobian = 4.0f * float(M_PI);
+
+// queryNode (Traversal.h:37-49): the leaf a point of the unit square falls in
+template <typename N>
+static uint32_t dqtQuery(const N *nodes, float px, float py, Box2 &rect) {
+  rect = {0.f, 0.f, 1.f, 1.f};
+  uint32_t idx = 0;
+  while (nodes[idx].child > 0) {
+    uint32_t c = 0;
+    if (px >= 0.5f) { px -= 0.5f; c += 1; }
+    if (py >= 0.5f) { py -= 0.5f; c += 2; }
+    px *= 2.0f;
+    py *= 2.0f;
+    rect = rect.child(c);
+    idx = nodes[idx].child + c;
+  }
+  return idx;
+}
+
+// Footprint splat (Traversal.h:61-90): a box of footprintFactor times the size
+// of the leaf the point falls in, centred on the point and clipped to the unit
+// square; every leaf it overlaps receives the overlap's share of the box area.
+// Leaves are visited depth first, children in order 0..3.
+template <typename F>
+static void dqtSplatVisit(std::vector<DqtStatsNode> &nodes, const Box2 &filter, float filterArea, uint32_t i,
+                          Box2 rect, F &apply) {
+  const float a = filter.intersect(rect).area();
+  if (a == 0.0f) return;
+  if (nodes[i].child == 0) {
+    apply(nodes[i], a / filterArea);
+    return;
+  }
+  for (uint32_t c = 0; c < 4; ++c) dqtSplatVisit(nodes, filter, filterArea, nodes[i].child + c, rect.child(c), apply);
+}
+
+static void dqtBuildSplit(std::vector<DqtStatsNode> &nodes, uint32_t p, uint32_t i) {  // DQTFactory.h:313-324
+  DqtStatsNode &n = nodes[i];
+  const DqtStatsNode &par = nodes[p];
+  n.child = 0;
+  n.numSamples = par.numSamples / 4;
+  n.first = par.first / 4;
+  n.second = par.second / 4;
+  n.sampleWeight = par.sampleWeight / 4;
+  n.splitWeight = par.splitWeight / 4;
+}
+
+// buildRecursive (DQTFactory.h:283-311): the new tree in depth-first order,
+// the four children of a node allocated together when it is reached.
+static void dqtBuild(std::vector<DqtStatsNode> &out, const std::vector<DqtStatsNode> &old, const DqtConfig &cfg,
+                     uint32_t i, uint32_t j, uint32_t level) {
+  const DqtStatsNode on = old[i];
+  out[j] = on;
+  if (level < cfg.maxLevels && on.splitWeight > cfg.splitThreshold * old[0].splitWeight) {
+    const uint32_t c0 = uint32_t(out.size());
+    out[j].child = c0;
+    out.resize(out.size() + 4);
+    if (on.child > 0) {
+      for (uint32_t c = 0; c < 4; ++c) dqtBuild(out, old, cfg, on.child + c, c0 + c, level + 1);
+    } else {
+      for (uint32_t c = 0; c < 4; ++c) dqtBuildSplit(out, j, c0 + c);
+    }
+  } else {
+    out[j].child = 0;
+  }
+}
+
+// sample and split weights bottom-up (DQTFactory.h:232-263): a leaf's is its
+// first moment over the decayed sample count, an inner node's the sum of its
+// children's in order
+static void dqtWeights(std::vector<DqtStatsNode> &nodes, uint32_t i, float invN) {
+  DqtStatsNode &n = nodes[i];
+  if (n.child > 0) {
+    for (uint32_t c = 0; c < 4; ++c) dqtWeights(nodes, nodes[i].child + c, invN);
+    DqtStatsNode &m = nodes[i];
+    m.sampleWeight = 0.0f;
+    m.splitWeight = 0.0f;
+    for (uint32_t c = 0; c < 4; ++c) {
+      m.sampleWeight += nodes[m.child + c].sampleWeight;
+      m.splitWeight += nodes[m.child + c].splitWeight;
+    }
+  } else {
+    const float f = n.first * invN;
+    n.sampleWeight = f;
+    n.splitWeight = f;
+  }
+}
+
+static void dqtUpdate(DqtRegion &r, const Sample *S, size_t n, const DqtConfig &cfg) {  // DQTFactory.h:199-281
+  r.numSamples += float(n);
+  const float ff = cfg.footprintFactor;
+  for (size_t i = 0; i < n; ++i) {
+    const Sample &s = S[i];
+    const float first = s.weight;
+    const float second = s.weight * s.weight * s.pdf;
+    float px, py;
+    dqtDirToPoint(v3(s.dir[0], s.dir[1], s.dir[2]), px, py);
+    auto apply = [&](DqtStatsNode &node, float w) {
+      node.numSamples += w;
+      node.first += w * first;
+      node.second += w * second;
+    };
+    Box2 leaf;
+    const uint32_t li = dqtQuery(r.stats.data(), px, py, leaf);
+    if (ff > 0.0f) {
+      const float hx = ff * (leaf.x1 - leaf.x0) / 2.0f, hy = ff * (leaf.y1 - leaf.y0) / 2.0f;
+      const Box2 filter = Box2{px - hx, py - hy, px + hx, py + hy}.intersect(Box2{0.f, 0.f, 1.f, 1.f});
+      dqtSplatVisit(r.stats, filter, filter.area(), 0, Box2{0.f, 0.f, 1.f, 1.f}, apply);
+    } else {
+      apply(r.stats[li], 1.0f);
+    }
+  }
+  dqtWeights(r.stats, 0, 1.0f / r.numSamples);
+  std::vector<DqtStatsNode> old;
+  old.swap(r.stats);
+  r.stats.resize(1);
+  dqtBuild(r.stats, old, cfg, 0, 0, 0);
+  r.nodes.resize(r.stats.size());
+  for (size_t i = 0; i < r.stats.size(); ++i) r.nodes[i] = DqtNode{r.stats[i].child, r.stats[i].sampleWeight};
+}
+
+static void dqtDecay(DqtRegion &r, float a) {  // Statistics::decay (DQTFactory.h:109-116)
+  r.numSamples *= a;
+  for (DqtStatsNode &n : r.stats) {
+    n.numSamples *= a;
+    n.first *= a;
+    n.second *= a;
+  }
+}
+
+static void dqtFit(DqtRegion &r, const Sample *S, size_t n, const DqtConfig &cfg) {  // DQTFactory.h:149-155
+  for (int i = 0; i < 5; ++i) {
+    dqtDecay(r, 0.25f);
+    dqtUpdate(r, S, n, cfg);
+  }
+}
+
+static bool dqtValid(const DqtRegion &r) {  // DirectionalQuadtree::isValid (DQT.h:40-42)
+  return !std::isinf(r.nodes[0].weight) && r.nodes[0].weight > 0;
+}
+static bool dqtStatsValid(const DqtRegion &r) {  // Statistics::isValid (DQTFactory.h:95-107)
+  auto ok = [](float v) { return !std::isnan(v) && !std::isinf(v) && v >= 0; };
+  for (const DqtStatsNode &n : r.stats)
+    if (!ok(n.sampleWeight) || !ok(n.splitWeight) || !ok(n.numSamples) || !ok(n.first) || !ok(n.second)) return false;
+  return r.stats[0].sampleWeight > 0 && r.stats[0].splitWeight > 0;
+}
+
+// samplePdf (DQT.h:62-72, :115-153): a stochastic descent that picks the
+// left/right half by u.x and the top/bottom half by u.y, each rescaled into
+// the chosen part; pdf = leaf weight / (root weight * leaf area) / 4pi
+static float dqtSamplePdf(const DqtRegion &r, float ux, float uy, V3 &dir) {
+  const std::vector<DqtNode> &N = r.nodes;
+  float span = 1.0f, x = 0.0f, y = 0.0f;
+  auto rescale = [](float t, float &u) {
+    if (u < t) {
+      u /= t;
+      return true;
+    }
+    u -= t;
+    u /= 1.0f - t;
+    return false;
+  };
+  uint32_t idx = 0;
+  while (N[idx].child > 0) {
+    span /= 2.0f;
+    uint32_t off = 0;
+    const DqtNode *c = &N[N[idx].child];
+    const float wl = c[0].weight + c[2].weight, wr = c[1].weight + c[3].weight;
+    if (!rescale(wl / (wl + wr), ux)) {
+      off += 1;
+      x += span;
+    }
+    const float wt = c[off].weight, wb = c[off + 2].weight;
+    if (!rescale(wt / (wt + wb), uy)) {
+      off += 2;
+      y += span;
+    }
+    idx = N[idx].child + off;
+  }
+  float pdf = N[idx].weight / (N[0].weight * span * span);
+  const float px = x + ux * span, py = y + uy * span;
+  pdf /= kDqtJacobian;
+  dir = dqtPointToDir(px, py);
+  return pdf;
+}
+static float dqtPdf(const DqtRegion &r, V3 d) {  // DQT.h:53-60, :155-159
+  float px, py;
+  dqtDirToPoint(d, px, py);
+  Box2 rect;
+  const uint32_t i = dqtQuery(r.nodes.data(), px, py, rect);
+  const float p = r.nodes[i].weight / (r.nodes[0].weight * rect.area()) / kDqtJacobian;
+  return smin(FLT_MAX, p);
+}
+
 struct SubField {
   Config cfg;
   bool isSurface = true;
@@ -1378,6 +1633,8 @@ struct SubField {
   bool kdInit = false;
   std::vector<Node> nodes;
   std::vector<Region> regions;
+  std::vector<DqtRegion> dqts;  // the quadtree field type: region i's quadtree and statistics
+  DqtConfig dqtCfg;
   std::vector<Neighbours> nbrs;
   std::vector<Sample> samples;
   int threads = 1;
@@ -1433,6 +1690,7 @@ struct SubField {
         regions[di].bounds[3 + dim] = pos;
         right.bounds[dim] = pos;
         regions.push_back(right);
+        if (cfg.dqt) dqts.push_back(dqts[di]);
         uint32_t rightIdx = uint32_t(regions.size() - 1);
         lr0 = uint32_t(nodes.size());
         nodes.push_back(Node{0.0f, 0});
@@ -1592,6 +1850,15 @@ struct SubField {
       std::memcpy(mean, r.stats.mean, 12);
       if (r.re - r.rb > 0) {
         if (cfg.deterministic) std::sort(samples.begin() + r.rb, samples.begin() + r.re, sampleLess);
+        if (cfg.dqt) {  // the quadtree factory prepares nothing (DQTFactory.h:146-147)
+          DqtRegion &q = dqts[n];
+          dqtFit(q, samples.data() + r.rb, r.re - r.rb, dqtCfg);
+          std::memcpy(q.pivot, mean, 12);
+          r.valid = dqtValid(q);
+          r.splitFlag = false;
+          r.rb = r.re = 0;
+          return;
+        }
         prepare(r, r.rb, r.re);
         asmFit(r, samples.data() + r.rb, r.re - r.rb, cfg);
         std::memcpy(r.vmm.pivot, mean, 12);
@@ -1610,14 +1877,24 @@ struct SubField {
     parallelRegions([&](size_t n) {
       Region &r = regions[n];
       if (r.splitFlag) {
-        suffDecay(r.suff, decay);
-        splitDecay(r.split, decay);
+        if (cfg.dqt) {
+          dqtDecay(dqts[n], decay);
+        } else {
+          suffDecay(r.suff, decay);
+          splitDecay(r.split, decay);
+        }
         r.splitFlag = false;
       }
       float mean[3];
       std::memcpy(mean, r.stats.mean, 12);
       if (r.re - r.rb > 0) {
         if (cfg.deterministic) std::sort(samples.begin() + r.rb, samples.begin() + r.re, sampleLess);
+        if (cfg.dqt) {  // no parallax compensation (DQT.h:28-30), no preparation
+          dqtUpdate(dqts[n], samples.data() + r.rb, r.re - r.rb, dqtCfg);
+          r.valid = dqtValid(dqts[n]) && dqtStatsValid(dqts[n]);
+          r.rb = r.re = 0;
+          return;
+        }
         if (cfg.parallax) {  // Field.h:476-482
           V3 shift = v3(r.vmm.pivot[0] - mean[0], r.vmm.pivot[1] - mean[1], r.vmm.pivot[2] - mean[2]);
           suffParallaxShift(r.suff, r.vmm, shift);
@@ -1643,6 +1920,7 @@ struct SubField {
       nodes.push_back(Node{0.0f, (3u << 30) | 0u});
       regions.clear();
       regions.push_back(newRegion());
+      dqts.assign(cfg.dqt ? 1 : 0, DqtRegion());
       std::memcpy(regions[0].bounds, sceneBounds, 24);
       updateTree();
       if (cfg.knn) buildKNN();
@@ -1701,6 +1979,21 @@ struct Field {
   uint64_t iteration = 0;
 };
 
+// A quadtree query (DQTSurfaceSamplingDistribution.h, DQTVolumeSamplingDistribution.h):
+// neither the cosine nor the Henyey-Greenstein product is supported, so the
+// surface, volume and phase-function queries all sample the region's quadtree.
+static void dqtQueryOut(const DqtRegion &r, const QueryIn &q, uint32_t leaf, QueryOut &o) {
+  V3 d;
+  const float pdf = dqtSamplePdf(r, q.u[0], q.u[1], d);
+  o.ok = 1;
+  o.id = leaf;
+  o.dir[0] = d.x;
+  o.dir[1] = d.y;
+  o.dir[2] = d.z;
+  o.pdf = pdf;
+  o.pdfLi = dqtPdf(r, d);
+}
+
 static void runQuery(const SubField &f, const QueryIn &q, QueryOut &o, bool cosine) {
   std::memset(&o, 0, sizeof(o));
   float s1d = q.s1d;
@@ -1715,6 +2008,7 @@ static void runQuery(const SubField &f, const QueryIn &q, QueryOut &o, bool cosi
   o.s1d = s1d;
   const Region &r = f.regions[reg];
   if (!r.valid) return;
+  if (f.cfg.dqt) return dqtQueryOut(f.dqts[reg], q, leaf, o);
   VMM li = r.vmm;
   V3 shift = v3(li.pivot[0] - q.pos[0], li.pivot[1] - q.pos[1], li.pivot[2] - q.pos[2]);
   if (f.cfg.parallax) vmmParallaxShift(li, shift);  // VMMSurfaceSamplingDistribution.h:41-46
@@ -1754,6 +2048,7 @@ static void runQueryHG(const SubField &f, const QueryIn &q, float meanCosine, Qu
   o.s1d = s1d;
   const Region &r = f.regions[reg];
   if (!r.valid) return;
+  if (f.cfg.dqt) return dqtQueryOut(f.dqts[reg], q, leaf, o);
   VMM li = r.vmm;
   V3 shift = v3(li.pivot[0] - q.pos[0], li.pivot[1] - q.pos[1], li.pivot[2] - q.pos[2]);
   if (f.cfg.parallax) vmmParallaxShift(li, shift);  // VMMSurfaceSamplingDistribution.h:41-46
@@ -1800,6 +2095,64 @@ struct Writer {
   void put(const T &v) { raw(&v, sizeof(T)); }
   void lanes(const float *a, int v) { raw(a + v * W, sizeof(float) * W); }
 };
+static void writeKnn(Writer &w, const SubField &f) {
+  w.put<uint8_t>(f.cfg.knn);
+  bool built = f.cfg.knn && !f.regions.empty() && f.initialized;
+  w.put<uint8_t>(built);
+  if (built) {
+    w.put<uint32_t>(uint32_t(f.regions.size()));
+    for (const Region &r : f.regions) {
+      float p[4] = {r.stats.mean[0], r.stats.mean[1], r.stats.mean[2], 0.0f};
+      w.raw(p, 16);
+    }
+  }
+}
+static void writeKdHead(Writer &w, const SubField &f) {
+  w.put<uint64_t>(f.cfg.minSamples);
+  w.put<uint64_t>(f.cfg.maxSamples);
+  w.put<uint64_t>(f.cfg.maxDepth);
+  w.put<uint8_t>(f.kdInit);
+  w.raw(f.kdBounds, 24);
+  w.put<uint64_t>(f.nodes.size());
+  for (const Node &n : f.nodes) {
+    w.put<float>(n.split);
+    w.put<uint32_t>(n.bits);
+  }
+  w.put<uint64_t>(f.regions.size());
+}
+static void writeRegionTail(Writer &w, const Region &r) {
+  w.raw(r.stats.mean, 12);
+  w.raw(r.stats.var, 12);
+  w.put<float>(r.stats.n);
+  w.raw(r.stats.lo, 12);
+  w.raw(r.stats.hi, 12);
+  w.put<uint8_t>(r.splitFlag);
+  w.put<uint64_t>(r.rb);
+  w.put<uint64_t>(r.re);
+}
+// The quadtree field after the common head: the factory configuration
+// (DQTFactory.h:59-61), the kd-tree, per region the validity flag, the
+// quadtree (DQT.h:88-93), the bounds, the training statistics
+// (DQTFactory.h:118-123) and the sample statistics, then the neighbour points.
+static void writeSubDqt(Writer &w, const SubField &f) {
+  w.put<DqtConfig>(f.dqtCfg);
+  writeKdHead(w, f);
+  for (size_t i = 0; i < f.regions.size(); ++i) {
+    const Region &r = f.regions[i];
+    const DqtRegion &q = f.dqts[i];
+    w.put<uint8_t>(r.valid);
+    w.raw(q.pivot, 12);
+    w.put<uint64_t>(q.nodes.size());
+    w.raw(q.nodes.data(), q.nodes.size() * sizeof(DqtNode));
+    w.raw(r.bounds, 24);
+    w.put<float>(q.numSamples);
+    w.put<uint64_t>(q.stats.size());
+    w.raw(q.stats.data(), q.stats.size() * sizeof(DqtStatsNode));
+    writeRegionTail(w, r);
+  }
+  writeKnn(w, f);
+}
+
 static void writeSub(Writer &w, const SubField &f) {  // same layout as Field::serialize (Field.h:240-267)
   w.put<uint8_t>(f.isSurface);
   w.put<float>(f.decay);
@@ -1813,6 +2166,7 @@ static void writeSub(Writer &w, const SubField &f) {  // same layout as Field::s
   float t[4] = {0, 0, 0, 0};
   w.raw(t, 16);
   const Config &c = f.cfg;
+  if (c.dqt) return writeSubDqt(w, f);
   w.put<uint64_t>(c.initK);
   w.put<float>(c.initKappa);
   w.put<uint64_t>(c.maxK);
@@ -1972,7 +2326,8 @@ uint64_t orc_field_store(void *h, char *out, uint64_t cap) {
   const char hdr[] = "OPENPGL_0.6.0_FIELD";
   w.raw(hdr, sizeof(hdr));
   w.put<int32_t>(0);                             // kd-tree
-  w.put<int32_t>(f->surface.cfg.parallax ? 0 : 2);  // PARALLAX_AWARE_VMM or VMM (types.h)
+  // PARALLAX_AWARE_VMM, QUADTREE or VMM (include/openpgl/types.h:8-13)
+  w.put<int32_t>(f->surface.cfg.dqt ? 1 : f->surface.cfg.parallax ? 0 : 2);
   w.put<uint64_t>(f->iteration);
   w.put<uint64_t>(0);
   writeSub(w, f->surface);
@@ -1992,6 +2347,13 @@ void orc_field_query(void *h, int volume, int cosine, const QueryIn *q, QueryOut
 void orc_field_set_parallax(void *h, int parallax) {
   Field *f = static_cast<Field *>(h);
   f->surface.cfg.parallax = f->volume.cfg.parallax = parallax != 0;
+}
+
+// The directional quadtree field type (PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE,
+// default factory arguments); call before the first update.
+void orc_field_set_dqt(void *h) {
+  Field *f = static_cast<Field *>(h);
+  f->surface.cfg.dqt = f->volume.cfg.dqt = true;
 }
 
 // Volume queries with the Henyey-Greenstein product, query i with mean cosine g[i]

@@ -47,6 +47,7 @@ def load():
         lib.orc_field_query.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, u64]
         lib.orc_field_query_hg.argtypes = [vp, vp, vp, vp, u64]
         lib.orc_field_set_parallax.argtypes = [vp, ctypes.c_int]
+        lib.orc_field_set_dqt.argtypes = [vp]
         lib.orc_field_leaf_of.argtypes = [vp, ctypes.c_int, vp, vp, u64]
         lib.orc_field_set_scene_bounds.argtypes = [vp, vp]
         for n in ("orc_fexp", "orc_flog", "orc_rcp", "orc_rsqrt"):
@@ -57,13 +58,17 @@ def load():
 
 
 class OracleField:
-    """Oracle restatement of a kd-tree PA-VMM field (deterministic CPU_8)."""
+    """Oracle restatement of a kd-tree field (deterministic CPU_8) with
+    parallax-aware VMMs, plain VMMs (parallax=False) or directional quadtrees
+    (dqt=True)."""
 
-    def __init__(self, max_samples_per_leaf=32000, deterministic=True, threads=1, parallax=True):
+    def __init__(self, max_samples_per_leaf=32000, deterministic=True, threads=1, parallax=True, dqt=False):
         self.lib = load()
         self.h = self.lib.orc_field_new(int(deterministic), int(max_samples_per_leaf), int(threads))
         if not parallax:
             self.lib.orc_field_set_parallax(self.h, 0)
+        if dqt:
+            self.lib.orc_field_set_dqt(self.h)
 
     def close(self):
         if self.h:
@@ -149,7 +154,7 @@ def reference_available():
 
 
 def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministic=True, threads=1, device=8,
-                  parallax=True):
+                  parallax=True, dqt=False):
     """Runs the reference library on ``frames`` (list of sample arrays) and
     returns (field file bytes, per-frame update ms, surface query out, volume
     query out, volume query out with the Henyey-Greenstein product of mean
@@ -173,6 +178,7 @@ def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministi
         env = dict(os.environ)
         env["PGL_ORACLE_THREADS"] = str(threads)
         env["PGL_REF_PLAIN_VMM"] = "0" if parallax else "1"
+        env["PGL_REF_DQT"] = "1" if dqt else "0"
         subprocess.run(args, check=True, env=env)
         field = open(os.path.join(td, "ref.field"), "rb").read()
         times = [float(x) for x in open(os.path.join(td, "ref.times")).read().split()]

@@ -68,13 +68,16 @@ int main(int argc, char **argv) {
   }
 
   openpgl::cpp::Device device(dev == 4 ? PGL_DEVICE_TYPE_CPU_4 : PGL_DEVICE_TYPE_CPU_8, size_t(threads));
-  // PGL_REF_PLAIN_VMM=1 selects the plain VMM field type instead of the parallax-aware one
+  // PGL_REF_PLAIN_VMM=1 selects the plain VMM field type instead of the
+  // parallax-aware one, PGL_REF_DQT=1 the directional quadtree
   const char *plain = std::getenv("PGL_REF_PLAIN_VMM");
+  const char *dqt = std::getenv("PGL_REF_DQT");
   const bool parallax = !(plain && std::atoi(plain) != 0);
+  PGL_DIRECTIONAL_DISTRIBUTION_TYPE kind =
+      parallax ? PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM : PGL_DIRECTIONAL_DISTRIBUTION_VMM;
+  if (dqt && std::atoi(dqt) != 0) kind = PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE;
   openpgl::cpp::FieldConfig cfg;
-  cfg.Init(PGL_SPATIAL_STRUCTURE_KDTREE,
-           parallax ? PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM : PGL_DIRECTIONAL_DISTRIBUTION_VMM, deterministic,
-           maxLeaf);
+  cfg.Init(PGL_SPATIAL_STRUCTURE_KDTREE, kind, deterministic, maxLeaf);
   openpgl::cpp::Field field(&device, cfg);
   openpgl::cpp::SampleStorage storage;
 

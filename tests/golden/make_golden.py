@@ -51,6 +51,9 @@ CASES = {
     "cube_plain_vmm": dict(gen="cube_face_samples",
                            frames=[dict(n=32768, seed=130 + i, volume_fraction=0.25) for i in range(3)],
                            queries=dict(n=4096, seed=133), leaf=4000, parallax=False),
+    # the directional quadtree field type (reference defaults of PGLDQTFactoryArguments)
+    "cube_dqt": dict(gen="cube_face_samples", frames=[dict(n=32768, seed=140 + i, volume_fraction=0.25) for i in range(2)],
+                     queries=dict(n=4096, seed=142), leaf=4000, dqt=True),
 }
 
 
@@ -88,7 +91,7 @@ def main():
     for name, case in CASES.items():
         frames, queries = build_inputs(case)
         field, _, sq, vq, hq = pyoracle.run_reference(frames, queries, max_samples_per_leaf=case["leaf"],
-                                                      parallax=case.get("parallax", True),
+                                                      parallax=case.get("parallax", True), dqt=case.get("dqt", False),
                                                   deterministic=True, threads=1, device=8)
         field = fieldfile.strip_timings(field)
         with gzip.open(os.path.join(HERE, f"{name}.field.gz"), "wb", compresslevel=9) as f:

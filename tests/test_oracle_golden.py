@@ -40,6 +40,11 @@ def _golden_path():
     yield
 
 
+def oracle_for(case):
+    return pyoracle.OracleField(case["leaf"], deterministic=True, threads=4, parallax=case.get("parallax", True),
+                                dqt=case.get("dqt", False))
+
+
 def golden(name):
     field = gzip.open(os.path.join(GOLDEN, f"{name}.field.gz")).read()
     q = np.load(os.path.join(GOLDEN, f"{name}.queries.npz"))
@@ -56,7 +61,7 @@ def test_generators_reproduce_golden_inputs(name):
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_field_is_the_reference_field(name):
     (frames, queries), case = inputs(name)
-    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4, parallax=case.get("parallax", True))
+    orc = oracle_for(case)
     for f in frames:
         orc.update(f)
     mine = fieldfile.strip_timings(orc.field_bytes())
@@ -68,7 +73,7 @@ def test_oracle_field_is_the_reference_field(name):
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_queries_are_the_reference_queries(name):
     (frames, queries), case = inputs(name)
-    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4, parallax=case.get("parallax", True))
+    orc = oracle_for(case)
     for f in frames:
         orc.update(f)
     _, rs, rv = golden(name)
@@ -83,7 +88,7 @@ def test_oracle_hg_queries_are_the_reference_queries(name):
     """Volume queries with the single-lobe Henyey-Greenstein product
     (VMMVolumeSamplingDistribution.h:54-80) over mean cosines -0.99 .. 0.99."""
     (frames, queries), case = inputs(name)
-    orc = pyoracle.OracleField(case["leaf"], deterministic=True, threads=4, parallax=case.get("parallax", True))
+    orc = oracle_for(case)
     for f in frames:
         orc.update(f)
     rh = np.load(os.path.join(GOLDEN, f"{name}.queries.npz"))["volume_hg"]
@@ -116,6 +121,24 @@ def test_oracle_matches_live_reference_on_fresh_seed():
     q = syn.queries(1024, 779)
     field, _, rs, rv, rh = pyoracle.run_reference(frames, q, max_samples_per_leaf=3000)
     orc = pyoracle.OracleField(3000, deterministic=True, threads=2)
+    for f in frames:
+        orc.update(f)
+    assert fieldfile.strip_timings(orc.field_bytes()) == fieldfile.strip_timings(field)
+    assert orc.query(q).tobytes() == rs.tobytes()
+    assert orc.query(q, volume=True, cosine=False).tobytes() == rv.tobytes()
+    assert orc.query_hg(q, pyoracle.hg_mean_cosines(len(q))).tobytes() == rh.tobytes()
+
+
+@pytest.mark.skipif(not pyoracle.reference_available(), reason="reference library not built here")
+def test_oracle_quadtree_matches_live_reference_on_fresh_seed():
+    """The directional quadtree field type (DQTFactory.h, DQT.h) on a fresh
+    seed: the same field file and the same query results."""
+    from openpgl_gb300 import synthetic as syn
+
+    frames = [syn.cube_face_samples(16000, 881 + i, volume_fraction=0.3) for i in range(3)]
+    q = syn.queries(1024, 884)
+    field, _, rs, rv, rh = pyoracle.run_reference(frames, q, max_samples_per_leaf=2500, dqt=True)
+    orc = pyoracle.OracleField(2500, deterministic=True, threads=2, dqt=True)
     for f in frames:
         orc.update(f)
     assert fieldfile.strip_timings(orc.field_bytes()) == fieldfile.strip_timings(field)
