@@ -1373,8 +1373,9 @@ struct Neighbours {
 // (dqt/DQT.h, DQTFactory.h, Traversal.h, Rect.h, SphereToSquare.h) at the
 // defaults of PGLDQTFactoryArguments (include/openpgl/config.h:95-102):
 // REJECTION_SAMPLING leaf estimator, MEAN split metric, split threshold 0.01,
-// footprint factor 1, 12 levels.  The other estimator / metric combinations
-// are not restated.
+// footprint factor 1, 12 levels; the PER_LEAF estimator, the SECOND_MOMENT
+// metric and a zero footprint are the factory's other branches
+// (DQTFactory.h:168-186).
 struct DqtConfig {  // DQTFactory.h:33-70, stored as the raw 20-byte struct
   int32_t leafEstimator = 0, splitMetric = 0;
   float splitThreshold = 0.01f, footprintFactor = 1.0f;
@@ -1495,13 +1496,18 @@ static void dqtBuild(std::vector<DqtStatsNode> &out, const std::vector<DqtStatsN
   }
 }
 
-// sample and split weights bottom-up (DQTFactory.h:232-263): a leaf's is its
-// first moment over the decayed sample count, an inner node's the sum of its
-// children's in order
-static void dqtWeights(std::vector<DqtStatsNode> &nodes, uint32_t i, float invN) {
+// SphereToSquareCylindrical::area (SphereToSquare.h:57-59)
+static inline float dqtArea(const Box2 &r) { return 4.0f * float(M_PI) * (r.x1 - r.x0) * (r.y1 - r.y0); }
+
+// sample and split weights bottom-up (DQTFactory.h:232-263): a leaf's sample
+// weight is its first moment times 1 / (decayed sample count) (rejection
+// sampling) or times its solid angle / its own sample count (per leaf); its
+// split weight is the same (mean) or sqrt(solid angle * second moment); an
+// inner node's are the sums of its children's in order
+static void dqtWeights(std::vector<DqtStatsNode> &nodes, uint32_t i, Box2 rect, const DqtConfig &cfg, float numSamples) {
   DqtStatsNode &n = nodes[i];
   if (n.child > 0) {
-    for (uint32_t c = 0; c < 4; ++c) dqtWeights(nodes, nodes[i].child + c, invN);
+    for (uint32_t c = 0; c < 4; ++c) dqtWeights(nodes, nodes[i].child + c, rect.child(c), cfg, numSamples);
     DqtStatsNode &m = nodes[i];
     m.sampleWeight = 0.0f;
     m.splitWeight = 0.0f;
@@ -1510,19 +1516,30 @@ static void dqtWeights(std::vector<DqtStatsNode> &nodes, uint32_t i, float invN)
       m.splitWeight += nodes[m.child + c].splitWeight;
     }
   } else {
-    const float f = n.first * invN;
-    n.sampleWeight = f;
-    n.splitWeight = f;
+    const float k = cfg.leafEstimator == 0 ? 1.0f / numSamples : dqtArea(rect) / n.numSamples;
+    const float first = n.first * k, second = n.second * k;
+    n.sampleWeight = first;
+    n.splitWeight = cfg.splitMetric == 0 ? first : std::sqrt(dqtArea(rect) * second);
   }
 }
 
 static void dqtUpdate(DqtRegion &r, const Sample *S, size_t n, const DqtConfig &cfg) {  // DQTFactory.h:199-281
+  // the dispatch of DQTFactory.h:168-185 runs no branch for other values
+  if (!(cfg.footprintFactor >= 0.0f) || (cfg.leafEstimator != 0 && cfg.leafEstimator != 1) ||
+      (cfg.splitMetric != 0 && cfg.splitMetric != 1))
+    return;
   r.numSamples += float(n);
   const float ff = cfg.footprintFactor;
   for (size_t i = 0; i < n; ++i) {
     const Sample &s = S[i];
-    const float first = s.weight;
-    const float second = s.weight * s.weight * s.pdf;
+    float first, second;
+    if (cfg.leafEstimator == 0) {  // REJECTION_SAMPLING
+      first = s.weight;
+      second = s.weight * s.weight * s.pdf;
+    } else {  // PER_LEAF
+      first = s.weight * s.pdf;
+      second = first * first;
+    }
     float px, py;
     dqtDirToPoint(v3(s.dir[0], s.dir[1], s.dir[2]), px, py);
     auto apply = [&](DqtStatsNode &node, float w) {
@@ -1540,7 +1557,7 @@ static void dqtUpdate(DqtRegion &r, const Sample *S, size_t n, const DqtConfig &
       apply(r.stats[li], 1.0f);
     }
   }
-  dqtWeights(r.stats, 0, 1.0f / r.numSamples);
+  dqtWeights(r.stats, 0, Box2{0.f, 0.f, 1.f, 1.f}, cfg, r.numSamples);
   std::vector<DqtStatsNode> old;
   old.swap(r.stats);
   r.stats.resize(1);
@@ -2354,6 +2371,18 @@ void orc_field_set_parallax(void *h, int parallax) {
 void orc_field_set_dqt(void *h) {
   Field *f = static_cast<Field *>(h);
   f->surface.cfg.dqt = f->volume.cfg.dqt = true;
+}
+// PGLDQTFactoryArguments other than the defaults (config.h:95-102)
+void orc_field_set_dqt_args(void *h, int leafEstimator, int splitMetric, float splitThreshold, float footprintFactor,
+                            uint32_t maxLevels) {
+  Field *f = static_cast<Field *>(h);
+  for (SubField *s : {&f->surface, &f->volume}) {
+    s->dqtCfg.leafEstimator = leafEstimator;
+    s->dqtCfg.splitMetric = splitMetric;
+    s->dqtCfg.splitThreshold = splitThreshold;
+    s->dqtCfg.footprintFactor = footprintFactor;
+    s->dqtCfg.maxLevels = maxLevels;
+  }
 }
 
 // Volume queries with the Henyey-Greenstein product, query i with mean cosine g[i]

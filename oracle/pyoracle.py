@@ -48,6 +48,8 @@ def load():
         lib.orc_field_query_hg.argtypes = [vp, vp, vp, vp, u64]
         lib.orc_field_set_parallax.argtypes = [vp, ctypes.c_int]
         lib.orc_field_set_dqt.argtypes = [vp]
+        lib.orc_field_set_dqt_args.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                               ctypes.c_uint32]
         lib.orc_field_leaf_of.argtypes = [vp, ctypes.c_int, vp, vp, u64]
         lib.orc_field_set_scene_bounds.argtypes = [vp, vp]
         for n in ("orc_fexp", "orc_flog", "orc_rcp", "orc_rsqrt"):
@@ -60,15 +62,18 @@ def load():
 class OracleField:
     """Oracle restatement of a kd-tree field (deterministic CPU_8) with
     parallax-aware VMMs, plain VMMs (parallax=False) or directional quadtrees
-    (dqt=True)."""
+    (dqt=True; dqt_args as for run_reference)."""
 
-    def __init__(self, max_samples_per_leaf=32000, deterministic=True, threads=1, parallax=True, dqt=False):
+    def __init__(self, max_samples_per_leaf=32000, deterministic=True, threads=1, parallax=True, dqt=False,
+                 dqt_args=None):
         self.lib = load()
         self.h = self.lib.orc_field_new(int(deterministic), int(max_samples_per_leaf), int(threads))
         if not parallax:
             self.lib.orc_field_set_parallax(self.h, 0)
         if dqt:
             self.lib.orc_field_set_dqt(self.h)
+            if dqt_args:
+                self.lib.orc_field_set_dqt_args(self.h, *dqt_args)
 
     def close(self):
         if self.h:
@@ -154,11 +159,13 @@ def reference_available():
 
 
 def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministic=True, threads=1, device=8,
-                  parallax=True, dqt=False):
+                  parallax=True, dqt=False, dqt_args=None):
     """Runs the reference library on ``frames`` (list of sample arrays) and
     returns (field file bytes, per-frame update ms, surface query out, volume
     query out, volume query out with the Henyey-Greenstein product of mean
-    cosine hg_mean_cosines(n))."""
+    cosine hg_mean_cosines(n)).  ``dqt_args`` = (leafEstimator, splitMetric,
+    splitThreshold, footprintFactor, maxLevels) overrides the quadtree
+    factory's defaults."""
     import sys
 
     sys.path.insert(0, os.path.dirname(HERE))
@@ -179,6 +186,7 @@ def run_reference(frames, queries=None, max_samples_per_leaf=32000, deterministi
         env["PGL_ORACLE_THREADS"] = str(threads)
         env["PGL_REF_PLAIN_VMM"] = "0" if parallax else "1"
         env["PGL_REF_DQT"] = "1" if dqt else "0"
+        env["PGL_REF_DQT_ARGS"] = ",".join(repr(v) for v in dqt_args) if dqt_args else ""
         subprocess.run(args, check=True, env=env)
         field = open(os.path.join(td, "ref.field"), "rb").read()
         times = [float(x) for x in open(os.path.join(td, "ref.times")).read().split()]

@@ -78,6 +78,28 @@ int main(int argc, char **argv) {
   if (dqt && std::atoi(dqt) != 0) kind = PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE;
   openpgl::cpp::FieldConfig cfg;
   cfg.Init(PGL_SPATIAL_STRUCTURE_KDTREE, kind, deterministic, maxLeaf);
+  // PGL_REF_DQT_ARGS="leafEstimator,splitMetric,splitThreshold,footprintFactor,maxLevels"
+  // overrides the quadtree factory's defaults.  FieldConfig's only member is
+  // its PGLFieldArguments (cpp/FieldConfig.h:57-60), which the C++ API keeps
+  // private, so the harness reaches it through the object's address.
+  const char *dqtArgs = std::getenv("PGL_REF_DQT_ARGS");
+  if (kind == PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE && dqtArgs && *dqtArgs) {
+    static_assert(sizeof(openpgl::cpp::FieldConfig) == sizeof(PGLFieldArguments), "FieldConfig layout");
+    PGLFieldArguments *args = reinterpret_cast<PGLFieldArguments *>(&cfg);
+    PGLDQTFactoryArguments *d = static_cast<PGLDQTFactoryArguments *>(args->directionalDistributionArguments);
+    int le = 0, sm = 0;
+    unsigned levels = 12;
+    float thr = 0.01f, ff = 1.0f;
+    if (std::sscanf(dqtArgs, "%d,%d,%f,%f,%u", &le, &sm, &thr, &ff, &levels) != 5) {
+      std::fprintf(stderr, "bad PGL_REF_DQT_ARGS\n");
+      return 1;
+    }
+    d->leafEstimator = PGLDQTLeafEstimator(le);
+    d->splitMetric = PGLDQTSplitMetric(sm);
+    d->splitThreshold = thr;
+    d->footprintFactor = ff;
+    d->maxLevels = levels;
+  }
   openpgl::cpp::Field field(&device, cfg);
   openpgl::cpp::SampleStorage storage;
 

@@ -54,6 +54,11 @@ CASES = {
     # the directional quadtree field type (reference defaults of PGLDQTFactoryArguments)
     "cube_dqt": dict(gen="cube_face_samples", frames=[dict(n=32768, seed=140 + i, volume_fraction=0.25) for i in range(2)],
                      queries=dict(n=4096, seed=142), leaf=4000, dqt=True),
+    # its other branches: PER_LEAF estimator, SECOND_MOMENT metric, threshold 0.02,
+    # footprint 0.5, 8 levels
+    "cube_dqt_per_leaf": dict(gen="cube_face_samples",
+                              frames=[dict(n=32768, seed=150 + i, volume_fraction=0.25) for i in range(2)],
+                              queries=dict(n=4096, seed=152), leaf=4000, dqt=True, dqt_args=[1, 1, 0.02, 0.5, 8]),
 }
 
 
@@ -92,6 +97,7 @@ def main():
         frames, queries = build_inputs(case)
         field, _, sq, vq, hq = pyoracle.run_reference(frames, queries, max_samples_per_leaf=case["leaf"],
                                                       parallax=case.get("parallax", True), dqt=case.get("dqt", False),
+                                                      dqt_args=case.get("dqt_args"),
                                                   deterministic=True, threads=1, device=8)
         field = fieldfile.strip_timings(field)
         with gzip.open(os.path.join(HERE, f"{name}.field.gz"), "wb", compresslevel=9) as f:

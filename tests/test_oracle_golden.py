@@ -42,7 +42,7 @@ def _golden_path():
 
 def oracle_for(case):
     return pyoracle.OracleField(case["leaf"], deterministic=True, threads=4, parallax=case.get("parallax", True),
-                                dqt=case.get("dqt", False))
+                                dqt=case.get("dqt", False), dqt_args=case.get("dqt_args"))
 
 
 def golden(name):
@@ -130,15 +130,19 @@ def test_oracle_matches_live_reference_on_fresh_seed():
 
 
 @pytest.mark.skipif(not pyoracle.reference_available(), reason="reference library not built here")
-def test_oracle_quadtree_matches_live_reference_on_fresh_seed():
+@pytest.mark.parametrize("dqt_args", [None, (0, 0, 0.01, 0.0, 12), (1, 0, 0.01, 1.0, 12), (0, 1, 0.01, 1.0, 12),
+                                      (1, 1, 0.02, 0.5, 8), (0, 0, 0.003, 2.0, 6)])
+def test_oracle_quadtree_matches_live_reference_on_fresh_seed(dqt_args):
     """The directional quadtree field type (DQTFactory.h, DQT.h) on a fresh
-    seed: the same field file and the same query results."""
+    seed, at the default factory arguments and each branch of the factory's
+    dispatch (leaf estimator x split metric x zero / non-zero footprint,
+    DQTFactory.h:168-185): the same field file and the same query results."""
     from openpgl_gb300 import synthetic as syn
 
     frames = [syn.cube_face_samples(16000, 881 + i, volume_fraction=0.3) for i in range(3)]
     q = syn.queries(1024, 884)
-    field, _, rs, rv, rh = pyoracle.run_reference(frames, q, max_samples_per_leaf=2500, dqt=True)
-    orc = pyoracle.OracleField(2500, deterministic=True, threads=2, dqt=True)
+    field, _, rs, rv, rh = pyoracle.run_reference(frames, q, max_samples_per_leaf=2500, dqt=True, dqt_args=dqt_args)
+    orc = pyoracle.OracleField(2500, deterministic=True, threads=2, dqt=True, dqt_args=dqt_args)
     for f in frames:
         orc.update(f)
     assert fieldfile.strip_timings(orc.field_bytes()) == fieldfile.strip_timings(field)
