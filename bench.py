@@ -399,6 +399,7 @@ def run_gpu(args, rank, world, local_rank):
     import torch
 
     import openpgl_gb300 as pgl
+    from openpgl_gb300 import replicas
 
     torch.cuda.set_device(local_rank)
     frames = make_frames()
@@ -430,9 +431,7 @@ def run_gpu(args, rank, world, local_rank):
                         int(ph["regions"]) * 2 * REGION_STATE_BYTES
 
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
+        replicas.barrier("cuda")
 
     for _ in range(args.warmup):
         step()
@@ -513,11 +512,7 @@ def run_gpu(args, rank, world, local_rank):
     e2e_ms = e0.elapsed_time(e1) / args.steps
     e2e_wall = (time.perf_counter() - t0) * 1e3 / args.steps
 
-    # max over ranks
-    vals = torch.tensor([ms, e2e_ms, q_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(vals, op=torch.distributed.ReduceOp.MAX)
-    ms, e2e_ms, q_ms = vals.tolist()
+    ms, e2e_ms, q_ms = replicas.max_over_ranks([ms, e2e_ms, q_ms], "cuda")
     if rank != 0:
         return None
 
@@ -530,7 +525,7 @@ def run_gpu(args, rank, world, local_rank):
         traffic = EM_TRAFFIC_PER_SAMPLE * em_samples[0] / max(em_launches[0], 1)
     out = {
         "metric": METRIC,
-        "value": round(ms * UNIT_SAMPLES / (SAMPLES_PER_STEP * world), 3),
+        "value": round(replicas.whole_job_ms_per_unit(ms, SAMPLES_PER_STEP, UNIT_SAMPLES, world), 3),
         "unit": UNIT,
         "n_gpus": world,
         "steps": args.steps,
@@ -550,7 +545,8 @@ def run_gpu(args, rank, world, local_rank):
                      "algorithmic_bytes_per_launch": int(em_bytes_per_launch),
                      "em_share_of_step": round(em_ms[0] / args.steps / ms, 3),
                      "note": "EM is FP32/SFU-bound; HBM fraction shown against minimum algorithmic bytes"},
-        "e2e": {"value": round(e2e_ms * UNIT_SAMPLES / (SAMPLES_PER_STEP * world), 3), "unit": UNIT,
+        "e2e": {"value": round(replicas.whole_job_ms_per_unit(e2e_ms, SAMPLES_PER_STEP, UNIT_SAMPLES, world), 3),
+                "unit": UNIT,
                 "h2d_bytes_per_step": SAMPLES_PER_STEP * 40, "d2h_bytes_per_step": d2h[0] // max(args.steps, 1),
                 "wall_ms_per_step": round(e2e_wall, 3)},
         "queries": {"queries_per_s": round(QUERIES / (q_ms * 1e-3)), "batch": QUERIES,
@@ -633,16 +629,15 @@ def main():
     if args.impl == "reference":
         out = run_reference(args, rank, world)
     else:
+        from openpgl_gb300 import replicas
+
         if world > 1:
             import torch
 
             torch.cuda.set_device(local_rank)
-            torch.distributed.init_process_group("nccl")
+            replicas.init("nccl")
         out = run_gpu(args, rank, world, local_rank)
-        if world > 1:
-            import torch
-
-            torch.distributed.destroy_process_group()
+        replicas.shutdown()
     if out is not None:
         print(json.dumps(out), flush=True)
 
