@@ -27,7 +27,7 @@ def barrier(device=None):
     if active():
         dist.barrier()
     if device is not None and torch.device(device).type == "cuda":
-        torch.cuda.synchronize(device)
+        torch.cuda.synchronize()
 
 
 def max_over_ranks(values, device="cpu"):
