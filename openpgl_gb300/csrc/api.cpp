@@ -84,8 +84,13 @@ static_assert(sizeof(PGLGuidedQueryResult) == sizeof(QueryOut), "query result la
 FieldConfig config_from(const PGLFieldArguments &args) {  // Device.h:99-136
   if (args.spatialStructureType != PGL_SPATIAL_STRUCTURE_KDTREE ||
       (args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM &&
-       args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_VMM))
+       args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_VMM)) {
+    // the field takes ownership of the argument structs (Device.h:109,136,184-207), refused or not
+    delete static_cast<PGLKDTreeArguments *>(args.spatialSturctureArguments);
+    if (args.directionalDistributionType == PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE)
+      delete static_cast<PGLDQTFactoryArguments *>(args.directionalDistributionArguments);
     throw std::runtime_error("only kd-tree fields with (parallax-aware) VMMs run on the GPU");
+  }
   FieldConfig c;
   // Device.h:139-178: the plain VMM is the same mixture without parallax compensation
   c.parallax = args.directionalDistributionType == PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM ? 1u : 0u;
