@@ -106,3 +106,19 @@ def leaf_log_likelihoods(field_bytes, samples, side="surface"):
         t = ww[good] * np.log(pdf[good])
         out[r] = (float(t.sum()), float(np.abs(t).sum()))
     return out
+
+
+def poisoned_frames():
+    """Two frames; the second carries samples with NaN directions, NaN
+    weights, infinite distances and zero weights."""
+    from openpgl_gb300 import synthetic as syn
+
+    frames = [syn.cube_face_samples(20000, 991 + i, volume_fraction=0.3) for i in range(2)]
+    f = frames[1].copy()
+    idx = np.random.default_rng(5).choice(len(f), 12, replace=False)
+    f["direction"][idx[:3]] = np.nan
+    f["weight"][idx[3:6]] = np.nan
+    f["distance"][idx[6:9]] = np.inf
+    f["weight"][idx[9:12]] = 0.0
+    frames[1] = f
+    return frames

@@ -1,5 +1,5 @@
 """GPU parity: the GB300 library against the oracle (a bit-exact CPU
-restatement of the reference, pinned by tests/test_oracle_reference.py) on
+restatement of the reference, pinned by tests/test_oracle_golden.py) on
 seeded inputs.
 
 Bar (per the field's specification): kd-tree split planes, leaf sample counts
@@ -107,6 +107,38 @@ def test_guided_queries_match_oracle(pgl):
     assert np.quantile(rel, 0.999) <= PDF_TOL, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
     ang = np.abs(out["dir"][ok] - ref["dir"][ok]).max(axis=1)
     assert np.quantile(ang, 0.999) <= 1e-3
+
+
+def test_poisoned_samples_flag_the_oracles_regions(pgl):
+    """Samples with NaN directions or weights, infinite distances and zero
+    weights in the second frame: the Update completes, the tree and the sample
+    statistics are the oracle's, the same regions are flagged invalid (the
+    oracle flags the reference's, tests/test_oracle_golden.py), and guided
+    queries agree."""
+    import fieldfile
+    from helpers import poisoned_frames
+    from openpgl_gb300 import synthetic as syn
+
+    dev, field, orc = _train(pgl, poisoned_frames(), 3000)
+    a, b = field.field_bytes(), orc.field_bytes()
+    invalid = 0
+    for side in ("surface", "volume"):
+        r = compare_fields(a, b, side)
+        assert r["tree_equal"] and r["stats_equal"], (side, r)
+        va = [x["valid"] for x in fieldfile.read_field_file(a)[side]["regions"]]
+        vb = [x["valid"] for x in fieldfile.read_field_file(b)[side]["regions"]]
+        assert va == vb, side
+        invalid += vb.count(False)
+    assert invalid > 0
+    q = syn.queries(2048, 993)
+    for volume in (False, True):
+        out = field.sample_batch(q, volume=volume, cosine=not volume)
+        ref = orc.query(q, volume=volume, cosine=not volume)
+        assert np.array_equal(out["ok"], ref["ok"]), volume
+        assert np.array_equal(out["id"], ref["id"]), volume
+        ok = ref["ok"] == 1
+        rel = np.abs(out["pdf"][ok] - ref["pdf"][ok]) / ref["pdf"][ok]
+        assert np.quantile(rel, 0.999) <= PDF_TOL, volume
 
 
 def test_per_object_api_matches_batch(pgl):

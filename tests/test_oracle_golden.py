@@ -149,3 +149,49 @@ def test_oracle_quadtree_matches_live_reference_on_fresh_seed(dqt_args):
     assert orc.query(q).tobytes() == rs.tobytes()
     assert orc.query(q, volume=True, cosine=False).tobytes() == rv.tobytes()
     assert orc.query_hg(q, pyoracle.hg_mean_cosines(len(q))).tobytes() == rh.tobytes()
+
+
+def region_flags(field_bytes, side):
+    f = fieldfile.read_field_file(field_bytes)[side]
+    return np.array([r["valid"] for r in f["regions"]]), fieldfile.canonical_tree(f)
+
+
+@pytest.mark.skipif(not pyoracle.reference_available(), reason="reference library not built here")
+@pytest.mark.parametrize("dqt", [False, True])
+def test_oracle_poisoned_samples_like_reference(dqt):
+    """Poisoned samples (NaN direction or weight, infinite distance, zero
+    weight) invalidate the same regions in the oracle as in the reference, and
+    guided queries give the same results.  For quadtrees the whole field file is
+    identical.  For VMMs the invalidated regions' mixtures are not compared:
+    the reference's 8-wide SIMD EM and the oracle's lane loop carry NaNs
+    through different lanes, so those regions' bytes differ while the tree,
+    the sample statistics, the validity flags and every query agree."""
+    from openpgl_gb300 import synthetic as syn
+
+    from helpers import poisoned_frames
+
+    frames = poisoned_frames()
+    q = syn.queries(2048, 993)
+    field, _, rs, rv, _ = pyoracle.run_reference(frames, q, max_samples_per_leaf=3000, dqt=dqt)
+    orc = pyoracle.OracleField(3000, deterministic=True, threads=2, dqt=dqt)
+    for f in frames:
+        orc.update(f)
+    mine = fieldfile.strip_timings(orc.field_bytes())
+    ref = fieldfile.strip_timings(field)
+    if dqt:
+        assert mine == ref
+    invalid = 0
+    for side in ("surface", "volume"):
+        va, ca = region_flags(mine, side)
+        vb, cb = region_flags(ref, side)
+        assert np.array_equal(ca["dim"], cb["dim"]) and np.array_equal(ca["split"], cb["split"])
+        assert np.array_equal(va, vb)
+        invalid += int((~va).sum())
+        A = fieldfile.read_field_file(mine)[side]["regions"]
+        B = fieldfile.read_field_file(ref)[side]["regions"]
+        for ra, rb in zip(A, B):
+            for key in ("mean", "var", "bounds"):
+                assert ra["stats"][key].tobytes() == rb["stats"][key].tobytes()
+    assert invalid > 0 or dqt  # the poison reached at least one VMM region
+    assert orc.query(q).tobytes() == rs.tobytes()
+    assert orc.query(q, volume=True, cosine=False).tobytes() == rv.tobytes()
