@@ -73,6 +73,11 @@ OPENPGL_CORE_INTERFACE void *pglDeviceGetCudaStream(PGLDevice device);
 // Number of the library's own CUDA kernels launched so far by this process
 // (the scan and sort kernels of CUB that it calls are not counted).
 OPENPGL_CORE_INTERFACE uint64_t pglGetKernelLaunchCount();
+// Failure detection without a GPU fault: one device thread waits, with the
+// EM kernel's bounded wait, on a flag that nothing sets; the wait gives up
+// after limitNs (at most 10 s) and records its error.  Returns that error
+// code (2: the wait ran out) or -1 on a CUDA error (pglGetLastError()).
+OPENPGL_CORE_INTERFACE int pglDebugBoundedWaitRunsOut(uint64_t limitNs);
 // Per-region counters of the last Update: region, EM iterations, splits,
 // merges, components (5 x u32 per region); returns the region count, writes
 // when capacity >= 5 x count.

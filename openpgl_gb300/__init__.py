@@ -151,6 +151,7 @@ C_API = {
                                                       ctypes.c_size_t]),
     "pglDeviceGetCudaStream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "pglGetKernelLaunchCount": (ctypes.c_uint64, []),
+    "pglDebugBoundedWaitRunsOut": (ctypes.c_int, [ctypes.c_uint64]),
     "pglNewGuidingServer": (ctypes.c_void_p, [ctypes.c_void_p, ctypes.c_size_t]),
     "pglReleaseGuidingServer": (None, [ctypes.c_void_p]),
     "pglGuidingServerSubmit": (ctypes.c_uint64, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
@@ -219,6 +220,16 @@ def load(build_if_missing=True):
 def kernel_launch_count():
     """Kernels of this library launched so far by the process."""
     return int(load().pglGetKernelLaunchCount())
+
+
+def bounded_wait_runs_out(limit_ns):
+    """One device thread waits, with the EM kernel's bounded wait, on a flag
+    that nothing sets; returns the error code the wait recorded (2: it ran out
+    after limit_ns).  Raises on a CUDA error."""
+    code = int(load().pglDebugBoundedWaitRunsOut(int(limit_ns)))
+    if code < 0:
+        raise RuntimeError(last_error())
+    return code
 
 
 def split_samples_device_noalloc(d_samples, n, d_surface, d_volume, d_counts, stream=None):

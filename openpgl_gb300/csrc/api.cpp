@@ -833,6 +833,14 @@ OPENPGL_CORE_INTERFACE bool pglGuidingServerStats(PGLGuidingServer server, doubl
   PGL_CATCH(false)
 }
 OPENPGL_CORE_INTERFACE uint64_t pglGetKernelLaunchCount() { return kernel_launches(); }
+OPENPGL_CORE_INTERFACE int pglDebugBoundedWaitRunsOut(uint64_t limitNs) {
+  PGL_TRY
+  if (limitNs > 10000000000ull) throw std::runtime_error("pglDebugBoundedWaitRunsOut: limit above 10 s");
+  int code = 0;
+  check(em_bounded_wait_probe(limitNs, &code, Context::get().stream), "bounded wait probe");
+  return code;
+  PGL_CATCH(-1)
+}
 OPENPGL_CORE_INTERFACE void *pglDeviceGetCudaStream(PGLDevice device) {
   PGL_TRY
   (void)device;

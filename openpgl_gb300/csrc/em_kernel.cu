@@ -1148,8 +1148,9 @@ __device__ __forceinline__ void bar_named(int id, int threads) {
 __device__ __forceinline__ void set_error(int *err, int code) { atomicCAS(err, 0, code); }
 __device__ __forceinline__ bool has_error(const int *err) { return *reinterpret_cast<const volatile int *>(err) != 0; }
 
-// Spins until *p >= want (true) or the launch failed / the wait ran out.
-__device__ bool wait_at_least(const uint32_t *p, uint32_t want, int *err) {
+// Spins until *p >= want (true) or the launch failed / the wait ran out
+// (after limitNs; the launch's error word then holds kErrSlotWait).
+__device__ bool wait_at_least(const uint32_t *p, uint32_t want, int *err, unsigned long long limitNs = kWaitNs) {
   unsigned long long t0 = 0;
   unsigned sleep = 64;
   for (uint32_t it = 0;; ++it) {
@@ -1158,7 +1159,7 @@ __device__ bool wait_at_least(const uint32_t *p, uint32_t want, int *err) {
       if (has_error(err)) return false;
       const unsigned long long now = global_ns();
       if (t0 == 0) t0 = now;
-      else if (now - t0 > kWaitNs) {
+      else if (now - t0 > limitNs) {
         set_error(err, kErrSlotWait);
         return false;
       }
@@ -2314,6 +2315,30 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Em
 }
 
 PGL_DEFINE_TABLE_UPLOAD(em_upload_tables)
+
+// One thread waits, with the EM kernel's bounded wait, on a flag that nothing
+// sets: the wait gives up after limitNs and records its error in *err.
+__global__ void bounded_wait_probe_kernel(const uint32_t *flag, int *err, unsigned long long limitNs) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) wait_at_least(flag, 1u, err, limitNs);
+}
+cudaError_t em_bounded_wait_probe(unsigned long long limitNs, int *errOut, cudaStream_t s) {
+  uint32_t *flag = nullptr;
+  int *err = nullptr;
+  cudaError_t e = cudaMalloc(&flag, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(flag, 0, sizeof(uint32_t), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), s);
+  if (e == cudaSuccess) {
+    bounded_wait_probe_kernel<<<1, 32, 0, s>>>(flag, err, limitNs);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(errOut, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (flag) cudaFree(flag);
+  if (err) cudaFree(err);
+  return e;
+}
 
 size_t em_shared_bytes() { return sizeof(EmShared); }
 

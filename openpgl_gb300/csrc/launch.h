@@ -36,6 +36,9 @@ cudaError_t split_samples_noalloc(const PGLSampleRecord *in, size_t n, PGLSample
                                   uint32_t *counts, cudaStream_t s);
 
 cudaError_t em_upload_tables();
+// Launches one thread that waits, with the EM kernel's bounded wait, on a flag
+// nothing sets; *errOut receives the error the wait recorded (2: it ran out).
+cudaError_t em_bounded_wait_probe(unsigned long long limitNs, int *errOut, cudaStream_t s);
 cudaError_t spatial_upload_tables();
 cudaError_t query_upload_tables();
 
