@@ -1,8 +1,8 @@
 // ORACLE (test infrastructure only).  A CPU restatement of Open PGL v0.6.0's
-// field-training and guided-query path (kd-tree PA-VMM field,
-// FieldConfig::Init(KDTREE, PARALLAX_AWARE_VMM, deterministic, maxLeaf),
-// device type CPU_8), written to reproduce the reference's arithmetic in
-// the reference's order:
+// field-training and guided-query path (kd-tree field,
+// FieldConfig::Init(KDTREE, PARALLAX_AWARE_VMM | VMM | QUADTREE,
+// deterministic, maxLeaf), device type CPU_8), written to reproduce the
+// reference's arithmetic in the reference's order:
 //  * 8-lane SIMD vectors are emulated lane by lane; horizontal sums follow the
 //    vfloat8 reduce tree ((0+1)+(2+3))+((4+5)+(6+7))
 //    (third-party/embreeSrc/common/simd/vfloat8_avx.h:677-683);
@@ -12,7 +12,9 @@
 //  * fastapprox exp/log/sin/acos restate the published ispc/syrah polynomials
 //    (math/transcendental.h:333-472);
 //  * float expressions that C++ promotes to double (M_PI literals) are
-//    evaluated in double, as the reference's compiler does.
+//    evaluated in double, as the reference's compiler does;
+//  * the quadtree's sphere-to-square map calls the C library's atan2f, cosf
+//    and sinf, as the reference does (directional/dqt/SphereToSquare.h).
 // It is compiled with -ffp-contract=off, like oracle/_ref.  Only tests/,
 // __graft_entry__.smoke() and bench.py's CPU baseline use it.
 #include <algorithm>
