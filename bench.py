@@ -62,15 +62,33 @@ WORKLOAD = ("multi-frame: 8 frames x 2,097,152 samples (25% inside-volume, cube 
 # (3008 B) read and written once
 EM_BYTES_PER_SAMPLE = 32
 REGION_STATE_BYTES = 3008
-# DRAM bytes (read + write) per sample of one EM launch, from the ncu capture summarised in
-# profiles/em_leaf_kernel_multiframe_131k.md (7.70 MB for 131,072 samples); traffic scales with
-# the samples of a launch
-EM_TRAFFIC_PER_SAMPLE = 58.7
 
 
 # the port against the compiled reference (CPU_8, AVX2) on x86, first frame
 # of this workload, 8 threads: 2005 ms against 518 ms
 PORT_NOTE = "oracle port; the compiled reference ran 3.3-3.9x faster than this port per frame on x86"
+
+
+def host_info():
+    """Host cores and CPU model string (lscpu, else /proc/cpuinfo)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if model is None:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"nproc": os.cpu_count(), "cpu_model": model or "unknown", "machine": os.uname().machine}
 
 
 def frame_seed(f):
@@ -293,8 +311,9 @@ def run_widened(pgl, dev, stream, field, queries, frames, d_frames, steps, warmu
 # ----------------------------------------------------------------- CPU baseline
 def cpu_baseline(frames, budget_s=20.0, threads=None):
     """Times the oracle (the CPU restatement of the reference's Update, with the
-    reference's arithmetic) on the first frames of the workload, as many as
-    fit in about budget_s, and scales to ms per 16M samples."""
+    reference's arithmetic) on the frames of the workload, as many as fit in
+    about budget_s, and scales to ms per 16M samples.  Returns the baseline
+    and the oracle field (trained on all frames when they fit)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
@@ -308,27 +327,40 @@ def cpu_baseline(frames, budget_s=20.0, threads=None):
         done += 1
         if t_total >= budget_s:
             break
-    orc.close()
     samples = done * FRAME_SAMPLES
     value = t_total * 1e3 * UNIT_SAMPLES / samples
-    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"frames 1-{done} of 8 ({samples} samples, fresh field), oracle Update wall time scaled to "
-                      f"16,777,216 samples",
-            "note": PORT_NOTE}
+    return ({"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+             "sample": f"frames 1-{done} of 8 ({samples} samples, fresh field), oracle Update wall time scaled to "
+                       f"16,777,216 samples",
+             "note": PORT_NOTE, "host": host_info()}, orc if done == len(frames) else None)
 
 
-def cpu_queries(frames, queries, threads=None, n=131072):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
+def parity_block(orc, gpu_field_bytes, gpu_queries, queries):
+    """The GPU's field after the timed step against the oracle's field trained
+    on the same frames (surface and volume: tree, numbering and leaf sample
+    statistics equal, regions with equal mixture bytes, worst per-leaf
+    relative PDF error on the 64x64 grid, leaves above 1e-3 and lobe-count
+    flips), and the GPU's guided-query batch against the oracle's on the same
+    queries (ok flags, region ids and sample1D bits equal, worst pdf error).
+    Also times the oracle's queries on 131,072 of them."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import compare_fields, compare_queries
 
-    threads = threads or os.cpu_count()
-    orc = pyoracle.OracleField(MAX_SAMPLES_PER_LEAF, deterministic=True, threads=threads)
-    orc.update(frames[0])
+    out = {}
+    for side in ("surface", "volume"):
+        r = compare_fields(gpu_field_bytes, orc.field_bytes(), side)
+        out[side] = {k: r.get(k) for k in ("tree_equal", "numbering_equal", "stats_equal", "regions",
+                                           "bit_exact_regions", "worst_pdf_rel")}
+        out[side]["leaves_over_1e-3"] = r.get("over_tol", [])[:8]
+        out[side]["k_flips"] = r.get("k_flips", [])[:8]
+    n = 131072
     t0 = time.perf_counter()
     orc.query(queries[:n])
-    dt = time.perf_counter() - t0
-    orc.close()
-    return n / dt
+    qps = n / (time.perf_counter() - t0)
+    ref = orc.query(queries)
+    out["queries"] = compare_queries(gpu_queries, ref)
+    out["queries"]["count"] = len(queries)
+    return out, qps
 
 
 # ----------------------------------------------------------------- serving
@@ -411,24 +443,12 @@ def run_gpu(args, rank, world, local_rank):
     d_frames = [torch.from_numpy(f.view(np.uint8)).to("cuda") for f in frames]
     torch.cuda.synchronize()
 
-    em_ms, em_launches, em_bytes, em_samples = [0.0], [0], [0], [0]
-
-    def step(record=False):
+    def step():
         field.reset()
         for f, d in zip(frames, d_frames):
             storage.clear()
             storage.add_samples_device(d.data_ptr(), len(f))
             field.update(storage)
-            if record:
-                # one EM launch serves both sub-fields of an Update (both report its time)
-                live = [ph for ph in (field.phases(False), field.phases(True)) if ph["samples"] > 0]
-                if live:
-                    em_ms[0] += live[0]["em_kernel"]
-                    em_launches[0] += 1
-                for ph in live:
-                    em_samples[0] += int(ph["samples"])
-                    em_bytes[0] += int(ph["samples"]) * EM_BYTES_PER_SAMPLE + \
-                        int(ph["regions"]) * 2 * REGION_STATE_BYTES
 
     def barrier():
         replicas.barrier("cuda")
@@ -442,12 +462,17 @@ def run_gpu(args, rank, world, local_rank):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for _ in range(args.steps):
-        step(record=True)
+        step()
     ev1.record(stream)
     barrier()
     launches = pgl.kernel_launch_count() - launches0
     ms = ev0.elapsed_time(ev1) / args.steps
     clk = clocks.stop()
+    gpu_field_bytes = field.field_bytes()
+    # one more (untimed) step for the EM launch's counters: its CUDA-event time
+    # per Update and the work its passes did (the step is deterministic, so the
+    # timed steps did the same work)
+    em_work = em_counters(field, storage, frames, d_frames)
 
     # ---- guided queries on the trained field (device buffers)
     qdev = torch.from_numpy(queries.view(np.uint8)).to("cuda")
@@ -467,6 +492,8 @@ def run_gpu(args, rank, world, local_rank):
     torch.cuda.synchronize()
     lat_ms = sorted(a.elapsed_time(b) for a, b in lat)
     q_ms = statistics.median(lat_ms)
+    gpu_queries = np.frombuffer(rdev.cpu().numpy().tobytes(), dtype=pgl.QUERY_RESULT_DTYPE).copy()
+    query_work = query_counters(field, gpu_queries)
     # host-buffer queries (copies inside)
     t0 = time.perf_counter()
     for _ in range(reps):
@@ -475,8 +502,10 @@ def run_gpu(args, rank, world, local_rank):
 
     # ---- rows beyond the core path: HG queries, path-segment samples, plain VMM,
     # and the plain drop-in form of the Update beside the batched one
-    widened = run_widened(pgl, dev, stream, field, queries, frames, d_frames, args.steps, args.warmup)
-    widened["plain_update"]["batched_speedup"] = round(widened["plain_update"]["value"] / ms, 2)
+    widened = None
+    if args.widened:
+        widened = run_widened(pgl, dev, stream, field, queries, frames, d_frames, args.steps, args.warmup)
+        widened["plain_update"]["batched_speedup"] = round(widened["plain_update"]["value"] / ms, 2)
 
     # ---- clustered workload, default and autotuned EM schedule
     clustered = run_clustered(pgl, dev, stream, args.steps, 1) if args.clustered else None
@@ -516,13 +545,12 @@ def run_gpu(args, rank, world, local_rank):
     if rank != 0:
         return None
 
-    em_avg_ms = em_ms[0] / max(em_launches[0], 1)
-    em_bytes_per_launch = em_bytes[0] / max(em_launches[0], 1)
-    achieved = em_bytes_per_launch / (em_avg_ms * 1e-3) / 1e9
-    peak = measured_peak("hbm_gbs", 6800.0)
-    traffic = None
-    if EM_TRAFFIC_PER_SAMPLE is not None:
-        traffic = EM_TRAFFIC_PER_SAMPLE * em_samples[0] / max(em_launches[0], 1)
+    sm_mhz = clk.get("sm_mhz") or measured_peak("sm_max_mhz", 2070.0)[0]
+    roofline = em_roofline(em_work, sm_mhz, ms)
+    query_roof = kernel_roofline(query_work["flop"], query_work["sfu"], query_work["bytes"], q_ms, sm_mhz)
+    query_roof.update(kernel="query_kernel", mean_lobes=query_work["mean_lobes"],
+                      work="per query with K lobes and one SamplePDF: 62K + (50 + 12K) + 64 flop, "
+                           "7K + (6 + K) SFU, 36 B in + 32 B out")
     out = {
         "metric": METRIC,
         "value": round(replicas.whole_job_ms_per_unit(ms, SAMPLES_PER_STEP, UNIT_SAMPLES, world), 3),
@@ -539,12 +567,7 @@ def run_gpu(args, rank, world, local_rank):
         "config": {"workload": WORKLOAD, "samples_per_step": SAMPLES_PER_STEP, "frames": FRAMES,
                    "max_samples_per_leaf": MAX_SAMPLES_PER_LEAF, "l2": "inputs (671 MB) larger than L2",
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"kernel": "em_leaf_kernel", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak[0],
-                     "peak_source": peak[1], "unit": "GB/s", "frac": round(achieved / peak[0], 4),
-                     "traffic": traffic, "avg_launch_ms": round(em_avg_ms, 3),
-                     "algorithmic_bytes_per_launch": int(em_bytes_per_launch),
-                     "em_share_of_step": round(em_ms[0] / args.steps / ms, 3),
-                     "note": "EM is FP32/SFU-bound; HBM fraction shown against minimum algorithmic bytes"},
+        "roofline": roofline,
         "e2e": {"value": round(replicas.whole_job_ms_per_unit(e2e_ms, SAMPLES_PER_STEP, UNIT_SAMPLES, world), 3),
                 "unit": UNIT,
                 "h2d_bytes_per_step": SAMPLES_PER_STEP * 40, "d2h_bytes_per_step": d2h[0] // max(args.steps, 1),
@@ -552,7 +575,7 @@ def run_gpu(args, rank, world, local_rank):
         "queries": {"queries_per_s": round(QUERIES / (q_ms * 1e-3)), "batch": QUERIES,
                     "p50_ms": round(statistics.median(lat_ms), 3),
                     "p99_ms": round(lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))], 3),
-                    "e2e_queries_per_s": round(QUERIES / (q_e2e_ms * 1e-3))},
+                    "e2e_queries_per_s": round(QUERIES / (q_e2e_ms * 1e-3)), "roofline": query_roof},
         "serving": serving,
         "clustered": clustered,
         "widened": widened,
@@ -560,9 +583,133 @@ def run_gpu(args, rank, world, local_rank):
         "clocks": clk,
     }
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(frames, budget_s=args.cpu_budget)
-        out["cpu_baseline"]["queries_per_s"] = round(cpu_queries(frames, queries))
+        out["cpu_baseline"], orc = cpu_baseline(frames, budget_s=args.cpu_budget)
+        if orc is not None:
+            out["parity"], qps = parity_block(orc, gpu_field_bytes, gpu_queries, queries)
+            out["cpu_baseline"]["queries_per_s"] = round(qps)
+            orc.close()
     return out
+
+
+# ----------------------------------------------------------------- roofline
+# Counting convention of the path's measurement: an exp, log, sqrt, rsqrt, rcp
+# or sincos is one SFU op, a division one rcp plus one FMA, an FMA two flop.
+ESTEP_FLOP_LOBE, ESTEP_SFU_LOBE = 21, 1      # per (sample, lobe, E-step pass)
+ESTEP_FLOP_SAMPLE, ESTEP_SFU_SAMPLE = 4, 2   # per (sample, E-step pass)
+DIST_FLOP_LOBE, DIST_SFU_LOBE = 30, 1        # per (sample, lobe) of a distance pass
+SPLIT_FLOP_LOBE, SPLIT_SFU_LOBE = 70, 3      # per (sample, lobe) of a split-statistics pass
+SMS, FP32_LANES_PER_SM, SFU_PER_SM = 152, 128, 16
+
+
+def derived_peaks(sm_mhz):
+    """FP32 and SFU peaks derived from the SM count, the lanes per SM (128
+    FP32, 16 SFU per clock) and the SM clock measured during the run (FMA = 2
+    flop); HBM from the measured copy bandwidth."""
+    hz = sm_mhz * 1e6
+    hbm, src = measured_peak("hbm_gbs", 6800.0)
+    return {"fp32_tflops": SMS * FP32_LANES_PER_SM * 2 * hz / 1e12, "sfu_tops": SMS * SFU_PER_SM * hz / 1e12,
+            "hbm_gbs": hbm, "hbm_source": src, "sm_mhz": sm_mhz}
+
+
+def kernel_roofline(flop, sfu, nbytes, ms, sm_mhz):
+    """t_roof = max(F / F_peak, SFU / SFU_peak, B / B_peak) for one launch of
+    `ms` milliseconds; the binding resource names the bound, `achieved` is that
+    resource's rate and `frac` = t_roof / t_measured."""
+    p = derived_peaks(sm_mhz)
+    t = {"fp32": flop / (p["fp32_tflops"] * 1e12), "sfu": sfu / (p["sfu_tops"] * 1e12),
+         "hbm": nbytes / (p["hbm_gbs"] * 1e9)}
+    bound = max(t, key=t.get)
+    sec = ms * 1e-3
+    rate = {"fp32": (flop / sec / 1e12, p["fp32_tflops"], "TFLOP/s", "derived"),
+            "sfu": (sfu / sec / 1e12, p["sfu_tops"], "Tops/s", "derived"),
+            "hbm": (nbytes / sec / 1e9, p["hbm_gbs"], "GB/s", p["hbm_source"])}
+    a, peak, unit, src = rate[bound]
+    return {"bound": bound, "achieved": round(a, 4), "peak": round(peak, 2), "unit": unit, "peak_source": src,
+            "frac": round(t[bound] / sec, 5), "t_roof_ms": round(t[bound] * 1e3, 5), "avg_launch_ms": round(ms, 4),
+            "per_resource_frac": {k: round(v / sec, 5) for k, v in t.items()},
+            "algorithmic": {"flop": int(flop), "sfu": int(sfu), "bytes": int(nbytes)}}
+
+
+def em_counters(field, storage, frames, d_frames):
+    """One step, keeping per Update the EM launch's CUDA-event time and the
+    algorithmic work of its passes (per-region pass and lobe counters of the
+    launch's profile)."""
+    import torch
+
+    out = []
+    field.reset()
+    for f, d in zip(frames, d_frames):
+        storage.clear()
+        storage.add_samples_device(d.data_ptr(), len(f))
+        field.update(storage)
+        torch.cuda.synchronize()
+        live = [(v, field.phases(v)) for v in (False, True)]
+        live = [(v, ph) for v, ph in live if ph["samples"] > 0]
+        if not live:
+            continue
+        flop = sfu = nbytes = samples = 0
+        for v, ph in live:
+            prof = field.profile(v).astype(np.float64)
+            cnt, ep, el, dl, sl = prof[:, 1], prof[:, 2], prof[:, 18], prof[:, 19], prof[:, 20]
+            flop += float((cnt * (ESTEP_FLOP_LOBE * el + ESTEP_FLOP_SAMPLE * ep + DIST_FLOP_LOBE * dl
+                                  + SPLIT_FLOP_LOBE * sl)).sum())
+            sfu += float((cnt * (ESTEP_SFU_LOBE * el + ESTEP_SFU_SAMPLE * ep + DIST_SFU_LOBE * dl
+                                 + SPLIT_SFU_LOBE * sl)).sum())
+            nbytes += int(ph["samples"]) * EM_BYTES_PER_SAMPLE + int(ph["regions"]) * 2 * REGION_STATE_BYTES
+            samples += int(ph["samples"])
+        # one EM launch serves both sub-fields of an Update (both report its time)
+        out.append({"ms": live[0][1]["em_kernel"], "update_ms": max(ph["total"] for _, ph in live),
+                    "flop": flop, "sfu": sfu, "bytes": nbytes, "samples": samples})
+    return out
+
+
+def em_roofline(work, sm_mhz, step_ms):
+    """Roofline of the average EM launch of a step (the dominant kernel)."""
+    n = max(len(work), 1)
+    avg = {k: sum(w[k] for w in work) / n for k in ("ms", "flop", "sfu", "bytes", "samples")}
+    r = kernel_roofline(avg["flop"], avg["sfu"], avg["bytes"], avg["ms"], sm_mhz)
+    r["kernel"] = "em_leaf_kernel"
+    r["launches_per_step"] = len(work)
+    r["em_share_of_step"] = round(sum(w["ms"] for w in work) / step_ms, 3)
+    r["per_launch_ms"] = [round(w["ms"], 3) for w in work]
+    r["traffic"] = None
+    r["work"] = ("per (sample, lobe, E-step pass) 21 flop + 1 SFU; per (sample, E-step pass) 4 flop + 2 SFU; "
+                 "per (sample, lobe) of a distance pass 30 flop + 1 SFU, of a split-statistics pass 70 flop + "
+                 "3 SFU; 32 B per sample and 2 x 3008 B per region of HBM; pass and lobe counts from the "
+                 "launch's own per-region counters")
+    return r
+
+
+def query_counters(field, out):
+    """Algorithmic work of the guided-query batch from the lobe count of each
+    query's region (the last Update's per-region reports)."""
+    rep = field.reports(False)
+    k_of = {int(r[0]): int(r[4]) for r in rep}
+    ok = out["ok"] == 1
+    ks = np.array([k_of.get(int(i), 0) for i in out["id"][ok]], dtype=np.float64)
+    flop = float((62 * ks + 50 + 12 * ks + 64).sum())
+    sfu = float((7 * ks + 6 + ks).sum())
+    return {"flop": flop, "sfu": sfu, "bytes": len(out) * (36 + 32), "mean_lobes": round(float(ks.mean()), 2)
+            if len(ks) else 0.0}
+
+
+def em_capture():
+    """One Update of a fresh field on the first frame of the workload (2,097,152
+    samples), for a profiler to capture that Update's EM launch."""
+    import torch
+
+    import openpgl_gb300 as pgl
+    from openpgl_gb300 import synthetic as syn
+
+    frame = syn.cube_face_samples(FRAME_SAMPLES, frame_seed(0), volume_fraction=0.25)
+    d = torch.from_numpy(frame.view(np.uint8)).to("cuda")
+    dev = pgl.Device()
+    field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF))
+    storage = pgl.SampleStorage()
+    storage.add_samples_device(d.data_ptr(), len(frame))
+    field.update(storage)
+    torch.cuda.synchronize()
+    field.release()
 
 
 def measured_peak(key, fallback):
@@ -585,28 +732,45 @@ def run_reference(args, rank, world):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
-    # each step: a fresh field trained on the first frame (a bounded sample of
-    # the workload), scaled to ms per 16M samples
-    for _ in range(args.warmup):
-        pass
-    times = []
-    for _ in range(args.steps):
+    # each step is the GPU arm's step: a fresh field, then for every frame of
+    # the workload an Update on that frame's samples
+    def step():
         orc = pyoracle.OracleField(MAX_SAMPLES_PER_LEAF, deterministic=True, threads=threads)
         t0 = time.perf_counter()
-        orc.update(frames[0])
-        times.append(time.perf_counter() - t0)
-        orc.close()
-    ms = statistics.median(times) * 1e3
-    value = ms * UNIT_SAMPLES / FRAME_SAMPLES
+        for f in frames:
+            orc.update(f)
+        dt = time.perf_counter() - t0
+        return orc, dt
+
+    for _ in range(args.warmup):
+        step()[0].close()
+    times = []
+    orc = None
+    for _ in range(args.steps):
+        if orc is not None:
+            orc.close()
+        orc, dt = step()
+        times.append(dt)
+    ms = sum(times) * 1e3 / len(times)
+    value = ms * UNIT_SAMPLES / SAMPLES_PER_STEP
+    queries = make_queries()
+    n = 131072
+    t0 = time.perf_counter()
+    orc.query(queries[:n])
+    qps = n / (time.perf_counter() - t0)
+    orc.close()
     return {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "samples_per_step": FRAME_SAMPLES,
-                   "parallelism": "host threads"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators of the "
+                                                                        "configured shapes)",
+        "config": {"workload": WORKLOAD, "samples_per_step": SAMPLES_PER_STEP, "frames": FRAMES,
+                   "max_samples_per_leaf": MAX_SAMPLES_PER_LEAF, "parallelism": "host threads"},
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "frame 1 of 8 (2,097,152 samples, fresh field) per step, scaled to 16,777,216",
-                         "note": PORT_NOTE},
+                         "sample": "the whole step per step: a fresh field, then Updates on frames 1-8 "
+                                   "(16,777,216 samples)",
+                         "note": PORT_NOTE, "host": host_info()},
+        "queries": {"queries_per_s": round(qps), "sample": f"{n} guided queries on the trained field"},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -622,7 +786,15 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--no-clustered", dest="clustered", action="store_false",
                     help="skip the clustered workload (default and autotuned EM schedule)")
+    ap.add_argument("--no-widened", dest="widened", action="store_false",
+                    help="skip the rows beyond the core path (HG queries, path samples, plain VMM, plain form)")
+    ap.add_argument("--em-capture", action="store_true",
+                    help="profiling case: one Update of a fresh field on the workload's first frame (one EM "
+                         "launch), nothing timed or printed")
     args = ap.parse_args()
+    if args.em_capture:
+        em_capture()
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

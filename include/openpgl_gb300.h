@@ -82,15 +82,17 @@ OPENPGL_CORE_INTERFACE int pglDebugBoundedWaitRunsOut(uint64_t limitNs);
 // merges, components (5 x u32 per region); returns the region count, writes
 // when capacity >= 5 x count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int volume, uint32_t *out, size_t capacity);
-// Where the EM kernel spent the last Update, per region (18 x u64 each):
+// Where the EM kernel spent the last Update, per region (21 x u64 each):
 // region, samples, E-step passes, distance passes, split-statistics passes,
 // then SM clock cycles in E-steps, distance passes, split-statistics passes,
 // merging, M-steps and in total, then inside the passes the cycles of the
 // producing threads and of the slowest summing thread, for E-steps and for
 // split-statistics passes, then the E-step chunks of the region, those made
 // by its own block (the others by blocks that had no region left), and the
-// cycles a summing thread waited for chunks.  Returns the region count;
-// writes when capacity >= 18 x count.
+// cycles a summing thread waited for chunks, then the lobes summed over the
+// E-step, distance and split-statistics passes (the sum of the mixture's
+// lobe count over the passes of each kind).  Returns the region count;
+// writes when capacity >= 21 x count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int volume, uint64_t *out,
                                                            size_t capacity);
 // Schedule parameters of the field's EM launch (no reference counterpart;

@@ -851,10 +851,10 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
   PGL_TRY
   const SubField &sf = volume ? F(field)->volume : F(field)->surface;
   size_t n = sf.lastProfiles.size();
-  if (out && cap >= 18 * n)
+  if (out && cap >= 21 * n)
     for (size_t i = 0; i < n; ++i) {
       const LeafProfile &p = sf.lastProfiles[i];
-      uint64_t *o = out + 18 * i;
+      uint64_t *o = out + 21 * i;
       o[0] = sf.lastReportRegion[i];
       o[1] = p.count;
       o[2] = p.estepPasses;
@@ -873,6 +873,9 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
       o[15] = p.chunks;
       o[16] = p.chunksOwn;
       o[17] = p.cycWaitE;
+      o[18] = p.estepLobes;
+      o[19] = p.distLobes;
+      o[20] = p.splitLobes;
     }
   return n;
   PGL_CATCH(0)

@@ -1913,6 +1913,7 @@ __device__ int em_loop(EmShared &S, const LeafSamples &L, SuffState &prev, bool 
     if (tid < 32) {  // the M-step by warp 0, lane k on lobe k
       if (tid == 0) {
         S.prof.estepPasses++;
+        S.prof.estepLobes += S.vmm.K;
         if (S.un.sw > 0.0f && S.cur.K < kMaxK) {  // handleUnassignedSampleStats (WEMFactory.h:731-748)
           int t = int(S.cur.K);
           S.cur.K++;
@@ -2025,7 +2026,7 @@ __device__ void recursive_splitting(EmShared &S, const LeafSamples &L, const Fie
     __syncthreads();
     {
       PGL_PROF_BEGIN(tp0)
-      if (threadIdx.x == 0) S.prof.splitPasses++;
+      if (threadIdx.x == 0) { S.prof.splitPasses++; S.prof.splitLobes += S.lsplit.K; }
       pass_split_stats(S, L, S.lsplit);
       PGL_PROF_END(tp0, cycSplit)
     }
@@ -2069,7 +2070,7 @@ __device__ void asm_fit(EmShared &S, const LeafSamples &L, const FieldConfig &cf
   S.report.emIterations += em_loop(S, L, S.suff, false, cfg);
   {
     PGL_PROF_BEGIN(tp0)
-    if (threadIdx.x == 0) S.prof.distPasses++;
+    if (threadIdx.x == 0) { S.prof.distPasses++; S.prof.distLobes += S.vmm.K; }
     pass_distances(S, L, true);
     PGL_PROF_END(tp0, cycDist)
   }
@@ -2081,7 +2082,7 @@ __device__ void asm_fit(EmShared &S, const LeafSamples &L, const FieldConfig &cf
     __syncthreads();
     {
       PGL_PROF_BEGIN(tp1)
-      if (threadIdx.x == 0) S.prof.splitPasses++;
+      if (threadIdx.x == 0) { S.prof.splitPasses++; S.prof.splitLobes += S.split.K; }
       pass_split_stats(S, L, S.split);
       PGL_PROF_END(tp1, cycSplit)
     }
@@ -2092,7 +2093,7 @@ __device__ void asm_fit(EmShared &S, const LeafSamples &L, const FieldConfig &cf
   }
   {
     PGL_PROF_BEGIN(tp1)
-    if (threadIdx.x == 0) S.prof.distPasses++;
+    if (threadIdx.x == 0) { S.prof.distPasses++; S.prof.distLobes += S.vmm.K; }
     pass_distances(S, L, true);
     PGL_PROF_END(tp1, cycDist)
   }
@@ -2118,7 +2119,7 @@ __device__ void asm_update(EmShared &S, const LeafSamples &L, const FieldConfig 
     __syncthreads();
     {
       PGL_PROF_BEGIN(tp2)
-      if (threadIdx.x == 0) S.prof.splitPasses++;
+      if (threadIdx.x == 0) { S.prof.splitPasses++; S.prof.splitLobes += S.split.K; }
       pass_split_stats(S, L, S.split);
       PGL_PROF_END(tp2, cycSplit)
     }
@@ -2164,7 +2165,7 @@ __device__ void asm_update(EmShared &S, const LeafSamples &L, const FieldConfig 
   }
   {
     PGL_PROF_BEGIN(tp2)
-    if (threadIdx.x == 0) S.prof.distPasses++;
+    if (threadIdx.x == 0) { S.prof.distPasses++; S.prof.distLobes += S.vmm.K; }
     pass_distances(S, L, false);
     PGL_PROF_END(tp2, cycDist)
   }
@@ -2246,7 +2247,8 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Em
     }
     const long long leafStart = clock64();
     if (threadIdx.x == 0) {
-      S.prof = LeafProfile{t.count, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      S.prof = LeafProfile{};
+      S.prof.count = t.count;
       afterSplit = R.afterSplit;
       afterMerge = R.afterMerge;
       S.report = LeafReport{0, 0, 0, 0};

@@ -103,6 +103,9 @@ struct LeafProfile {
   // E-step chunks of the leaf, those its own block produced (the rest came
   // from helper blocks), and the cycles a summing thread waited for chunks
   uint64_t chunks, chunksOwn, cycWaitE;
+  // lobes summed over the passes of each kind (sum of K per pass): the
+  // algorithmic work of a pass is samples x lobes
+  uint64_t estepLobes, distLobes, splitLobes;
 };
 
 // Integer position statistics of one kd child (IntegerSampleStatistics).

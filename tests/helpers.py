@@ -26,8 +26,13 @@ def vmm_pdf64(vmm, dirs):
     return (w * norm * np.exp(k * np.minimum(ct - 1.0, 0.0))).sum(axis=1)
 
 
-def compare_fields(gpu_bytes, orc_bytes, side="surface"):
-    """Returns a dict describing how the GPU field matches the oracle field."""
+def compare_fields(gpu_bytes, orc_bytes, side="surface", tol=1e-3):
+    """Returns a dict describing how the GPU field matches the oracle field:
+    tree and numbering equality, leaf sample statistics, regions whose
+    mixture bytes are equal, the worst per-leaf relative PDF error on the
+    64x64 grid, the leaves above `tol` (`over_tol`: region, error, lobe counts
+    of both sides) and the leaves whose lobe count differs (`k_flips`: a split
+    or merge decision that went the other way)."""
     A = fieldfile.read_field_file(gpu_bytes)[side]
     B = fieldfile.read_field_file(orc_bytes)[side]
     ca, cb = fieldfile.canonical_tree(A), fieldfile.canonical_tree(B)
@@ -44,7 +49,8 @@ def compare_fields(gpu_bytes, orc_bytes, side="surface"):
     worst = 0.0
     stats_equal = True
     rel_errs = []
-    for ra, rb in zip(A["regions"], B["regions"]):
+    over, flips = [], []
+    for ri, (ra, rb) in enumerate(zip(A["regions"], B["regions"])):
         for key in ("mean", "var", "bounds"):
             if not np.array_equal(ra["stats"][key].view(np.uint32), rb["stats"][key].view(np.uint32)):
                 stats_equal = False
@@ -59,12 +65,41 @@ def compare_fields(gpu_bytes, orc_bytes, side="surface"):
             continue
         if va["K"] != vb["K"]:
             kdiff += 1
+            flips.append((ri, int(va["K"]), int(vb["K"])))
         pa, pb = vmm_pdf64(va, dirs), vmm_pdf64(vb, dirs)
         rel = np.abs(pa - pb) / np.maximum(np.abs(pb), 1e-12)
         rel_errs.append(rel.max())
         worst = max(worst, float(rel.max()))
+        if rel.max() > tol:
+            over.append((ri, float(rel.max()), int(va["K"]), int(vb["K"])))
     res.update(bit_exact_regions=bit, k_differs=kdiff, worst_pdf_rel=worst, stats_equal=stats_equal,
-               rel_errs=np.array(rel_errs))
+               rel_errs=np.array(rel_errs), over_tol=over, k_flips=flips)
+    return res
+
+
+def summary(r):
+    """The comparison without the per-leaf error array (for messages and
+    bench lines)."""
+    return {k: v for k, v in r.items() if k != "rel_errs"}
+
+
+def compare_queries(out, ref):
+    """Guided-query agreement: same ok flags, region ids and rescaled sample1D
+    bits; worst relative pdf error and direction difference over valid
+    queries."""
+    ok = ref["ok"] == 1
+    res = dict(ok_equal=bool(np.array_equal(out["ok"], ref["ok"])),
+               id_equal=bool(np.array_equal(out["id"][ok], ref["id"][ok])),
+               sample1d_equal=bool(np.array_equal(out["sample1d"][ok].view(np.uint32),
+                                                  ref["sample1d"][ok].view(np.uint32))),
+               valid=int(ok.sum()))
+    if ok.any():
+        rel = np.abs(out["pdf"][ok].astype(np.float64) - ref["pdf"][ok]) / ref["pdf"][ok]
+        res["worst_pdf_rel"] = float(rel.max())
+        res["worst_dir"] = float(np.abs(out["dir"][ok] - ref["dir"][ok]).max())
+        res["pdf_bit_exact_frac"] = float(np.mean(out["pdf"][ok].view(np.uint32) == ref["pdf"][ok].view(np.uint32)))
+    else:
+        res.update(worst_pdf_rel=0.0, worst_dir=0.0, pdf_bit_exact_frac=1.0)
     return res
 
 

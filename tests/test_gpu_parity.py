@@ -10,7 +10,7 @@ and return the same pdf within 1e-3 relative (directions within 1e-3)."""
 import numpy as np
 import pytest
 
-from helpers import compare_fields
+from helpers import compare_fields, compare_queries, summary
 
 pytestmark = pytest.mark.gpu
 
@@ -40,17 +40,47 @@ def _train(pgl, frames, leaf, deterministic=True):
     return dev, field, orc
 
 
-@pytest.mark.parametrize("n,leaf", [(262144, 32000), (131072, 4000)])
+def _check_field(field, orc, side="surface"):
+    """The bar on every leaf: tree, numbering and sample statistics equal, no
+    leaf above PDF_TOL (the message names the leaves and their lobe counts)."""
+    r = compare_fields(field.field_bytes(), orc.field_bytes(), side, tol=PDF_TOL)
+    s = summary(r)
+    assert r["tree_equal"], (side, s)
+    assert r["numbering_equal"], (side, s)
+    if r["regions"]:
+        assert r["stats_equal"], (side, s)
+        assert not r["over_tol"] and r["worst_pdf_rel"] <= PDF_TOL, (side, s)
+    print(side, "regions", r["regions"], "bit-exact", r.get("bit_exact_regions"), "K flips", r.get("k_flips"),
+          "worst pdf rel %.2e" % r.get("worst_pdf_rel", 0.0))
+    return r
+
+
+def _check_queries(out, ref, what=""):
+    r = compare_queries(out, ref)
+    assert r["ok_equal"] and r["id_equal"] and r["sample1d_equal"], (what, r)
+    assert r["worst_pdf_rel"] <= PDF_TOL and r["worst_dir"] <= 1e-3, (what, r)
+    return r
+
+
+@pytest.mark.parametrize("n,leaf", [(262144, 32000), (131072, 4000), (1048576, 16000)])
 def test_first_build_matches_oracle(pgl, n, leaf):
     from openpgl_gb300 import synthetic as syn
 
     dev, field, orc = _train(pgl, [syn.cube_face_samples(n, 21)], leaf)
-    r = compare_fields(field.field_bytes(), orc.field_bytes())
-    assert r["tree_equal"], r
-    assert r["numbering_equal"], r
-    assert r["stats_equal"], r
-    assert r["worst_pdf_rel"] <= PDF_TOL, r
-    print("bit-exact regions", r["bit_exact_regions"], "of", r["regions"])
+    _check_field(field, orc)
+
+
+def test_single_update_configuration(pgl):
+    """The single-Update configuration at its full size: 1,048,576 cube-face
+    samples, maxSamplesPerLeaf 32000, one Update, then 1,048,576 guided queries
+    (cosine product, one SamplePDF each)."""
+    from openpgl_gb300 import synthetic as syn
+
+    dev, field, orc = _train(pgl, [syn.cube_face_samples(1 << 20, 1001)], 32000)
+    _check_field(field, orc)
+    q = syn.queries(1 << 20, 1002)
+    r = _check_queries(field.sample_batch(q), orc.query(q), "1M queries")
+    print(r)
 
 
 def test_leaf_log_likelihood_matches_oracle(pgl):
@@ -76,9 +106,7 @@ def test_multiframe_surface_and_volume(pgl):
     frames = [syn.cube_face_samples(131072, 30 + i, volume_fraction=0.25) for i in range(3)]
     dev, field, orc = _train(pgl, frames, 4000)
     for side in ("surface", "volume"):
-        r = compare_fields(field.field_bytes(), orc.field_bytes(), side)
-        assert r["tree_equal"] and r["stats_equal"], (side, r)
-        assert r["worst_pdf_rel"] <= PDF_TOL, (side, r)
+        _check_field(field, orc, side)
 
 
 def test_clustered_update(pgl):
@@ -86,10 +114,24 @@ def test_clustered_update(pgl):
 
     frames = [syn.cluster_samples(200000, 40 + i, num_clusters=256) for i in range(2)]
     dev, field, orc = _train(pgl, frames, 2000)
-    r = compare_fields(field.field_bytes(), orc.field_bytes())
-    assert r["tree_equal"] and r["stats_equal"], r
-    frac = float(np.mean(r["rel_errs"] <= PDF_TOL))
-    assert frac >= 0.99, r
+    _check_field(field, orc)
+
+
+def test_clustered_many_leaves(pgl):
+    """The clustered distribution at 4096 clusters (Zipf masses, 1-6 lobes,
+    near-delta lobes), 2,097,152 samples in two frames at maxSamplesPerLeaf
+    16000 (leaves from a few hundred to 16000 samples), then queries drawn
+    from the clusters."""
+    from openpgl_gb300 import synthetic as syn
+
+    frames = [syn.cluster_samples(1 << 20, 140 + i, volume_fraction=0.25) for i in range(2)]
+    dev, field, orc = _train(pgl, frames, 16000)
+    for side in ("surface", "volume"):
+        _check_field(field, orc, side)
+    q = syn.queries(1 << 18, 142, model_seed=1234)
+    for volume in (False, True):
+        _check_queries(field.sample_batch(q, volume=volume, cosine=not volume),
+                       orc.query(q, volume=volume, cosine=not volume), f"volume={volume}")
 
 
 def test_guided_queries_match_oracle(pgl):
@@ -97,16 +139,7 @@ def test_guided_queries_match_oracle(pgl):
 
     dev, field, orc = _train(pgl, [syn.cube_face_samples(262144, 50)], 8000)
     q = syn.queries(8192, 51)
-    out = field.sample_batch(q)
-    ref = orc.query(q)
-    assert np.array_equal(out["ok"], ref["ok"])
-    assert np.array_equal(out["id"], ref["id"])
-    assert np.array_equal(out["sample1d"].view(np.uint32), ref["sample1d"].view(np.uint32))
-    ok = ref["ok"] == 1
-    rel = np.abs(out["pdf"][ok] - ref["pdf"][ok]) / ref["pdf"][ok]
-    assert np.quantile(rel, 0.999) <= PDF_TOL, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
-    ang = np.abs(out["dir"][ok] - ref["dir"][ok]).max(axis=1)
-    assert np.quantile(ang, 0.999) <= 1e-3
+    _check_queries(field.sample_batch(q), orc.query(q))
 
 
 def test_poisoned_samples_flag_the_oracles_regions(pgl):
@@ -132,13 +165,8 @@ def test_poisoned_samples_flag_the_oracles_regions(pgl):
     assert invalid > 0
     q = syn.queries(2048, 993)
     for volume in (False, True):
-        out = field.sample_batch(q, volume=volume, cosine=not volume)
-        ref = orc.query(q, volume=volume, cosine=not volume)
-        assert np.array_equal(out["ok"], ref["ok"]), volume
-        assert np.array_equal(out["id"], ref["id"]), volume
-        ok = ref["ok"] == 1
-        rel = np.abs(out["pdf"][ok] - ref["pdf"][ok]) / ref["pdf"][ok]
-        assert np.quantile(rel, 0.999) <= PDF_TOL, volume
+        _check_queries(field.sample_batch(q, volume=volume, cosine=not volume),
+                       orc.query(q, volume=volume, cosine=not volume), f"volume={volume}")
 
 
 def test_per_object_api_matches_batch(pgl):
@@ -222,10 +250,10 @@ def test_hg_product_matches_oracle_and_per_object(pgl, tmp_path):
     assert np.array_equal(out["id"][ok], ref["id"][ok])
     assert np.array_equal(out["sample1d"][ok].view(np.uint32), ref["sample1d"][ok].view(np.uint32))
     rel = np.abs(out["pdf"][ok] - ref["pdf"][ok]) / ref["pdf"][ok]
-    assert np.quantile(rel, 0.999) <= PDF_TOL, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
+    assert rel.max() <= PDF_TOL, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
     relli = np.abs(out["pdfLi"][ok] - ref["pdfLi"][ok]) / ref["pdfLi"][ok]
-    assert np.quantile(relli, 0.999) <= PDF_TOL
-    assert np.quantile(np.abs(out["dir"][ok] - ref["dir"][ok]).max(axis=1), 0.999) <= 1e-3
+    assert relli.max() <= PDF_TOL
+    assert np.abs(out["dir"][ok] - ref["dir"][ok]).max() <= 1e-3
     vsd = pgl.VolumeSamplingDistribution(field)
     assert vsd.supports_hg_product()
     for i in range(0, len(q), 128):
