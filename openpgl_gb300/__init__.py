@@ -280,6 +280,15 @@ class SampleStorage:
         self.h = self.lib.pglNewSampleStorage()
         _check(self.h, "pglNewSampleStorage")
 
+    @classmethod
+    def from_file(cls, path):
+        """pglNewSampleStorageFromFile: a storage from a file in the reference's layout."""
+        s = cls.__new__(cls)
+        s.lib = load()
+        s.h = s.lib.pglNewSampleStorageFromFile(os.fsencode(path))
+        _check(s.h, "pglNewSampleStorageFromFile")
+        return s
+
     def add_samples(self, samples):
         s = np.ascontiguousarray(samples, dtype=PGL_SAMPLE_DTYPE)
         self.lib.pglSampleStorageAddSamples(self.h, s.ctypes.data, len(s))

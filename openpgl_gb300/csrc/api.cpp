@@ -68,17 +68,35 @@ static_assert(sizeof(PGLGuidedQueryResult) == sizeof(QueryOut), "query result la
 #define PGL_TRY \
   try {         \
     g_lastError.clear();
-#define PGL_CATCH(ret)            \
-  }                               \
-  catch (const std::exception &e) { \
-    fail(__func__, e);            \
-    return ret;                   \
+// As the reference's catch blocks (api/api.cpp:33-72): a failed allocation,
+// any std::exception and anything else are caught; none crosses the ABI.
+#define PGL_CATCH(ret)                                                              \
+  }                                                                                 \
+  catch (const std::bad_alloc &) {                                                  \
+    fail(__func__, std::runtime_error("unable to allocate memory"));                \
+    return ret;                                                                     \
+  }                                                                                 \
+  catch (const std::exception &e) {                                                 \
+    fail(__func__, e);                                                              \
+    return ret;                                                                     \
+  }                                                                                 \
+  catch (...) {                                                                     \
+    fail(__func__, std::runtime_error("an unrecognized exception was caught"));     \
+    return ret;                                                                     \
   }
-#define PGL_CATCH_VOID            \
-  }                               \
-  catch (const std::exception &e) { \
-    fail(__func__, e);            \
-    return;                       \
+#define PGL_CATCH_VOID                                                              \
+  }                                                                                 \
+  catch (const std::bad_alloc &) {                                                  \
+    fail(__func__, std::runtime_error("unable to allocate memory"));                \
+    return;                                                                         \
+  }                                                                                 \
+  catch (const std::exception &e) {                                                 \
+    fail(__func__, e);                                                              \
+    return;                                                                         \
+  }                                                                                 \
+  catch (...) {                                                                     \
+    fail(__func__, std::runtime_error("an unrecognized exception was caught"));     \
+    return;                                                                         \
   }
 
 FieldConfig config_from(const PGLFieldArguments &args) {  // Device.h:99-136
@@ -596,14 +614,21 @@ OPENPGL_CORE_INTERFACE bool pglSampleStorageCompare(PGLSampleStorage a, PGLSampl
   // SampleDataStorage::operator== (SampleDataStorage.h:230-279): both sides
   // sorted, compared over the first storage's size (its size check is missing)
   PGL_TRY
+  // SampleDataEqual (SampleData.h:69-80): member-wise float comparison
+  // (+0 equals -0, a NaN equals nothing) and equal flags
+  auto equal = [](const PGLSampleRecord &p, const PGLSampleRecord &q) {
+    return p.px == q.px && p.py == q.py && p.pz == q.pz && p.dx == q.dx && p.dy == q.dy && p.dz == q.dz &&
+           p.weight == q.weight && p.pdf == q.pdf && p.distance == q.distance && p.flags == q.flags;
+  };
+  bool same = true;
   for (bool vol : {false, true}) {
     std::vector<PGLSampleRecord> x = S(a)->download(vol), y = S(b)->download(vol);
     std::sort(x.begin(), x.end(), sample_less);
     std::sort(y.begin(), y.end(), sample_less);
     for (size_t i = 0; i < x.size() && i < y.size(); ++i)
-      if (std::memcmp(&x[i], &y[i], sizeof(PGLSampleRecord)) != 0) return false;
+      if (!equal(x[i], y[i])) same = false;
   }
-  return true;
+  return same;
   PGL_CATCH(false)
 }
 

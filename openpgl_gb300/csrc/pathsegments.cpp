@@ -86,11 +86,19 @@ using namespace pgl;
 #define PGL_PS_TRY \
   try {            \
     api_clear_error();
-#define PGL_PS_CATCH(ret)             \
-  }                                   \
-  catch (const std::exception &e) {   \
-    api_error(__func__, e);           \
-    return ret;                       \
+#define PGL_PS_CATCH(ret)                                                           \
+  }                                                                                 \
+  catch (const std::bad_alloc &) {                                                  \
+    api_error(__func__, std::runtime_error("unable to allocate memory"));           \
+    return ret;                                                                     \
+  }                                                                                 \
+  catch (const std::exception &e) {                                                 \
+    api_error(__func__, e);                                                         \
+    return ret;                                                                     \
+  }                                                                                 \
+  catch (...) {                                                                     \
+    api_error(__func__, std::runtime_error("an unrecognized exception was caught")); \
+    return ret;                                                                     \
   }
 
 extern "C" {

@@ -147,6 +147,8 @@ void GuidingServer::dispatchLoop() {
     dispatch();
   } catch (const std::exception &e) {
     fail(e);
+  } catch (...) {
+    fail(std::runtime_error("an unrecognized exception was caught"));
   }
 }
 
@@ -251,6 +253,8 @@ void GuidingServer::trainLoop() {
     train();
   } catch (const std::exception &e) {
     fail(e);
+  } catch (...) {
+    fail(std::runtime_error("an unrecognized exception was caught"));
   }
 }
 

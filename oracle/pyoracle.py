@@ -154,6 +154,38 @@ def run_reference_paths(segments, begin, max_distance):
     return counts, samples, pixel
 
 
+def run_reference_storage(samples):
+    """The reference's SampleStorage holding ``samples`` (AddSamples), stored by
+    SampleStorage::Store; returns (file bytes, (equal, surface size, volume
+    size) of the storage read back from the file and compared with the
+    original by operator==)."""
+    import sys
+
+    sys.path.insert(0, os.path.dirname(HERE))
+    from openpgl_gb300 import synthetic
+
+    with tempfile.TemporaryDirectory() as td:
+        fpath = os.path.join(td, "frames.bin")
+        with open(fpath, "wb") as f:
+            f.write(synthetic.frames_blob([samples]))
+        env = dict(os.environ, PGL_REF_STORE_SAMPLES="1", PGL_ORACLE_THREADS="1")
+        subprocess.run([REF_HARNESS, fpath, os.path.join(td, "ref"), "8", "1", "32000", "1"], check=True, env=env)
+        data = open(os.path.join(td, "ref.storage"), "rb").read()
+        eq, ns, nv = (int(x) for x in open(os.path.join(td, "ref.storage_cmp")).read().split())
+    return data, (eq, ns, nv)
+
+
+def reference_sources():
+    """The reference source tree as oracle/Makefile.ref finds it (its REF), or
+    None when the sources are absent (as on the GPU hosts)."""
+    try:
+        out = subprocess.run(["make", "-s", "-C", HERE, "-f", "Makefile.ref", "print-ref"], capture_output=True,
+                             text=True, timeout=60).stdout.strip()
+    except (OSError, subprocess.SubprocessError):
+        return None
+    return out or None
+
+
 def reference_available():
     return os.path.exists(REF_HARNESS)
 

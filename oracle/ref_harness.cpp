@@ -15,6 +15,12 @@
 //              <out_prefix>.volhgq.bin same, volume field with the Henyey-Greenstein
 //                                      product: direction = the query's normal,
 //                                      mean cosine of query i = hg_mean_cosine(i)
+//              <out_prefix>.storage    with PGL_REF_STORE_SAMPLES=1: the sample
+//                                      storage holding the last frame, stored by
+//                                      SampleStorage::Store before that frame's
+//                                      Update, then read back by the
+//                                      SampleStorage(file) constructor and compared
+//                                      with operator== (result in .storage_cmp)
 #include <openpgl/cpp/OpenPGL.h>
 
 #include <chrono>
@@ -114,6 +120,14 @@ int main(int argc, char **argv) {
     p += 8;
     storage.AddSamples(reinterpret_cast<const PGLSampleData *>(p), size_t(n));
     p += n * sizeof(PGLSampleData);
+    const char *storeSamples = std::getenv("PGL_REF_STORE_SAMPLES");
+    if (f + 1 == numFrames && storeSamples && std::atoi(storeSamples) != 0) {
+      storage.Store(prefix + ".storage");
+      openpgl::cpp::SampleStorage back(prefix + ".storage");
+      FILE *c = std::fopen((prefix + ".storage_cmp").c_str(), "w");
+      std::fprintf(c, "%d %zu %zu\n", (back == storage) ? 1 : 0, back.GetSizeSurface(), back.GetSizeVolume());
+      std::fclose(c);
+    }
     auto t0 = std::chrono::steady_clock::now();
     field.Update(storage);
     auto t1 = std::chrono::steady_clock::now();

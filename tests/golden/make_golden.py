@@ -15,7 +15,8 @@ Each case stores:
                     the query's normal, mean cosine pyoracle.hg_mean_cosines)
 and paths.npz the samples and pixel estimates of the reference's path
 segment storage on synthetic paths (counts per flag set and path, samples,
-pixel estimates); manifest.json records the generator calls and the SHA-256
+pixel estimates), and storage.samples.gz a sample storage file written by the
+reference's SampleStorage::Store (STORAGE below); manifest.json records the generator calls and the SHA-256
 of every generated input, so a test can check that the generators still produce the
 same inputs before it compares outputs.
 
@@ -85,12 +86,46 @@ def build_paths(case):
     return syn.path_segments(case["num_paths"], case["seed"], case["max_len"])
 
 
+# sample storage file case: generator arguments (2,000 records, 30 % inside-volume)
+STORAGE = dict(n=2000, seed=7, volume_fraction=0.3)
+
+
+def build_storage(case):
+    from openpgl_gb300 import synthetic as syn
+
+    return syn.cube_face_samples(**case)
+
+
+def write_storage(pyoracle, manifest):
+    """A sample storage file (SampleDataStorage.h:176-216) written by the
+    reference's SampleStorage::Store, and what the reference reads back."""
+    samples = build_storage(STORAGE)
+    data, (eq, ns, nv) = pyoracle.run_reference_storage(samples)
+    with gzip.GzipFile(os.path.join(HERE, "storage.samples.gz"), "wb", compresslevel=9, mtime=0) as f:
+        f.write(data)
+    manifest["storage"] = dict(STORAGE, samples_sha256=sha(samples), file_sha256=hashlib.sha256(data).hexdigest(),
+                               reference_reads_back_equal=bool(eq), surface=ns, volume=nv)
+    print("storage", len(data), "bytes,", ns, "surface,", nv, "volume, read back equal:", bool(eq))
+
+
 def main():
+    import argparse
+
     import fieldfile
     import pyoracle
 
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", choices=["storage"], help="regenerate one fixture, keep the others and the manifest")
+    args = ap.parse_args()
     if not pyoracle.reference_available():
         sys.exit("oracle/_ref/ref_harness is missing: build it with oracle/Makefile.ref first")
+    if args.only == "storage":
+        with open(os.path.join(HERE, "manifest.json")) as f:
+            manifest = json.load(f)
+        write_storage(pyoracle, manifest)
+        with open(os.path.join(HERE, "manifest.json"), "w") as f:
+            json.dump(manifest, f, indent=1)
+        return
     manifest = {"generator": "openpgl_gb300.synthetic", "reference": "Open PGL 0.6.0, CPU_8, deterministic, serial",
                 "cases": {}}
     for name, case in CASES.items():
@@ -112,6 +147,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "paths.npz"), counts=counts, samples=samples, pixel=pixel)
     manifest["paths"] = dict(PATHS, segments_sha256=sha(segs), begin_sha256=sha(begin))
     print("paths", len(begin) - 1, "paths,", len(segs), "segments,", len(samples), "samples")
+    write_storage(pyoracle, manifest)
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1)
 
