@@ -24,7 +24,8 @@ schedule and with the schedule the EM autotuner picks on the Update before
 beyond the core path: volume guided queries with the Henyey-Greenstein
 product, training samples made from path segments on the device, the
 multi-frame step with the plain VMM field type, and the multi-frame step in
-the plain drop-in form (one EM launch per region) beside the batched one.
+the plain drop-in form (per Update and sub-field one EM launch with one block
+per region, no work queue and no helper blocks) beside the batched one.
 
 `--impl reference` times the CPU restatement of the reference algorithm (the
 oracle, built with the reference's arithmetic) with all host threads on a
@@ -62,6 +63,10 @@ WORKLOAD = ("multi-frame: 8 frames x 2,097,152 samples (25% inside-volume, cube 
 # (3008 B) read and written once
 EM_BYTES_PER_SAMPLE = 32
 REGION_STATE_BYTES = 3008
+# DRAM bytes (read + write) per sample of an EM launch, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on the first Update's launch of
+# this workload (`bench.py --em-capture`: 2,097,152 samples, 127.7 MB)
+EM_TRAFFIC_PER_SAMPLE = 60.9
 
 
 # the port against the compiled reference (CPU_8, AVX2) on x86, first frame
@@ -295,16 +300,37 @@ def run_widened(pgl, dev, stream, field, queries, frames, d_frames, steps, warmu
     b.record(stream)
     torch.cuda.synchronize()
     out["plain_vmm_update"] = {"value": round(a.elapsed_time(b), 3), "unit": UNIT}
-    # the plain drop-in form of the Update: one single-block EM launch per region
+    # the plain drop-in form of the Update: per sub-field one EM launch with a
+    # block per region (all SMs; no queue, no helper blocks, no shared passes)
     per_region = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF))
     per_region.set_plain_update(True)
-    torch.cuda.synchronize()
-    a.record(stream)
     step(per_region)
-    b.record(stream)
     torch.cuda.synchronize()
-    out["plain_update"] = {"value": round(a.elapsed_time(b), 3), "unit": UNIT,
-                           "form": "one single-block EM launch per region, one after the other"}
+    times = []
+    for _ in range(max(2, min(steps, 3))):
+        a.record(stream)
+        step(per_region)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    out["plain_update"] = {"value": round(statistics.median(times), 3), "unit": UNIT,
+                           "form": "per Update and sub-field one EM launch with one block per region (all SMs, "
+                                   "no work queue, no helper blocks)",
+                           "same_field": per_region.field_bytes() == field_bytes_of(pgl, dev, frames, d_frames)}
+    return out
+
+
+def field_bytes_of(pgl, dev, frames, d_frames):
+    """The batched form's field after the multi-frame step (for comparisons)."""
+    f = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF))
+    st = pgl.SampleStorage()
+    for fr, d in zip(frames, d_frames):
+        st.clear()
+        st.add_samples_device(d.data_ptr(), len(fr))
+        f.update(st)
+    out = f.field_bytes()
+    f.release()
+    st.release()
     return out
 
 
@@ -672,7 +698,9 @@ def em_roofline(work, sm_mhz, step_ms):
     r["launches_per_step"] = len(work)
     r["em_share_of_step"] = round(sum(w["ms"] for w in work) / step_ms, 3)
     r["per_launch_ms"] = [round(w["ms"], 3) for w in work]
-    r["traffic"] = None
+    r["traffic"] = round(EM_TRAFFIC_PER_SAMPLE * avg["samples"])
+    r["traffic_source"] = ("ncu DRAM bytes per sample of the first Update's EM launch (2,097,152 samples), "
+                           "times the samples of the average launch")
     r["work"] = ("per (sample, lobe, E-step pass) 21 flop + 1 SFU; per (sample, E-step pass) 4 flop + 2 SFU; "
                  "per (sample, lobe) of a distance pass 30 flop + 1 SFU, of a split-statistics pass 70 flop + "
                  "3 SFU; 32 B per sample and 2 x 3008 B per region of HBM; pass and lobe counts from the "

@@ -29,6 +29,32 @@ typedef struct {
   float pdfLi;        // IncomingRadiancePDF(direction)
 } PGLGuidedQueryResult;
 
+// A path vertex with four SamplePDF calls on one initialised distribution
+// (76 bytes): position, normal (for the cosine product), outgoing direction
+// and roughness (carried for the caller; the reference's surface
+// distribution uses neither), the 1D random number of the region choice and
+// one 2D random number per sample.
+typedef struct {
+  pgl_point3f position;
+  pgl_vec3f normal;
+  pgl_vec3f wo;
+  float roughness;
+  float sample1D;
+  pgl_point2f sample2D[4];
+} PGLGuidedVertex;
+
+// Result of Init + cosine product + four SamplePDF calls (76 bytes): the
+// sampled direction and its pdf per 2D random number.
+typedef struct {
+  uint32_t valid;     // Init succeeded
+  uint32_t id;        // kd leaf (GetId)
+  float sample1D;     // sample1D after the region choice rescaled it
+  struct {
+    pgl_vec3f direction;
+    float pdf;
+  } sample[4];
+} PGLGuidedVertexResult;
+
 // Guided queries on host buffers: copies the queries in, runs one kernel,
 // copies the results out.  Same results as the per-object calls.
 OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceBatch(PGLField field, const PGLGuidedQuery *queries, size_t n,
@@ -53,6 +79,17 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHG(PGLField field, const PG
 OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHGDevice(PGLField field, const PGLGuidedQuery *dQueries,
                                                               const float *dMeanCosines, size_t n,
                                                               PGLGuidedQueryResult *dResults, void *cudaStream);
+// Path-vertex queries (no reference counterpart; what a renderer does per
+// vertex with SurfaceSamplingDistribution: Init, ApplyCosineProduct, then
+// SamplePDF for each of the vertex's four 2D random numbers,
+// VMMSurfaceSamplingDistribution.h:67-103), in one kernel: host buffers
+// (copies in and out, synchronises) or device buffers enqueued on
+// `cudaStream` (null: the library's stream; does not synchronise).
+OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceVertices(PGLField field, const PGLGuidedVertex *vertices, size_t n,
+                                                          PGLGuidedVertexResult *results);
+OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceVerticesDevice(PGLField field, const PGLGuidedVertex *dVertices,
+                                                                size_t n, PGLGuidedVertexResult *dResults,
+                                                                void *cudaStream);
 // Adds samples that already live in device memory.
 OPENPGL_CORE_INTERFACE void pglSampleStorageAddSamplesDevice(PGLSampleStorage sampleStorage,
                                                              const PGLSampleData *dSamples, size_t numSamples);
@@ -156,7 +193,9 @@ OPENPGL_CORE_INTERFACE size_t pglPathSegmentsPropagateSamplesDevice(const PGLPat
 // per call (larger batches are rejected with an error), and calls that may
 // overlap in time (other threads or streams) must be serialised by the caller.
 // The first call on each device looks the array up (cudaGetSymbolAddress);
-// make it before any stream capture.
+// make it before any stream capture.  The address found is kept for the
+// life of the process, so do not use this entry point on a device after
+// cudaDeviceReset (the array's storage is then gone).
 OPENPGL_CORE_INTERFACE bool pglSplitSamplesDeviceNoAlloc(const PGLSampleData *dSamples, size_t numSamples,
                                                          PGLSampleData *dSurface, PGLSampleData *dVolume,
                                                          uint32_t *dCounts, void *cudaStream);

@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .synthetic import PGL_QUERY_DTYPE, PGL_SAMPLE_DTYPE
+from .synthetic import PGL_QUERY_DTYPE, PGL_SAMPLE_DTYPE, PGL_VERTEX_DTYPE
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libopenpgl_gb300.so")
@@ -30,6 +30,9 @@ QUERY_RESULT_DTYPE = np.dtype(
     [("ok", "<u4"), ("id", "<u4"), ("sample1d", "<f4"), ("dir", "<f4", (3,)), ("pdf", "<f4"), ("pdfLi", "<f4")]
 )
 assert QUERY_RESULT_DTYPE.itemsize == 32
+# PGLGuidedVertexResult: per SamplePDF call k, sample[k] = (direction xyz, pdf)
+VERTEX_RESULT_DTYPE = np.dtype([("ok", "<u4"), ("id", "<u4"), ("sample1d", "<f4"), ("sample", "<f4", (4, 4))])
+assert VERTEX_RESULT_DTYPE.itemsize == 76
 
 
 class Vec3(ctypes.Structure):
@@ -142,6 +145,10 @@ C_API = {
     "pglFieldSampleVolumeBatchHGDevice": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                           ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
     "pglSampleStorageAddSamplesDevice": (None, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "pglFieldSampleSurfaceVertices": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                      ctypes.c_void_p]),
+    "pglFieldSampleSurfaceVerticesDevice": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                            ctypes.c_void_p, ctypes.c_void_p]),
     "pglFieldStoreToBuffer": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     "pglFieldGetLastUpdateTimings": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "pglFieldGetLastUpdateReports": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
@@ -474,6 +481,19 @@ class Field:
             ok = self.lib.pglFieldSampleSurfaceBatch(self.h, q.ctypes.data, len(q), out.ctypes.data, cosine)
         _check(ok, "pglFieldSampleBatch")
         return out
+
+    def sample_vertices(self, vertices):
+        """Path-vertex queries: Init + cosine product + four SamplePDF calls per
+        vertex, in one launch (pglFieldSampleSurfaceVertices)."""
+        v = np.ascontiguousarray(vertices, dtype=PGL_VERTEX_DTYPE)
+        out = np.zeros(len(v), dtype=VERTEX_RESULT_DTYPE)
+        _check(self.lib.pglFieldSampleSurfaceVertices(self.h, v.ctypes.data, len(v), out.ctypes.data),
+               "pglFieldSampleSurfaceVertices")
+        return out
+
+    def sample_vertices_device(self, v_ptr, n, out_ptr, stream=None):
+        _check(self.lib.pglFieldSampleSurfaceVerticesDevice(self.h, v_ptr, n, out_ptr, stream),
+               "pglFieldSampleSurfaceVerticesDevice")
 
     def sample_batch_hg(self, queries, mean_cosines):
         """Volume guided queries with the Henyey-Greenstein product (the query's

@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libopenpgl_gb300.so")
+LIBM_TABLE = os.path.join(OUT, "libm_exceptions.bin")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 CUDA_SOURCES = ["em_kernel.cu", "spatial_kernels.cu", "query_kernels.cu", "noalloc.cu", "path_kernels.cu"]
@@ -79,7 +80,14 @@ def build(verbose=False, ptxas_info=False):
                 if verbose and out.strip():
                     print(out)
     if _stale(LIB, objs):
-        _run([nvcc, GENCODE, "-shared", "-Xlinker", "--no-undefined", "-o", LIB] + objs + ["-lcudart"])
+        _run([nvcc, GENCODE, "-shared", "-Xlinker", "--no-undefined", "-o", LIB] + objs + ["-lcudart", "-ldl"])
+    # the host C library's expf/cosf exceptions (read by the library at CUDA set-up)
+    gen_src = os.path.join(CSRC, "gen_libm_exceptions.cpp")
+    gen = os.path.join(OUT, "gen_libm_exceptions")
+    if _stale(gen, [gen_src]):
+        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", gen_src, "-o", gen, "-lpthread"])
+    if _stale(LIBM_TABLE, [gen]):
+        _run([gen, LIBM_TABLE, str(os.cpu_count() or 1)])
     return LIB
 
 

@@ -64,6 +64,9 @@ GpuSamplingDistribution *D(void *d) { return reinterpret_cast<GpuSamplingDistrib
 static_assert(sizeof(PGLSampleData) == sizeof(PGLSampleRecord), "sample record layout");
 static_assert(sizeof(PGLGuidedQuery) == sizeof(QueryIn), "query layout");
 static_assert(sizeof(PGLGuidedQueryResult) == sizeof(QueryOut), "query result layout");
+static_assert(sizeof(PGLGuidedVertex) == sizeof(QueryInS4) && sizeof(PGLGuidedVertex) == 76, "vertex layout");
+static_assert(sizeof(PGLGuidedVertexResult) == sizeof(QueryOutS4) && sizeof(PGLGuidedVertexResult) == 76,
+              "vertex result layout");
 
 #define PGL_TRY \
   try {         \
@@ -748,6 +751,47 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHG(PGLField field, const PG
                reinterpret_cast<PGLGuidedQueryResult *>(dr.p), false, dg.p, c.stream);
   check(cudaMemcpyAsync(results, dr.p, n * sizeof(QueryOut), cudaMemcpyDeviceToHost, c.stream), "D2H results");
   check(cudaStreamSynchronize(c.stream), "queries");
+  return true;
+  PGL_CATCH(false)
+}
+static void launch_vertices(PGLField field, const PGLGuidedVertex *dv, size_t n, PGLGuidedVertexResult *dr,
+                            cudaStream_t s) {
+  if (!field) throw std::runtime_error("null field");
+  if (n > 0 && (!dv || !dr)) throw std::runtime_error("null buffer");
+  if (n > 0xFFFFFFFFull) throw std::runtime_error("at most 2^32 - 1 vertices per call");
+  QueryParams p{};
+  p.f = F(field)->surface.view();
+  p.cosKappa = 2.18853f;
+  p.cosNorm = cosine_lobe_normalization();
+  p.cosine = 1;
+  p.samplesPerQuery = kVertexSamples;
+  check(launch_query_s4(p, reinterpret_cast<const QueryInS4 *>(dv), reinterpret_cast<QueryOutS4 *>(dr), uint32_t(n),
+                        s),
+        "vertex queries");
+}
+OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceVerticesDevice(PGLField field, const PGLGuidedVertex *dVertices,
+                                                                size_t n, PGLGuidedVertexResult *dResults,
+                                                                void *cudaStream) {
+  PGL_TRY
+  Context &c = Context::get();
+  launch_vertices(field, dVertices, n, dResults, cudaStream ? static_cast<cudaStream_t>(cudaStream) : c.stream);
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceVertices(PGLField field, const PGLGuidedVertex *vertices, size_t n,
+                                                          PGLGuidedVertexResult *results) {
+  PGL_TRY
+  Context &c = Context::get();
+  if (n == 0) return true;
+  static thread_local DevArray<QueryInS4> dv;
+  static thread_local DevArray<QueryOutS4> dr;
+  dv.reserve(n);
+  dr.reserve(n);
+  check(cudaMemcpyAsync(dv.p, vertices, n * sizeof(QueryInS4), cudaMemcpyHostToDevice, c.stream), "H2D vertices");
+  launch_vertices(field, reinterpret_cast<const PGLGuidedVertex *>(dv.p), n,
+                  reinterpret_cast<PGLGuidedVertexResult *>(dr.p), c.stream);
+  check(cudaMemcpyAsync(results, dr.p, n * sizeof(QueryOutS4), cudaMemcpyDeviceToHost, c.stream), "D2H results");
+  check(cudaStreamSynchronize(c.stream), "vertex queries");
   return true;
   PGL_CATCH(false)
 }

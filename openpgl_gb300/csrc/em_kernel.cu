@@ -2225,8 +2225,10 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Em
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
-  for (;;) {
-    if (threadIdx.x == 0) taskId = atomicAdd(queue, 1u);
+  // the plain form: block b fits region task b and exits (no queue, no help)
+  const bool plain = tune.plainLaunches != 0;
+  for (uint32_t round = 0;; ++round) {
+    if (threadIdx.x == 0) taskId = plain ? (round == 0 ? blockIdx.x : numTasks) : atomicAdd(queue, 1u);
     __syncthreads();
     if (taskId >= numTasks) break;
     const LeafTask t = tasks[taskId];
@@ -2313,7 +2315,7 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Em
     __syncthreads();
   }
   // no leaves left: produce for the blocks still working on theirs
-  help_others(S, boards, rings, finished, numTasks);
+  if (!plain) help_others(S, boards, rings, finished, numTasks);
 }
 
 PGL_DEFINE_TABLE_UPLOAD(em_upload_tables)
@@ -2355,6 +2357,7 @@ bool em_tuning_valid(const EmTuning &t) {
          (t.plainLaunches == 0 || t.plainLaunches == 1);
 }
 size_t em_share_bytes(int blocks) { return share_header_bytes(blocks) + size_t(blocks) * kRingFloats * sizeof(float); }
+size_t em_share_bytes_plain(int blocks) { return share_header_bytes(blocks); }
 size_t em_share_error_offset(int blocks) { return size_t(blocks) * sizeof(Board); }
 
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, const EmSides &sides,
@@ -2376,7 +2379,9 @@ cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *qu
   uint32_t *finished = reinterpret_cast<uint32_t *>(base + em_share_error_offset(blocks) + sizeof(int));
   float *rings = reinterpret_cast<float *>(base + share_header_bytes(blocks));
   // persistent blocks (one per SM: shared memory bound) take leaves from the
-  // queue; blocks without a leaf help the others' E-step passes
+  // queue; blocks without a leaf help the others' E-step passes.  The plain
+  // form launches one block per region (blocks == numTasks); its blocks use
+  // their own boards only, never a chunk ring.
   count_launch();
   em_leaf_kernel<<<unsigned(blocks), kEmThreads, smem, stream>>>(tasks, numTasks, queue, sides, reports, profiles,
                                                                  boards, rings, err, finished, tune);

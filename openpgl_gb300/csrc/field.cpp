@@ -3,8 +3,11 @@
 // decisions, quantisation frames) must produce the reference's bits.
 #include "field.h"
 
+#include <dlfcn.h>
+
 #include <algorithm>
 #include <cstdlib>
+#include <fstream>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -18,6 +21,37 @@ void check(cudaError_t e, const char *what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// The host C library's expf/cosf exception table (gen_libm_exceptions.cpp),
+// written by the build next to this library as libm_exceptions.bin, copied
+// to device memory that lives until the process exits.
+static LibmTables load_libm_tables() {
+  Dl_info info{};
+  if (!dladdr(reinterpret_cast<void *>(&load_libm_tables), &info) || !info.dli_fname)
+    throw std::runtime_error("cannot locate the library to find libm_exceptions.bin");
+  std::string path = info.dli_fname;
+  const size_t slash = path.rfind('/');
+  path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/libm_exceptions.bin";
+  std::ifstream is(path, std::ios::binary);
+  char magic[8];
+  uint32_t n[2] = {0, 0};
+  if (!is.read(magic, 8) || std::memcmp(magic, "PGLLIBM1", 8) != 0 || !is.read(reinterpret_cast<char *>(n), 8))
+    throw std::runtime_error("missing or bad " + path + " (the build writes it)");
+  std::vector<float2> v(size_t(n[0]) + n[1]);
+  if (!is.read(reinterpret_cast<char *>(v.data()), std::streamsize(v.size() * sizeof(float2))))
+    throw std::runtime_error("truncated " + path);
+  float2 *d = nullptr;
+  if (!v.empty()) {
+    check(cudaMalloc(&d, v.size() * sizeof(float2)), "libm table");
+    check(cudaMemcpy(d, v.data(), v.size() * sizeof(float2), cudaMemcpyHostToDevice), "libm table");
+  }
+  LibmTables t;
+  t.expf = d;
+  t.cosf = d ? d + n[0] : nullptr;
+  t.numExpf = n[0];
+  t.numCosf = n[1];
+  return t;
+}
+
 Context &Context::get() {
   // thread-safe one-time set-up (C++ static initialisation)
   static Context c = [] {
@@ -25,9 +59,10 @@ Context &Context::get() {
     check(cudaGetDevice(&x.device), "cudaGetDevice");
     check(cudaDeviceGetAttribute(&x.numSMs, cudaDevAttrMultiProcessorCount, x.device), "SM count");
     check(cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking), "stream");
-    check(em_upload_tables(), "tables (em)");
-    check(spatial_upload_tables(), "tables (spatial)");
-    check(query_upload_tables(), "tables (query)");
+    const LibmTables libm = load_libm_tables();
+    check(em_upload_tables(libm), "tables (em)");
+    check(spatial_upload_tables(libm), "tables (spatial)");
+    check(query_upload_tables(libm), "tables (query)");
     return x;
   }();
   return c;
@@ -994,30 +1029,51 @@ void GpuField::runEm(SubField *const *sides, int count) {
   std::vector<LeafReport> reports(T);
   std::vector<LeafProfile> profiles(T);
   int emError = 0;
+  // the plain form: the surface regions, then the volume regions, each side
+  // one launch with one block per region
+  const bool plain = tuning.plainLaunches != 0;
+  uint32_t sideCount[2] = {0, 0};
+  for (const LeafTask &t : all) ++sideCount[(t.flags & kTaskVolume) ? 1 : 0];
+  const uint32_t plainMax = std::max(sideCount[0], sideCount[1]);
+  int emErrors[2] = {0, 0};
   if (T > 0) {
     tasks_.reserve(T);
     reports_.reserve(T);
     profiles_.reserve(T);
     queue_.reserve(1);
-    emShare_.reserve(em_share_bytes(c.numSMs));
+    emShare_.reserve(plain ? 2 * em_share_bytes_plain(int(plainMax)) : em_share_bytes(c.numSMs));
     check(cudaMemcpyAsync(tasks_.p, all.data(), T * sizeof(LeafTask), cudaMemcpyHostToDevice, s), "tasks");
     check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), s), "queue");
   }
   check(cudaEventRecord(emStart, s), "event");
   // the batched form: one persistent launch for every region of both
-  // sub-fields; the plain form: one single-block launch per region, in order
-  // (its launches run one after the other; each sees only its own region)
-  const int blocks = tuning.plainLaunches ? 1 : c.numSMs;
-  if (T > 0 && !tuning.plainLaunches)
+  // sub-fields (blocks take regions from a queue and, once out of regions,
+  // help the others' E-step passes)
+  const int blocks = c.numSMs;
+  if (T > 0 && !plain)
     check(launch_em(tasks_.p, T, queue_.p, es, reports_.p, profiles_.p, emShare_.p, blocks, tuning, s), "em");
-  for (uint32_t k = 0; T > 0 && tuning.plainLaunches && k < T; ++k) {
-    if (k > 0) check(cudaMemsetAsync(queue_.p, 0, sizeof(unsigned int), s), "queue");
-    check(launch_em(tasks_.p + k, 1, queue_.p, es, reports_.p + k, profiles_.p + k, emShare_.p, 1, tuning, s), "em");
-    if ((k & 63u) == 63u) {  // a failed launch stops the chain
-      check(cudaMemcpyAsync(&emError, emShare_.p + em_share_error_offset(1), sizeof(int), cudaMemcpyDeviceToHost, s),
+  std::vector<uint32_t> plainOrder;  // task index of launch position k (plain form)
+  if (T > 0 && plain) {
+    std::vector<LeafTask> bySide;
+    for (int side = 0; side < 2; ++side)
+      for (uint32_t k = 0; k < T; ++k)
+        if (((all[k].flags & kTaskVolume) ? 1 : 0) == side) {
+          bySide.push_back(all[k]);
+          plainOrder.push_back(k);
+        }
+    check(cudaMemcpyAsync(tasks_.p, bySide.data(), T * sizeof(LeafTask), cudaMemcpyHostToDevice, s), "tasks");
+    uint32_t first = 0;
+    for (int side = 0; side < 2; ++side) {
+      const uint32_t n = sideCount[side];
+      if (n == 0) continue;
+      unsigned char *share = emShare_.p + size_t(side) * em_share_bytes_plain(int(plainMax));
+      check(launch_em(tasks_.p + first, n, queue_.p, es, reports_.p + first, profiles_.p + first, share, int(n),
+                      tuning, s),
+            "em (plain)");
+      check(cudaMemcpyAsync(&emErrors[side], share + em_share_error_offset(int(n)), sizeof(int),
+                            cudaMemcpyDeviceToHost, s),
             "EM status");
-      check(cudaStreamSynchronize(s), "plain EM");
-      if (emError != 0) break;
+      first += n;
     }
   }
   check(cudaEventRecord(emEnd, s), "event");
@@ -1025,11 +1081,24 @@ void GpuField::runEm(SubField *const *sides, int count) {
     check(cudaMemcpyAsync(profiles.data(), profiles_.p, T * sizeof(LeafProfile), cudaMemcpyDeviceToHost, s),
           "profiles");
     check(cudaMemcpyAsync(reports.data(), reports_.p, T * sizeof(LeafReport), cudaMemcpyDeviceToHost, s), "reports");
-    check(cudaMemcpyAsync(&emError, emShare_.p + em_share_error_offset(blocks), sizeof(int),
-                          cudaMemcpyDeviceToHost, s),
-          "EM status");
+    if (!plain)
+      check(cudaMemcpyAsync(&emError, emShare_.p + em_share_error_offset(blocks), sizeof(int),
+                            cudaMemcpyDeviceToHost, s),
+            "EM status");
   }
   check(cudaStreamSynchronize(s), "update");
+  if (plain) {
+    emError = emErrors[0] != 0 ? emErrors[0] : emErrors[1];
+    // back to the order of `all`
+    std::vector<LeafReport> r(T);
+    std::vector<LeafProfile> p(T);
+    for (uint32_t k = 0; k < T; ++k) {
+      r[plainOrder[k]] = reports[k];
+      p[plainOrder[k]] = profiles[k];
+    }
+    reports.swap(r);
+    profiles.swap(p);
+  }
   if (emError != 0) {
     cudaEventDestroy(emStart);
     cudaEventDestroy(emEnd);
@@ -1212,7 +1281,15 @@ struct Reader {
     return v;
   }
   void lanes(float *a, int v) { raw(a + v * kLanes, sizeof(float) * kLanes); }
+  // a count of records of at least `minBytes` each that the rest of the file
+  // can hold (checked before anything is allocated for them)
+  uint64_t count(uint64_t minBytes) {
+    const uint64_t n = get<uint64_t>();
+    if (n > (b.size() - o) / minBytes) throw std::runtime_error("field file is truncated");
+    return n;
+  }
 };
+size_t bytes_left(const Reader &r) { return r.b.size() - r.o; }
 void read_sub(Reader &r, SubField &f) {  // Field::deserialize (Field.h:269-301), CPU_8 lane layout
   FieldConfig &c = f.cfg;
   f.isSurface = r.get<uint8_t>() != 0;
@@ -1248,14 +1325,16 @@ void read_sub(Reader &r, SubField &f) {  // Field::deserialize (Field.h:269-301)
   c.maxDepth = r.get<uint64_t>();
   f.kdInit = r.get<uint8_t>() != 0;
   r.raw(f.kdBounds, 24);
-  const uint64_t numNodes = r.get<uint64_t>();
+  const uint64_t numNodes = r.count(8);  // float split + u32 per node
   if (numNodes > (uint64_t(1) << 30)) throw std::runtime_error("field file: bad node count");
   f.nodes.resize(numNodes);
   for (KDNode &n : f.nodes) {
     n.split = r.get<float>();
     n.bits = r.get<uint32_t>();
   }
-  const uint64_t numRegions = r.get<uint64_t>();
+  // a region record (valid flag, mixture, bounds, statistics) takes well over
+  // 1 KB; 512 bytes bounds it from below
+  const uint64_t numRegions = r.count(512);
   if (numRegions > (uint64_t(1) << 30)) throw std::runtime_error("field file: bad region count");
   std::vector<RegionDir> dir(numRegions);
   f.regions.assign(numRegions, RegionHost());
@@ -1320,6 +1399,7 @@ void read_sub(Reader &r, SubField &f) {  // Field::deserialize (Field.h:269-301)
   c.knn = r.get<uint8_t>() != 0;
   if (r.get<uint8_t>() != 0) {  // KNN points (the region means), rebuilt below
     const uint32_t np = r.get<uint32_t>();
+    if (np > (bytes_left(r)) / 16) throw std::runtime_error("field file is truncated");
     std::vector<float> pts(size_t(np) * 4);
     r.raw(pts.data(), pts.size() * sizeof(float));
   }

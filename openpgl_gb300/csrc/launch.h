@@ -35,12 +35,15 @@ size_t split_max_records();
 cudaError_t split_samples_noalloc(const PGLSampleRecord *in, size_t n, PGLSampleRecord *surf, PGLSampleRecord *vol,
                                   uint32_t *counts, cudaStream_t s);
 
-cudaError_t em_upload_tables();
+cudaError_t em_upload_tables(const LibmTables &libm);
+// Path-vertex queries: Init + cosine product, then kVertexSamples SamplePDF calls.
+cudaError_t launch_query_s4(const QueryParams &p, const QueryInS4 *in, QueryOutS4 *out, uint32_t n,
+                            cudaStream_t s);
 // Launches one thread that waits, with the EM kernel's bounded wait, on a flag
 // nothing sets; *errOut receives the error the wait recorded (2: it ran out).
 cudaError_t em_bounded_wait_probe(unsigned long long limitNs, int *errOut, cudaStream_t s);
-cudaError_t spatial_upload_tables();
-cudaError_t query_upload_tables();
+cudaError_t spatial_upload_tables(const LibmTables &libm);
+cudaError_t query_upload_tables(const LibmTables &libm);
 
 // ingest: AoS batch (device) -> surface / volume SoA, stable per class.
 cudaError_t ingest_samples(const PGLSampleRecord *in, uint32_t n, Scratch &scratch, SoAView surf, SoAView vol,
@@ -106,7 +109,8 @@ struct EmTuning {
   int chunkDiv = 1;
   int stageCap = 8;
   int orderByCost = 0;
-  int plainLaunches = 0;  // 1: one single-block launch per region (the plain form), same results
+  int plainLaunches = 0;  // 1: the plain form (one launch per sub-field, one block per region,
+                          // no queue and no helper blocks), same results
 };
 bool em_tuning_valid(const EmTuning &t);
 // Device memory through which the EM launch's blocks share E-step passes
@@ -114,6 +118,7 @@ bool em_tuning_valid(const EmTuning &t);
 // the launch the int at em_share_error_offset(blocks) is non-zero if a wait
 // of the launch ran out (its results are then not valid).
 size_t em_share_bytes(int blocks);
+size_t em_share_bytes_plain(int blocks);  // the plain form: boards and error word only
 size_t em_share_error_offset(int blocks);
 cudaError_t launch_em(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, const EmSides &sides,
                       LeafReport *reports, LeafProfile *profiles, void *share, int blocks, const EmTuning &tune,

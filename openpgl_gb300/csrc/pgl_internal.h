@@ -137,6 +137,22 @@ struct QueryOut {  // 32 bytes
   float s1d, dx, dy, dz, pdf, pdfLi;
 };
 
+// A path vertex with several SamplePDF calls on one initialised
+// distribution (76 bytes): position, normal, outgoing direction and
+// roughness (carried; the surface distribution consumes only the normal,
+// through the cosine product), the region-choice random number and one 2D
+// random number per sample.
+constexpr int kVertexSamples = 4;
+struct QueryInS4 {
+  float px, py, pz, nx, ny, nz, wox, woy, woz, roughness, s1d;
+  float u[kVertexSamples][2];
+};
+struct QueryOutS4 {  // 76 bytes
+  uint32_t ok, id;
+  float s1d;
+  float s[kVertexSamples][4];  // direction xyz, pdf of each SamplePDF
+};
+
 struct FieldView {
   const KDNode *nodes;
   const RegionDir *regions;

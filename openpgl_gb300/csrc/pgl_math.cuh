@@ -20,6 +20,8 @@
 #include <cmath>
 #include <cfloat>
 
+#include <vector_types.h>
+
 #ifdef __CUDACC__
 #define PGL_HD __host__ __device__ __forceinline__
 #else
@@ -40,12 +42,24 @@ namespace pgl {
 // rcp/rsqrt seed tables: the host reads the static arrays of
 // x86_approx_tables.h; every CUDA translation unit has its own constant-memory
 // copy, filled by the upload function that PGL_DEFINE_TABLE_UPLOAD defines.
+// Inputs at which the host C library's expf and cosf differ from the
+// double-precision function rounded once (gen_libm_exceptions.cpp writes
+// them, the library loads them into device memory when it sets up CUDA):
+// sorted {x, host result} pairs.
+struct LibmTables {
+  const float2 *expf;
+  const float2 *cosf;
+  uint32_t numExpf, numCosf;
+};
 #ifdef __CUDACC__
 static __constant__ uint32_t d_rcp_table[2048];
 static __constant__ uint32_t d_rsqrt_table[2048];
+static __constant__ LibmTables d_libm;
 #define PGL_DEFINE_TABLE_UPLOAD(fn)                                                                  \
-  cudaError_t fn() {                                                                                 \
+  cudaError_t fn(const LibmTables &libm) {                                                           \
     cudaError_t e = cudaMemcpyToSymbol(d_rcp_table, pgl_x86_rcp_table, sizeof(pgl_x86_rcp_table));     \
+    if (e != cudaSuccess) return e;                                                                  \
+    e = cudaMemcpyToSymbol(d_libm, &libm, sizeof(LibmTables));                                       \
     if (e != cudaSuccess) return e;                                                                  \
     return cudaMemcpyToSymbol(d_rsqrt_table, pgl_x86_rsqrt_table, sizeof(pgl_x86_rsqrt_table));       \
   }
@@ -156,10 +170,24 @@ PGL_HD float floorf_(float x) {
 // evaluated in double and rounded once to float: that is the correctly rounded
 // result except where the exact value lies within ~2^-29 ulp of a rounding
 // boundary, and it equals the C library's float result wherever that one is
-// correctly rounded (glibc's expf/logf/sinf/cosf are, bar rare inputs).
+// correctly rounded.  glibc's expf and cosf are not on about 0.07 % and 0.2 %
+// of inputs; lib_expf and lib_cosf take the host library's result for those
+// inputs (and for those near a rounding boundary) from its exception table.
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ float libm_lookup(const float2 *t, uint32_t n, float x, float r) {
+  if (t == nullptr || n == 0 || !(x >= t[0].x && x <= t[n - 1].x)) return r;
+  uint32_t lo = 0, hi = n - 1;  // t[lo].x <= x <= t[hi].x
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (t[mid].x < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return t[lo].x == x ? t[lo].y : r;
+}
+#endif
 PGL_HD float lib_expf(float x) {
 #ifdef __CUDA_ARCH__
-  return float(exp(double(x)));
+  return libm_lookup(d_libm.expf, d_libm.numExpf, x, float(exp(double(x))));
 #else
   return std::exp(x);
 #endif
@@ -173,7 +201,7 @@ PGL_HD float lib_logf(float x) {
 }
 PGL_HD float lib_cosf(float x) {
 #ifdef __CUDA_ARCH__
-  return float(cos(double(x)));
+  return libm_lookup(d_libm.cosf, d_libm.numCosf, x, float(cos(double(x))));
 #else
   return std::cos(x);
 #endif

@@ -262,6 +262,54 @@ __global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, ui
   if (lane == 0) out[gw] = o;
 }
 
+// Batched path-vertex query: Init + cosine product once, then one SamplePDF
+// per 2D random number on the same distribution (the sampled distribution
+// is not changed by sampling: VMMSurfaceSamplingDistribution.h:67-103), as a
+// renderer does per vertex and openpgl_bench's lookup loop does per
+// initialised distribution (openpgl_bench.cpp:343-362).
+__global__ void query_s4_kernel(QueryParams P, const QueryInS4 *in, QueryOutS4 *out, uint32_t n) {
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= n) return;
+  const QueryInS4 q = in[gw];
+  const FieldView &f = P.f;
+  QueryOutS4 o;
+  o.ok = 0;
+  o.id = 0;
+  o.s1d = q.s1d;
+#pragma unroll
+  for (int k = 0; k < kVertexSamples; ++k) o.s[k][0] = o.s[k][1] = o.s[k][2] = o.s[k][3] = 0.0f;
+  bool inside = f.iteration > 0 && q.px >= f.bounds[0] && q.px <= f.bounds[3] && q.py >= f.bounds[1] &&
+                q.py <= f.bounds[4] && q.pz >= f.bounds[2] && q.pz <= f.bounds[5];
+  if (inside) {
+    uint32_t leaf = kd_leaf(f, q.px, q.py, q.pz);
+    uint32_t reg = leaf;
+    float s1d = q.s1d;
+    if (f.knn && s1d >= 0.f) reg = choose_region(f, leaf, q.px, q.py, q.pz, s1d, lane);
+    o.s1d = s1d;
+    const RegionDir &R = f.regions[reg];
+    if (R.valid) {
+      const int K = int(R.vmm.K), cnt = vec_count(K);
+      Lobe g = load_shifted(R.vmm, lane, q.px, q.py, q.pz, f.parallax != 0);
+      if (P.cosine) {
+        float integral;
+        g = product_lobe(g, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, 1.0f, cnt, lane, integral);
+      }
+#pragma unroll
+      for (int k = 0; k < kVertexSamples; ++k) {
+        const V3 d = mixture_sample(g, K, (q.u[k][0] - 0.0f) / 1.0f, q.u[k][1], lane);
+        o.s[k][0] = d.x;
+        o.s[k][1] = d.y;
+        o.s[k][2] = d.z;
+        o.s[k][3] = 0.0f + 1.0f * mixture_pdf(g, d, cnt, lane);
+      }
+      o.ok = 1;
+      o.id = leaf;
+    }
+  }
+  if (lane == 0) out[gw] = o;
+}
+
 // ---------------------------------------------------------------- per-object path
 // State of one SurfaceSamplingDistribution / VolumeSamplingDistribution on the
 // device: the shifted mixture (for IncomingRadiancePDF) and the product one.
@@ -354,8 +402,8 @@ __global__ void ssd_pdf_kernel(const SSDState *st, float dx, float dy, float dz,
 
 // ---------------------------------------------------------------- launchers
 PGL_DEFINE_TABLE_UPLOAD(query_upload_seed_tables)
-cudaError_t query_upload_tables() {
-  cudaError_t e = query_upload_seed_tables();
+cudaError_t query_upload_tables(const LibmTables &libm) {
+  cudaError_t e = query_upload_seed_tables(libm);
   if (e != cudaSuccess) return e;
   return cudaMemcpyToSymbol(c_hg, kHgTable, sizeof(kHgTable));
 }
@@ -367,6 +415,15 @@ cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out,
   unsigned blocks = unsigned((warps * 32 + threads - 1) / threads);
   count_launch();
   query_kernel<<<blocks, threads, 0, s>>>(p, in, out, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_query_s4(const QueryParams &p, const QueryInS4 *in, QueryOutS4 *out, uint32_t n,
+                            cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const unsigned threads = 256;
+  unsigned blocks = unsigned((uint64_t(n) * 32 + threads - 1) / threads);
+  count_launch();
+  query_s4_kernel<<<blocks, threads, 0, s>>>(p, in, out, n);
   return cudaGetLastError();
 }
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,

@@ -38,6 +38,13 @@ PGL_QUERY_DTYPE = np.dtype(
 )
 assert PGL_QUERY_DTYPE.itemsize == 36
 
+# Path vertex with four 2D random numbers (PGLGuidedVertex, 76 bytes).
+PGL_VERTEX_DTYPE = np.dtype(
+    [("position", "<f4", (3,)), ("normal", "<f4", (3,)), ("wo", "<f4", (3,)), ("roughness", "<f4"),
+     ("sample1d", "<f4"), ("u", "<f4", (4, 2))]
+)
+assert PGL_VERTEX_DTYPE.itemsize == 76
+
 FLAG_INSIDE_VOLUME = 2
 _LN2 = 0.6931471805599453
 _INV_4PI = 0.07957747154594767
@@ -212,6 +219,35 @@ def queries(n, seed, model_seed=None, num_clusters=4096):
     # float32 values strictly below 1 (the reference asserts sample1D < 1)
     q["sample1d"] = np.minimum(rng.random(n), 0.99999994).astype(np.float32)
     q["u"] = np.minimum(rng.random((n, 2)), 0.99999994).astype(np.float32)
+    return q
+
+
+def vertices(n, seed, model_seed=1234, num_clusters=4096):
+    """Path vertices of the serving workload: position drawn from the cluster
+    model, normal and outgoing direction uniform on the sphere, roughness,
+    sample1D and four 2D random numbers uniform in [0,1)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    v = np.zeros(n, dtype=PGL_VERTEX_DTYPE)
+    m = cluster_model(model_seed, num_clusters)
+    cdf = np.cumsum(m["mass"])
+    c = np.minimum(np.searchsorted(cdf, rng.random(n) * cdf[-1], side="right"), num_clusters - 1)
+    v["position"] = (m["centers"][c] + m["sigma"][c][:, None] * _normal(rng, (n, 3))).astype(np.float32)
+    v["normal"] = _unit_sphere(rng, n).astype(np.float32)
+    v["wo"] = _unit_sphere(rng, n).astype(np.float32)
+    v["roughness"] = rng.random(n).astype(np.float32)
+    v["sample1d"] = np.minimum(rng.random(n), 0.99999994).astype(np.float32)
+    v["u"] = np.minimum(rng.random((n, 4, 2)), 0.99999994).astype(np.float32)
+    return v
+
+
+def vertex_queries(v, k):
+    """The single-sample guided queries equal to SamplePDF call k of each
+    vertex (same position, normal and sample1D, the k-th 2D random number)."""
+    q = np.zeros(len(v), dtype=PGL_QUERY_DTYPE)
+    q["position"] = v["position"]
+    q["normal"] = v["normal"]
+    q["sample1d"] = v["sample1d"]
+    q["u"] = v["u"][:, k]
     return q
 
 

@@ -89,3 +89,16 @@ def test_bad_files_are_rejected(pgl, tmp_path):
     p.write_bytes(ref[: len(ref) // 2])
     with pytest.raises(RuntimeError):
         pgl.Field.from_file(dev, str(p))
+    # a node count far beyond what the file holds is refused before anything
+    # is allocated for it (no attempt at a 2^29-node tree)
+    import struct
+
+    import fieldfile
+
+    surf = fieldfile.read_field_file(ref)["surface"]
+    n = len(surf["nodes"])
+    first = struct.pack("<fI", float(surf["nodes"]["split"][0]), int(surf["nodes"]["bits"][0]))
+    at = ref.index(struct.pack("<Q", n) + first)
+    p.write_bytes(ref[:at] + struct.pack("<Q", 1 << 29) + ref[at + 8:])
+    with pytest.raises(RuntimeError, match="truncated"):
+        pgl.Field.from_file(dev, str(p))

@@ -7,6 +7,8 @@ and sample-to-leaf assignment bit-exact; per leaf, the relative PDF error on a
 fixed 64x64 direction grid at most 1e-3; guided queries choose the same region
 and return the same pdf within 1e-3 relative (directions within 1e-3)."""
 
+import os
+
 import numpy as np
 import pytest
 
@@ -31,7 +33,7 @@ def _train(pgl, frames, leaf, deterministic=True):
     dev = pgl.Device()
     field = pgl.Field(dev, pgl.FieldConfig(deterministic=deterministic, max_samples_per_leaf=leaf))
     storage = pgl.SampleStorage()
-    orc = pyoracle.OracleField(leaf, deterministic=deterministic, threads=8)
+    orc = pyoracle.OracleField(leaf, deterministic=deterministic, threads=os.cpu_count() or 8)
     for f in frames:
         storage.add_samples(f)
         field.update(storage)
@@ -268,3 +270,20 @@ def test_hg_product_matches_oracle_and_per_object(pgl, tmp_path):
         assert np.float32(vsd.pdf(d)) == out["pdf"][i]
         assert np.float32(vsd.incoming_radiance_pdf(d)) == out["pdfLi"][i]
     vsd.release()
+
+
+def test_multiframe_configuration(pgl):
+    """The multi-frame configuration the bench times, at its full size: 8
+    frames of 2,097,152 samples (25 % inside-volume), maxSamplesPerLeaf
+    32000, the storage cleared after every Update; then 1,048,576 guided
+    queries.  Every leaf of both sub-fields within the bar (in fact every
+    mixture bit-exact) and every query within it."""
+    from openpgl_gb300 import synthetic as syn
+
+    frames = [syn.cube_face_samples(2097152, 9000 + f, volume_fraction=0.25) for f in range(8)]
+    dev, field, orc = _train(pgl, frames, 32000)
+    for side in ("surface", "volume"):
+        r = _check_field(field, orc, side)
+        assert r["bit_exact_regions"] == r["regions"], (side, summary(r))
+    q = syn.queries(1 << 20, 4242)
+    _check_queries(field.sample_batch(q), orc.query(q), "1M queries")
