@@ -112,6 +112,8 @@ template struct DevArray<LeafProfile>;
 template struct DevArray<IStatsAcc>;
 template struct DevArray<QueryIn>;
 template struct DevArray<QueryOut>;
+template struct DevArray<QueryInS4>;
+template struct DevArray<QueryOutS4>;
 template struct DevArray<unsigned long long>;
 template struct DevArray<unsigned char>;
 
