@@ -74,6 +74,11 @@ EM_TRAFFIC_PER_SAMPLE = 60.9
 PORT_NOTE = "oracle port; the compiled reference ran 3.3-3.9x faster than this port per frame on x86"
 
 
+def log(msg):
+    """Progress of the benchmark's legs (stderr; the JSON line goes to stdout)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def host_info():
     """Host cores and CPU model string (lscpu, else /proc/cpuinfo)."""
     model = None
@@ -183,10 +188,12 @@ def run_clustered(pgl, dev, stream, steps, warmup):
     storage = pgl.SampleStorage()
     torch.cuda.synchronize()
 
-    def update(tuning=None, autotune=False):
+    def update(tuning=None, autotune=False, plain=False):
         field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF))
         if tuning:
             field.set_em_tuning(**tuning)
+        if plain:
+            field.set_plain_update(True)
         if autotune:
             field.autotune_next_update()
         storage.clear()
@@ -216,14 +223,24 @@ def run_clustered(pgl, dev, stream, steps, warmup):
     same = tuned_field.field_bytes() == ref.field_bytes()
     field, ms_tuned, em_tuned = timed(chosen)
     same = same and field.field_bytes() == ref.field_bytes()
-    return {"workload": "clustered: 16,777,216 surface samples around 4096 Gaussian clusters (Zipf(1.1) masses, "
-                        "1-6 vMF lobes each), maxSamplesPerLeaf 32000, deterministic; one Update of a fresh field",
-            "regions": int(ref.phases(False)["regions"]),
-            "update_ms": round(ms_default, 3), "em_kernel_ms": round(em_default, 3),
-            "autotuned": {"update_ms": round(ms_tuned, 3), "em_kernel_ms": round(em_tuned, 3), "schedule": chosen,
-                          "trials": len(trials), "tuning_update_ms": round(tune_ms, 1),
-                          "best_trial_ms": round(min(t["ms"] for t in trials), 3) if trials else None},
-            "same_field": bool(same)}
+    # the plain drop-in form on the same Update (per sub-field one EM launch,
+    # one block per region)
+    plain_times = []
+    for _ in range(2):
+        pf, t = update(plain=True)
+        plain_times.append(t)
+    plain_same = pf.field_bytes() == ref.field_bytes()
+    out = {"workload": "clustered: 16,777,216 surface samples around 4096 Gaussian clusters (Zipf(1.1) masses, "
+                       "1-6 vMF lobes each), maxSamplesPerLeaf 32000, deterministic; one Update of a fresh field",
+           "regions": int(ref.phases(False)["regions"]),
+           "update_ms": round(ms_default, 3), "em_kernel_ms": round(em_default, 3),
+           "autotuned": {"update_ms": round(ms_tuned, 3), "em_kernel_ms": round(em_tuned, 3), "schedule": chosen,
+                         "trials": len(trials), "tuning_update_ms": round(tune_ms, 1),
+                         "best_trial_ms": round(min(t["ms"] for t in trials), 3) if trials else None},
+           "same_field": bool(same),
+           "plain_update": {"update_ms": round(min(plain_times), 3), "same_field": bool(plain_same),
+                            "batched_speedup": round(min(plain_times) / ms_default, 2)}}
+    return out, ref
 
 
 # ----------------------------------------------------------------- widened rows
@@ -452,6 +469,283 @@ def run_serving(pgl, field, frames, queries, seconds=6.0, submitters=8, update_e
             "served_vs_plain": round(st["queries"] / wall / plain_qps, 1)}
 
 
+# ----------------------------------------------------------------- serving workload
+SERVE_BUDGET = 40 << 30
+SERVE_POOL = 1 << 20       # vertices the request stream draws its batches from
+SERVE_MIN, SERVE_MAX = 1024, 1 << 20
+UPDATE_EVERY = 500         # batches between interleaved Updates
+UPDATE_SAMPLES = 2_097_152
+
+
+def run_serving_c3(pgl, field, batches_per_rate=1000, loads=(0.25, 0.5, 0.75, 0.9, 1.0, 1.25), plain_seconds=3.0):
+    """The serving workload on the clustered field: batches of path vertices
+    (sizes log-uniform in 1,024-1,048,576; position from the clusters, normal,
+    wo, roughness, sample1D, four 2D random numbers; per vertex Init + cosine
+    product + 4 SamplePDF) arriving by Poisson at rates swept to saturation,
+    a 2,097,152-sample Update interleaved every 500 batches, a 40 GB HBM
+    budget.  Per rate: offered and achieved vertices/s and p50/p99/p99.9
+    request latency (arrival to results in host memory).  Beside it the plain
+    drop-in: the per-object C API driven from C++ threads (one vertex at a
+    time, as a renderer's threads call the reference)."""
+    import queue as queue_mod
+
+    import torch
+
+    from openpgl_gb300 import synthetic as syn
+
+    pool = torch.from_numpy(syn.vertices(SERVE_POOL, 3303).view(np.uint8)).pin_memory()
+    verts = pool.numpy().view(syn.PGL_VERTEX_DTYPE)
+    out_pool = torch.empty(8 * SERVE_POOL * 76, dtype=torch.uint8).pin_memory()
+    outs = out_pool.numpy().view(pgl.VERTEX_RESULT_DTYPE)
+    rng = np.random.default_rng(3304)
+    train = [syn.cluster_samples(UPDATE_SAMPLES, 3400 + k) for k in range(2)]
+    server = pgl.GuidingServer(field, hbm_budget_bytes=SERVE_BUDGET)
+
+    def run(rate, nb):
+        """nb batches arriving at `rate` batches/s (None: all at once)."""
+        sizes = np.exp(rng.uniform(np.log(SERVE_MIN), np.log(SERVE_MAX), size=nb)).astype(np.int64)
+        gaps = rng.exponential(1.0 / rate, size=nb) if rate else np.zeros(nb)
+        arrivals = np.cumsum(gaps)
+        done_q = queue_mod.Queue()
+        lat = np.zeros(nb)
+        out_at = [0]
+        updates = []
+
+        def waiter():
+            while True:
+                item = done_q.get()
+                if item is None:
+                    return
+                i, t, t_arr, t_sub = item
+                ms, _ = server.wait(t)
+                lat[i] = ms + (t_sub - t_arr) * 1e3
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        server.reset_stats()
+        t0 = time.perf_counter()
+        for i in range(nb):
+            n = int(sizes[i])
+            now = time.perf_counter() - t0
+            if arrivals[i] > now:
+                time.sleep(arrivals[i] - now)
+            off = int(rng.integers(0, SERVE_POOL - n + 1))
+            o = out_at[0] if out_at[0] + n <= len(outs) else 0
+            out_at[0] = o + n
+            t_sub = time.perf_counter() - t0
+            t, _ = server.submit_vertices(verts[off:off + n], outs[o:o + n])
+            done_q.put((i, t, t0 + arrivals[i] if rate else t0, t0 + t_sub))
+            if (i + 1) % UPDATE_EVERY == 0:
+                server.add_samples(train[(i // UPDATE_EVERY) % len(train)])
+                updates.append(server.update())
+        done_q.put(None)
+        th.join()
+        wall = time.perf_counter() - t0
+        for u in updates:
+            server.wait_update(u)
+        st = server.stats()
+        return sizes, lat, wall, st
+
+    # service capacity: all batches of a closed burst
+    sizes, lat, wall, st = run(None, max(100, batches_per_rate // 4))
+    capacity = len(sizes) / wall
+    log(f"serving capacity {capacity:.1f} batches/s ({float(sizes.sum()) / wall / 1e6:.1f} M vertices/s)")
+    points = []
+    for load in loads:
+        rate = load * capacity
+        sizes, lat, wall, st = run(rate, batches_per_rate)
+        log(f"load {load}: {float(sizes.sum()) / wall / 1e6:.1f} M vertices/s, p99 {np.percentile(lat, 99):.2f} ms")
+        points.append({"load": load, "offered_batches_per_s": round(rate, 1),
+                       "offered_vertices_per_s": round(rate * float(sizes.mean())),
+                       "vertices_per_s": round(float(sizes.sum()) / wall),
+                       "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                       "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                       "p999_ms": round(float(np.percentile(lat, 99.9)), 3),
+                       "batches": int(len(sizes)), "updates": int(st["updates"])})
+    mem = server.stats()
+    server.release()
+    # the plain drop-in: per-object calls from C++ threads (the field through its file)
+    plain = run_plain_driver(pgl, field, verts[:65536], seconds=plain_seconds)
+    out = {"workload": "path vertices on the clustered field: batches log-uniform in 1,024-1,048,576 vertices, "
+                       "Poisson arrivals swept to saturation, Init + cosine product + 4 SamplePDF per vertex, "
+                       "a 2,097,152-sample Update every 500 batches, 40 GB HBM budget",
+           "batches_per_rate": batches_per_rate, "saturation_batches_per_s": round(capacity, 1),
+           "points": points, "device_bytes": int(mem["device_bytes"]), "budget_bytes": int(mem["budget_bytes"]),
+           "plain": plain}
+    if plain:
+        # matched p99: the plain form serving the same request sizes one vertex
+        # at a time takes n / (vertices/s) per request; the served form's best
+        # throughput among the rates whose p99 is no worse than that
+        plain_p99 = float(np.percentile(sizes, 99)) / plain["vertices_per_s"] * 1e3
+        ok = [p for p in points if p["p99_ms"] <= plain_p99]
+        best = max(ok, key=lambda p: p["vertices_per_s"]) if ok else None
+        out["matched_p99"] = {"plain_p99_request_ms": round(plain_p99, 1),
+                              "served_vertices_per_s": best["vertices_per_s"] if best else None,
+                              "served_vs_plain": round(best["vertices_per_s"] / plain["vertices_per_s"], 1)
+                              if best else None}
+    return out
+
+
+def run_plain_driver(pgl, field, verts, seconds=3.0, threads=None):
+    """Runs the per-object query driver (C++ threads, one vertex at a time)
+    on a copy of `field` read from its file."""
+    import tempfile
+
+    exe = os.path.join(ROOT, "openpgl_gb300", "_build", "plain_query_driver")
+    if not os.path.exists(exe):
+        return None
+    threads = threads or min(16, os.cpu_count() or 1)
+    with tempfile.TemporaryDirectory() as td:
+        fpath, vpath = os.path.join(td, "f.field"), os.path.join(td, "v.bin")
+        field.store(fpath)
+        with open(vpath, "wb") as f:
+            f.write(np.uint64(len(verts)).tobytes())
+            f.write(np.ascontiguousarray(verts).tobytes())
+        r = subprocess.run([exe, fpath, vpath, str(threads), str(seconds)], capture_output=True, text=True,
+                           timeout=seconds + 120)
+    if r.returncode != 0:
+        return {"error": r.stderr[-300:]}
+    done, wall, vps, p50, p99, p999 = (float(x) for x in r.stdout.split())
+    return {"threads": threads, "vertices": int(done), "vertices_per_s": round(vps, 1),
+            "p50_us": p50, "p99_us": p99, "p999_us": p999,
+            "form": "per-object C API (Init, ApplyCosineProduct, 4 SamplePDF) from C++ threads, one vertex per "
+                    "call chain"}
+
+
+# ----------------------------------------------------------------- scale workload
+SCALE_SAMPLES = 64 << 20
+SCALE_FRAMES = 16
+SCALE_LEAF = 16000
+
+
+def cluster_frame_device(n, seed, model, volume_fraction=0.25):
+    """A frame of the clustered distribution made on the device (torch's
+    seeded generator): cluster by mass, Gaussian offset, a lobe of the
+    cluster's mixture by weight, a vMF direction, lognormal(0,2) weight, pdf
+    1/(4 pi), distance U[0.05, 2], 25 % flagged inside-volume.  Records of
+    40 bytes (PGLSampleData).  Deterministic for a seed on a given device; it
+    stands in for the host generator, which is too slow at 64M samples."""
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    dev = "cuda"
+    cdf = torch.cumsum(model["mass"], 0)
+    c = torch.clamp(torch.searchsorted(cdf, torch.rand(n, device=dev, generator=g) * cdf[-1]), max=len(cdf) - 1)
+    pos = model["centers"][c] + model["sigma"][c, None] * torch.randn(n, 3, device=dev, generator=g)
+    lw = model["lobe_w"][c]
+    lcdf = torch.cumsum(lw, 1)
+    u = torch.rand(n, 1, device=dev, generator=g) * lcdf[:, -1:]
+    lobe = torch.clamp((lcdf < u).sum(1), max=5)
+    mu = model["mu"][c, lobe]
+    kappa = model["kappa"][c, lobe]
+    ux = torch.rand(n, device=dev, generator=g)
+    w = torch.clamp(1.0 + torch.log(ux + (1.0 - ux) * torch.exp(-2.0 * kappa)) / kappa, -1.0, 1.0)
+    phi = 2.0 * np.pi * torch.rand(n, device=dev, generator=g)
+    r = torch.sqrt(torch.clamp(1.0 - w * w, min=0.0))
+    local = torch.stack([r * torch.cos(phi), r * torch.sin(phi), w], 1)
+    # frame around mu
+    a = torch.where(mu[:, 2:3].abs() < 0.999, torch.tensor([0.0, 0.0, 1.0], device=dev),
+                    torch.tensor([1.0, 0.0, 0.0], device=dev))
+    t1 = torch.nn.functional.normalize(torch.cross(a, mu, dim=1), dim=1)
+    t2 = torch.cross(mu, t1, dim=1)
+    d = local[:, :1] * t1 + local[:, 1:2] * t2 + local[:, 2:3] * mu
+    rec = torch.empty(n, 10, dtype=torch.float32, device=dev)
+    rec[:, 0:3] = pos
+    rec[:, 3:6] = d
+    rec[:, 6] = torch.exp(2.0 * torch.randn(n, device=dev, generator=g))
+    rec[:, 7] = 0.07957747154594767
+    rec[:, 8] = 0.05 + 1.95 * torch.rand(n, device=dev, generator=g)
+    flags = (torch.rand(n, device=dev, generator=g) < volume_fraction).to(torch.int32) * 2
+    rec[:, 9] = flags.view(torch.float32)
+    return rec
+
+
+def run_scale(pgl, dev, serve_rate=None, frames=SCALE_FRAMES, n=SCALE_SAMPLES):
+    """The scale workload: 16 frames of 64M clustered samples (25 % volume),
+    maxSamplesPerLeaf 16000, each frame's Update run by the guiding server
+    (40 GB budget covering the double-buffered field, the sample storage and
+    the query buffers) while path-vertex batches keep arriving at
+    `serve_rate` batches/s (half of the serving workload's saturation)."""
+    import torch
+
+    from openpgl_gb300 import synthetic as syn
+
+    m = syn.cluster_model(1234)
+    model = {k: torch.from_numpy(np.asarray(v, dtype=np.float32)).cuda() for k, v in m.items()}
+    field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=SCALE_LEAF))
+    server = pgl.GuidingServer(field, hbm_budget_bytes=SERVE_BUDGET)
+    pool = torch.from_numpy(syn.vertices(SERVE_POOL, 3313).view(np.uint8)).pin_memory()
+    verts = pool.numpy().view(syn.PGL_VERTEX_DTYPE)
+    outs = torch.empty(4 * SERVE_POOL * 76, dtype=torch.uint8).pin_memory().numpy().view(pgl.VERTEX_RESULT_DTYPE)
+    stop = threading.Event()
+    lat = []
+    rng = np.random.default_rng(3314)
+
+    def load():
+        """Poisson batches of path vertices until stopped (from the second frame on)."""
+        out_at = 0
+        t_next = time.perf_counter()
+        pendingq = []
+        while not stop.is_set():
+            t_next += rng.exponential(1.0 / serve_rate)
+            now = time.perf_counter()
+            if t_next > now:
+                time.sleep(t_next - now)
+            nv = int(np.exp(rng.uniform(np.log(SERVE_MIN), np.log(SERVE_MAX))))
+            off = int(rng.integers(0, SERVE_POOL - nv + 1))
+            o = out_at if out_at + nv <= len(outs) else 0
+            out_at = o + nv
+            t, _ = server.submit_vertices(verts[off:off + nv], outs[o:o + nv])
+            pendingq.append(t)
+            while len(pendingq) > 64:
+                ms, _ = server.wait(pendingq.pop(0))
+                lat.append(ms)
+        for t in pendingq:
+            ms, _ = server.wait(t)
+            lat.append(ms)
+
+    per_frame, em_ms, regions, peak = [], [], [], 0
+    th = None
+    try:
+        for f in range(frames):
+            rec = cluster_frame_device(n, 5000 + f, model)
+            torch.cuda.synchronize()
+            server.add_samples_device(rec.data_ptr(), n)
+            del rec
+            t0 = time.perf_counter()
+            server.wait_update(server.update())
+            per_frame.append((time.perf_counter() - t0) * 1e3)
+            ph = [field.phases(False), field.phases(True)]
+            em_ms.append(ph[0]["em_kernel"])
+            regions.append(int(ph[0]["regions"] + ph[1]["regions"]))
+            peak = max(peak, int(server.stats()["device_bytes"]))
+            log(f"scale frame {f}: update {per_frame[-1]:.1f} ms, em {em_ms[-1]:.1f} ms, {regions[-1]} regions")
+            if f == 0 and serve_rate:
+                th = threading.Thread(target=load, daemon=True)
+                th.start()
+    finally:
+        stop.set()
+        if th:
+            th.join()
+    server.release()
+    field.release()
+    lat = np.array(lat) if lat else np.zeros(1)
+    total = sum(per_frame)
+    return {"workload": "16 frames x 67,108,864 clustered samples (25% inside-volume), maxSamplesPerLeaf 16000, "
+                        "Updates through the guiding server (40 GB budget) with path-vertex batches arriving "
+                        "at half the serving workload's saturation from the second frame on",
+            "frames": frames, "samples_per_frame": n, "update_ms_per_frame": [round(x, 1) for x in per_frame],
+            "em_kernel_ms_per_frame": [round(x, 1) for x in em_ms], "regions_per_frame": regions,
+            "ms_per_16M_samples": round(total * UNIT_SAMPLES / (frames * n), 3),
+            "concurrent_queries": {"batches_per_s": round(serve_rate, 1) if serve_rate else None,
+                                   "requests": int(len(lat)), "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                                   "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                                   "p999_ms": round(float(np.percentile(lat, 99.9)), 3)},
+            "peak_device_bytes": peak, "budget_bytes": SERVE_BUDGET,
+            "data": "generated on the device from the cluster model (torch seeded generator)"}
+
+
 # ----------------------------------------------------------------- GPU arm
 def run_gpu(args, rank, world, local_rank):
     import torch
@@ -479,8 +773,10 @@ def run_gpu(args, rank, world, local_rank):
     def barrier():
         replicas.barrier("cuda")
 
+    log("warm-up steps")
     for _ in range(args.warmup):
         step()
+    log("timed steps")
     clocks = ClockSampler(local_rank)
     clocks.start()
     barrier()
@@ -500,6 +796,7 @@ def run_gpu(args, rank, world, local_rank):
     # timed steps did the same work)
     em_work = em_counters(field, storage, frames, d_frames)
 
+    log(f"step {ms:.2f} ms; counter step and queries")
     # ---- guided queries on the trained field (device buffers)
     qdev = torch.from_numpy(queries.view(np.uint8)).to("cuda")
     rdev = torch.empty(QUERIES * 32, dtype=torch.uint8, device="cuda")
@@ -528,17 +825,30 @@ def run_gpu(args, rank, world, local_rank):
 
     # ---- rows beyond the core path: HG queries, path-segment samples, plain VMM,
     # and the plain drop-in form of the Update beside the batched one
+    log("widened rows")
     widened = None
     if args.widened:
         widened = run_widened(pgl, dev, stream, field, queries, frames, d_frames, args.steps, args.warmup)
         widened["plain_update"]["batched_speedup"] = round(widened["plain_update"]["value"] / ms, 2)
 
     # ---- clustered workload, default and autotuned EM schedule
-    clustered = run_clustered(pgl, dev, stream, args.steps, 1) if args.clustered else None
+    log("clustered workload")
+    clustered, clustered_field = run_clustered(pgl, dev, stream, args.steps, 1) if args.clustered else (None, None)
 
     # ---- served guided queries (continuous batching, background updates)
+    log("serving (closed loop)")
     serving = run_serving(pgl, field, frames[:2], queries, seconds=args.serve_seconds) if args.serve_seconds > 0 else None
+    serving_c3 = None
+    if clustered_field is not None and args.serve_batches > 0:
+        log("serving workload on the clustered field")
+        serving_c3 = run_serving_c3(pgl, clustered_field, batches_per_rate=args.serve_batches)
+    scale = None
+    if args.scale_frames > 0:
+        rate = 0.5 * serving_c3["saturation_batches_per_s"] if serving_c3 else None
+        log("scale workload")
+        scale = run_scale(pgl, dev, serve_rate=rate, frames=args.scale_frames)
 
+    log("end to end")
     # ---- end to end: host (pinned) sample records through the C API
     pinned = [torch.from_numpy(f.view(np.uint8)).pin_memory() for f in frames]
     host_views = [p.numpy().view(frames[0].dtype) for p in pinned]
@@ -603,12 +913,15 @@ def run_gpu(args, rank, world, local_rank):
                     "p99_ms": round(lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))], 3),
                     "e2e_queries_per_s": round(QUERIES / (q_e2e_ms * 1e-3)), "roofline": query_roof},
         "serving": serving,
+        "serving_clustered": serving_c3,
+        "scale": scale,
         "clustered": clustered,
         "widened": widened,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
     if not args.no_cpu_baseline:
+        log("CPU baseline and parity")
         out["cpu_baseline"], orc = cpu_baseline(frames, budget_s=args.cpu_budget)
         if orc is not None:
             out["parity"], qps = parity_block(orc, gpu_field_bytes, gpu_queries, queries)
@@ -814,6 +1127,10 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--no-clustered", dest="clustered", action="store_false",
                     help="skip the clustered workload (default and autotuned EM schedule)")
+    ap.add_argument("--serve-batches", type=int, default=1000,
+                    help="batches per arrival rate of the serving workload on the clustered field (0: skip)")
+    ap.add_argument("--scale-frames", type=int, default=SCALE_FRAMES,
+                    help="frames of the 64M-sample scale workload (0: skip)")
     ap.add_argument("--no-widened", dest="widened", action="store_false",
                     help="skip the rows beyond the core path (HG queries, path samples, plain VMM, plain form)")
     ap.add_argument("--em-capture", action="store_true",

@@ -211,8 +211,13 @@ OPENPGL_CORE_INTERFACE bool pglSplitSamplesDeviceNoAlloc(const PGLSampleData *dS
 struct GuidingServer;
 #endif
 typedef struct GuidingServer *PGLGuidingServer;
-// hbmBudgetBytes bounds the device memory of queries in flight (68 bytes per
-// query); larger requests run in several launches.
+// hbmBudgetBytes bounds the device memory that the server and its field use:
+// the field's state and Update working set, two snapshots of it that queries
+// read, the samples of the next Update (AddSamples refuses a batch whose
+// Update would not fit) and the buffers of two query launches in flight
+// (given at most a quarter of what the field leaves; larger requests run in
+// several launches).  While the server runs, the field's EM launches leave 8
+// SMs to the query launches, so queries keep being answered during an Update.
 OPENPGL_CORE_INTERFACE PGLGuidingServer pglNewGuidingServer(PGLField field, size_t hbmBudgetBytes);
 OPENPGL_CORE_INTERFACE void pglReleaseGuidingServer(PGLGuidingServer server);
 // Queues n queries; `queries` and `results` (host memory) must stay valid until
@@ -227,12 +232,28 @@ OPENPGL_CORE_INTERFACE bool pglGuidingServerWait(PGLGuidingServer server, uint64
 // Training samples for the next Update (copied).
 OPENPGL_CORE_INTERFACE bool pglGuidingServerAddSamples(PGLGuidingServer server, const PGLSampleData *samples,
                                                        size_t n);
+// Training samples in device memory (copied into the server's own device
+// buffer before the call returns).
+OPENPGL_CORE_INTERFACE bool pglGuidingServerAddSamplesDevice(PGLGuidingServer server, const PGLSampleData *dSamples,
+                                                             size_t n);
 // Starts an Update with the samples added so far; returns a ticket.
 OPENPGL_CORE_INTERFACE uint64_t pglGuidingServerUpdate(PGLGuidingServer server);
 OPENPGL_CORE_INTERFACE bool pglGuidingServerWaitUpdate(PGLGuidingServer server, uint64_t ticket);
+// Queues n path vertices (Init, cosine product, four SamplePDF calls each;
+// buffers as for pglGuidingServerSubmit).  Returns a ticket (0 on error).
+OPENPGL_CORE_INTERFACE uint64_t pglGuidingServerSubmitVertices(PGLGuidingServer server,
+                                                               const PGLGuidedVertex *vertices, size_t n,
+                                                               PGLGuidedVertexResult *results);
 // queries served, requests done, latency p50 / p99 / p99.9 (ms), launches,
 // updates done, field iteration being served
 OPENPGL_CORE_INTERFACE bool pglGuidingServerStats(PGLGuidingServer server, double out8[8]);
+// The same eight values, then the device bytes the server and its field hold,
+// the budget and the queries one launch takes at most; writes min(count, 11)
+// values and returns 11.
+OPENPGL_CORE_INTERFACE size_t pglGuidingServerStatsEx(PGLGuidingServer server, double *out, size_t count);
+// Starts a new measurement window (latencies, queries and launches counted
+// from here on).
+OPENPGL_CORE_INTERFACE bool pglGuidingServerResetStats(PGLGuidingServer server);
 // Message of the error raised by the last library call on this thread ("" if
 // that call succeeded).
 OPENPGL_CORE_INTERFACE const char *pglGetLastError();

@@ -169,6 +169,11 @@ C_API = {
     "pglGuidingServerUpdate": (ctypes.c_uint64, [ctypes.c_void_p]),
     "pglGuidingServerWaitUpdate": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_uint64]),
     "pglGuidingServerStats": (ctypes.c_bool, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "pglGuidingServerStatsEx": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t]),
+    "pglGuidingServerResetStats": (ctypes.c_bool, [ctypes.c_void_p]),
+    "pglGuidingServerAddSamplesDevice": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "pglGuidingServerSubmitVertices": (ctypes.c_uint64, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                         ctypes.c_void_p]),
     "pglSplitSamplesDeviceNoAlloc": (ctypes.c_bool, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
                                                      ctypes.c_void_p, ctypes.c_void_p]),
     "pglFieldGetLastUpdateProfile": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
@@ -687,6 +692,18 @@ class GuidingServer:
         self._keep[t] = (q, out)
         return t, out
 
+    def submit_vertices(self, vertices, out=None):
+        """Queue path vertices (Init + cosine product + four SamplePDF each);
+        returns (ticket, result array filled when done).  `vertices` and `out`
+        are kept alive until the request is waited for."""
+        v = np.ascontiguousarray(vertices, dtype=PGL_VERTEX_DTYPE)
+        if out is None:
+            out = np.zeros(len(v), dtype=VERTEX_RESULT_DTYPE)
+        t = self.lib.pglGuidingServerSubmitVertices(self.h, v.ctypes.data, len(v), out.ctypes.data)
+        _check(t != 0, "pglGuidingServerSubmitVertices")
+        self._keep[t] = (v, out)
+        return t, out
+
     def wait(self, ticket):
         """(latency ms, field iteration of the results)"""
         lat = ctypes.c_double()
@@ -700,6 +717,9 @@ class GuidingServer:
         s = np.ascontiguousarray(samples, dtype=PGL_SAMPLE_DTYPE)
         _check(self.lib.pglGuidingServerAddSamples(self.h, s.ctypes.data, len(s)), "pglGuidingServerAddSamples")
 
+    def add_samples_device(self, ptr, n):
+        _check(self.lib.pglGuidingServerAddSamplesDevice(self.h, ptr, n), "pglGuidingServerAddSamplesDevice")
+
     def update(self):
         t = self.lib.pglGuidingServerUpdate(self.h)
         _check(t != 0, "pglGuidingServerUpdate")
@@ -709,10 +729,14 @@ class GuidingServer:
         _check(self.lib.pglGuidingServerWaitUpdate(self.h, ticket), "pglGuidingServerWaitUpdate")
 
     def stats(self):
-        out = (ctypes.c_double * 8)()
-        _check(self.lib.pglGuidingServerStats(self.h, out), "pglGuidingServerStats")
-        keys = ("queries", "requests", "p50_ms", "p99_ms", "p999_ms", "launches", "updates", "iteration")
+        out = (ctypes.c_double * 11)()
+        _check(self.lib.pglGuidingServerStatsEx(self.h, out, 11) == 11, "pglGuidingServerStatsEx")
+        keys = ("queries", "requests", "p50_ms", "p99_ms", "p999_ms", "launches", "updates", "iteration",
+                "device_bytes", "budget_bytes", "launch_capacity")
         return dict(zip(keys, list(out)))
+
+    def reset_stats(self):
+        _check(self.lib.pglGuidingServerResetStats(self.h), "pglGuidingServerResetStats")
 
     def release(self):
         if self.h:

@@ -81,6 +81,12 @@ def build(verbose=False, ptxas_info=False):
                     print(out)
     if _stale(LIB, objs):
         _run([nvcc, GENCODE, "-shared", "-Xlinker", "--no-undefined", "-o", LIB] + objs + ["-lcudart", "-ldl"])
+    # the plain per-object query driver the benchmark times (links the library)
+    drv_src = os.path.join(CSRC, "plain_query_driver.cpp")
+    drv = os.path.join(OUT, "plain_query_driver")
+    if _stale(drv, [drv_src, LIB]):
+        _run(["g++", "-std=c++17", "-O2", "-Wall", "-I" + INCLUDE, "-I" + os.path.join(cuda, "include"), drv_src, "-o",
+              drv, "-L" + OUT, "-lopenpgl_gb300", "-Wl,-rpath,$ORIGIN", "-lpthread"])
     # the host C library's expf/cosf exceptions (read by the library at CUDA set-up)
     gen_src = os.path.join(CSRC, "gen_libm_exceptions.cpp")
     gen = os.path.join(OUT, "gen_libm_exceptions")

@@ -881,6 +881,15 @@ OPENPGL_CORE_INTERFACE bool pglGuidingServerAddSamples(PGLGuidingServer server, 
   return true;
   PGL_CATCH(false)
 }
+OPENPGL_CORE_INTERFACE bool pglGuidingServerAddSamplesDevice(PGLGuidingServer server, const PGLSampleData *dSamples,
+                                                             size_t n) {
+  PGL_TRY
+  if (!server || (n > 0 && !dSamples)) throw std::runtime_error("null pointer");
+  reinterpret_cast<pgl::GuidingServer *>(server)->addSamplesDevice(
+      reinterpret_cast<const PGLSampleRecord *>(dSamples), n);
+  return true;
+  PGL_CATCH(false)
+}
 OPENPGL_CORE_INTERFACE uint64_t pglGuidingServerUpdate(PGLGuidingServer server) {
   PGL_TRY
   if (!server) throw std::runtime_error("null server");
@@ -897,9 +906,36 @@ OPENPGL_CORE_INTERFACE bool pglGuidingServerWaitUpdate(PGLGuidingServer server, 
 OPENPGL_CORE_INTERFACE bool pglGuidingServerStats(PGLGuidingServer server, double out8[8]) {
   PGL_TRY
   if (!server || !out8) throw std::runtime_error("null pointer");
-  reinterpret_cast<pgl::GuidingServer *>(server)->stats(out8);
+  double all[11];
+  reinterpret_cast<pgl::GuidingServer *>(server)->stats(all);
+  std::memcpy(out8, all, 8 * sizeof(double));
   return true;
   PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE size_t pglGuidingServerStatsEx(PGLGuidingServer server, double *out, size_t count) {
+  PGL_TRY
+  if (!server) throw std::runtime_error("null pointer");
+  double all[11];
+  reinterpret_cast<pgl::GuidingServer *>(server)->stats(all);
+  if (out) std::memcpy(out, all, std::min<size_t>(count, 11) * sizeof(double));
+  return 11;
+  PGL_CATCH(0)
+}
+OPENPGL_CORE_INTERFACE bool pglGuidingServerResetStats(PGLGuidingServer server) {
+  PGL_TRY
+  if (!server) throw std::runtime_error("null pointer");
+  reinterpret_cast<pgl::GuidingServer *>(server)->resetStats();
+  return true;
+  PGL_CATCH(false)
+}
+OPENPGL_CORE_INTERFACE uint64_t pglGuidingServerSubmitVertices(PGLGuidingServer server,
+                                                               const PGLGuidedVertex *vertices, size_t n,
+                                                               PGLGuidedVertexResult *results) {
+  PGL_TRY
+  if (!server || (n > 0 && (!vertices || !results))) throw std::runtime_error("null pointer");
+  return reinterpret_cast<pgl::GuidingServer *>(server)->submitVertices(
+      reinterpret_cast<const QueryInS4 *>(vertices), reinterpret_cast<QueryOutS4 *>(results), n);
+  PGL_CATCH(0)
 }
 OPENPGL_CORE_INTERFACE uint64_t pglGetKernelLaunchCount() { return kernel_launches(); }
 OPENPGL_CORE_INTERFACE int pglDebugBoundedWaitRunsOut(uint64_t limitNs) {
@@ -956,6 +992,7 @@ OPENPGL_CORE_INTERFACE bool pglFieldSetEmTuning(PGLField field, const int *tunin
   if (!field || !tuning) throw std::runtime_error("null argument");
   EmTuning t{tuning[0], tuning[1], tuning[2], tuning[3]};
   t.plainLaunches = F(field)->tuning.plainLaunches;
+  t.reservedSMs = F(field)->tuning.reservedSMs;
   if (!em_tuning_valid(t)) throw std::runtime_error("EM tuning out of range");
   F(field)->tuning = t;
   return true;

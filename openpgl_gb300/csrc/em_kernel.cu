@@ -1196,7 +1196,7 @@ __device__ __forceinline__ uint32_t grab_gen(unsigned long long w) { return uint
 __device__ __forceinline__ uint32_t grab_chunks(unsigned long long w) { return uint32_t(w >> kGrabIdxBits) & kGrabMask; }
 __device__ __forceinline__ uint32_t grab_next(unsigned long long w) { return uint32_t(w) & kGrabMask; }
 // Chunk shape of an E-step pass with `cnt` lobe vectors: consumers need
-// 4 Kp + 5 chains in warps of one kind each (chain_role), one warp loads
+// 4 Kp + 5 chains in three warps (chain_role), one warp loads
 // chunks made by other blocks, producers get
 // the remaining warps (P threads, one chunk of C = P / parts samples).  A
 // chunk holds rows of RS = C + 4 floats (RS / 4 odd, so the consumers'
@@ -1212,7 +1212,7 @@ __device__ __forceinline__ EStepShape estep_shape(int cnt, const EmTuning &tune)
   e.cnt = cnt;
   e.Kp = cnt * kLanes;
   e.parts = cnt == 3 ? 4 : cnt;
-  e.consWarps = 2 + (3 * e.Kp + 31) / 32;  // a w | (d a) w | per-sample rows
+  e.consWarps = 3;  // a w and (d_x a) w | (d_y a) w and (d_z a) w | per-sample rows
   e.cons0 = kEmThreads - 32 * e.consWarps;  // consumers: threads [cons0, 512)
   e.P = e.cons0 - 32;                       // producers [0, P), then the loader warp
   e.C = ((e.P / e.parts) / tune.chunkDiv) & ~7;
@@ -1386,39 +1386,97 @@ __device__ __noinline__ float chain_rows(uint32_t A, uint32_t D, uint32_t W, int
   }
   return acc;
 }
-// The chain of consumer thread c.  Warps hold one kind of chain each, so no
-// warp runs two loops one after the other: the first warp sums a_k w (k =
-// lane), the next ceil(3 Kp / 32) warps sum (d_q a_k) w, the last warp the
-// five per-sample rows; other lanes are idle (kind -1).
+// Two chains of lobe k in one consumer thread, so that the thread reads the
+// a_k row once for both: kind 0 sums a_k w and (d_x a_k) w, kind 1 sums
+// (d_y a_k) w and (d_z a_k) w.  The two chains' additions alternate (each
+// chain still adds its terms in sample order, one rounding per addition).
+template <int kKind>
+__device__ __forceinline__ void add_group2(float &acc0, float &acc1, float4 a, float4 d0, float4 d1, float4 w) {
+  const float2 a01 = make_float2(a.x, a.y), a23 = make_float2(a.z, a.w);
+  const float2 w01 = make_float2(w.x, w.y), w23 = make_float2(w.z, w.w);
+  float2 p01, p23;
+  if (kKind == 0) {
+    p01 = __fmul2_rn(a01, w01);
+    p23 = __fmul2_rn(a23, w23);
+  } else {
+    p01 = __fmul2_rn(__fmul2_rn(make_float2(d0.x, d0.y), a01), w01);
+    p23 = __fmul2_rn(__fmul2_rn(make_float2(d0.z, d0.w), a23), w23);
+  }
+  const float2 q01 = __fmul2_rn(__fmul2_rn(make_float2(d1.x, d1.y), a01), w01);
+  const float2 q23 = __fmul2_rn(__fmul2_rn(make_float2(d1.z, d1.w), a23), w23);
+  acc0 += p01.x;
+  acc1 += q01.x;
+  acc0 += p01.y;
+  acc1 += q01.y;
+  acc0 += p23.x;
+  acc1 += q23.x;
+  acc0 += p23.y;
+  acc1 += q23.y;
+}
+// Rows start at 32-bit shared addresses A, D0 (kind 1 only), D1, W (bytes);
+// n4 samples; three groups of four samples in flight as in chain_rows.
+template <int kKind>
+__device__ __noinline__ float2 chain_rows2(uint32_t A, uint32_t D0, uint32_t D1, uint32_t W, int n4, float2 acc) {
+  constexpr int kD0 = kKind == 1;
+  float a0c = acc.x, a1c = acc.y;
+  float4 a0 = lds4(A), e0 = lds_if<kD0>(D0), f0 = lds4(D1), w0 = lds4(W);
+  float4 a1 = lds4(A + 16), e1 = lds_if<kD0>(D0 + 16), f1 = lds4(D1 + 16), w1 = lds4(W + 16);
+  int s = 0;
+  for (; s + 12 <= n4; s += 12) {
+    const uint32_t o2 = uint32_t(s + 8) * 4u;
+    const float4 a2 = lds4(A + o2), e2 = lds_if<kD0>(D0 + o2), f2 = lds4(D1 + o2), w2 = lds4(W + o2);
+    add_group2<kKind>(a0c, a1c, a0, e0, f0, w0);
+    const uint32_t o3 = uint32_t(s + 12 < n4 ? s + 12 : 0) * 4u;
+    a0 = lds4(A + o3);
+    e0 = lds_if<kD0>(D0 + o3);
+    f0 = lds4(D1 + o3);
+    w0 = lds4(W + o3);
+    add_group2<kKind>(a0c, a1c, a1, e1, f1, w1);
+    const uint32_t o4 = uint32_t(s + 16 < n4 ? s + 16 : 0) * 4u;
+    a1 = lds4(A + o4);
+    e1 = lds_if<kD0>(D0 + o4);
+    f1 = lds4(D1 + o4);
+    w1 = lds4(W + o4);
+    add_group2<kKind>(a0c, a1c, a2, e2, f2, w2);
+  }
+  if (s < n4) add_group2<kKind>(a0c, a1c, a0, e0, f0, w0);
+  if (s + 4 < n4) add_group2<kKind>(a0c, a1c, a1, e1, f1, w1);
+  if (s + 8 < n4) {
+    const uint32_t o2 = uint32_t(s + 8) * 4u;
+    add_group2<kKind>(a0c, a1c, lds4(A + o2), lds_if<kD0>(D0 + o2), lds4(D1 + o2), lds4(W + o2));
+  }
+  return make_float2(a0c, a1c);
+}
+// The chains of consumer thread c: three consumer warps, lane k of the first
+// summing a_k w and (d_x a_k) w, lane k of the second (d_y a_k) w and
+// (d_z a_k) w, lanes 0-4 of the third the five per-sample rows; other lanes
+// are idle (kind -1).  Every a_k row is read by one lane only; the direction
+// and weight rows are read by whole warps at one address (broadcasts).
 struct ChainRole {
   int kind, k, q;
 };
 __device__ __forceinline__ ChainRole chain_role(const EStepShape &e, int c) {
-  const int heavyWarps = e.consWarps - 2;
   const int cw = c >> 5, lane = c & 31;
   ChainRole r{-1, 0, 0};
-  if (cw == 0) {
-    if (lane < e.Kp) r = ChainRole{0, lane, 3};
-  } else if (cw <= heavyWarps) {
-    const int h = (cw - 1) * 32 + lane;
-    if (h < 3 * e.Kp) r = ChainRole{1, h % e.Kp, h / e.Kp};
-  } else if (lane < 5) {
+  if (cw < 2) {
+    if (lane < e.Kp) r = ChainRole{cw, lane, 0};
+  } else if (cw == 2 && lane < 5) {
     r = ChainRole{2, lane, 0};
   }
   return r;
 }
 __device__ __forceinline__ void estep_chunk_chain(const float *B, const EStepShape &e, const ChainRole &role, int n4,
-                                                  float &acc) {
+                                                  float2 &acc) {
   const int Kp = e.Kp;
   const uint32_t base = smem_u32(B), row = uint32_t(e.RS) * 4u;
-  const uint32_t W = base + uint32_t(Kp + 3) * row;
+  const uint32_t A = base + uint32_t(role.k) * row, X = base + uint32_t(Kp) * row, W = base + uint32_t(Kp + 3) * row;
   if (role.kind == 0) {
-    acc = chain_rows<0>(base + uint32_t(role.k) * row, W, W, n4, acc);
+    acc = chain_rows2<0>(A, X, X, W, n4, acc);
   } else if (role.kind == 1) {
-    acc = chain_rows<1>(base + uint32_t(role.k) * row, base + uint32_t(Kp + role.q) * row, W, n4, acc);
+    acc = chain_rows2<1>(A, X + row, X + 2u * row, W, n4, acc);
   } else if (role.kind == 2) {
-    const uint32_t X = base + uint32_t(Kp + 4 + role.k) * row;
-    acc = chain_rows<2>(X, X, X, n4, acc);
+    const uint32_t R = base + uint32_t(Kp + 4 + role.k) * row;
+    acc.x = chain_rows<2>(R, R, R, n4, acc.x);
   }
 }
 
@@ -1436,10 +1494,10 @@ __device__ __forceinline__ uint32_t chunks_done(const EmShared &S, const EStepSh
 
 // Consumer warps (threads [cons0, 512)): chunk k is added once stage
 // k % stages is full; each warp then records its progress.
-__device__ __forceinline__ float consume_estep(EmShared &S, const EStepShape &e, uint32_t N, uint32_t count) {
+__device__ __forceinline__ float2 consume_estep(EmShared &S, const EStepShape &e, uint32_t N, uint32_t count) {
   const int r = int(threadIdx.x) - e.cons0;
   const ChainRole role = chain_role(e, r);
-  float acc = 0.0f;
+  float2 acc = make_float2(0.0f, 0.0f);
   const int lane = int(threadIdx.x & 31);
   long long waited = 0;
   for (uint32_t k = 0; k < N; ++k) {
@@ -1659,7 +1717,7 @@ __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
     __threadfence();
     atomicExch(&b.grab, grab_word(gen, N, 0));
   }
-  float acc = 0.0f;
+  float2 acc = make_float2(0.0f, 0.0f);
   const long long t0 = clock64();
   if (tid < e.P) produce_own(S, e, L, seqBase);
   else if (tid < e.cons0) load_chunks(S, e, N, seqBase);
@@ -1671,18 +1729,18 @@ __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
   if (tid >= e.cons0) {
     const ChainRole role = chain_role(e, tid - e.cons0);
     if (role.kind == 0) {
-      S.cur.w[role.k] = acc;
+      S.cur.w[role.k] = acc.x;
+      S.cur.dx[role.k] = acc.y;
     } else if (role.kind == 1) {
-      if (role.q == 0) S.cur.dx[role.k] = acc;
-      else if (role.q == 1) S.cur.dy[role.k] = acc;
-      else S.cur.dz[role.k] = acc;
+      S.cur.dy[role.k] = acc.x;
+      S.cur.dz[role.k] = acc.y;
     } else if (role.kind == 2) {
       const int x = role.k;
-      if (x == 0) S.ll = acc;
-      else if (x == 1) S.un.sw = acc;
-      else if (x == 2) S.un.dx = acc;
-      else if (x == 3) S.un.dy = acc;
-      else S.un.dz = acc;
+      if (x == 0) S.ll = acc.x;
+      else if (x == 1) S.un.sw = acc.x;
+      else if (x == 2) S.un.dx = acc.x;
+      else if (x == 3) S.un.dy = acc.x;
+      else S.un.dz = acc.x;
     }
   }
   if (tid == 0) {
@@ -2354,7 +2412,7 @@ static size_t share_header_bytes(int blocks) {
 bool em_tuning_valid(const EmTuning &t) {
   return t.maxHelpers >= 0 && t.maxHelpers <= 64 && t.chunkDiv >= 1 && t.chunkDiv <= 4 && t.stageCap >= 2 &&
          t.stageCap <= kMaxStages && (t.orderByCost == 0 || t.orderByCost == 1) &&
-         (t.plainLaunches == 0 || t.plainLaunches == 1);
+         (t.plainLaunches == 0 || t.plainLaunches == 1) && t.reservedSMs >= 0 && t.reservedSMs < 4096;
 }
 size_t em_share_bytes(int blocks) { return share_header_bytes(blocks) + size_t(blocks) * kRingFloats * sizeof(float); }
 size_t em_share_bytes_plain(int blocks) { return share_header_bytes(blocks); }

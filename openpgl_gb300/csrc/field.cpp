@@ -1051,7 +1051,7 @@ void GpuField::runEm(SubField *const *sides, int count) {
   // the batched form: one persistent launch for every region of both
   // sub-fields (blocks take regions from a queue and, once out of regions,
   // help the others' E-step passes)
-  const int blocks = c.numSMs;
+  const int blocks = std::max(1, c.numSMs - std::max(0, tuning.reservedSMs));
   if (T > 0 && !plain)
     check(launch_em(tasks_.p, T, queue_.p, es, reports_.p, profiles_.p, emShare_.p, blocks, tuning, s), "em");
   std::vector<uint32_t> plainOrder;  // task index of launch position k (plain form)
@@ -1123,6 +1123,18 @@ void GpuField::runEm(SubField *const *sides, int count) {
   }
   cudaEventDestroy(emStart);
   cudaEventDestroy(emEnd);
+}
+
+size_t SubField::workBytes() const {
+  return posA_.bytes() + posB_.bytes() + sP_.bytes() + sD_.bytes() + tmpP_.bytes() + tmpD_.bytes() + sPdf_.bytes() +
+         tmpPdf_.bytes() + dist_.bytes() + node_.bytes() + nodeB_.bytes() + jobOf_.bytes() + isLeft_.bytes() +
+         scanLeft_.bytes() + keys_.bytes() + vals_.bytes() + nodeToJob_.bytes() + leafSeg_.bytes() + copyIdx_.bytes() +
+         keysB_.bytes() + valsB_.bytes() + routeNodes_.bytes() + keys64_.bytes() + jobs_.bytes() + acc_.bytes() +
+         means_.bytes() + bounds6_.bytes() + scratch_.bytes;
+}
+size_t GpuField::deviceBytes() const {
+  return surface.stateBytes() + surface.workBytes() + volume.stateBytes() + volume.workBytes() + tuneSnap_.bytes() +
+         tasks_.bytes() + reports_.bytes() + profiles_.bytes() + queue_.bytes() + emShare_.bytes();
 }
 
 void GpuField::setSceneBounds(const float b[6]) {  // SurfaceVolumeField.h:87-93

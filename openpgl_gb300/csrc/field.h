@@ -33,6 +33,7 @@ struct DevArray {
   size_t cap = 0;
   void reserve(size_t n, bool keep = false);
   void release();
+  size_t bytes() const { return cap * sizeof(T); }
   ~DevArray() { release(); }
   DevArray() = default;
   DevArray(const DevArray &) = delete;
@@ -57,6 +58,7 @@ struct SampleSide {
   DevArray<uint32_t> flags;
   uint64_t n = 0;
   void reserve(uint64_t count);
+  size_t deviceBytes() const { return P.bytes() + D.bytes() + pdf.bytes() + flags.bytes(); }
 };
 
 // SampleDataStorage on the device (SampleDataStorage.h:18-324): surface and
@@ -78,6 +80,7 @@ class Storage {
   PGLSampleRecord get(bool volume, uint64_t idx);
   std::vector<PGLSampleRecord> download(bool volume);
   bool validate();
+  size_t deviceBytes() const { return surf.deviceBytes() + vol.deviceBytes() + staging_.bytes() + scratch_.bytes; }
   uint64_t lastH2DBytes = 0;
 
  private:
@@ -152,6 +155,10 @@ class SubField {
   void uploadRegions(const std::vector<RegionDir> &r);
   void uploadTree();
   bool valid() const;
+  // device memory the sub-field holds: its state (regions, nodes,
+  // neighbours) and, separately, its Update working set
+  size_t stateBytes() const { return dRegions.bytes() + dNodes.bytes() + dNbrs.bytes() + dUniformDirs.bytes(); }
+  size_t workBytes() const;
 
  private:
   void buildTree(uint32_t n, const float4 *P);
@@ -185,6 +192,8 @@ class GpuField {
   void setSceneBounds(const float b[6]);
   void sceneBounds(float out[6]) const;
   void reset();
+  // device memory of both sub-fields' state and working sets and of the EM launch
+  size_t deviceBytes() const;
   std::string serialize() const;  // byte layout of pglFieldStoreToFile (CPU_8 lanes)
   void deserialize(const std::string &bytes);  // the same layout (pglDeviceNewFieldFromFile)
   bool equals(const GpuField &o) const;

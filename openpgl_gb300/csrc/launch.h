@@ -111,6 +111,8 @@ struct EmTuning {
   int orderByCost = 0;
   int plainLaunches = 0;  // 1: the plain form (one launch per sub-field, one block per region,
                           // no queue and no helper blocks), same results
+  int reservedSMs = 0;    // SMs the batched launch leaves free (for queries on other streams
+                          // while a served field trains), same results
 };
 bool em_tuning_valid(const EmTuning &t);
 // Device memory through which the EM launch's blocks share E-step passes

@@ -9,16 +9,48 @@
 namespace pgl {
 
 namespace {
-constexpr size_t kQueryBytes = sizeof(QueryIn) + sizeof(QueryOut);
+// bytes of a path vertex in flight (input and result; the larger kind)
+constexpr size_t kVertexBytes = sizeof(QueryInS4) + sizeof(QueryOutS4);
+constexpr size_t kMaxLaunch = size_t(1) << 24;  // queries per launch at most
+}  // namespace
+
+size_t GuidingServer::fieldBytes() const {
+  return field_->surface.stateBytes() + field_->volume.stateBytes();
 }
 
-GuidingServer::GuidingServer(GpuField *field, size_t budgetBytes) : field_(field) {
+size_t GuidingServer::deviceBytesInUse() const {
+  size_t b = field_->deviceBytes() + storage_.deviceBytes();
+  for (const Snapshot &s : snap_)
+    for (int k = 0; k < 2; ++k) b += s.regions[k].bytes() + s.nodes[k].bytes() + s.nbrs[k].bytes();
+  for (const Slot &s : slots_) b += s.dIn.bytes() + s.dOut.bytes();
+  return b + incomingDev_.bytes();
+}
+
+size_t GuidingServer::projectedBytes(size_t samples) const {
+  const size_t training = field_->deviceBytes() + storage_.deviceBytes();
+  const size_t others = deviceBytesInUse() - training;
+  return others + std::max(training, fieldBytes() + samples * kUpdateBytesPerSample);
+}
+
+GuidingServer::GuidingServer(GpuField *field, size_t budgetBytes, int reservedSMs)
+    : field_(field), budget_(budgetBytes) {
   if (!field) throw std::runtime_error("null field");
   Context &c = Context::get();
-  capacity_ = std::min<size_t>(std::max<size_t>(budgetBytes / kQueryBytes, 1024), size_t(1) << 24);
-  dIn_.reserve(capacity_);
-  dOut_.reserve(capacity_);
-  check(cudaStreamCreateWithFlags(&qstream_, cudaStreamNonBlocking), "query stream");
+  // the field's EM launches leave these SMs to the query stream
+  field_->tuning.reservedSMs = std::max(0, std::min(reservedSMs, c.numSMs - 1));
+  // query buffers: two launches in flight, each of up to capacity_ queries of
+  // the largest kind; they take at most a quarter of what the budget leaves
+  // after the field and its two snapshots (the rest is for training)
+  const size_t fixed = 3 * fieldBytes() + field_->deviceBytes();
+  if (budgetBytes <= fixed + 2 * 1024 * kVertexBytes)
+    throw std::runtime_error("HBM budget of the guiding server is below the field's own memory");
+  capacity_ = std::min<size_t>(std::max<size_t>((budgetBytes - fixed) / 4 / (2 * kVertexBytes), 1024), kMaxLaunch);
+  for (Slot &s : slots_) {
+    s.dIn.reserve(capacity_ * sizeof(QueryInS4));
+    s.dOut.reserve(capacity_ * sizeof(QueryOutS4));
+    check(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming), "event");
+    check(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "query stream");
+  }
   for (Snapshot &s : snap_) check(cudaEventCreateWithFlags(&s.lastRead, cudaEventDisableTiming), "event");
   takeSnapshot(0);
   active_ = 0;
@@ -44,9 +76,14 @@ GuidingServer::~GuidingServer() {
   if (dispatcher_.joinable()) dispatcher_.join();
   if (trainer_.joinable()) trainer_.join();
   for (auto &kv : requests_) delete kv.second;
+  for (Slot &s : slots_) {
+    if (s.done) cudaEventDestroy(s.done);
+    if (s.stream) cudaStreamDestroy(s.stream);
+  }
   for (Snapshot &s : snap_)
     if (s.lastRead) cudaEventDestroy(s.lastRead);
-  if (qstream_) cudaStreamDestroy(qstream_);
+  if (copyStream_) cudaStreamDestroy(copyStream_);
+  field_->tuning.reservedSMs = 0;
 }
 
 // Copies what queries read (regions, nodes, neighbours of both kinds) into
@@ -88,11 +125,41 @@ void GuidingServer::takeSnapshot(int slot) {
 
 uint64_t GuidingServer::submit(const QueryIn *in, QueryOut *out, size_t n, bool volume, bool cosine) {
   Request *r = new Request();
+  r->kind = RequestKind::Query;
   r->in = in;
   r->out = out;
   r->n = n;
   r->volume = volume;
   r->cosine = cosine && !volume;
+  r->t0 = std::chrono::steady_clock::now();
+  {
+    std::lock_guard<std::mutex> lk(m_);
+    if (stop_) {
+      delete r;
+      throw std::runtime_error("server is shutting down");
+    }
+    r->id = nextId_++;
+    requests_[r->id] = r;
+    if (n == 0) {
+      r->finished = true;
+      r->version = snap_[active_].version;
+    } else {
+      pending_.push_back(r);
+    }
+  }
+  if (n == 0) cvDone_.notify_all();
+  else cvWork_.notify_one();
+  return r->id;
+}
+
+uint64_t GuidingServer::submitVertices(const QueryInS4 *in, QueryOutS4 *out, size_t n) {
+  Request *r = new Request();
+  r->kind = RequestKind::Vertex;
+  r->in = in;
+  r->out = out;
+  r->n = n;
+  r->volume = false;
+  r->cosine = true;
   r->t0 = std::chrono::steady_clock::now();
   {
     std::lock_guard<std::mutex> lk(m_);
@@ -152,64 +219,13 @@ void GuidingServer::dispatchLoop() {
   }
 }
 
-void GuidingServer::dispatch() {
-  struct Seg {
-    Request *r;
-    size_t off, cnt, pos;
-  };
-  std::vector<Seg> segs;
-  for (;;) {
-    std::unique_lock<std::mutex> lk(m_);
-    cvWork_.wait(lk, [&] { return stop_ || !pending_.empty(); });
-    if (stop_) return;
-    // one launch: the queries of the head request's kind, first come first
-    // served, up to the launch capacity; each request stays on the snapshot
-    // its first queries used
-    Request *head = pending_.front();
-    const int snap = head->snap >= 0 ? head->snap : active_;
-    segs.clear();
-    size_t total = 0;
-    for (Request *r : pending_) {
-      if (total >= capacity_) break;
-      if (r->volume != head->volume || r->cosine != head->cosine) continue;
-      if ((r->snap >= 0 ? r->snap : active_) != snap) continue;
-      const size_t take = std::min(r->n - r->sent, capacity_ - total);
-      if (r->snap < 0) {
-        r->snap = snap;
-        r->version = snap_[snap].version;
-        pinned_[snap]++;
-      }
-      segs.push_back(Seg{r, r->sent, take, total});
-      r->sent += take;
-      total += take;
-    }
-    pending_.erase(std::remove_if(pending_.begin(), pending_.end(), [](Request *r) { return r->sent == r->n; }),
-                   pending_.end());
-    const FieldView view = snap_[snap].view[head->volume ? 1 : 0];
-    const bool cosine = head->cosine;
-    lk.unlock();
-
-    for (const Seg &g : segs)
-      check(cudaMemcpyAsync(dIn_.p + g.pos, g.r->in + g.off, g.cnt * sizeof(QueryIn), cudaMemcpyHostToDevice,
-                            qstream_),
-            "H2D queries");
-    QueryParams p{};
-    p.f = view;
-    p.cosKappa = 2.18853f;
-    p.cosNorm = cosine_lobe_normalization();
-    p.cosine = cosine ? 1 : 0;
-    p.samplesPerQuery = 1;
-    check(launch_query(p, dIn_.p, dOut_.p, uint32_t(total), qstream_), "query launch");
-    check(cudaEventRecord(snap_[snap].lastRead, qstream_), "event");
-    for (const Seg &g : segs)
-      check(cudaMemcpyAsync(g.r->out + g.off, dOut_.p + g.pos, g.cnt * sizeof(QueryOut), cudaMemcpyDeviceToHost,
-                            qstream_),
-            "D2H results");
-    check(cudaStreamSynchronize(qstream_), "queries");
-
-    lk.lock();
+// Results of a finished launch: its requests' pieces are done.
+void GuidingServer::complete(Slot &slot) {
+  check(cudaEventSynchronize(slot.done), "queries");
+  {
+    std::lock_guard<std::mutex> lk(m_);
     const auto now = std::chrono::steady_clock::now();
-    for (const Seg &g : segs) {
+    for (const Seg &g : slot.segs) {
       Request *r = g.r;
       r->done += g.cnt;
       if (r->done == r->n) {
@@ -221,14 +237,117 @@ void GuidingServer::dispatch() {
       }
     }
     launches_++;
-    lk.unlock();
-    cvDone_.notify_all();
-    cvTrain_.notify_all();
   }
+  slot.segs.clear();
+  slot.busy = false;
+  cvDone_.notify_all();
+  cvTrain_.notify_all();
+}
+
+// Continuous batching with two launches in flight: while one launch runs,
+// the next is formed from whatever requests are pending (first come, first
+// served, of the head request's kind, up to the launch capacity) and its
+// copies and kernel are enqueued behind it; a launch's requests complete when
+// its results are back in their host buffers.
+void GuidingServer::dispatch() {
+  int next = 0;
+  for (;;) {
+    Slot &slot = slots_[next];
+    Slot &other = slots_[1 - next];
+    if (slot.busy) complete(slot);
+    std::unique_lock<std::mutex> lk(m_);
+    cvWork_.wait(lk, [&] { return stop_ || !pending_.empty() || other.busy; });
+    if (stop_) return;
+    if (pending_.empty()) {  // nothing new: finish the launch in flight
+      lk.unlock();
+      complete(other);
+      continue;
+    }
+    Request *head = pending_.front();
+    const RequestKind kind = head->kind;
+    const int snap = head->snap >= 0 ? head->snap : active_;
+    size_t total = 0;
+    for (Request *r : pending_) {
+      if (total >= capacity_) break;
+      if (r->kind != kind || r->volume != head->volume || r->cosine != head->cosine) continue;
+      if ((r->snap >= 0 ? r->snap : active_) != snap) continue;
+      const size_t take = std::min(r->n - r->sent, capacity_ - total);
+      if (r->snap < 0) {
+        r->snap = snap;
+        r->version = snap_[snap].version;
+        pinned_[snap]++;
+      }
+      slot.segs.push_back(Seg{r, r->sent, take, total});
+      r->sent += take;
+      total += take;
+    }
+    pending_.erase(std::remove_if(pending_.begin(), pending_.end(), [](Request *r) { return r->sent == r->n; }),
+                   pending_.end());
+    const FieldView view = snap_[snap].view[head->volume ? 1 : 0];
+    const bool cosine = head->cosine;
+    lk.unlock();
+
+    const size_t inBytes = kind == RequestKind::Vertex ? sizeof(QueryInS4) : sizeof(QueryIn);
+    const size_t outBytes = kind == RequestKind::Vertex ? sizeof(QueryOutS4) : sizeof(QueryOut);
+    for (const Seg &g : slot.segs)
+      check(cudaMemcpyAsync(slot.dIn.p + g.pos * inBytes, static_cast<const unsigned char *>(g.r->in) + g.off * inBytes,
+                            g.cnt * inBytes, cudaMemcpyHostToDevice, slot.stream),
+            "H2D queries");
+    QueryParams p{};
+    p.f = view;
+    p.cosKappa = 2.18853f;
+    p.cosNorm = cosine_lobe_normalization();
+    p.cosine = cosine ? 1 : 0;
+    if (kind == RequestKind::Vertex) {
+      p.samplesPerQuery = kVertexSamples;
+      check(launch_query_s4(p, reinterpret_cast<const QueryInS4 *>(slot.dIn.p),
+                            reinterpret_cast<QueryOutS4 *>(slot.dOut.p), uint32_t(total), slot.stream),
+            "vertex query launch");
+    } else {
+      p.samplesPerQuery = 1;
+      check(launch_query(p, reinterpret_cast<const QueryIn *>(slot.dIn.p), reinterpret_cast<QueryOut *>(slot.dOut.p),
+                         uint32_t(total), slot.stream),
+            "query launch");
+    }
+    check(cudaEventRecord(snap_[snap].lastRead, slot.stream), "event");
+    for (const Seg &g : slot.segs)
+      check(cudaMemcpyAsync(static_cast<unsigned char *>(g.r->out) + g.off * outBytes, slot.dOut.p + g.pos * outBytes,
+                            g.cnt * outBytes, cudaMemcpyDeviceToHost, slot.stream),
+            "D2H results");
+    check(cudaEventRecord(slot.done, slot.stream), "event");
+    slot.busy = true;
+    slot.queries = total;
+    next = 1 - next;
+  }
+}
+
+void GuidingServer::addSamplesDevice(const PGLSampleRecord *d, size_t n) {
+  std::lock_guard<std::mutex> lk(incomingMutex_);
+  // the server's own copy of the records grows (by at most its reserve's headroom)
+  const size_t grow = incomingDev_.cap < incomingDevN_ + n
+                          ? (incomingDevN_ + n + (incomingDevN_ + n) / 4) * sizeof(PGLSampleRecord) - incomingDev_.bytes()
+                          : 0;
+  const size_t projected = projectedBytes(incoming_.size() + incomingDevN_ + n) + grow;
+  if (projected > budget_)
+    throw std::runtime_error("training batch over the guiding server's HBM budget (" + std::to_string(projected) +
+                             " > " + std::to_string(budget_) + " bytes)");
+  if (!copyStream_) check(cudaStreamCreateWithFlags(&copyStream_, cudaStreamNonBlocking), "copy stream");
+  incomingDev_.reserve(incomingDevN_ + n, true);
+  check(cudaMemcpyAsync(incomingDev_.p + incomingDevN_, d, n * sizeof(PGLSampleRecord), cudaMemcpyDeviceToDevice,
+                        copyStream_),
+        "training samples");
+  check(cudaStreamSynchronize(copyStream_), "training samples");
+  incomingDevN_ += n;
 }
 
 void GuidingServer::addSamples(const PGLSampleRecord *s, size_t n) {
   std::lock_guard<std::mutex> lk(incomingMutex_);
+  // admission by the HBM budget: the next Update's samples and working set
+  // beside what the field's snapshots and the query buffers hold
+  const size_t projected = projectedBytes(incoming_.size() + incomingDevN_ + n);
+  if (projected > budget_)
+    throw std::runtime_error("training batch over the guiding server's HBM budget (" + std::to_string(projected) +
+                             " > " + std::to_string(budget_) + " bytes)");
   incoming_.insert(incoming_.end(), s, s + n);
 }
 
@@ -269,6 +388,12 @@ void GuidingServer::train() {
     {
       std::lock_guard<std::mutex> lk(incomingMutex_);
       batch.swap(incoming_);
+      if (incomingDevN_ > 0) {
+        storage_.ingestDevice(incomingDev_.p, incomingDevN_);
+        // the ingest has read the buffer before the next addSamplesDevice may write it
+        check(cudaStreamSynchronize(Context::get().stream), "training samples");
+      }
+      incomingDevN_ = 0;
     }
     if (!batch.empty()) storage_.add(batch.data(), batch.size());
     field_->update(storage_, true, true);
@@ -282,7 +407,7 @@ void GuidingServer::train() {
       cvTrain_.wait(lk, [&] { return stop_ || pinned_[slot] == 0; });
       if (stop_) return;
     }
-    check(cudaEventSynchronize(snap_[slot].lastRead), "snapshot reader");
+    check(cudaEventSynchronize(snap_[slot].lastRead), "snapshot reader");  // its last launch is done
     takeSnapshot(slot);
     {
       std::lock_guard<std::mutex> lk(m_);
@@ -293,7 +418,7 @@ void GuidingServer::train() {
   }
 }
 
-void GuidingServer::stats(double out[8]) {
+void GuidingServer::stats(double out[11]) {
   std::lock_guard<std::mutex> lk(m_);
   std::vector<double> l = latencies_;
   std::sort(l.begin(), l.end());
@@ -306,6 +431,16 @@ void GuidingServer::stats(double out[8]) {
   out[5] = double(launches_);
   out[6] = double(updatesDone_);
   out[7] = double(snap_[active_].version);
+  out[8] = double(deviceBytesInUse());
+  out[9] = double(budget_);
+  out[10] = double(capacity_);
+}
+
+void GuidingServer::resetStats() {
+  std::lock_guard<std::mutex> lk(m_);
+  latencies_.clear();
+  served_ = 0;
+  launches_ = 0;
 }
 
 }  // namespace pgl

@@ -287,3 +287,32 @@ def test_multiframe_configuration(pgl):
         assert r["bit_exact_regions"] == r["regions"], (side, summary(r))
     q = syn.queries(1 << 20, 4242)
     _check_queries(field.sample_batch(q), orc.query(q), "1M queries")
+
+
+def test_path_vertex_queries(pgl):
+    """Path-vertex queries (Init, cosine product, four SamplePDF calls on the
+    clustered field, vertices from the clusters): SamplePDF call k equals the
+    oracle's single guided query with the k-th 2D random number (sampling
+    does not change the distribution), region and sample1D bit for bit,
+    pdfs within the bar."""
+    from openpgl_gb300 import synthetic as syn
+
+    frames = [syn.cluster_samples(1 << 19, 160 + i) for i in range(2)]
+    dev, field, orc = _train(pgl, frames, 8000)
+    v = syn.vertices(1 << 16, 161)
+    out = field.sample_vertices(v)
+    assert out["ok"].sum() > len(v) // 2
+    for k in range(4):
+        q = syn.vertex_queries(v, k)
+        ref = orc.query(q)
+        got = np.zeros(len(v), dtype=pgl.QUERY_RESULT_DTYPE)
+        got["ok"], got["id"], got["sample1d"] = out["ok"], out["id"], out["sample1d"]
+        got["dir"], got["pdf"] = out["sample"][:, k, :3], out["sample"][:, k, 3]
+        r = compare_queries(got, ref)
+        assert r["ok_equal"] and r["id_equal"] and r["sample1d_equal"], (k, r)
+        assert r["worst_pdf_rel"] <= PDF_TOL and r["worst_dir"] <= 1e-3, (k, r)
+        # and the batch with one sample per query, on the GPU, bit for bit
+        one = field.sample_batch(q)
+        ok = one["ok"] == 1
+        assert np.array_equal(one["pdf"][ok].view(np.uint32), got["pdf"][ok].view(np.uint32)), k
+        assert np.array_equal(one["dir"][ok].view(np.uint32), got["dir"][ok].view(np.uint32)), k

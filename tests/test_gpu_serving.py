@@ -33,7 +33,9 @@ def test_results_alone_equal_results_in_the_mix():
     batches = [(syn.queries(int(n), 6000 + i), bool(i % 3 == 2)) for i, n in enumerate(sizes)]
     alone = [field.sample_batch(q, volume=vol, cosine=not vol) for q, vol in batches]
 
-    server = pgl.GuidingServer(field, hbm_budget_bytes=1 << 20)  # ~15k queries per launch
+    # a budget that leaves a few thousand queries per launch (the field's own
+    # memory, its two snapshots and two launches' buffers all count)
+    server = pgl.GuidingServer(field, hbm_budget_bytes=64 << 20)
     results = [None] * len(batches)
 
     def worker(idx):
@@ -54,7 +56,10 @@ def test_results_alone_equal_results_in_the_mix():
         assert lat > 0.0
     s = server.stats()
     assert s["queries"] == sizes.sum() and s["requests"] == len(batches)
-    assert s["launches"] < len(batches) + sizes.sum() // 15000 + 2
+    cap = int(s["launch_capacity"])
+    assert cap >= 1024, cap
+    assert s["launches"] < len(batches) + sizes.sum() // cap + 2
+    assert s["device_bytes"] <= s["budget_bytes"]
     server.release()
 
 
@@ -68,7 +73,7 @@ def test_queries_during_background_update_come_from_one_field_state():
     expect = {field.iteration: field.sample_batch(q), after.iteration: after.sample_batch(q)}
     assert field.iteration + 1 == after.iteration
 
-    server = pgl.GuidingServer(field, hbm_budget_bytes=1 << 22)
+    server = pgl.GuidingServer(field, hbm_budget_bytes=256 << 20)
     server.add_samples(syn.cube_face_samples(60000, 5101, volume_fraction=0.25))
     ticket = server.update()
     seen = set()
@@ -85,3 +90,36 @@ def test_queries_during_background_update_come_from_one_field_state():
     assert server.stats()["updates"] == 1
     server.release()
     assert field.compare(after)
+
+
+def test_vertices_in_the_mix_and_the_budget():
+    """Path-vertex requests (four SamplePDF calls per vertex) served beside
+    single-sample requests give the same bytes as the direct call; a training
+    batch whose Update would not fit in the budget is refused, and the
+    server's device memory stays within the budget."""
+    import openpgl_gb300 as pgl
+    from openpgl_gb300 import synthetic as syn
+
+    dev, field = _trained(pgl, syn, 5300)
+    verts = [syn.vertices(int(n), 5400 + i) for i, n in enumerate((3000, 70000, 20000))]
+    qs = [syn.queries(int(n), 5500 + i) for i, n in enumerate((5000, 90000))]
+    alone_v = [field.sample_vertices(v) for v in verts]
+    alone_q = [field.sample_batch(q) for q in qs]
+    server = pgl.GuidingServer(field, hbm_budget_bytes=96 << 20)
+    tickets = []
+    for i in range(3):
+        tickets.append(("v", i) + server.submit_vertices(verts[i]))
+        if i < 2:
+            tickets.append(("q", i) + server.submit(qs[i]))
+    for kind, i, t, out in tickets:
+        server.wait(t)
+        ref = alone_v[i] if kind == "v" else alone_q[i]
+        assert out.tobytes() == ref.tobytes(), (kind, i)
+    s = server.stats()
+    assert s["device_bytes"] <= s["budget_bytes"]
+    with pytest.raises(RuntimeError, match="budget"):
+        server.add_samples(syn.cube_face_samples(1 << 20, 5600))
+    server.add_samples(syn.cube_face_samples(20000, 5601, volume_fraction=0.25))
+    server.wait_update(server.update())
+    assert server.stats()["updates"] == 1
+    server.release()
