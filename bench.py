@@ -674,7 +674,8 @@ def run_scale(pgl, dev, serve_rate=None, frames=SCALE_FRAMES, n=SCALE_SAMPLES):
     m = syn.cluster_model(1234)
     model = {k: torch.from_numpy(np.asarray(v, dtype=np.float32)).cuda() for k, v in m.items()}
     field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=SCALE_LEAF))
-    server = pgl.GuidingServer(field, hbm_budget_bytes=SERVE_BUDGET)
+    # the query load takes about half of the GPU: the EM leaves half the SMs to it
+    server = pgl.GuidingServer(field, hbm_budget_bytes=SERVE_BUDGET, reserved_sms=76 if serve_rate else 0)
     pool = torch.from_numpy(syn.vertices(SERVE_POOL, 3313).view(np.uint8)).pin_memory()
     verts = pool.numpy().view(syn.PGL_VERTEX_DTYPE)
     outs = torch.empty(4 * SERVE_POOL * 76, dtype=torch.uint8).pin_memory().numpy().view(pgl.VERTEX_RESULT_DTYPE)
@@ -734,7 +735,8 @@ def run_scale(pgl, dev, serve_rate=None, frames=SCALE_FRAMES, n=SCALE_SAMPLES):
     total = sum(per_frame)
     return {"workload": "16 frames x 67,108,864 clustered samples (25% inside-volume), maxSamplesPerLeaf 16000, "
                         "Updates through the guiding server (40 GB budget) with path-vertex batches arriving "
-                        "at half the serving workload's saturation from the second frame on",
+                        "at half the serving workload's saturation from the second frame on (EM launches "
+                        "leave 76 of 152 SMs to the queries)",
             "frames": frames, "samples_per_frame": n, "update_ms_per_frame": [round(x, 1) for x in per_frame],
             "em_kernel_ms_per_frame": [round(x, 1) for x in em_ms], "regions_per_frame": regions,
             "ms_per_16M_samples": round(total * UNIT_SAMPLES / (frames * n), 3),

@@ -1,3 +1,8 @@
+// Copyright 2021 Intel Corporation
+// SPDX-License-Identifier: Apache-2.0
+// (The declarations restate the Open PGL 0.6.0 C API header of the same name,
+// which is licensed under Apache-2.0, so that code written against it builds
+// unchanged.)
 // Device (reference: include/openpgl/device.h:22-28; api.cpp:83-114).
 #pragma once
 #include "common.h"

@@ -219,6 +219,11 @@ typedef struct GuidingServer *PGLGuidingServer;
 // several launches).  While the server runs, the field's EM launches leave 8
 // SMs to the query launches, so queries keep being answered during an Update.
 OPENPGL_CORE_INTERFACE PGLGuidingServer pglNewGuidingServer(PGLField field, size_t hbmBudgetBytes);
+// The same with the number of SMs the field's EM launches leave to queries
+// (default 8; at most all but one): more keeps query latency low under a
+// heavy query load while the field trains, fewer lets Updates finish sooner.
+OPENPGL_CORE_INTERFACE PGLGuidingServer pglNewGuidingServerEx(PGLField field, size_t hbmBudgetBytes,
+                                                              int reservedSMs);
 OPENPGL_CORE_INTERFACE void pglReleaseGuidingServer(PGLGuidingServer server);
 // Queues n queries; `queries` and `results` (host memory) must stay valid until
 // the request is waited for.  Returns a ticket (0 on error).

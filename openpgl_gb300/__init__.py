@@ -160,6 +160,7 @@ C_API = {
     "pglGetKernelLaunchCount": (ctypes.c_uint64, []),
     "pglDebugBoundedWaitRunsOut": (ctypes.c_int, [ctypes.c_uint64]),
     "pglNewGuidingServer": (ctypes.c_void_p, [ctypes.c_void_p, ctypes.c_size_t]),
+    "pglNewGuidingServerEx": (ctypes.c_void_p, [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]),
     "pglReleaseGuidingServer": (None, [ctypes.c_void_p]),
     "pglGuidingServerSubmit": (ctypes.c_uint64, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                                  ctypes.c_bool, ctypes.c_bool]),
@@ -676,10 +677,13 @@ class GuidingServer:
     """A field served while it trains (pglNewGuidingServer): submit guided
     queries from any thread, add samples, start Updates in the background."""
 
-    def __init__(self, field, hbm_budget_bytes=1 << 30):
+    def __init__(self, field, hbm_budget_bytes=1 << 30, reserved_sms=None):
         self.lib = load()
         self.field = field
-        self.h = self.lib.pglNewGuidingServer(field.h, hbm_budget_bytes)
+        if reserved_sms is None:
+            self.h = self.lib.pglNewGuidingServer(field.h, hbm_budget_bytes)
+        else:
+            self.h = self.lib.pglNewGuidingServerEx(field.h, hbm_budget_bytes, int(reserved_sms))
         _check(self.h, "pglNewGuidingServer")
         self._keep = {}
 

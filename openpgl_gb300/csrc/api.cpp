@@ -850,6 +850,14 @@ OPENPGL_CORE_INTERFACE PGLGuidingServer pglNewGuidingServer(PGLField field, size
   return reinterpret_cast<PGLGuidingServer>(new pgl::GuidingServer(F(field), hbmBudgetBytes));
   PGL_CATCH(nullptr)
 }
+OPENPGL_CORE_INTERFACE PGLGuidingServer pglNewGuidingServerEx(PGLField field, size_t hbmBudgetBytes,
+                                                              int reservedSMs) {
+  PGL_TRY
+  if (!field) throw std::runtime_error("null field provided to pglNewGuidingServerEx");
+  if (reservedSMs < 0) throw std::runtime_error("negative SM reservation");
+  return reinterpret_cast<PGLGuidingServer>(new pgl::GuidingServer(F(field), hbmBudgetBytes, reservedSMs));
+  PGL_CATCH(nullptr)
+}
 OPENPGL_CORE_INTERFACE void pglReleaseGuidingServer(PGLGuidingServer server) {
   PGL_TRY
   delete reinterpret_cast<pgl::GuidingServer *>(server);

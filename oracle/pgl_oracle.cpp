@@ -29,7 +29,7 @@
 #include <thread>
 #include <vector>
 
-#include "x86_approx_tables.h"
+#include "../openpgl_gb300/csrc/x86_approx_tables.h"  // the one copy of the measured tables
 #include "../openpgl_gb300/csrc/hg_table.h"
 
 namespace orc {
@@ -48,7 +48,7 @@ static float rcpss(float x) {
   uint32_t u = fbits(x), s = u & 0x80000000u, e = (u >> 23) & 0xFF, m = u & 0x7FFFFF;
   if (e == 0) return bitsf(s | 0x7F800000u);
   if (e == 255) return m ? x : bitsf(s);
-  uint32_t t = orc_rcp_table[m >> 12];
+  uint32_t t = pgl_x86_rcp_table[m >> 12];
   int re = int((t >> 23) & 0xFF) - (int(e) - 127);
   if (re <= 0) return bitsf(s);
   if (re >= 255) return bitsf(s | 0x7F800000u);
@@ -61,7 +61,7 @@ static float rsqrtss(float x) {
   if (e == 0) return INFINITY;
   if (e == 255) return m ? x : 0.0f;
   int ue = int(e) - 127, p = ue & 1, q = ue >> 1;
-  uint32_t t = orc_rsqrt_table[p * 1024 + (m >> 13)];
+  uint32_t t = pgl_x86_rsqrt_table[p * 1024 + (m >> 13)];
   int re = int((t >> 23) & 0xFF) - q;
   return bitsf((uint32_t(re) << 23) | (t & 0x7FFFFF));
 }
