@@ -24,6 +24,7 @@ PGL_DEVICE_TYPE_CPU_4, PGL_DEVICE_TYPE_CPU_8, PGL_DEVICE_TYPE_CPU_16, PGL_DEVICE
 PGL_DEVICE_TYPE_GPU_SM103 = 4
 PGL_SPATIAL_STRUCTURE_KDTREE = 0
 PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM = 0
+PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE = 1
 PGL_DIRECTIONAL_DISTRIBUTION_VMM = 2
 
 QUERY_RESULT_DTYPE = np.dtype(
@@ -50,6 +51,11 @@ class Box3(ctypes.Structure):
 class SampleData(ctypes.Structure):
     _fields_ = [("position", Vec3), ("direction", Vec3), ("weight", ctypes.c_float), ("pdf", ctypes.c_float),
                 ("distance", ctypes.c_float), ("flags", ctypes.c_uint32)]
+
+
+class DQTFactoryArguments(ctypes.Structure):  # PGLDQTFactoryArguments (config.h)
+    _fields_ = [("leafEstimator", ctypes.c_int), ("splitMetric", ctypes.c_int), ("splitThreshold", ctypes.c_float),
+                ("footprintFactor", ctypes.c_float), ("maxLevels", ctypes.c_uint32)]
 
 
 class FieldArguments(ctypes.Structure):  # PGLFieldArguments (config.h)
@@ -280,11 +286,19 @@ class Device:
 class FieldConfig:
     """FieldConfig::Init (cpp/FieldConfig.h:62-64)."""
 
-    def __init__(self, deterministic=True, max_samples_per_leaf=32000, parallax=True):
+    def __init__(self, deterministic=True, max_samples_per_leaf=32000, parallax=True, dqt=False, dqt_args=None):
+        """dqt: the directional quadtree field type; dqt_args = (leafEstimator,
+        splitMetric, splitThreshold, footprintFactor, maxLevels) overrides the
+        factory's defaults."""
         self.args = FieldArguments()
         kind = PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM if parallax else PGL_DIRECTIONAL_DISTRIBUTION_VMM
+        if dqt:
+            kind = PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE
         load().pglFieldArgumentsSetDefaults(ctypes.byref(self.args), PGL_SPATIAL_STRUCTURE_KDTREE, kind,
                                             deterministic, max_samples_per_leaf)
+        if dqt and dqt_args:
+            a = ctypes.cast(self.args.directionalDistributionArguments, ctypes.POINTER(DQTFactoryArguments)).contents
+            a.leafEstimator, a.splitMetric, a.splitThreshold, a.footprintFactor, a.maxLevels = dqt_args
 
 
 class SampleStorage:

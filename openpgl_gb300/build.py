@@ -20,7 +20,7 @@ LIB = os.path.join(OUT, "libopenpgl_gb300.so")
 LIBM_TABLE = os.path.join(OUT, "libm_exceptions.bin")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CUDA_SOURCES = ["em_kernel.cu", "spatial_kernels.cu", "query_kernels.cu", "noalloc.cu", "path_kernels.cu"]
+CUDA_SOURCES = ["em_kernel.cu", "spatial_kernels.cu", "query_kernels.cu", "noalloc.cu", "path_kernels.cu", "dqt_kernels.cu"]
 HOST_SOURCES = ["field.cpp", "api.cpp", "serve.cpp", "pathsegments.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 

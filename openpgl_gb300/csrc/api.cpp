@@ -105,12 +105,34 @@ static_assert(sizeof(PGLGuidedVertexResult) == sizeof(QueryOutS4) && sizeof(PGLG
 FieldConfig config_from(const PGLFieldArguments &args) {  // Device.h:99-136
   if (args.spatialStructureType != PGL_SPATIAL_STRUCTURE_KDTREE ||
       (args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_PARALLAX_AWARE_VMM &&
-       args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_VMM)) {
+       args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_VMM &&
+       args.directionalDistributionType != PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE)) {
     // the field takes ownership of the argument structs (Device.h:109,136,184-207), refused or not
     delete static_cast<PGLKDTreeArguments *>(args.spatialSturctureArguments);
-    if (args.directionalDistributionType == PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE)
-      delete static_cast<PGLDQTFactoryArguments *>(args.directionalDistributionArguments);
-    throw std::runtime_error("only kd-tree fields with (parallax-aware) VMMs run on the GPU");
+    throw std::runtime_error("only kd-tree fields (parallax-aware VMM, VMM, quadtree) run on the GPU");
+  }
+  if (args.directionalDistributionType == PGL_DIRECTIONAL_DISTRIBUTION_QUADTREE) {  // Device.h:185-210
+    std::unique_ptr<PGLKDTreeArguments> kd(static_cast<PGLKDTreeArguments *>(args.spatialSturctureArguments));
+    std::unique_ptr<PGLDQTFactoryArguments> dq(
+        static_cast<PGLDQTFactoryArguments *>(args.directionalDistributionArguments));
+    if (!kd || !dq) throw std::runtime_error("null field arguments");
+    FieldConfig c;
+    c.dqt = 1;
+    c.parallax = 0;  // a quadtree has no parallax compensation (DQT.h:28-30)
+    c.deterministic = args.deterministic ? 1u : 0u;
+    c.fitRegions = args.debugArguments.fitRegions ? 1u : 0u;
+    c.knn = kd->knnLookup ? 1u : 0u;
+    c.minSamples = kd->minSamples;
+    c.maxSamples = kd->maxSamples;
+    c.maxDepth = kd->maxDepth;
+    c.dqtArgs.leafEstimator = int32_t(dq->leafEstimator);
+    c.dqtArgs.splitMetric = int32_t(dq->splitMetric);
+    c.dqtArgs.splitThreshold = dq->splitThreshold;
+    c.dqtArgs.footprintFactor = dq->footprintFactor;
+    c.dqtArgs.maxLevels = dq->maxLevels;
+    if (dqt_max_nodes(c.dqtArgs) > (uint64_t(1) << 18))
+      throw std::runtime_error("quadtree factory arguments allow trees of more than 262144 nodes");
+    return c;
   }
   FieldConfig c;
   // Device.h:139-178: the plain VMM is the same mixture without parallax compensation
@@ -367,16 +389,26 @@ OPENPGL_CORE_INTERFACE bool pglFieldInitVolumeSamplingDistribution(PGLField fiel
   return init_distribution(F(field), D(d), true, position, sample1D);
   PGL_CATCH(false)
 }
+static bool dist_dqt(const GpuSamplingDistribution *d) { return d->field->surface.cfg.dqt != 0; }
+static FieldView dist_view(const GpuSamplingDistribution *d) {
+  return (d->volume ? d->field->volume : d->field->surface).view();
+}
 static pgl_vec3f dist_sample(GpuSamplingDistribution *d, pgl_point2f u, float *pdf) {
   Context &c = Context::get();
-  check(launch_ssd_sample(d->dState, u.x, u.y, pdf ? 1 : 0, d->hRes, c.stream), "sample");
+  if (dist_dqt(d))
+    check(launch_ssd_dqt_sample(dist_view(d), d->dState, u.x, u.y, d->hRes, c.stream), "sample");
+  else
+    check(launch_ssd_sample(d->dState, u.x, u.y, pdf ? 1 : 0, d->hRes, c.stream), "sample");
   check(cudaStreamSynchronize(c.stream), "sample");
   if (pdf) *pdf = d->hRes->pdf;
   return pgl_vec3f{d->hRes->dx, d->hRes->dy, d->hRes->dz};
 }
 static float dist_pdf(GpuSamplingDistribution *d, pgl_vec3f dir, bool li) {
   Context &c = Context::get();
-  check(launch_ssd_pdf(d->dState, dir.x, dir.y, dir.z, li ? 1 : 0, d->hRes, c.stream), "pdf");
+  if (dist_dqt(d))  // a quadtree's incoming-radiance pdf is its pdf
+    check(launch_ssd_dqt_pdf(dist_view(d), d->dState, dir.x, dir.y, dir.z, d->hRes, c.stream), "pdf");
+  else
+    check(launch_ssd_pdf(d->dState, dir.x, dir.y, dir.z, li ? 1 : 0, d->hRes, c.stream), "pdf");
   check(cudaStreamSynchronize(c.stream), "pdf");
   return d->hRes->pdf;
 }
@@ -394,13 +426,14 @@ OPENPGL_CORE_INTERFACE void pglSurfaceSamplingDistributionApplyCosineProduct(PGL
                                                                              pgl_vec3f normal) {
   PGL_TRY
   if (D(d)->numDistributions == 0) return;  // VMMSurfaceSamplingDistribution.h:52-60
+  if (dist_dqt(D(d))) return;                // not supported by quadtrees (DQTSurfaceSamplingDistribution.h:20-27)
   Context &c = Context::get();
   check(launch_ssd_cosine(D(d)->dState, normal.x, normal.y, normal.z, 2.18853f, cosine_lobe_normalization(), c.stream),
         "cosine product");
   PGL_CATCH_VOID
 }
-OPENPGL_CORE_INTERFACE bool pglSurfaceSamplingDistributionSupportsApplyCosineProduct(PGLSurfaceSamplingDistribution) {
-  return true;
+OPENPGL_CORE_INTERFACE bool pglSurfaceSamplingDistributionSupportsApplyCosineProduct(PGLSurfaceSamplingDistribution d) {
+  return d && !dist_dqt(D(d));
 }
 OPENPGL_CORE_INTERFACE pgl_vec3f pglSurfaceSamplingDistributionSample(PGLSurfaceSamplingDistribution d,
                                                                       pgl_point2f sample) {
@@ -479,14 +512,15 @@ OPENPGL_CORE_INTERFACE void pglVolumeSamplingDistributionApplySingleLobeHenyeyGr
     PGLVolumeSamplingDistribution d, pgl_vec3f dir, const float meanCosine) {
   PGL_TRY
   if (D(d)->numDistributions == 0) return;
+  if (dist_dqt(D(d))) return;  // not supported by quadtrees
   Context &c = Context::get();
   check(launch_ssd_hg(D(d)->dState, dir.x, dir.y, dir.z, meanCosine, c.stream), "Henyey-Greenstein product");
   D(d)->numDistributions = kMaxProducts;
   PGL_CATCH_VOID
 }
 OPENPGL_CORE_INTERFACE bool pglVolumeSamplingDistributionSupportsApplySingleLobeHenyeyGreensteinProduct(
-    PGLVolumeSamplingDistribution) {
-  return true;
+    PGLVolumeSamplingDistribution d) {
+  return d && !dist_dqt(D(d));
 }
 OPENPGL_CORE_INTERFACE PGLRegion pglVolumeSamplingGetRegion(PGLVolumeSamplingDistribution d) {
   return reinterpret_cast<PGLRegion>(const_cast<void *>(D(d)->regionTag));

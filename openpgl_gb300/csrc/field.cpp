@@ -21,7 +21,7 @@ void check(cudaError_t e, const char *what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// The host C library's expf/cosf exception table (gen_libm_exceptions.cpp),
+// The host C library's expf/cosf/sinf exception table (gen_libm_exceptions.cpp),
 // written by the build next to this library as libm_exceptions.bin, copied
 // to device memory that lives until the process exits.
 static LibmTables load_libm_tables() {
@@ -33,10 +33,10 @@ static LibmTables load_libm_tables() {
   path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) + "/libm_exceptions.bin";
   std::ifstream is(path, std::ios::binary);
   char magic[8];
-  uint32_t n[2] = {0, 0};
-  if (!is.read(magic, 8) || std::memcmp(magic, "PGLLIBM1", 8) != 0 || !is.read(reinterpret_cast<char *>(n), 8))
+  uint32_t n[3] = {0, 0, 0};
+  if (!is.read(magic, 8) || std::memcmp(magic, "PGLLIBM2", 8) != 0 || !is.read(reinterpret_cast<char *>(n), 12))
     throw std::runtime_error("missing or bad " + path + " (the build writes it)");
-  std::vector<float2> v(size_t(n[0]) + n[1]);
+  std::vector<float2> v(size_t(n[0]) + n[1] + n[2]);
   if (!is.read(reinterpret_cast<char *>(v.data()), std::streamsize(v.size() * sizeof(float2))))
     throw std::runtime_error("truncated " + path);
   float2 *d = nullptr;
@@ -47,8 +47,10 @@ static LibmTables load_libm_tables() {
   LibmTables t;
   t.expf = d;
   t.cosf = d ? d + n[0] : nullptr;
+  t.sinf = d ? d + n[0] + n[1] : nullptr;
   t.numExpf = n[0];
   t.numCosf = n[1];
+  t.numSinf = n[2];
   return t;
 }
 
@@ -113,6 +115,10 @@ template struct DevArray<IStatsAcc>;
 template struct DevArray<QueryIn>;
 template struct DevArray<QueryOut>;
 template struct DevArray<QueryInS4>;
+template struct DevArray<DqtHead>;
+template struct DevArray<DqtStatsNode>;
+template struct DevArray<DqtNode>;
+template struct DevArray<Box2>;
 template struct DevArray<QueryOutS4>;
 template struct DevArray<unsigned long long>;
 template struct DevArray<unsigned char>;
@@ -692,6 +698,10 @@ bool SubField::prepare(SampleSide &in) {
     std::memcpy(regions[0].bounds, sceneBounds, 24);
     dRegions.reserve(1);
     check(cudaMemsetAsync(dRegions.p, 0, sizeof(RegionDir), stream()), "region 0");
+    if (cfg.dqt) {
+      dqtReserve(1);
+      check(launch_dqt_init(dDqtHeads.p, dDqtStats.p, dDqtNodes.p, dqtStride, 0, 1, stream()), "quadtree 0");
+    }
   }
   const uint32_t oldNodes = uint32_t(nodes.size()), oldRegions = uint32_t(regions.size());
   splitNodes_.clear();
@@ -709,6 +719,12 @@ bool SubField::prepare(SampleSide &in) {
     copyIdx_.reserve(idx.size());
     check(cudaMemcpyAsync(copyIdx_.p, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, stream()), "copy idx");
     check(copy_regions(dRegions.p, copyIdx_.p, copyIdx_.p + (R - oldRegions), R - oldRegions, stream()), "copy");
+    if (cfg.dqt) {
+      dqtReserve(R);
+      check(launch_dqt_copy(dDqtHeads.p, dDqtStats.p, dDqtNodes.p, dqtStride, copyIdx_.p, copyIdx_.p + (R - oldRegions),
+                            R - oldRegions, stream()),
+            "copy quadtrees");
+    }
   }
   if (cfg.knn) {  // Field.h:362-387 -> KNN.h:189-266
     std::vector<float4> m(R);
@@ -812,7 +828,28 @@ FieldView SubField::view() const {
   v.knn = cfg.knn;
   v.numNodes = uint32_t(nodes.size());
   v.parallax = cfg.parallax;
+  v.dqt = cfg.dqt;
+  v.dqtHeads = dDqtHeads.p;
+  v.dqtNodes = dDqtNodes.p;
+  v.dqtStride = dqtStride;
   return v;
+}
+
+// Node slots per region for the factory's arguments (at most the tree the
+// arguments allow); growing the region count keeps the existing quadtrees.
+void SubField::dqtReserve(uint32_t R) {
+  const uint64_t bound = dqt_max_nodes(cfg.dqtArgs);
+  if (bound > (uint64_t(1) << 18))
+    throw std::runtime_error("quadtree factory arguments allow trees of more than 262144 nodes");
+  const uint32_t stride = uint32_t(bound);
+  if (dqtStride != 0 && dqtStride != stride) throw std::runtime_error("quadtree node stride changed");
+  dqtStride = stride;
+  dDqtHeads.reserve(R, true);
+  dDqtStats.reserve(size_t(R) * stride, true);
+  dDqtNodes.reserve(size_t(R) * stride, true);
+}
+DqtSide SubField::dqtSide() {
+  return DqtSide{dDqtHeads.p, dDqtStats.p, dDqtNodes.p, dqtStride, sD_.p, sPdf_.p, cfg.dqtArgs, cfg.decayOnSpatialSplit};
 }
 
 std::vector<RegionDir> SubField::downloadRegions() const {
@@ -850,6 +887,14 @@ void SubField::uploadRegions(const std::vector<RegionDir> &r) {
 }
 
 bool SubField::valid() const {  // Field::isValid (Field.h:307-317)
+  if (cfg.dqt) {
+    std::vector<DqtHead> h(regions.size());
+    if (!h.empty())
+      check(cudaMemcpy(h.data(), dDqtHeads.p, h.size() * sizeof(DqtHead), cudaMemcpyDeviceToHost), "D2H");
+    for (const DqtHead &q : h)
+      if (!q.valid) return false;
+    return true;
+  }
   for (const RegionDir &r : downloadRegions())
     if (!r.valid) return false;
   return true;
@@ -899,8 +944,76 @@ void GpuField::update(Storage &s, bool doSurface, bool doVolume) {  // SurfaceVo
   } else if (vol) {
     if (volume.prepare(s.vol)) sides[count++] = &volume;
   }
-  if (count > 0) runEm(sides, count);
+  if (count > 0) {
+    if (surface.cfg.dqt) runDqt(sides, count);
+    else runEm(sides, count);
+  }
   iteration++;
+}
+
+// The quadtree field type's fit / update of every region of the prepared
+// sub-fields (Field.h:389-511 -> DQTFactory.h:149-281), one launch for both:
+// persistent blocks take regions, largest first, from a queue.
+void GpuField::runDqt(SubField *const *sides, int count) {
+  Context &c = Context::get();
+  cudaStream_t s = c.stream;
+  std::vector<std::pair<uint32_t, LeafTask>> keyed;
+  DqtSides ds{};
+  uint32_t stride = 0;
+  for (int i = 0; i < count; ++i) {
+    SubField &f = *sides[i];
+    check(cudaStreamWaitEvent(s, f.events[3], 0), "wait");
+    const uint32_t side = f.isSurface ? 0u : kTaskVolume;
+    ds.side[f.isSurface ? 0 : 1] = f.dqtSide();
+    stride = std::max(stride, f.dqtStride);
+    if (!f.cfg.fitRegions) continue;
+    for (LeafTask t : f.pending) {
+      t.flags |= side;
+      keyed.emplace_back(t.count, t);
+    }
+  }
+  std::stable_sort(keyed.begin(), keyed.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+  std::vector<LeafTask> all;
+  for (auto &k : keyed) all.push_back(k.second);
+  const uint32_t T = uint32_t(all.size());
+  const int blocks = int(std::min<uint32_t>(std::max<uint32_t>(T, 1), uint32_t(2 * c.numSMs)));
+  cudaEvent_t emStart, emEnd;
+  check(cudaEventCreate(&emStart), "event");
+  check(cudaEventCreate(&emEnd), "event");
+  int err = 0;
+  if (T > 0) {
+    tasks_.reserve(T);
+    queue_.reserve(2);
+    dqtRects_.reserve(size_t(blocks) * stride);
+    dqtBuild_.reserve(size_t(blocks) * stride);
+    dqtLeaves_.reserve(size_t(blocks) * stride);
+    check(cudaMemcpyAsync(tasks_.p, all.data(), T * sizeof(LeafTask), cudaMemcpyHostToDevice, s), "tasks");
+    check(cudaMemsetAsync(queue_.p, 0, 2 * sizeof(unsigned int), s), "queue");
+  }
+  check(cudaEventRecord(emStart, s), "event");
+  if (T > 0)
+    check(launch_dqt_update(tasks_.p, T, queue_.p, ds, dqtRects_.p, dqtBuild_.p, dqtLeaves_.p, stride, blocks,
+                            reinterpret_cast<int *>(queue_.p + 1), s),
+          "quadtree update");
+  check(cudaEventRecord(emEnd, s), "event");
+  if (T > 0)
+    check(cudaMemcpyAsync(&err, queue_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s), "quadtree status");
+  check(cudaStreamSynchronize(s), "update");
+  if (err != 0) {
+    cudaEventDestroy(emStart);
+    cudaEventDestroy(emEnd);
+    throw std::runtime_error("quadtree update: a tree outgrew its node slots");
+  }
+  for (int i = 0; i < count; ++i) {
+    SubField &f = *sides[i];
+    std::vector<uint32_t> region;
+    for (const LeafTask &t : all)
+      if (((t.flags & kTaskVolume) != 0) == !f.isSurface) region.push_back(t.region);
+    f.finish(std::vector<LeafReport>(region.size()), std::vector<LeafProfile>(region.size()), std::move(region),
+             emStart, emEnd);
+  }
+  cudaEventDestroy(emStart);
+  cudaEventDestroy(emEnd);
 }
 
 // Directional fit / update of every region of the prepared sub-fields
@@ -1134,7 +1247,8 @@ size_t SubField::workBytes() const {
 }
 size_t GpuField::deviceBytes() const {
   return surface.stateBytes() + surface.workBytes() + volume.stateBytes() + volume.workBytes() + tuneSnap_.bytes() +
-         tasks_.bytes() + reports_.bytes() + profiles_.bytes() + queue_.bytes() + emShare_.bytes();
+         tasks_.bytes() + reports_.bytes() + profiles_.bytes() + queue_.bytes() + emShare_.bytes() +
+         dqtRects_.bytes() + dqtBuild_.bytes() + dqtLeaves_.bytes();
 }
 
 void GpuField::setSceneBounds(const float b[6]) {  // SurfaceVolumeField.h:87-93
@@ -1172,6 +1286,76 @@ struct Writer {
   void put(const T &v) { raw(&v, sizeof(T)); }
   void lanes(const float *a, int v) { raw(a + v * kLanes, sizeof(float) * kLanes); }
 };
+void write_region_tail(Writer &w, const RegionHost &h) {  // sample statistics and range (Region.h:63-71)
+  w.raw(h.stats.mean, 12);
+  w.raw(h.stats.var, 12);
+  w.put<float>(h.stats.n);
+  w.raw(h.stats.lo, 12);
+  w.raw(h.stats.hi, 12);
+  w.put<uint8_t>(h.splitFlag);
+  w.put<uint64_t>(h.rb);
+  w.put<uint64_t>(h.re);
+}
+void write_knn(Writer &w, const SubField &f) {  // KNN.h:320-331
+  w.put<uint8_t>(f.cfg.knn != 0);
+  bool built = f.cfg.knn && !f.regions.empty() && f.initialized;
+  w.put<uint8_t>(built);
+  if (built) {
+    w.put<uint32_t>(uint32_t(f.regions.size()));
+    for (const RegionHost &h : f.regions) {
+      float p[4] = {h.stats.mean[0], h.stats.mean[1], h.stats.mean[2], 0.0f};
+      w.raw(p, 16);
+    }
+  }
+}
+// The quadtree field type after the common head: the factory's arguments
+// (DQTFactory.h:59-61), the kd-tree, per region its validity, quadtree
+// (DQT.h:88-93), bounds, training statistics (DQTFactory.h:118-123) and
+// sample statistics, then the neighbour points.
+void write_sub_dqt(Writer &w, const SubField &f) {
+  const FieldConfig &c = f.cfg;
+  w.put<DqtArgs>(c.dqtArgs);
+  w.put<uint64_t>(c.minSamples);
+  w.put<uint64_t>(c.maxSamples);
+  w.put<uint64_t>(c.maxDepth);
+  w.put<uint8_t>(f.kdInit);
+  w.raw(f.kdBounds, 24);
+  w.put<uint64_t>(f.nodes.size());
+  for (const KDNode &n : f.nodes) {
+    w.put<float>(n.split);
+    w.put<uint32_t>(n.bits);
+  }
+  const size_t R = f.regions.size();
+  w.put<uint64_t>(R);
+  std::vector<DqtHead> heads(R);
+  std::vector<DqtStatsNode> stats(R * size_t(f.dqtStride));
+  std::vector<DqtNode> nodes(R * size_t(f.dqtStride));
+  if (R > 0) {
+    Context &cx = Context::get();
+    check(cudaMemcpyAsync(heads.data(), f.dDqtHeads.p, R * sizeof(DqtHead), cudaMemcpyDeviceToHost, cx.stream), "D2H");
+    check(cudaMemcpyAsync(stats.data(), f.dDqtStats.p, stats.size() * sizeof(DqtStatsNode), cudaMemcpyDeviceToHost,
+                          cx.stream),
+          "D2H");
+    check(cudaMemcpyAsync(nodes.data(), f.dDqtNodes.p, nodes.size() * sizeof(DqtNode), cudaMemcpyDeviceToHost,
+                          cx.stream),
+          "D2H");
+    check(cudaStreamSynchronize(cx.stream), "sync");
+  }
+  for (size_t i = 0; i < R; ++i) {
+    const DqtHead &q = heads[i];
+    const size_t o = i * f.dqtStride;
+    w.put<uint8_t>(q.valid != 0);
+    w.raw(q.pivot, 12);
+    w.put<uint64_t>(q.numNodes);
+    w.raw(nodes.data() + o, q.numNodes * sizeof(DqtNode));
+    w.raw(f.regions[i].bounds, 24);
+    w.put<float>(q.numSamples);
+    w.put<uint64_t>(q.numNodes);
+    w.raw(stats.data() + o, q.numNodes * sizeof(DqtStatsNode));
+    write_region_tail(w, f.regions[i]);
+  }
+  write_knn(w, f);
+}
 void write_sub(Writer &w, const SubField &f) {  // Field::serialize (Field.h:240-267), CPU_8 lane layout
   const FieldConfig &c = f.cfg;
   w.put<uint8_t>(f.isSurface);
@@ -1185,6 +1369,7 @@ void write_sub(Writer &w, const SubField &f) {  // Field::serialize (Field.h:240
   w.put<uint8_t>(f.initialized);
   float t[4] = {0, 0, 0, 0};
   w.raw(t, 16);
+  if (c.dqt) return write_sub_dqt(w, f);
   w.put<uint64_t>(c.initK);
   w.put<float>(c.initKappa);
   w.put<uint64_t>(c.maxK);
@@ -1304,6 +1489,82 @@ struct Reader {
   }
 };
 size_t bytes_left(const Reader &r) { return r.b.size() - r.o; }
+void read_region_tail(Reader &r, RegionHost &h) {
+  r.raw(h.stats.mean, 12);
+  r.raw(h.stats.var, 12);
+  h.stats.n = r.get<float>();
+  r.raw(h.stats.lo, 12);
+  r.raw(h.stats.hi, 12);
+  h.splitFlag = r.get<uint8_t>() != 0;
+  h.rb = r.get<uint64_t>();
+  h.re = r.get<uint64_t>();
+}
+void read_knn(Reader &r, SubField &f) {
+  f.cfg.knn = r.get<uint8_t>() != 0;
+  if (r.get<uint8_t>() != 0) {  // KNN points (the region means), rebuilt on upload
+    const uint32_t np = r.get<uint32_t>();
+    if (np > (bytes_left(r)) / 16) throw std::runtime_error("field file is truncated");
+    std::vector<float> pts(size_t(np) * 4);
+    r.raw(pts.data(), pts.size() * sizeof(float));
+  }
+}
+// The quadtree field type's layout (see write_sub_dqt).
+void read_sub_dqt(Reader &r, SubField &f) {
+  FieldConfig &c = f.cfg;
+  c.dqtArgs = r.get<DqtArgs>();
+  c.minSamples = r.get<uint64_t>();
+  c.maxSamples = r.get<uint64_t>();
+  c.maxDepth = r.get<uint64_t>();
+  f.kdInit = r.get<uint8_t>() != 0;
+  r.raw(f.kdBounds, 24);
+  const uint64_t numNodes = r.count(8);
+  if (numNodes > (uint64_t(1) << 30)) throw std::runtime_error("field file: bad node count");
+  f.nodes.resize(numNodes);
+  for (KDNode &n : f.nodes) {
+    n.split = r.get<float>();
+    n.bits = r.get<uint32_t>();
+  }
+  const uint64_t numRegions = r.count(150);  // a region record takes at least 150 bytes
+  if (numRegions > (uint64_t(1) << 30)) throw std::runtime_error("field file: bad region count");
+  f.regions.assign(numRegions, RegionHost());
+  f.dqtStride = 0;
+  f.dqtReserve(uint32_t(std::max<uint64_t>(numRegions, 1)));
+  const size_t stride = f.dqtStride;
+  std::vector<DqtHead> heads(numRegions);
+  std::vector<DqtStatsNode> stats(numRegions * stride);
+  std::vector<DqtNode> nodes(numRegions * stride);
+  for (size_t i = 0; i < numRegions; ++i) {
+    DqtHead &q = heads[i];
+    q = DqtHead{};
+    q.valid = r.get<uint8_t>() != 0;
+    r.raw(q.pivot, 12);
+    const uint64_t nn = r.count(8);
+    if (nn == 0 || nn > stride) throw std::runtime_error("field file: quadtree larger than its arguments allow");
+    r.raw(nodes.data() + i * stride, nn * sizeof(DqtNode));
+    r.raw(f.regions[i].bounds, 24);
+    q.numSamples = r.get<float>();
+    const uint64_t ns = r.count(24);
+    if (ns != nn) throw std::runtime_error("field file: quadtree and statistics differ in size");
+    r.raw(stats.data() + i * stride, ns * sizeof(DqtStatsNode));
+    q.numNodes = uint32_t(nn);
+    for (size_t k = 0; k < nn; ++k) {
+      const uint32_t ch = stats[i * stride + k].child;
+      if (ch != nodes[i * stride + k].child || (ch != 0 && (ch <= k || ch + 4 > nn)))
+        throw std::runtime_error("field file: bad quadtree");
+    }
+    read_region_tail(r, f.regions[i]);
+  }
+  for (const KDNode &n : f.nodes)
+    if (child_of(n) >= (is_leaf(n) ? numRegions : numNodes)) throw std::runtime_error("field file: bad tree");
+  read_knn(r, f);
+  if (numRegions > 0) {
+    check(cudaMemcpy(f.dDqtHeads.p, heads.data(), heads.size() * sizeof(DqtHead), cudaMemcpyHostToDevice), "H2D");
+    check(cudaMemcpy(f.dDqtStats.p, stats.data(), stats.size() * sizeof(DqtStatsNode), cudaMemcpyHostToDevice), "H2D");
+    check(cudaMemcpy(f.dDqtNodes.p, nodes.data(), nodes.size() * sizeof(DqtNode), cudaMemcpyHostToDevice), "H2D");
+  }
+  f.uploadRegions(std::vector<RegionDir>(numRegions));  // (mixture state unused by quadtree fields)
+  f.uploadTree();
+}
 void read_sub(Reader &r, SubField &f) {  // Field::deserialize (Field.h:269-301), CPU_8 lane layout
   FieldConfig &c = f.cfg;
   f.isSurface = r.get<uint8_t>() != 0;
@@ -1317,6 +1578,7 @@ void read_sub(Reader &r, SubField &f) {  // Field::deserialize (Field.h:269-301)
   f.initialized = r.get<uint8_t>() != 0;
   float t[4];
   r.raw(t, 16);  // timings of the last update
+  if (c.dqt) return read_sub_dqt(r, f);
   c.initK = uint32_t(r.get<uint64_t>());
   c.initKappa = r.get<float>();
   c.maxK = uint32_t(r.get<uint64_t>());
@@ -1423,14 +1685,14 @@ void read_sub(Reader &r, SubField &f) {  // Field::deserialize (Field.h:269-301)
 }  // namespace
 
 // PGL_SPATIAL_STRUCTURE_TYPE / PGL_DIRECTIONAL_DISTRIBUTION_TYPE values (types.h)
-constexpr int32_t kSpatialKdTree = 0, kDirParallaxVmm = 0, kDirVmm = 2;
+constexpr int32_t kSpatialKdTree = 0, kDirParallaxVmm = 0, kDirDqt = 1, kDirVmm = 2;
 
 std::string GpuField::serialize() const {  // SurfaceVolumeField::storeToFile (SurfaceVolumeField.h:171-214)
   Writer w;
   const char hdr[] = "OPENPGL_0.6.0_FIELD";
   w.raw(hdr, sizeof(hdr));
   w.put<int32_t>(kSpatialKdTree);
-  w.put<int32_t>(surface.cfg.parallax ? kDirParallaxVmm : kDirVmm);
+  w.put<int32_t>(surface.cfg.dqt ? kDirDqt : surface.cfg.parallax ? kDirParallaxVmm : kDirVmm);
   w.put<uint64_t>(iteration);
   w.put<uint64_t>(totalSPP);
   write_sub(w, surface);
@@ -1444,9 +1706,10 @@ void GpuField::deserialize(const std::string &bytes) {  // Device::newFieldFromF
   r.raw(hdr, sizeof(hdr));
   if (std::memcmp(hdr, "OPENPGL_0.6.0_FIELD", sizeof(hdr)) != 0) throw std::runtime_error("not an Open PGL 0.6.0 field file");
   const int32_t spatial = r.get<int32_t>(), directional = r.get<int32_t>();
-  if (spatial != kSpatialKdTree || (directional != kDirParallaxVmm && directional != kDirVmm))
-    throw std::runtime_error("field file: only kd-tree fields with (parallax-aware) VMMs are supported");
+  if (spatial != kSpatialKdTree || (directional != kDirParallaxVmm && directional != kDirVmm && directional != kDirDqt))
+    throw std::runtime_error("field file: only kd-tree fields (parallax-aware VMM, VMM, quadtree) are supported");
   const uint32_t parallax = directional == kDirParallaxVmm ? 1u : 0u;
+  surface.cfg.dqt = volume.cfg.dqt = directional == kDirDqt ? 1u : 0u;
   iteration = r.get<uint64_t>();
   totalSPP = r.get<uint64_t>();
   read_sub(r, surface);
@@ -1496,7 +1759,28 @@ bool config_equal(const FieldConfig &a, const FieldConfig &b) {
          a.mcPriorStrength == b.mcPriorStrength && a.mcPrior == b.mcPrior && a.splitThreshold == b.splitThreshold &&
          a.mergeThreshold == b.mergeThreshold && a.useSplitMerge == b.useSplitMerge &&
          a.partialReFit == b.partialReFit && a.maxSplitItr == b.maxSplitItr && a.minSplit == b.minSplit &&
-         a.minRefit == b.minRefit && a.minMerge == b.minMerge;
+         a.minRefit == b.minRefit && a.minMerge == b.minMerge && a.dqt == b.dqt &&
+         (!a.dqt || std::memcmp(&a.dqtArgs, &b.dqtArgs, sizeof(DqtArgs)) == 0);
+}
+// A sub-field's quadtrees in host memory (heads; nodes and statistics at the
+// head's stride).
+struct DqtHostState {
+  std::vector<DqtHead> heads;
+  std::vector<DqtStatsNode> stats;
+  std::vector<DqtNode> nodes;
+};
+DqtHostState download_dqt(const SubField &f) {
+  DqtHostState d;
+  const size_t R = f.regions.size();
+  d.heads.resize(R);
+  d.stats.resize(R * size_t(f.dqtStride));
+  d.nodes.resize(R * size_t(f.dqtStride));
+  if (R == 0) return d;
+  check(cudaMemcpy(d.heads.data(), f.dDqtHeads.p, R * sizeof(DqtHead), cudaMemcpyDeviceToHost), "D2H");
+  check(cudaMemcpy(d.stats.data(), f.dDqtStats.p, d.stats.size() * sizeof(DqtStatsNode), cudaMemcpyDeviceToHost),
+        "D2H");
+  check(cudaMemcpy(d.nodes.data(), f.dDqtNodes.p, d.nodes.size() * sizeof(DqtNode), cudaMemcpyDeviceToHost), "D2H");
+  return d;
 }
 bool sub_equal(const SubField &a, const SubField &b) {
   if (!a.initialized && !b.initialized) return true;
@@ -1511,6 +1795,23 @@ bool sub_equal(const SubField &a, const SubField &b) {
   if (na.size() != nb.size() || da.size() != db.size() || a.regions.size() != b.regions.size()) return false;
   for (size_t i = 0; i < na.size(); ++i)
     if (na[i].split != nb[i].split || na[i].bits != nb[i].bits) eq = false;
+  if (a.cfg.dqt) {  // quadtrees and their statistics (Field.h:552-601)
+    const DqtHostState qa = download_dqt(a), qb = download_dqt(b);
+    for (size_t i = 0; i < da.size(); ++i) {
+      const DqtHead &x = qa.heads[da[i]], &y = qb.heads[db[i]];
+      const RegionHost &hx = a.regions[da[i]], &hy = b.regions[db[i]];
+      if (std::memcmp(&x, &y, sizeof(DqtHead)) != 0) {
+        eq = false;
+        continue;
+      }
+      const size_t oa = size_t(da[i]) * a.dqtStride, ob = size_t(db[i]) * b.dqtStride;
+      if (std::memcmp(&qa.stats[oa], &qb.stats[ob], x.numNodes * sizeof(DqtStatsNode)) != 0) eq = false;
+      if (std::memcmp(&qa.nodes[oa], &qb.nodes[ob], x.numNodes * sizeof(DqtNode)) != 0) eq = false;
+      if (std::memcmp(&hx.stats, &hy.stats, sizeof(Stats)) != 0 || hx.splitFlag != hy.splitFlag) eq = false;
+      if (std::memcmp(hx.bounds, hy.bounds, 24) != 0 || hx.rb != hy.rb || hx.re != hy.re) eq = false;
+    }
+    return eq;
+  }
   std::vector<RegionDir> ra = a.downloadRegions(), rb = b.downloadRegions();
   for (size_t i = 0; i < da.size(); ++i) {
     const RegionDir &x = ra[da[i]], &y = rb[db[i]];

@@ -137,6 +137,13 @@ class SubField {
   DevArray<KDNode> dNodes;
   DevArray<Neighbours> dNbrs;
   DevArray<float> dUniformDirs;
+  // the quadtree field type: per region a head and dqtStride node slots
+  DevArray<DqtHead> dDqtHeads;
+  DevArray<DqtStatsNode> dDqtStats;
+  DevArray<DqtNode> dDqtNodes;
+  uint32_t dqtStride = 0;
+  void dqtReserve(uint32_t regions);  // keeps the existing regions' quadtrees
+  DqtSide dqtSide();
 
   // An Update runs in three steps so that one EM launch serves both
   // sub-fields: prepare() builds the tree, gathers the samples in leaf order
@@ -157,7 +164,10 @@ class SubField {
   bool valid() const;
   // device memory the sub-field holds: its state (regions, nodes,
   // neighbours) and, separately, its Update working set
-  size_t stateBytes() const { return dRegions.bytes() + dNodes.bytes() + dNbrs.bytes() + dUniformDirs.bytes(); }
+  size_t stateBytes() const {
+    return dRegions.bytes() + dNodes.bytes() + dNbrs.bytes() + dUniformDirs.bytes() + dDqtHeads.bytes() +
+           dDqtStats.bytes() + dDqtNodes.bytes();
+  }
   size_t workBytes() const;
 
  private:
@@ -210,6 +220,10 @@ class GpuField {
 
  private:
   void runEm(SubField *const *sides, int count);
+  void runDqt(SubField *const *sides, int count);  // the quadtree field type's fit / update
+  DevArray<Box2> dqtRects_;                      // per block of the quadtree launch: scratch
+  DevArray<DqtStatsNode> dqtBuild_;
+  DevArray<uint32_t> dqtLeaves_;
   std::vector<LeafTask> emOrder(SubField *const *sides, int count, bool byCost) const;
   void autotuneEm(SubField *const *sides, int count, cudaStream_t s);
   DevArray<unsigned char> tuneSnap_;  // state an EM launch changes, kept while trials run

@@ -1,5 +1,5 @@
-// Writes the inputs at which the host C library's single-precision expf and
-// cosf differ from the double-precision function rounded once to float, the
+// Writes the inputs at which the host C library's single-precision expf,
+// cosf and sinf differ from the double-precision function rounded once to float, the
 // form the device evaluates (libm_exceptions.bin, read by the library when
 // its CUDA context is set up).  The reference calls std::exp(float) and
 // std::cos(float) on a few sites of the directional fit (merged and split
@@ -12,12 +12,14 @@
 // different implementation, could round the other way).
 //
 // Ranges: expf over every float in [-104, 89] (outside it both give 0 or
-// infinity), cosf over every float in [0, 4] (its one call site takes the
-// length of a 2D vector of unit-vector components, at most about 1.5).
+// infinity), cosf and sinf over every float in [0, 4] (their call sites take
+// the length of a 2D vector of unit-vector components, at most about 1.5,
+// and the azimuth of a quadtree point, within [-pi, pi]; the C library's
+// cosf is even and its sinf odd, so callers look up |x|).
 //
 // usage: gen_libm_exceptions <out.bin> [threads]
-// file : "PGLLIBM1", u32 nExp, u32 nCos, then nExp and nCos pairs
-//        {float x, float hostResult}, each list sorted by x.
+// file : "PGLLIBM2", u32 nExp, u32 nCos, u32 nSin, then the three lists of
+//        pairs {float x, float hostResult}, each sorted by x.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -96,19 +98,24 @@ int main(int argc, char **argv) {
   std::vector<Pair> exn = scan(0x80000000u, bits(-104.0f), expf_, exp_, threads);
   ex.insert(ex.end(), exn.begin(), exn.end());
   std::vector<Pair> co = scan(0u, bits(4.0f), cosf_, cos_, threads);
+  auto sinf_ = [](float x) { return std::sin(x); };
+  auto sin_ = [](double x) { return std::sin(x); };
+  std::vector<Pair> si = scan(0u, bits(4.0f), sinf_, sin_, threads);
   auto byX = [](const Pair &a, const Pair &b) { return a.x < b.x; };
   std::sort(ex.begin(), ex.end(), byX);
   std::sort(co.begin(), co.end(), byX);
+  std::sort(si.begin(), si.end(), byX);
   FILE *f = std::fopen(argv[1], "wb");
   if (!f) {
     std::perror(argv[1]);
     return 1;
   }
-  const uint32_t ne = uint32_t(ex.size()), nc = uint32_t(co.size());
-  bool ok = std::fwrite("PGLLIBM1", 1, 8, f) == 8 && std::fwrite(&ne, 4, 1, f) == 1 && std::fwrite(&nc, 4, 1, f) == 1 &&
-            std::fwrite(ex.data(), sizeof(Pair), ex.size(), f) == ex.size() &&
-            std::fwrite(co.data(), sizeof(Pair), co.size(), f) == co.size();
+  const uint32_t ne = uint32_t(ex.size()), nc = uint32_t(co.size()), ns = uint32_t(si.size());
+  bool ok = std::fwrite("PGLLIBM2", 1, 8, f) == 8 && std::fwrite(&ne, 4, 1, f) == 1 && std::fwrite(&nc, 4, 1, f) == 1 &&
+            std::fwrite(&ns, 4, 1, f) == 1 && std::fwrite(ex.data(), sizeof(Pair), ex.size(), f) == ex.size() &&
+            std::fwrite(co.data(), sizeof(Pair), co.size(), f) == co.size() &&
+            std::fwrite(si.data(), sizeof(Pair), si.size(), f) == si.size();
   ok = (std::fclose(f) == 0) && ok;
-  std::printf("expf: %u inputs, cosf: %u inputs\n", ne, nc);
+  std::printf("expf: %u inputs, cosf: %u inputs, sinf: %u inputs\n", ne, nc, ns);
   return ok ? 0 : 1;
 }

@@ -36,6 +36,33 @@ cudaError_t split_samples_noalloc(const PGLSampleRecord *in, size_t n, PGLSample
                                   uint32_t *counts, cudaStream_t s);
 
 cudaError_t em_upload_tables(const LibmTables &libm);
+cudaError_t dqt_upload_tables(const LibmTables &libm);
+// The directional quadtree field type (dqt_kernels.cu): one sub-field's
+// quadtrees (a head per region, `stride` node slots per region), its
+// sorted samples and its factory arguments.
+struct DqtSide {
+  DqtHead *heads;
+  DqtStatsNode *stats;
+  DqtNode *nodes;
+  uint32_t stride;
+  const float4 *dirw;
+  const float *pdf;
+  DqtArgs args;
+  float decay;  // on a spatial split
+};
+struct DqtSides {
+  DqtSide side[2];
+};
+// Fit or update of every task's region (persistent blocks on a queue; per
+// block `scratchStride` rectangles, build nodes and leaf indices of scratch);
+// *err becomes non-zero when a tree outgrows its node slots.
+cudaError_t launch_dqt_update(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, const DqtSides &sides,
+                              Box2 *rects, DqtStatsNode *builds, uint32_t *leaves, uint32_t scratchStride, int blocks,
+                              int *err, cudaStream_t s);
+cudaError_t launch_dqt_copy(DqtHead *heads, DqtStatsNode *stats, DqtNode *nodes, uint32_t stride, const uint32_t *dst,
+                            const uint32_t *src, uint32_t n, cudaStream_t s);
+cudaError_t launch_dqt_init(DqtHead *heads, DqtStatsNode *stats, DqtNode *nodes, uint32_t stride, uint32_t first,
+                            uint32_t n, cudaStream_t s);
 // Path-vertex queries: Init + cosine product, then kVertexSamples SamplePDF calls.
 cudaError_t launch_query_s4(const QueryParams &p, const QueryInS4 *in, QueryOutS4 *out, uint32_t n,
                             cudaStream_t s);
@@ -143,5 +170,10 @@ cudaError_t launch_ssd_cosine(SSDState *st, float nx, float ny, float nz, float 
 cudaError_t launch_ssd_hg(SSDState *st, float dx, float dy, float dz, float meanCosine, cudaStream_t s);
 cudaError_t launch_ssd_sample(const SSDState *st, float ux, float uy, int withPdf, SSDResult *res, cudaStream_t s);
 cudaError_t launch_ssd_pdf(const SSDState *st, float dx, float dy, float dz, int li, SSDResult *res, cudaStream_t s);
+// the same for a quadtree region (the region Init chose, read from the field)
+cudaError_t launch_ssd_dqt_sample(const FieldView &f, const SSDState *st, float ux, float uy, SSDResult *res,
+                                  cudaStream_t s);
+cudaError_t launch_ssd_dqt_pdf(const FieldView &f, const SSDState *st, float dx, float dy, float dz, SSDResult *res,
+                               cudaStream_t s);
 
 }  // namespace pgl

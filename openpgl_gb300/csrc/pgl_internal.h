@@ -3,6 +3,7 @@
 
 #include <cstdint>
 
+#include "dqt.cuh"
 #include "pgl_math.cuh"
 
 namespace pgl {
@@ -27,6 +28,8 @@ struct FieldConfig {
   float maxMeanCosineSplit = 0.0f;   // KappaToMeanCosine(32000)
   uint32_t laneWidth = 8;            // merging stops at K <= lane width (CPU_8)
   uint32_t parallax = 1;             // PARALLAX_AWARE_VMM (1) or VMM (0): reprojection and shifts
+  uint32_t dqt = 0;                  // QUADTREE (Device.h:185-210): quadtrees instead of mixtures
+  DqtArgs dqtArgs;                   // the quadtree factory's arguments
 };
 
 // Parallax-aware vMF mixture, lane-major (lobe k at index k), as
@@ -162,6 +165,11 @@ struct FieldView {
   uint32_t knn;
   uint32_t numNodes;
   uint32_t parallax;  // shift the region's mixture to the query point
+  // the quadtree field type: per region a head and `dqtStride` tree nodes
+  const DqtHead *dqtHeads;
+  const DqtNode *dqtNodes;
+  uint32_t dqtStride;
+  uint32_t dqt;
 };
 
 struct Lobe {
@@ -177,6 +185,7 @@ struct SSDState {
   float hw[kMaxProducts];         // the products' weights (their integrals, normalised)
   uint32_t K;
   uint32_t numProducts;           // 0: sample and evaluate g; else h[0, numProducts)
+  uint32_t region;                // the region chosen at Init (quadtree fields sample its tree)
 };
 
 struct SSDResult {

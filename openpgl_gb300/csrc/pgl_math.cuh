@@ -49,7 +49,8 @@ namespace pgl {
 struct LibmTables {
   const float2 *expf;
   const float2 *cosf;
-  uint32_t numExpf, numCosf;
+  const float2 *sinf;
+  uint32_t numExpf, numCosf, numSinf;
 };
 #ifdef __CUDACC__
 static __constant__ uint32_t d_rcp_table[2048];
@@ -202,6 +203,24 @@ PGL_HD float lib_logf(float x) {
 PGL_HD float lib_cosf(float x) {
 #ifdef __CUDA_ARCH__
   return libm_lookup(d_libm.cosf, d_libm.numCosf, x, float(cos(double(x))));
+#else
+  return std::cos(x);
+#endif
+}
+// sinf of the host C library (odd: the table holds x >= 0)
+PGL_HD float lib_sinf(float x) {
+#ifdef __CUDA_ARCH__
+  const float a = fabsf(x);
+  const float r = libm_lookup(d_libm.sinf, d_libm.numSinf, a, float(sin(double(a))));
+  return x < 0.0f ? -r : r;
+#else
+  return std::sin(x);
+#endif
+}
+// cosf of the host C library for any sign (even)
+PGL_HD float lib_cosf_any(float x) {
+#ifdef __CUDA_ARCH__
+  return lib_cosf(fabsf(x));
 #else
   return std::cos(x);
 #endif

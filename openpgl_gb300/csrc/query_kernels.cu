@@ -9,6 +9,7 @@
 // j+24 summed in vector order, then the 8-lane tree).
 #include <cuda_runtime.h>
 
+#include "dqt.cuh"
 #include "hg_table.h"
 #include "launch.h"
 #include "pgl_internal.h"
@@ -216,6 +217,80 @@ __device__ __forceinline__ V3 products_sample(const Lobe h[kHgLobes], const floa
   return d;
 }
 
+// ---------------------------------------------------------------- quadtree regions
+// SphereToSquareCylindrical::pointToDirection (SphereToSquare.h:40-55), with
+// the host C library's cosf and sinf of the azimuth
+__device__ V3 dqt_point_to_dir(float px, float py) {
+  px = dqt_clamp(px, 0.f, 1.f);
+  py = dqt_clamp(py, 0.f, 1.f);
+  const float cosTheta = 2.0f * px - 1.0f;
+  const float sinTheta = sqrtf(1.0f - cosTheta * cosTheta);
+  const float phi = float((double(py) - 0.5) * 2.0 * kPiD);
+  return mk(dqt_clamp(sinTheta * lib_cosf_any(phi), -1.f, 1.f), dqt_clamp(sinTheta * lib_sinf(phi), -1.f, 1.f),
+            dqt_clamp(cosTheta, -1.f, 1.f));
+}
+// samplePdf (DQT.h:62-72, :115-153): a stochastic descent that picks the
+// left or right half by u.x and the lower or upper half by u.y, each
+// rescaled into the chosen part; pdf = leaf weight / (root weight x leaf
+// area) / 4 pi
+__device__ float dqt_sample_pdf(const DqtNode *N, float ux, float uy, V3 &dir) {
+  float span = 1.0f, x = 0.0f, y = 0.0f;
+  auto rescale = [](float t, float &u) {
+    if (u < t) {
+      u /= t;
+      return true;
+    }
+    u -= t;
+    u /= 1.0f - t;
+    return false;
+  };
+  uint32_t idx = 0;
+  while (N[idx].child > 0) {
+    span /= 2.0f;
+    uint32_t off = 0;
+    const DqtNode *c = &N[N[idx].child];
+    const float wl = c[0].weight + c[2].weight, wr = c[1].weight + c[3].weight;
+    if (!rescale(wl / (wl + wr), ux)) {
+      off += 1;
+      x += span;
+    }
+    const float wt = c[off].weight, wb = c[off + 2].weight;
+    if (!rescale(wt / (wt + wb), uy)) {
+      off += 2;
+      y += span;
+    }
+    idx = N[idx].child + off;
+  }
+  float pdf = N[idx].weight / (N[0].weight * span * span);
+  const float px = x + ux * span, py = y + uy * span;
+  pdf /= kDqtJacobian;
+  dir = dqt_point_to_dir(px, py);
+  return pdf;
+}
+// pdf (DQT.h:53-60, :155-159)
+__device__ float dqt_pdf(const DqtNode *N, V3 d) {
+  float px, py;
+  dqt_dir_to_point(d.x, d.y, d.z, px, py);
+  Box2 rect;
+  const uint32_t i = dqt_query(N, px, py, rect);
+  const float p = N[i].weight / (N[0].weight * rect.area()) / kDqtJacobian;
+  return smin(FLT_MAX, p);
+}
+// A guided query on a quadtree region (DQTSurfaceSamplingDistribution.h /
+// DQTVolumeSamplingDistribution.h: no products, pdfLi = pdf); lane 0 writes.
+__device__ void dqt_query_out(const FieldView &f, uint32_t reg, uint32_t leaf, float ux, float uy, QueryOut &o) {
+  if (!f.dqtHeads[reg].valid) return;
+  const DqtNode *N = f.dqtNodes + size_t(reg) * f.dqtStride;
+  V3 d;
+  o.pdf = dqt_sample_pdf(N, ux, uy, d);
+  o.ok = 1;
+  o.id = leaf;
+  o.dx = d.x;
+  o.dy = d.y;
+  o.dz = d.z;
+  o.pdfLi = dqt_pdf(N, d);
+}
+
 // Batched guided query: Init + optional cosine product (surface) or
 // Henyey-Greenstein product (volume) + SamplePDF (+ pdfLi).
 __global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, uint32_t n) {
@@ -235,7 +310,9 @@ __global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, ui
     if (f.knn && s1d >= 0.f) reg = choose_region(f, leaf, q.px, q.py, q.pz, s1d, lane);
     o.s1d = s1d;
     const RegionDir &R = f.regions[reg];
-    if (R.valid) {
+    if (f.dqt) {
+      if (lane == 0) dqt_query_out(f, reg, leaf, q.ux, q.uy, o);
+    } else if (R.valid) {
       const int K = int(R.vmm.K), cnt = vec_count(K);
       Lobe li = load_shifted(R.vmm, lane, q.px, q.py, q.pz, f.parallax != 0);
       V3 d;
@@ -288,7 +365,21 @@ __global__ void query_s4_kernel(QueryParams P, const QueryInS4 *in, QueryOutS4 *
     if (f.knn && s1d >= 0.f) reg = choose_region(f, leaf, q.px, q.py, q.pz, s1d, lane);
     o.s1d = s1d;
     const RegionDir &R = f.regions[reg];
-    if (R.valid) {
+    if (f.dqt) {  // a quadtree region: four samples of its quadtree (no cosine product)
+      if (f.dqtHeads[reg].valid) {
+        const DqtNode *N = f.dqtNodes + size_t(reg) * f.dqtStride;
+        if (lane == 0)
+          for (int k = 0; k < kVertexSamples; ++k) {
+            V3 d;
+            o.s[k][3] = dqt_sample_pdf(N, q.u[k][0], q.u[k][1], d);
+            o.s[k][0] = d.x;
+            o.s[k][1] = d.y;
+            o.s[k][2] = d.z;
+          }
+        o.ok = 1;
+        o.id = leaf;
+      }
+    } else if (R.valid) {
       const int K = int(R.vmm.K), cnt = vec_count(K);
       Lobe g = load_shifted(R.vmm, lane, q.px, q.py, q.pz, f.parallax != 0);
       if (P.cosine) {
@@ -326,7 +417,13 @@ __global__ void ssd_init_kernel(FieldView f, float px, float py, float pz, float
     if (f.knn && s1d >= 0.f) reg = choose_region(f, leaf, px, py, pz, s1d, lane);
     r.s1d = s1d;
     const RegionDir &R = f.regions[reg];
-    if (R.valid) {
+    if (f.dqt) {  // the quadtree is read from the field when sampled
+      if (f.dqtHeads[reg].valid) {
+        if (lane == 0) st->region = reg;
+        r.ok = 1;
+        r.id = leaf;
+      }
+    } else if (R.valid) {
       Lobe li = load_shifted(R.vmm, lane, px, py, pz, f.parallax != 0);
       st->li[lane] = li;
       st->g[lane] = li;
@@ -400,6 +497,22 @@ __global__ void ssd_pdf_kernel(const SSDState *st, float dx, float dy, float dz,
   if (lane == 0) res->pdf = pdf;
 }
 
+// Per-object Sample / SamplePDF / PDF / IncomingRadiancePDF of a quadtree
+// region (DQTSurfaceSamplingDistribution.h:28-45: pdfLi is the pdf).
+__global__ void ssd_dqt_sample_kernel(FieldView f, const SSDState *st, float ux, float uy, SSDResult *res) {
+  const DqtNode *N = f.dqtNodes + size_t(st->region) * f.dqtStride;
+  V3 d;
+  const float pdf = dqt_sample_pdf(N, ux, uy, d);
+  res->dx = d.x;
+  res->dy = d.y;
+  res->dz = d.z;
+  res->pdf = pdf;
+}
+__global__ void ssd_dqt_pdf_kernel(FieldView f, const SSDState *st, float dx, float dy, float dz, SSDResult *res) {
+  const DqtNode *N = f.dqtNodes + size_t(st->region) * f.dqtStride;
+  res->pdf = dqt_pdf(N, mk(dx, dy, dz));
+}
+
 // ---------------------------------------------------------------- launchers
 PGL_DEFINE_TABLE_UPLOAD(query_upload_seed_tables)
 cudaError_t query_upload_tables(const LibmTables &libm) {
@@ -453,4 +566,19 @@ cudaError_t launch_ssd_pdf(const SSDState *st, float dx, float dy, float dz, int
   return cudaGetLastError();
 }
 
+}  // namespace pgl
+
+namespace pgl {
+cudaError_t launch_ssd_dqt_sample(const FieldView &f, const SSDState *st, float ux, float uy, SSDResult *res,
+                                  cudaStream_t s) {
+  count_launch();
+  ssd_dqt_sample_kernel<<<1, 1, 0, s>>>(f, st, ux, uy, res);
+  return cudaGetLastError();
+}
+cudaError_t launch_ssd_dqt_pdf(const FieldView &f, const SSDState *st, float dx, float dy, float dz, SSDResult *res,
+                               cudaStream_t s) {
+  count_launch();
+  ssd_dqt_pdf_kernel<<<1, 1, 0, s>>>(f, st, dx, dy, dz, res);
+  return cudaGetLastError();
+}
 }  // namespace pgl

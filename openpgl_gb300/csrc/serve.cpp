@@ -35,6 +35,7 @@ size_t GuidingServer::projectedBytes(size_t samples) const {
 GuidingServer::GuidingServer(GpuField *field, size_t budgetBytes, int reservedSMs)
     : field_(field), budget_(budgetBytes) {
   if (!field) throw std::runtime_error("null field");
+  if (field->surface.cfg.dqt) throw std::runtime_error("the guiding server serves mixture fields, not quadtree fields");
   Context &c = Context::get();
   // the field's EM launches leave these SMs to the query stream
   field_->tuning.reservedSMs = std::max(0, std::min(reservedSMs, c.numSMs - 1));

@@ -16,8 +16,8 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
-# the GPU field holds (parallax-aware) VMMs; the quadtree cases pin the oracle only
-VMM_CASES = sorted(n for n, c in MANIFEST["cases"].items() if not c.get("dqt", False))
+# every field type of the goldens: parallax-aware VMM, plain VMM, directional quadtree
+CASES = sorted(MANIFEST["cases"])
 
 
 @pytest.fixture(scope="module")
@@ -28,7 +28,7 @@ def pgl():
     return openpgl_gb300
 
 
-@pytest.mark.parametrize("name", VMM_CASES)
+@pytest.mark.parametrize("name", CASES)
 def test_reference_field_file_answers_like_the_reference(pgl, name, tmp_path):
     sys.path.insert(0, GOLDEN)
     import make_golden

@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 MANIFEST = json.load(open(os.path.join(GOLDEN, "manifest.json")))
-# the GPU field holds (parallax-aware) VMMs; the quadtree cases pin the oracle only
+# mixture fields; the quadtree cases are held by test_gpu_dqt.py
 CASES = sorted(n for n, c in MANIFEST["cases"].items() if not c.get("dqt", False))
 PDF_TOL = 1e-3
 

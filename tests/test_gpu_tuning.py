@@ -73,8 +73,9 @@ def test_out_of_range_tuning_is_rejected(pgl):
 
 
 def test_plain_launches_give_the_same_field(pgl):
-    """The plain form (one single-block EM launch per region) trains the same
-    field as the batched launch."""
+    """The plain form (per Update and sub-field one EM launch with one block
+    per region, no work queue or helpers) trains the same field as the
+    batched launch."""
     frames = _frames()[:2]
     _, ref = _train(pgl, frames)
     dev = pgl.Device()
