@@ -251,8 +251,9 @@ def run_widened(pgl, dev, stream, field, queries, frames, d_frames, steps, warmu
     """The rows built beyond the core path, each timed on the device with CUDA
     events: volume guided queries with the Henyey-Greenstein product (mean
     cosines uniform in [-0.9, 0.9]), training samples made from 131,072
-    synthetic paths, and one
-    multi-frame step with the plain VMM field type."""
+    synthetic paths, one multi-frame step with the plain VMM field type and
+    one with the directional quadtree field type (plus its guided queries),
+    and the plain drop-in form of the Update."""
     import torch
 
     from openpgl_gb300 import synthetic as syn
@@ -317,6 +318,32 @@ def run_widened(pgl, dev, stream, field, queries, frames, d_frames, steps, warmu
     b.record(stream)
     torch.cuda.synchronize()
     out["plain_vmm_update"] = {"value": round(a.elapsed_time(b), 3), "unit": UNIT}
+    # the directional quadtree field type on the multi-frame workload (one step
+    # after one warm-up), and its guided queries on the trained field
+    quad = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF, dqt=True))
+    step(quad)
+    torch.cuda.synchronize()
+    a.record(stream)
+    step(quad)
+    b.record(stream)
+    torch.cuda.synchronize()
+    dqt_ms = a.elapsed_time(b)
+    rq = torch.empty(n * 32, dtype=torch.uint8, device="cuda")
+    for _ in range(max(warmup, 3)):
+        quad.sample_batch_device(qd.data_ptr(), n, rq.data_ptr(), stream=dev.cuda_stream())
+    a.record(stream)
+    for _ in range(reps):
+        quad.sample_batch_device(qd.data_ptr(), n, rq.data_ptr(), stream=dev.cuda_stream())
+    b.record(stream)
+    torch.cuda.synchronize()
+    qms = a.elapsed_time(b) / reps
+    out["dqt_update"] = {"value": round(dqt_ms, 3), "unit": UNIT,
+                         "queries_per_s": round(n / (qms * 1e-3)), "ms_per_query_batch": round(qms, 3),
+                         "factory": "rejection-sampling estimator, mean split metric, threshold 0.01, "
+                                    "footprint 1, 12 levels"}
+    out["_dqt_field"] = quad.field_bytes()
+    out["_dqt_queries"] = np.frombuffer(rq.cpu().numpy().tobytes(), dtype=pgl.QUERY_RESULT_DTYPE).copy()
+    quad.release()
     # the plain drop-in form of the Update: per sub-field one EM launch with a
     # block per region (all SMs; no queue, no helper blocks, no shared passes)
     per_region = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=MAX_SAMPLES_PER_LEAF))
@@ -335,6 +362,90 @@ def run_widened(pgl, dev, stream, field, queries, frames, d_frames, steps, warmu
                                    "no work queue, no helper blocks)",
                            "same_field": per_region.field_bytes() == field_bytes_of(pgl, dev, frames, d_frames)}
     return out
+
+
+def run_single_update(pgl, dev, stream, steps):
+    """The single-Update configuration: 1,048,576 cube-face surface samples,
+    maxSamplesPerLeaf 32000, one Update of a fresh field (batched form and the
+    plain drop-in form, samples already in device memory), then 1,048,576
+    guided queries (cosine product, one SamplePDF) on device buffers.  Returns
+    the numbers, the frame and the batched form's field bytes (for the oracle
+    comparison of the CPU leg)."""
+    import torch
+
+    from openpgl_gb300 import synthetic as syn
+
+    frame = syn.cube_face_samples(1 << 20, 1001)
+    d = torch.from_numpy(frame.view(np.uint8)).to("cuda")
+    q = syn.queries(1 << 20, 1002)
+    qd = torch.from_numpy(q.view(np.uint8)).to("cuda")
+    rd = torch.empty(len(q) * 32, dtype=torch.uint8, device="cuda")
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    st = pgl.SampleStorage()
+    out, fields = {}, {}
+    for form in ("batched", "plain"):
+        field = pgl.Field(dev, pgl.FieldConfig(deterministic=True, max_samples_per_leaf=32000))
+        field.set_plain_update(form == "plain")
+        times = []
+        for i in range(max(3, min(steps, 5)) + 1):
+            field.reset()
+            st.clear()
+            st.add_samples_device(d.data_ptr(), len(frame))
+            torch.cuda.synchronize()
+            a.record(stream)
+            field.update(st)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if i:  # the first Update is a warm-up
+                times.append(a.elapsed_time(b))
+        out[f"{form}_update_ms"] = round(statistics.median(times), 3)
+        fields[form] = field
+    field = fields["batched"]
+    for _ in range(3):
+        field.sample_batch_device(qd.data_ptr(), len(q), rd.data_ptr(), stream=dev.cuda_stream())
+    reps = 10
+    a.record(stream)
+    for _ in range(reps):
+        field.sample_batch_device(qd.data_ptr(), len(q), rd.data_ptr(), stream=dev.cuda_stream())
+    b.record(stream)
+    torch.cuda.synchronize()
+    qms = a.elapsed_time(b) / reps
+    out.update(batched_speedup=round(out["plain_update_ms"] / out["batched_update_ms"], 2),
+               same_field=fields["plain"].field_bytes() == field.field_bytes(),
+               queries_per_s=round(len(q) / (qms * 1e-3)), ms_per_query_batch=round(qms, 3),
+               workload="1,048,576 cube-face surface samples, maxSamplesPerLeaf 32000, one Update of a fresh "
+                        "field; 1,048,576 guided queries (cosine product, one SamplePDF)")
+    gq = np.frombuffer(rd.cpu().numpy().tobytes(), dtype=pgl.QUERY_RESULT_DTYPE).copy()
+    fb = field.field_bytes()
+    for f in fields.values():
+        f.release()
+    st.release()
+    return out, (frame, q, fb, gq)
+
+
+def single_update_cpu(frame, q, gpu_field_bytes, gpu_queries):
+    """The oracle on the single-Update configuration (all host threads, one
+    Update of a fresh field, timed) and the comparison of its field and
+    queries with the GPU's."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pyoracle
+    from helpers import compare_fields, compare_queries
+
+    threads = os.cpu_count()
+    orc = pyoracle.OracleField(32000, deterministic=True, threads=threads)
+    t0 = time.perf_counter()
+    orc.update(frame)
+    ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    ref = orc.query(q)
+    qps = len(q) / (time.perf_counter() - t0)
+    r = compare_fields(gpu_field_bytes, orc.field_bytes(), "surface")
+    par = {k: r.get(k) for k in ("tree_equal", "numbering_equal", "stats_equal", "regions", "bit_exact_regions",
+                                 "worst_pdf_rel")}
+    par["queries"] = compare_queries(gpu_queries, ref)
+    orc.close()
+    return {"update_ms": round(ms, 1), "queries_per_s": round(qps), "cores": threads, "kind": "port"}, par
 
 
 def field_bytes_of(pgl, dev, frames, d_frames):
@@ -404,6 +515,30 @@ def parity_block(orc, gpu_field_bytes, gpu_queries, queries):
     out["queries"] = compare_queries(gpu_queries, ref)
     out["queries"]["count"] = len(queries)
     return out, qps
+
+
+def dqt_parity(frames, queries, gpu_field_bytes, gpu_queries):
+    """The oracle's quadtree field on the same 8 frames (timed: the quadtree
+    field type's CPU baseline, all host threads) against the GPU's
+    (compare_dqt_fields per side), and the guided queries against the
+    oracle's."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pyoracle
+    from helpers import compare_dqt_fields, compare_queries
+
+    threads = os.cpu_count()
+    orc = pyoracle.OracleField(MAX_SAMPLES_PER_LEAF, deterministic=True, threads=threads, dqt=True)
+    t0 = time.perf_counter()
+    for f in frames:
+        orc.update(f)
+    ms = (time.perf_counter() - t0) * 1e3 * UNIT_SAMPLES / (len(frames) * FRAME_SAMPLES)
+    base = {"value": round(ms, 1), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "frames 1-8 of 8, fresh quadtree field"}
+    par = {side: compare_dqt_fields(gpu_field_bytes, orc.field_bytes(), side) for side in ("surface", "volume")}
+    par["queries"] = compare_queries(gpu_queries, orc.query(queries))
+    orc.close()
+    return base, par
 
 
 # ----------------------------------------------------------------- serving
@@ -833,6 +968,10 @@ def run_gpu(args, rank, world, local_rank):
         widened = run_widened(pgl, dev, stream, field, queries, frames, d_frames, args.steps, args.warmup)
         widened["plain_update"]["batched_speedup"] = round(widened["plain_update"]["value"] / ms, 2)
 
+    # ---- the single-Update configuration (1M samples, one Update, 1M queries)
+    log("single-Update configuration")
+    single, single_data = run_single_update(pgl, dev, stream, args.steps) if args.widened else (None, None)
+
     # ---- clustered workload, default and autotuned EM schedule
     log("clustered workload")
     clustered, clustered_field = run_clustered(pgl, dev, stream, args.steps, 1) if args.clustered else (None, None)
@@ -917,6 +1056,7 @@ def run_gpu(args, rank, world, local_rank):
         "serving": serving,
         "serving_clustered": serving_c3,
         "scale": scale,
+        "single_update": single,
         "clustered": clustered,
         "widened": widened,
         "gpu_launches": int(launches),
@@ -929,6 +1069,16 @@ def run_gpu(args, rank, world, local_rank):
             out["parity"], qps = parity_block(orc, gpu_field_bytes, gpu_queries, queries)
             out["cpu_baseline"]["queries_per_s"] = round(qps)
             orc.close()
+        if single is not None:
+            log("single-Update oracle and parity")
+            single["cpu_baseline"], single["parity"] = single_update_cpu(*single_data)
+        if widened is not None and "_dqt_field" in widened:
+            log("quadtree oracle and parity")
+            widened["dqt_update"]["cpu_baseline"], widened["dqt_update"]["parity"] = dqt_parity(
+                frames, queries, widened["_dqt_field"], widened["_dqt_queries"])
+    if widened is not None:
+        widened.pop("_dqt_field", None)
+        widened.pop("_dqt_queries", None)
     return out
 
 

@@ -19,8 +19,7 @@ import sys
 import numpy as np
 import pytest
 
-import fieldfile
-from helpers import compare_queries
+from helpers import compare_dqt_fields, compare_queries
 
 pytestmark = pytest.mark.gpu
 
@@ -37,41 +36,6 @@ def pgl():
 
     openpgl_gb300.load()
     return openpgl_gb300
-
-
-def compare_dqt_fields(a_bytes, b_bytes, side):
-    """kd-tree, sample statistics, quadtree structure and relative differences
-    of node weights and training statistics (region by region, canonical
-    order)."""
-    A, B = fieldfile.read_field_file(a_bytes)[side], fieldfile.read_field_file(b_bytes)[side]
-    ca, cb = fieldfile.canonical_tree(A), fieldfile.canonical_tree(B)
-    res = dict(regions=len(A["regions"]), tree_equal=bool(np.array_equal(ca["dim"], cb["dim"])
-                                                          and np.array_equal(ca["split"], cb["split"])),
-               numbering_equal=bool(np.array_equal(A["nodes"]["bits"], B["nodes"]["bits"])))
-    if not res["tree_equal"] or len(A["regions"]) != len(B["regions"]):
-        return res
-    worst, bit, structure, stats, valid = 0.0, 0, True, True, True
-    for ra, rb in zip(A["regions"], B["regions"]):
-        for key in ("mean", "var", "bounds"):
-            if not np.array_equal(ra["stats"][key].view(np.uint32), rb["stats"][key].view(np.uint32)):
-                stats = False
-        valid &= ra["valid"] == rb["valid"]
-        na, nb = ra["dqt"]["nodes"], rb["dqt"]["nodes"]
-        if len(na) != len(nb) or not np.array_equal(na["offsetChildren"], nb["offsetChildren"]):
-            structure = False
-            continue
-        sa, sb = ra["dqt_stats"]["nodes"], rb["dqt_stats"]["nodes"]
-        same = na.tobytes() == nb.tobytes() and sa.tobytes() == sb.tobytes()
-        bit += int(same)
-        for x, y in ((na["sampleWeight"], nb["sampleWeight"]), (sa["sampleWeight"], sb["sampleWeight"]),
-                     (sa["splitWeight"], sb["splitWeight"]), (sa["numSamples"], sb["numSamples"]),
-                     (sa["firstMoment"], sb["firstMoment"]), (sa["secondMoment"], sb["secondMoment"])):
-            x, y = x.astype(np.float64), y.astype(np.float64)
-            rel = np.abs(x - y) / np.maximum(np.abs(y), 1e-30)
-            worst = max(worst, float(rel.max()) if len(rel) else 0.0)
-    res.update(structure_equal=structure, stats_equal=stats, valid_equal=bool(valid), bit_exact_regions=bit,
-               worst_rel=worst)
-    return res
 
 
 def _check(a_bytes, b_bytes):
