@@ -119,7 +119,7 @@ OPENPGL_CORE_INTERFACE int pglDebugBoundedWaitRunsOut(uint64_t limitNs);
 // merges, components (5 x u32 per region); returns the region count, writes
 // when capacity >= 5 x count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int volume, uint32_t *out, size_t capacity);
-// Where the EM kernel spent the last Update, per region (21 x u64 each):
+// Where the EM kernel spent the last Update, per region (23 x u64 each):
 // region, samples, E-step passes, distance passes, split-statistics passes,
 // then SM clock cycles in E-steps, distance passes, split-statistics passes,
 // merging, M-steps and in total, then inside the passes the cycles of the
@@ -128,8 +128,9 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateReports(PGLField field, int v
 // by its own block (the others by blocks that had no region left), and the
 // cycles a summing thread waited for chunks, then the lobes summed over the
 // E-step, distance and split-statistics passes (the sum of the mixture's
-// lobe count over the passes of each kind).  Returns the region count;
-// writes when capacity >= 21 x count.
+// lobe count over the passes of each kind), then the device's global timer
+// (ns) when a block took the region and when it was done with it.  Returns
+// the region count; writes when capacity >= 23 x count.
 OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int volume, uint64_t *out,
                                                            size_t capacity);
 // Schedule parameters of the field's EM launch (no reference counterpart;

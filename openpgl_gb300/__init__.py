@@ -465,7 +465,7 @@ class Field:
     def profile(self, volume=False):
         """Per-region EM profile of the last Update (see pglFieldGetLastUpdateProfile)."""
         n = self.lib.pglFieldGetLastUpdateProfile(self.h, int(volume), None, 0)
-        out = np.zeros((n, 21), dtype=np.uint64)
+        out = np.zeros((n, 23), dtype=np.uint64)
         if n:
             self.lib.pglFieldGetLastUpdateProfile(self.h, int(volume), out.ctypes.data, out.size)
         return out

@@ -998,10 +998,10 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
   PGL_TRY
   const SubField &sf = volume ? F(field)->volume : F(field)->surface;
   size_t n = sf.lastProfiles.size();
-  if (out && cap >= 21 * n)
+  if (out && cap >= 23 * n)
     for (size_t i = 0; i < n; ++i) {
       const LeafProfile &p = sf.lastProfiles[i];
-      uint64_t *o = out + 21 * i;
+      uint64_t *o = out + 23 * i;
       o[0] = sf.lastReportRegion[i];
       o[1] = p.count;
       o[2] = p.estepPasses;
@@ -1023,6 +1023,8 @@ OPENPGL_CORE_INTERFACE size_t pglFieldGetLastUpdateProfile(PGLField field, int v
       o[18] = p.estepLobes;
       o[19] = p.distLobes;
       o[20] = p.splitLobes;
+      o[21] = p.tBegin;
+      o[22] = p.tEnd;
     }
   return n;
   PGL_CATCH(0)

@@ -2309,6 +2309,7 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Em
     if (threadIdx.x == 0) {
       S.prof = LeafProfile{};
       S.prof.count = t.count;
+      S.prof.tBegin = global_ns();
       afterSplit = R.afterSplit;
       afterMerge = R.afterMerge;
       S.report = LeafReport{0, 0, 0, 0};
@@ -2366,6 +2367,7 @@ em_leaf_kernel(const LeafTask *tasks, uint32_t numTasks, unsigned int *queue, Em
       if (reports) reports[taskId] = S.report;
       if (profiles) {
         S.prof.cycTotal = uint64_t(clock64() - leafStart);
+        S.prof.tEnd = global_ns();
         profiles[taskId] = S.prof;
       }
       atomicAdd(finished, 1u);

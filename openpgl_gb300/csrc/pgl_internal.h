@@ -109,6 +109,9 @@ struct LeafProfile {
   // lobes summed over the passes of each kind (sum of K per pass): the
   // algorithmic work of a pass is samples x lobes
   uint64_t estepLobes, distLobes, splitLobes;
+  // the device's global timer (ns) when the block took the region and when
+  // it was done with it
+  uint64_t tBegin, tEnd;
 };
 
 // Integer position statistics of one kd child (IntegerSampleStatistics).
