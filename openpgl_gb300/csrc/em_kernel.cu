@@ -39,6 +39,7 @@ constexpr int kMaxPairs = kMaxK * (kMaxK - 1) / 2;
 // ring, from where the home block's loader warp copies them into the stages
 // with bulk copies.  The consumer warps add the chunks in chunk order.
 constexpr int kMaxStages = 8;                          // consumer pipeline stages
+constexpr int kMaxChunk = 384;                         // E-step samples per chunk at most (chunk divisor 1)
 constexpr uint32_t kRingFloats = 65536;                // ring per block (256 KB)
 constexpr uint32_t kRingMaxSlots = 64;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // longest wait before the launch fails
@@ -1215,7 +1216,14 @@ __device__ __forceinline__ EStepShape estep_shape(int cnt, const EmTuning &tune)
   e.consWarps = 3;  // a w and (d_x a) w | (d_y a) w and (d_z a) w | per-sample rows
   e.cons0 = kEmThreads - 32 * e.consWarps;  // consumers: threads [cons0, 512)
   e.P = e.cons0 - 32;                       // producers [0, P), then the loader warp
-  e.C = ((e.P / e.parts) / tune.chunkDiv) & ~7;
+  // as many producer rounds per chunk as keep two stages in the pipeline
+  // buffer, up to kMaxChunk samples: a consumer warp spends a few hundred
+  // cycles per chunk outside its chains
+  const int slots = e.P / e.parts;
+  const int fit = (2 * kStageFloats / 2) / (e.Kp + 9) - 4;  // C + 4 floats per row, two stages
+  int rounds = min(kMaxChunk, fit) / slots;
+  rounds = rounds < 1 ? 1 : rounds;
+  e.C = ((rounds * slots) / tune.chunkDiv) & ~7;
   e.RS = e.C + 4;
   e.stageFloats = (e.Kp + 9) * e.RS;
   e.stages = min(min(kMaxStages, tune.stageCap), 2 * kStageFloats / e.stageFloats);
