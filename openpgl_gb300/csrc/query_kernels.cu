@@ -60,6 +60,31 @@ __device__ uint32_t choose_region(const FieldView &f, uint32_t leaf, float p0, f
   return nb.ids[chosenKey & 7u];
 }
 
+// The same choice by one thread (quadtree fields: a thread per query): the
+// lowest neighbour slot whose key has rank `sel`, else slot 0's.
+__device__ uint32_t choose_region_1(const FieldView &f, uint32_t leaf, float p0, float p1, float p2, float &s1d) {
+  const Neighbours &nb = f.nbrs[leaf];
+  uint32_t size = min(4u, nb.size);
+  uint32_t sel = uint32_t(s1d * float(size));
+  s1d = (s1d - float(sel) / float(size)) * float(size);
+  sel = min(sel, size - 1);
+  uint32_t key[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    V3 d = mk(nb.px[j] - p0, nb.py[j] - p1, nb.pz[j] - p2);
+    float dd = dot(d, d);
+    key[j] = (f2u(dd) & ~7u) | uint32_t(j);
+    if (nb.ids[j] == ~0u) key[j] = f2u(INFINITY);
+  }
+  for (int j = 0; j < 8; ++j) {
+    uint32_t rank = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) rank += (u2f(key[k]) < u2f(key[j])) ? 1u : 0u;
+    if (rank == sel && key[j] != f2u(INFINITY)) return nb.ids[key[j] & 7u];
+  }
+  return nb.ids[key[0] & 7u];
+}
+
 // vfloat8 horizontal sum of lane values over the mixture: per group lane j
 // sums lanes j, j+8, ... over cnt vectors, then the 8-lane tree.
 __device__ __forceinline__ float lane_sum(float v, int cnt, int lane) {
@@ -94,9 +119,9 @@ static_assert(kHgLobes == kMaxProducts, "a distribution holds one product per lo
 static __constant__ HgLobeFit c_hg[kHgFits][kHgLobes];
 
 // PAVMM::product with a single lobe of weight `weight` (the cosine lobe, or a
-// lobe of the phase function's fit); integral = the product's integral
-__device__ __forceinline__ Lobe product_lobe(Lobe L, V3 n, float kappa, float normalization, float weight, int cnt,
-                                             int lane, float &integral) {
+// lobe of the phase function's fit), before the normalisation by the
+// product's integral
+__device__ __forceinline__ Lobe product_terms(const Lobe &L, V3 n, float kappa, float normalization, float weight) {
   V3 mu = mk(L.mx, L.my, L.mz);
   V3 nm = mu * L.kappa + n * kappa;
   float nk = sqrtf(dot(nm, nm));
@@ -113,19 +138,30 @@ __device__ __forceinline__ Lobe product_lobe(Lobe L, V3 n, float kappa, float no
   scale *= L.w * weight;
   Lobe R;
   R.w = scale; R.kappa = nk; R.mx = nm.x; R.my = nm.y; R.mz = nm.z; R.norm = nn; R.e2k = ne;
+  return R;
+}
+// the product; integral = the product's integral
+__device__ __forceinline__ Lobe product_lobe(Lobe L, V3 n, float kappa, float normalization, float weight, int cnt,
+                                             int lane, float &integral) {
+  Lobe R = product_terms(L, n, kappa, normalization, weight);
   integral = lane_sum(lane < cnt * kLanes ? R.w : 0.0f, cnt, lane);
   R.w /= integral;
   return R;
 }
 
-__device__ __forceinline__ float mixture_pdf(const Lobe &L, V3 d, int cnt, int lane) {
+// one lobe's term of the mixture's pdf in direction d
+__device__ __forceinline__ float mixture_term(const Lobe &L, V3 d) {
   float ct = dot(d, mk(L.mx, L.my, L.mz));
   float cm1 = emin(ct - 1.0f, 0.0f);
   float ev = L.norm * fexp(L.kappa * cm1);
-  float t = lane < cnt * kLanes ? L.w * ev : 0.0f;
-  return lane_sum(t, cnt, lane);
+  return L.w * ev;
+}
+__device__ __forceinline__ float mixture_pdf(const Lobe &L, V3 d, int cnt, int lane) {
+  const float t = mixture_term(L, d);
+  return lane_sum(lane < cnt * kLanes ? t : 0.0f, cnt, lane);
 }
 
+__device__ V3 lobe_direction(float k, float e2k, V3 mu, float ux, float u1);
 // PAVMM::sample (PAVMM.h:737-806)
 __device__ V3 mixture_sample(const Lobe &L, int K, float ux, float uy, int lane) {
   // per-vector sums of the weights
@@ -155,6 +191,11 @@ __device__ V3 mixture_sample(const Lobe &L, int K, float ux, float uy, int lane)
   int s = int(sv * kLanes + sc);
   float k = __shfl_sync(0xFFFFFFFFu, L.kappa, s), e2k = __shfl_sync(0xFFFFFFFFu, L.e2k, s);
   V3 mu = mk(__shfl_sync(0xFFFFFFFFu, L.mx, s), __shfl_sync(0xFFFFFFFFu, L.my, s), __shfl_sync(0xFFFFFFFFu, L.mz, s));
+  return lobe_direction(k, e2k, mu, ux, u1);
+}
+// A direction of the chosen lobe (kappa k, e^{-2k}, mean mu) from the
+// rescaled uniform u1 and ux (PAVMM.h:779-806)
+__device__ V3 lobe_direction(float k, float e2k, V3 mu, float ux, float u1) {
   V3 d;
   if (k == 0.0f) {
     float z = 1.0f - 2.0f * u1;
@@ -291,6 +332,203 @@ __device__ void dqt_query_out(const FieldView &f, uint32_t reg, uint32_t leaf, f
   o.pdfLi = dqt_pdf(N, d);
 }
 
+// ---------------------------------------------------------------- four queries per warp
+// A group of eight lanes per query: lane j of a group holds lobes j, j + 8,
+// j + 16 and j + 24 (the vfloat8 lane j of each lobe vector), so the sums over
+// the mixture keep the warp-per-query order (per lane over the vectors, then
+// the 8-lane tree) and mixtures of up to eight lobes keep every lane busy.
+// Shuffles stay inside the group (width 8, the group's lane mask): groups of
+// one warp may take different paths.
+struct LobeSet {
+  Lobe l[4];
+};
+__device__ __forceinline__ float group_sum(const float v[4], int cnt, unsigned gm) {
+  float acc = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (q < cnt) acc += v[q];
+  acc += __shfl_xor_sync(gm, acc, 1, 8);
+  acc += __shfl_xor_sync(gm, acc, 2, 8);
+  acc += __shfl_xor_sync(gm, acc, 4, 8);
+  return __shfl_sync(gm, acc, 0, 8);
+}
+__device__ __forceinline__ Lobe pick(const LobeSet &L, uint32_t q) {  // q uniform in the group
+  Lobe r = L.l[0];
+  if (q == 1) r = L.l[1];
+  if (q == 2) r = L.l[2];
+  if (q == 3) r = L.l[3];
+  return r;
+}
+__device__ __forceinline__ LobeSet load_shifted_g(const VMMState &v, int j, float p0, float p1, float p2,
+                                                  bool parallax) {
+  LobeSet L;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) L.l[q] = load_shifted(v, q * kLanes + j, p0, p1, p2, parallax);
+  return L;
+}
+__device__ __forceinline__ LobeSet product_lobe_g(const LobeSet &L, V3 n, float kappa, float normalization,
+                                                  float weight, int cnt, unsigned gm) {
+  LobeSet R;
+  float w[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    R.l[q] = product_terms(L.l[q], n, kappa, normalization, weight);
+    w[q] = R.l[q].w;
+  }
+  const float integral = group_sum(w, cnt, gm);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) R.l[q].w /= integral;
+  return R;
+}
+__device__ __forceinline__ float mixture_pdf_g(const LobeSet &L, V3 d, int cnt, unsigned gm) {
+  float t[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) t[q] = q < cnt ? mixture_term(L.l[q], d) : 0.0f;
+  return group_sum(t, cnt, gm);
+}
+// PAVMM::sample (PAVMM.h:737-806) by a group
+__device__ V3 mixture_sample_g(const LobeSet &L, int K, float ux, float uy, unsigned gm) {
+  float vecSum[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float g = L.l[q].w;
+    g += __shfl_xor_sync(gm, g, 1, 8);
+    g += __shfl_xor_sync(gm, g, 2, 8);
+    g += __shfl_xor_sync(gm, g, 4, 8);
+    vecSum[q] = __shfl_sync(gm, g, 0, 8);
+  }
+  uint32_t sv = 0, sc = 0;
+  float searched = uy, sumW = 0.0f, cdf = 0.0f;
+  uint32_t quot = uint32_t((K - 1) / kLanes), rem = uint32_t((K - 1) % kLanes);
+  for (;;) {
+    cdf = sv == 0 ? vecSum[0] : sv == 1 ? vecSum[1] : sv == 2 ? vecSum[2] : vecSum[3];
+    if (sumW + cdf >= searched || sv + 1 >= quot + 1) break;
+    sumW += cdf;
+    sv++;
+  }
+  const Lobe V = pick(L, sv);
+  uint32_t maxSel = (sv == quot) ? rem + 1 : kLanes;
+  for (;;) {
+    cdf = __shfl_sync(gm, V.w, int(sc), 8);
+    if (sumW + cdf >= searched || sc + 1 >= maxSel) break;
+    sumW += cdf;
+    sc++;
+  }
+  float u1 = smin(1.0f - FLT_EPSILON, (searched - sumW) / cdf);
+  const int s = int(sc);
+  float k = __shfl_sync(gm, V.kappa, s, 8), e2k = __shfl_sync(gm, V.e2k, s, 8);
+  V3 mu = mk(__shfl_sync(gm, V.mx, s, 8), __shfl_sync(gm, V.my, s, 8), __shfl_sync(gm, V.mz, s, 8));
+  return lobe_direction(k, e2k, mu, ux, u1);
+}
+// choose_region by a group: lane j ranks neighbour j
+__device__ uint32_t choose_region_g(const FieldView &f, uint32_t leaf, float p0, float p1, float p2, float &s1d,
+                                    int j, int lane, unsigned gm) {
+  const Neighbours &nb = f.nbrs[leaf];
+  uint32_t size = min(4u, nb.size);
+  uint32_t sel = uint32_t(s1d * float(size));
+  s1d = (s1d - float(sel) / float(size)) * float(size);
+  sel = min(sel, size - 1);
+  V3 d = mk(nb.px[j] - p0, nb.py[j] - p1, nb.pz[j] - p2);
+  float dd = dot(d, d);
+  uint32_t key = (f2u(dd) & ~7u) | uint32_t(j);
+  if (nb.ids[j] == ~0u) key = f2u(INFINITY);
+  uint32_t rank = 0;
+  for (int jj = 0; jj < 8; ++jj) {
+    uint32_t kj = __shfl_sync(gm, key, jj, 8);
+    rank += (u2f(kj) < u2f(key)) ? 1u : 0u;
+  }
+  const uint32_t hit = (__ballot_sync(gm, rank == sel && key != f2u(INFINITY)) >> (lane & 24)) & 0xFFu;
+  int src = __ffs(hit) - 1;
+  uint32_t chosenKey = __shfl_sync(gm, key, src < 0 ? 0 : src, 8);
+  return nb.ids[chosenKey & 7u];
+}
+
+// Batched guided queries without the Henyey-Greenstein product, four per
+// warp: Init + optional cosine product + SamplePDF (+ pdfLi).
+__global__ void query_g_kernel(QueryParams P, const QueryIn *in, QueryOut *out, uint32_t n) {
+  const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const int lane = threadIdx.x & 31, j = lane & 7;
+  const unsigned gm = 0xFFu << (lane & 24);
+  if (gid >= n) return;
+  const QueryIn q = in[gid];
+  const FieldView &f = P.f;
+  QueryOut o;
+  o.ok = 0; o.id = 0; o.s1d = q.s1d; o.dx = o.dy = o.dz = 0.0f; o.pdf = 0.0f; o.pdfLi = 0.0f;
+  bool inside = f.iteration > 0 && q.px >= f.bounds[0] && q.px <= f.bounds[3] && q.py >= f.bounds[1] &&
+                q.py <= f.bounds[4] && q.pz >= f.bounds[2] && q.pz <= f.bounds[5];
+  if (inside) {
+    uint32_t leaf = kd_leaf(f, q.px, q.py, q.pz);
+    uint32_t reg = leaf;
+    float s1d = q.s1d;
+    if (f.knn && s1d >= 0.f) reg = choose_region_g(f, leaf, q.px, q.py, q.pz, s1d, j, lane, gm);
+    o.s1d = s1d;
+    const RegionDir &R = f.regions[reg];
+    if (R.valid) {
+      const int K = int(R.vmm.K), cnt = vec_count(K);
+      const LobeSet li = load_shifted_g(R.vmm, j, q.px, q.py, q.pz, f.parallax != 0);
+      V3 d;
+      if (P.cosine) {
+        const LobeSet g = product_lobe_g(li, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, 1.0f, cnt, gm);
+        d = mixture_sample_g(g, K, (q.ux - 0.0f) / 1.0f, q.uy, gm);
+        o.pdf = 0.0f + 1.0f * mixture_pdf_g(g, d, cnt, gm);
+      } else {
+        d = mixture_sample_g(li, K, (q.ux - 0.0f) / 1.0f, q.uy, gm);
+        o.pdf = 0.0f + 1.0f * mixture_pdf_g(li, d, cnt, gm);
+      }
+      o.ok = 1;
+      o.id = leaf;
+      o.dx = d.x; o.dy = d.y; o.dz = d.z;
+      o.pdfLi = mixture_pdf_g(li, d, cnt, gm);
+    }
+  }
+  if (j == 0) out[gid] = o;
+}
+// Batched path-vertex query, four per warp: Init + cosine product once, then
+// one SamplePDF per 2D random number on the same distribution (the sampled
+// distribution is not changed by sampling: VMMSurfaceSamplingDistribution.h:67-103),
+// as a renderer does per vertex and openpgl_bench's lookup loop does per
+// initialised distribution (openpgl_bench.cpp:343-362).
+__global__ void query_s4_g_kernel(QueryParams P, const QueryInS4 *in, QueryOutS4 *out, uint32_t n) {
+  const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const int lane = threadIdx.x & 31, j = lane & 7;
+  const unsigned gm = 0xFFu << (lane & 24);
+  if (gid >= n) return;
+  const QueryInS4 q = in[gid];
+  const FieldView &f = P.f;
+  QueryOutS4 o;
+  o.ok = 0;
+  o.id = 0;
+  o.s1d = q.s1d;
+#pragma unroll
+  for (int k = 0; k < kVertexSamples; ++k) o.s[k][0] = o.s[k][1] = o.s[k][2] = o.s[k][3] = 0.0f;
+  bool inside = f.iteration > 0 && q.px >= f.bounds[0] && q.px <= f.bounds[3] && q.py >= f.bounds[1] &&
+                q.py <= f.bounds[4] && q.pz >= f.bounds[2] && q.pz <= f.bounds[5];
+  if (inside) {
+    uint32_t leaf = kd_leaf(f, q.px, q.py, q.pz);
+    uint32_t reg = leaf;
+    float s1d = q.s1d;
+    if (f.knn && s1d >= 0.f) reg = choose_region_g(f, leaf, q.px, q.py, q.pz, s1d, j, lane, gm);
+    o.s1d = s1d;
+    const RegionDir &R = f.regions[reg];
+    if (R.valid) {
+      const int K = int(R.vmm.K), cnt = vec_count(K);
+      LobeSet g = load_shifted_g(R.vmm, j, q.px, q.py, q.pz, f.parallax != 0);
+      if (P.cosine) g = product_lobe_g(g, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, 1.0f, cnt, gm);
+#pragma unroll
+      for (int k = 0; k < kVertexSamples; ++k) {
+        const V3 d = mixture_sample_g(g, K, (q.u[k][0] - 0.0f) / 1.0f, q.u[k][1], gm);
+        o.s[k][0] = d.x;
+        o.s[k][1] = d.y;
+        o.s[k][2] = d.z;
+        o.s[k][3] = 0.0f + 1.0f * mixture_pdf_g(g, d, cnt, gm);
+      }
+      o.ok = 1;
+      o.id = leaf;
+    }
+  }
+  if (j == 0) out[gid] = o;
+}
+
 // Batched guided query: Init + optional cosine product (surface) or
 // Henyey-Greenstein product (volume) + SamplePDF (+ pdfLi).
 __global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, uint32_t n) {
@@ -339,16 +577,31 @@ __global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, ui
   if (lane == 0) out[gw] = o;
 }
 
-// Batched path-vertex query: Init + cosine product once, then one SamplePDF
-// per 2D random number on the same distribution (the sampled distribution
-// is not changed by sampling: VMMSurfaceSamplingDistribution.h:67-103), as a
-// renderer does per vertex and openpgl_bench's lookup loop does per
-// initialised distribution (openpgl_bench.cpp:343-362).
-__global__ void query_s4_kernel(QueryParams P, const QueryInS4 *in, QueryOutS4 *out, uint32_t n) {
-  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (gw >= n) return;
-  const QueryInS4 q = in[gw];
+// Batched guided queries on a quadtree field: a thread per query (a
+// quadtree's descent has no lobes to spread over a warp).
+__global__ void query_dqt_kernel(QueryParams P, const QueryIn *in, QueryOut *out, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const QueryIn q = in[i];
+  const FieldView &f = P.f;
+  QueryOut o;
+  o.ok = 0; o.id = 0; o.s1d = q.s1d; o.dx = o.dy = o.dz = 0.0f; o.pdf = 0.0f; o.pdfLi = 0.0f;
+  const bool inside = f.iteration > 0 && q.px >= f.bounds[0] && q.px <= f.bounds[3] && q.py >= f.bounds[1] &&
+                      q.py <= f.bounds[4] && q.pz >= f.bounds[2] && q.pz <= f.bounds[5];
+  if (inside) {
+    const uint32_t leaf = kd_leaf(f, q.px, q.py, q.pz);
+    uint32_t reg = leaf;
+    float s1d = q.s1d;
+    if (f.knn && s1d >= 0.f) reg = choose_region_1(f, leaf, q.px, q.py, q.pz, s1d);
+    o.s1d = s1d;
+    dqt_query_out(f, reg, leaf, q.ux, q.uy, o);
+  }
+  out[i] = o;
+}
+__global__ void query_s4_dqt_kernel(QueryParams P, const QueryInS4 *in, QueryOutS4 *out, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const QueryInS4 q = in[i];
   const FieldView &f = P.f;
   QueryOutS4 o;
   o.ok = 0;
@@ -356,49 +609,28 @@ __global__ void query_s4_kernel(QueryParams P, const QueryInS4 *in, QueryOutS4 *
   o.s1d = q.s1d;
 #pragma unroll
   for (int k = 0; k < kVertexSamples; ++k) o.s[k][0] = o.s[k][1] = o.s[k][2] = o.s[k][3] = 0.0f;
-  bool inside = f.iteration > 0 && q.px >= f.bounds[0] && q.px <= f.bounds[3] && q.py >= f.bounds[1] &&
-                q.py <= f.bounds[4] && q.pz >= f.bounds[2] && q.pz <= f.bounds[5];
+  const bool inside = f.iteration > 0 && q.px >= f.bounds[0] && q.px <= f.bounds[3] && q.py >= f.bounds[1] &&
+                      q.py <= f.bounds[4] && q.pz >= f.bounds[2] && q.pz <= f.bounds[5];
   if (inside) {
-    uint32_t leaf = kd_leaf(f, q.px, q.py, q.pz);
+    const uint32_t leaf = kd_leaf(f, q.px, q.py, q.pz);
     uint32_t reg = leaf;
     float s1d = q.s1d;
-    if (f.knn && s1d >= 0.f) reg = choose_region(f, leaf, q.px, q.py, q.pz, s1d, lane);
+    if (f.knn && s1d >= 0.f) reg = choose_region_1(f, leaf, q.px, q.py, q.pz, s1d);
     o.s1d = s1d;
-    const RegionDir &R = f.regions[reg];
-    if (f.dqt) {  // a quadtree region: four samples of its quadtree (no cosine product)
-      if (f.dqtHeads[reg].valid) {
-        const DqtNode *N = f.dqtNodes + size_t(reg) * f.dqtStride;
-        if (lane == 0)
-          for (int k = 0; k < kVertexSamples; ++k) {
-            V3 d;
-            o.s[k][3] = dqt_sample_pdf(N, q.u[k][0], q.u[k][1], d);
-            o.s[k][0] = d.x;
-            o.s[k][1] = d.y;
-            o.s[k][2] = d.z;
-          }
-        o.ok = 1;
-        o.id = leaf;
-      }
-    } else if (R.valid) {
-      const int K = int(R.vmm.K), cnt = vec_count(K);
-      Lobe g = load_shifted(R.vmm, lane, q.px, q.py, q.pz, f.parallax != 0);
-      if (P.cosine) {
-        float integral;
-        g = product_lobe(g, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, 1.0f, cnt, lane, integral);
-      }
-#pragma unroll
+    if (f.dqtHeads[reg].valid) {
+      const DqtNode *N = f.dqtNodes + size_t(reg) * f.dqtStride;
       for (int k = 0; k < kVertexSamples; ++k) {
-        const V3 d = mixture_sample(g, K, (q.u[k][0] - 0.0f) / 1.0f, q.u[k][1], lane);
+        V3 d;
+        o.s[k][3] = dqt_sample_pdf(N, q.u[k][0], q.u[k][1], d);
         o.s[k][0] = d.x;
         o.s[k][1] = d.y;
         o.s[k][2] = d.z;
-        o.s[k][3] = 0.0f + 1.0f * mixture_pdf(g, d, cnt, lane);
       }
       o.ok = 1;
       o.id = leaf;
     }
   }
-  if (lane == 0) out[gw] = o;
+  out[i] = o;
 }
 
 // ---------------------------------------------------------------- per-object path
@@ -524,9 +756,17 @@ cudaError_t query_upload_tables(const LibmTables &libm) {
 cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out, uint32_t n, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   const unsigned threads = 256;
+  count_launch();
+  if (p.f.dqt) {
+    query_dqt_kernel<<<unsigned((uint64_t(n) + threads - 1) / threads), threads, 0, s>>>(p, in, out, n);
+    return cudaGetLastError();
+  }
+  if (!p.hgMeanCosine) {  // four queries per warp
+    query_g_kernel<<<unsigned((uint64_t(n) * 8 + threads - 1) / threads), threads, 0, s>>>(p, in, out, n);
+    return cudaGetLastError();
+  }
   const uint64_t warps = n;
   unsigned blocks = unsigned((warps * 32 + threads - 1) / threads);
-  count_launch();
   query_kernel<<<blocks, threads, 0, s>>>(p, in, out, n);
   return cudaGetLastError();
 }
@@ -534,9 +774,12 @@ cudaError_t launch_query_s4(const QueryParams &p, const QueryInS4 *in, QueryOutS
                             cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   const unsigned threads = 256;
-  unsigned blocks = unsigned((uint64_t(n) * 32 + threads - 1) / threads);
   count_launch();
-  query_s4_kernel<<<blocks, threads, 0, s>>>(p, in, out, n);
+  if (p.f.dqt) {
+    query_s4_dqt_kernel<<<unsigned((uint64_t(n) + threads - 1) / threads), threads, 0, s>>>(p, in, out, n);
+    return cudaGetLastError();
+  }
+  query_s4_g_kernel<<<unsigned((uint64_t(n) * 8 + threads - 1) / threads), threads, 0, s>>>(p, in, out, n);
   return cudaGetLastError();
 }
 cudaError_t launch_ssd_init(const FieldView &f, float px, float py, float pz, float s1d, SSDState *st, SSDResult *res,

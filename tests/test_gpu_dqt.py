@@ -136,3 +136,32 @@ def test_quadtree_file_round_trip_and_per_object_api(pgl, tmp_path):
         n += 1
     assert n > 10
     ssd.release()
+
+
+def test_quadtree_vertices_match_single_queries_and_oracle(pgl):
+    """Path vertices on a quadtree field (four SamplePDF calls per Init): call
+    k equals the oracle's single guided query with the k-th 2D random number
+    and the GPU's own single-sample batch bit for bit."""
+    import pyoracle
+    from openpgl_gb300 import synthetic as syn
+
+    frames = [syn.cluster_samples(1 << 18, 730 + i) for i in range(2)]
+    dev, field = _train(pgl, frames, 8000)
+    orc = pyoracle.OracleField(8000, deterministic=True, threads=os.cpu_count() or 4, dqt=True)
+    for f in frames:
+        orc.update(f)
+    v = syn.vertices(1 << 15, 731)
+    out = field.sample_vertices(v)
+    assert out["ok"].sum() > len(v) // 2
+    for k in range(4):
+        q = syn.vertex_queries(v, k)
+        got = np.zeros(len(v), dtype=pgl.QUERY_RESULT_DTYPE)
+        got["ok"], got["id"], got["sample1d"] = out["ok"], out["id"], out["sample1d"]
+        got["dir"], got["pdf"] = out["sample"][:, k, :3], out["sample"][:, k, 3]
+        r = compare_queries(got, orc.query(q))
+        assert r["ok_equal"] and r["id_equal"] and r["sample1d_equal"], (k, r)
+        assert r["worst_pdf_rel"] <= TOL and r["worst_dir"] <= 1e-3, (k, r)
+        one = field.sample_batch(q)
+        ok = one["ok"] == 1
+        assert np.array_equal(one["pdf"][ok].view(np.uint32), got["pdf"][ok].view(np.uint32)), k
+        assert np.array_equal(one["dir"][ok].view(np.uint32), got["dir"][ok].view(np.uint32)), k
