@@ -1025,7 +1025,7 @@ def run_gpu(args, rank, world, local_rank):
     sm_mhz = clk.get("sm_mhz") or measured_peak("sm_max_mhz", 2070.0)[0]
     roofline = em_roofline(em_work, sm_mhz, ms)
     query_roof = kernel_roofline(query_work["flop"], query_work["sfu"], query_work["bytes"], q_ms, sm_mhz)
-    query_roof.update(kernel="query_kernel", mean_lobes=query_work["mean_lobes"],
+    query_roof.update(kernel="query_g_kernel", mean_lobes=query_work["mean_lobes"],
                       work="per query with K lobes and one SamplePDF: 62K + (50 + 12K) + 64 flop, "
                            "7K + (6 + K) SFU, 36 B in + 32 B out")
     out = {

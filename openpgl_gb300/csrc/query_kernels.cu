@@ -359,11 +359,13 @@ __device__ __forceinline__ Lobe pick(const LobeSet &L, uint32_t q) {  // q unifo
   if (q == 3) r = L.l[3];
   return r;
 }
+// the lobe vectors q < cnt of the mixture (the others are never read)
 __device__ __forceinline__ LobeSet load_shifted_g(const VMMState &v, int j, float p0, float p1, float p2,
-                                                  bool parallax) {
+                                                  bool parallax, int cnt) {
   LobeSet L;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) L.l[q] = load_shifted(v, q * kLanes + j, p0, p1, p2, parallax);
+  for (int q = 0; q < 4; ++q)
+    if (q < cnt) L.l[q] = load_shifted(v, q * kLanes + j, p0, p1, p2, parallax);
   return L;
 }
 __device__ __forceinline__ LobeSet product_lobe_g(const LobeSet &L, V3 n, float kappa, float normalization,
@@ -372,12 +374,13 @@ __device__ __forceinline__ LobeSet product_lobe_g(const LobeSet &L, V3 n, float 
   float w[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    R.l[q] = product_terms(L.l[q], n, kappa, normalization, weight);
-    w[q] = R.l[q].w;
+    if (q < cnt) R.l[q] = product_terms(L.l[q], n, kappa, normalization, weight);
+    w[q] = q < cnt ? R.l[q].w : 0.0f;
   }
   const float integral = group_sum(w, cnt, gm);
 #pragma unroll
-  for (int q = 0; q < 4; ++q) R.l[q].w /= integral;
+  for (int q = 0; q < 4; ++q)
+    if (q < cnt) R.l[q].w /= integral;
   return R;
 }
 __device__ __forceinline__ float mixture_pdf_g(const LobeSet &L, V3 d, int cnt, unsigned gm) {
@@ -388,14 +391,19 @@ __device__ __forceinline__ float mixture_pdf_g(const LobeSet &L, V3 d, int cnt, 
 }
 // PAVMM::sample (PAVMM.h:737-806) by a group
 __device__ V3 mixture_sample_g(const LobeSet &L, int K, float ux, float uy, unsigned gm) {
+  // per-vector sums of the weights (vectors past the mixture's last are never searched)
+  const int cnt = vec_count(K);
   float vecSum[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    float g = L.l[q].w;
-    g += __shfl_xor_sync(gm, g, 1, 8);
-    g += __shfl_xor_sync(gm, g, 2, 8);
-    g += __shfl_xor_sync(gm, g, 4, 8);
-    vecSum[q] = __shfl_sync(gm, g, 0, 8);
+    float g = q < cnt ? L.l[q].w : 0.0f;
+    if (q < cnt) {
+      g += __shfl_xor_sync(gm, g, 1, 8);
+      g += __shfl_xor_sync(gm, g, 2, 8);
+      g += __shfl_xor_sync(gm, g, 4, 8);
+      g = __shfl_sync(gm, g, 0, 8);
+    }
+    vecSum[q] = g;
   }
   uint32_t sv = 0, sc = 0;
   float searched = uy, sumW = 0.0f, cdf = 0.0f;
@@ -443,8 +451,45 @@ __device__ uint32_t choose_region_g(const FieldView &f, uint32_t leaf, float p0,
   return nb.ids[chosenKey & 7u];
 }
 
-// Batched guided queries without the Henyey-Greenstein product, four per
-// warp: Init + optional cosine product + SamplePDF (+ pdfLi).
+// Batched volume guided queries with the Henyey-Greenstein product, a warp
+// per query: Init + product with the phase function's fit + SamplePDF (+
+// pdfLi).  The three products of a mixture need three times the registers
+// of the cosine product, so a lane keeps one lobe here.
+__global__ void query_hg_kernel(QueryParams P, const QueryIn *in, QueryOut *out, uint32_t n) {
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= n) return;
+  const QueryIn q = in[gw];
+  const FieldView &f = P.f;
+  QueryOut o;
+  o.ok = 0; o.id = 0; o.s1d = q.s1d; o.dx = o.dy = o.dz = 0.0f; o.pdf = 0.0f; o.pdfLi = 0.0f;
+  bool inside = f.iteration > 0 && q.px >= f.bounds[0] && q.px <= f.bounds[3] && q.py >= f.bounds[1] &&
+                q.py <= f.bounds[4] && q.pz >= f.bounds[2] && q.pz <= f.bounds[5];
+  if (inside) {
+    uint32_t leaf = kd_leaf(f, q.px, q.py, q.pz);
+    uint32_t reg = leaf;
+    float s1d = q.s1d;
+    if (f.knn && s1d >= 0.f) reg = choose_region(f, leaf, q.px, q.py, q.pz, s1d, lane);
+    o.s1d = s1d;
+    const RegionDir &R = f.regions[reg];
+    if (R.valid) {
+      const int K = int(R.vmm.K), cnt = vec_count(K);
+      Lobe li = load_shifted(R.vmm, lane, q.px, q.py, q.pz, f.parallax != 0);
+      Lobe h[kHgLobes];
+      float w[kHgLobes];
+      hg_products(li, mk(q.nx, q.ny, q.nz), P.hgMeanCosine[gw], cnt, lane, h, w);
+      const V3 d = products_sample(h, w, kHgLobes, K, q.ux, q.uy, lane, o.pdf);
+      o.ok = 1;
+      o.id = leaf;
+      o.dx = d.x; o.dy = d.y; o.dz = d.z;
+      o.pdfLi = mixture_pdf(li, d, cnt, lane);
+    }
+  }
+  if (lane == 0) out[gw] = o;
+}
+
+// Batched guided queries, four per warp: Init + optional cosine product
+// (surface) + SamplePDF (+ pdfLi).
 __global__ void query_g_kernel(QueryParams P, const QueryIn *in, QueryOut *out, uint32_t n) {
   const uint32_t gid = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
   const int lane = threadIdx.x & 31, j = lane & 7;
@@ -465,7 +510,7 @@ __global__ void query_g_kernel(QueryParams P, const QueryIn *in, QueryOut *out, 
     const RegionDir &R = f.regions[reg];
     if (R.valid) {
       const int K = int(R.vmm.K), cnt = vec_count(K);
-      const LobeSet li = load_shifted_g(R.vmm, j, q.px, q.py, q.pz, f.parallax != 0);
+      const LobeSet li = load_shifted_g(R.vmm, j, q.px, q.py, q.pz, f.parallax != 0, cnt);
       V3 d;
       if (P.cosine) {
         const LobeSet g = product_lobe_g(li, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, 1.0f, cnt, gm);
@@ -512,7 +557,7 @@ __global__ void query_s4_g_kernel(QueryParams P, const QueryInS4 *in, QueryOutS4
     const RegionDir &R = f.regions[reg];
     if (R.valid) {
       const int K = int(R.vmm.K), cnt = vec_count(K);
-      LobeSet g = load_shifted_g(R.vmm, j, q.px, q.py, q.pz, f.parallax != 0);
+      LobeSet g = load_shifted_g(R.vmm, j, q.px, q.py, q.pz, f.parallax != 0, cnt);
       if (P.cosine) g = product_lobe_g(g, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, 1.0f, cnt, gm);
 #pragma unroll
       for (int k = 0; k < kVertexSamples; ++k) {
@@ -529,53 +574,6 @@ __global__ void query_s4_g_kernel(QueryParams P, const QueryInS4 *in, QueryOutS4
   if (j == 0) out[gid] = o;
 }
 
-// Batched guided query: Init + optional cosine product (surface) or
-// Henyey-Greenstein product (volume) + SamplePDF (+ pdfLi).
-__global__ void query_kernel(QueryParams P, const QueryIn *in, QueryOut *out, uint32_t n) {
-  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (gw >= n) return;
-  const QueryIn q = in[gw];
-  const FieldView &f = P.f;
-  QueryOut o;
-  o.ok = 0; o.id = 0; o.s1d = q.s1d; o.dx = o.dy = o.dz = 0.0f; o.pdf = 0.0f; o.pdfLi = 0.0f;
-  bool inside = f.iteration > 0 && q.px >= f.bounds[0] && q.px <= f.bounds[3] && q.py >= f.bounds[1] &&
-                q.py <= f.bounds[4] && q.pz >= f.bounds[2] && q.pz <= f.bounds[5];
-  if (inside) {
-    uint32_t leaf = kd_leaf(f, q.px, q.py, q.pz);
-    uint32_t reg = leaf;
-    float s1d = q.s1d;
-    if (f.knn && s1d >= 0.f) reg = choose_region(f, leaf, q.px, q.py, q.pz, s1d, lane);
-    o.s1d = s1d;
-    const RegionDir &R = f.regions[reg];
-    if (f.dqt) {
-      if (lane == 0) dqt_query_out(f, reg, leaf, q.ux, q.uy, o);
-    } else if (R.valid) {
-      const int K = int(R.vmm.K), cnt = vec_count(K);
-      Lobe li = load_shifted(R.vmm, lane, q.px, q.py, q.pz, f.parallax != 0);
-      V3 d;
-      if (P.hgMeanCosine) {
-        Lobe h[kHgLobes];
-        float w[kHgLobes];
-        hg_products(li, mk(q.nx, q.ny, q.nz), P.hgMeanCosine[gw], cnt, lane, h, w);
-        d = products_sample(h, w, kHgLobes, K, q.ux, q.uy, lane, o.pdf);
-      } else {
-        Lobe g = li;
-        if (P.cosine) {
-          float integral;
-          g = product_lobe(li, mk(q.nx, q.ny, q.nz), P.cosKappa, P.cosNorm, 1.0f, cnt, lane, integral);
-        }
-        d = mixture_sample(g, K, (q.ux - 0.0f) / 1.0f, q.uy, lane);
-        o.pdf = 0.0f + 1.0f * mixture_pdf(g, d, cnt, lane);
-      }
-      o.ok = 1;
-      o.id = leaf;
-      o.dx = d.x; o.dy = d.y; o.dz = d.z;
-      o.pdfLi = mixture_pdf(li, d, cnt, lane);
-    }
-  }
-  if (lane == 0) out[gw] = o;
-}
 
 // Batched guided queries on a quadtree field: a thread per query (a
 // quadtree's descent has no lobes to spread over a warp).
@@ -761,13 +759,11 @@ cudaError_t launch_query(const QueryParams &p, const QueryIn *in, QueryOut *out,
     query_dqt_kernel<<<unsigned((uint64_t(n) + threads - 1) / threads), threads, 0, s>>>(p, in, out, n);
     return cudaGetLastError();
   }
-  if (!p.hgMeanCosine) {  // four queries per warp
-    query_g_kernel<<<unsigned((uint64_t(n) * 8 + threads - 1) / threads), threads, 0, s>>>(p, in, out, n);
+  if (p.hgMeanCosine) {
+    query_hg_kernel<<<unsigned((uint64_t(n) * 32 + threads - 1) / threads), threads, 0, s>>>(p, in, out, n);
     return cudaGetLastError();
   }
-  const uint64_t warps = n;
-  unsigned blocks = unsigned((warps * 32 + threads - 1) / threads);
-  query_kernel<<<blocks, threads, 0, s>>>(p, in, out, n);
+  query_g_kernel<<<unsigned((uint64_t(n) * 8 + threads - 1) / threads), threads, 0, s>>>(p, in, out, n);
   return cudaGetLastError();
 }
 cudaError_t launch_query_s4(const QueryParams &p, const QueryInS4 *in, QueryOutS4 *out, uint32_t n,
