@@ -251,11 +251,21 @@ void Storage::flushIfPending() {
 }
 
 // Copies n host records to the device and splits them into the surface and
-// volume arrays.  Returns after the copy has completed (ingest_samples
-// synchronises), so the caller may reuse its buffer.
+// volume arrays.  Returns after the records have been read (ingest_samples
+// synchronises), so the caller may reuse its buffer.  Records in page-locked
+// host memory that the device addresses are read in place by the split
+// kernels over the host link; other host memory is staged by a copy.
 void Storage::ingest(const PGLSampleRecord *src, size_t count) {
   Context &c = Context::get();
   const uint32_t n = uint32_t(count);
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, src) == cudaSuccess && attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+    lastH2DBytes += uint64_t(n) * sizeof(PGLSampleRecord);
+    staging_.reserve(n);
+    ingestDevice(static_cast<const PGLSampleRecord *>(attr.devicePointer), count, staging_.p);
+    return;
+  }
+  (void)cudaGetLastError();  // an address unknown to CUDA is not an error here
   staging_.reserve(n);
   check(cudaMemcpyAsync(staging_.p, src, size_t(n) * sizeof(PGLSampleRecord), cudaMemcpyHostToDevice, c.stream),
         "H2D samples");
@@ -263,8 +273,9 @@ void Storage::ingest(const PGLSampleRecord *src, size_t count) {
   ingestDevice(staging_.p, count);
 }
 
-// Splits n device-resident records into the surface and volume arrays.
-void Storage::ingestDevice(const PGLSampleRecord *dsrc, size_t count) {
+// Splits n device-resident records (or host records the device addresses,
+// read once into `stage`) into the surface and volume arrays.
+void Storage::ingestDevice(const PGLSampleRecord *dsrc, size_t count, PGLSampleRecord *stage) {
   flushIfPending();
   Context &c = Context::get();
   const uint32_t n = uint32_t(count);
@@ -274,7 +285,7 @@ void Storage::ingestDevice(const PGLSampleRecord *dsrc, size_t count) {
   SoAView sv{surf.P.p, surf.D.p, surf.pdf.p, surf.flags.p, surf.n};
   SoAView vv{vol.P.p, vol.D.p, vol.pdf.p, vol.flags.p, vol.n};
   uint32_t numVol = 0;
-  check(ingest_samples(dsrc, n, scratch_, sv, vv, &numVol, c.stream), "ingest");
+  check(ingest_samples(dsrc, n, scratch_, sv, vv, &numVol, c.stream, stage), "ingest");
   vol.n += numVol;
   surf.n += n - numVol;
 }

@@ -70,7 +70,7 @@ class Storage {
   void add(const PGLSampleRecord *s, size_t n);
   void flush();
   void ingest(const PGLSampleRecord *src, size_t count);
-  void ingestDevice(const PGLSampleRecord *dsrc, size_t count);
+  void ingestDevice(const PGLSampleRecord *dsrc, size_t count, PGLSampleRecord *stage = nullptr);
   void flushIfPending();
   void reserve(size_t ns, size_t nv);
   void clearSurface() { flush(); surf.n = 0; }

@@ -72,9 +72,11 @@ cudaError_t em_bounded_wait_probe(unsigned long long limitNs, int *errOut, cudaS
 cudaError_t spatial_upload_tables(const LibmTables &libm);
 cudaError_t query_upload_tables(const LibmTables &libm);
 
-// ingest: AoS batch (device) -> surface / volume SoA, stable per class.
+// ingest: AoS batch (device, or host memory the device addresses when
+// `stage` is given: the records are then read once into stage) -> surface /
+// volume SoA, stable per class.
 cudaError_t ingest_samples(const PGLSampleRecord *in, uint32_t n, Scratch &scratch, SoAView surf, SoAView vol,
-                           uint32_t *numVolume, cudaStream_t s);
+                           uint32_t *numVolume, cudaStream_t s, PGLSampleRecord *stage = nullptr);
 cudaError_t export_samples(const float4 *P, const float4 *D, const float *pdf, const uint32_t *flags, uint64_t n,
                            PGLSampleRecord *out, cudaStream_t s);
 // min/max over positions [0, n) as order-preserving integers (6 x u32, device)

@@ -34,6 +34,16 @@ __global__ void ingest_flag_kernel(const PGLSampleRecord *in, uint32_t n, uint32
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) isVol[i] = (in[i].flags & 2u) ? 1u : 0u;
 }
+// The same for records in host memory: each record is read once over the
+// host link and kept in device memory for the scatter.
+__global__ void ingest_flag_stage_kernel(const PGLSampleRecord *in, uint32_t n, uint32_t *isVol,
+                                         PGLSampleRecord *stage) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PGLSampleRecord r = in[i];
+  stage[i] = r;
+  isVol[i] = (r.flags & 2u) ? 1u : 0u;
+}
 __global__ void ingest_scatter_kernel(const PGLSampleRecord *in, uint32_t n, const uint32_t *volRank,
                                       float4 *sP, float4 *sD, float *sPdf, uint32_t *sFlags, uint64_t sBase,
                                       float4 *vP, float4 *vD, float *vPdf, uint32_t *vFlags, uint64_t vBase) {
@@ -523,7 +533,7 @@ void scratch_free(Scratch &s) {
 static inline unsigned blocks_for(uint64_t n, unsigned t) { return unsigned((n + t - 1) / t); }
 
 cudaError_t ingest_samples(const PGLSampleRecord *in, uint32_t n, Scratch &scratch, SoAView surf, SoAView vol,
-                           uint32_t *numVolume, cudaStream_t s) {
+                           uint32_t *numVolume, cudaStream_t s, PGLSampleRecord *stage) {
   if (n == 0) { *numVolume = 0; return cudaSuccess; }
   size_t tempBytes = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, tempBytes, (uint32_t *)nullptr, (uint32_t *)nullptr, int(n), s);
@@ -535,7 +545,12 @@ cudaError_t ingest_samples(const PGLSampleRecord *in, uint32_t n, Scratch &scrat
   uint32_t *rank = isVol + (n + 1);
   void *temp = static_cast<char *>(scratch.ptr) + off;
   count_launch();
-  ingest_flag_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in, n, isVol);
+  if (stage) {
+    ingest_flag_stage_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in, n, isVol, stage);
+    in = stage;
+  } else {
+    ingest_flag_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in, n, isVol);
+  }
   cub::DeviceScan::ExclusiveSum(temp, tempBytes, isVol, rank, int(n), s);
   count_launch();
   ingest_scatter_kernel<<<blocks_for(n, 256), 256, 0, s>>>(in, n, rank, surf.P, surf.D, surf.pdf, surf.flags, surf.base,

@@ -118,3 +118,29 @@ def test_field_compare_detects_one_region(pgl, tmp_path):
     assert a.compare(a2) and a2.compare(a)
     for f in (a, b, a2):
         f.release()
+
+
+def test_page_locked_records_are_read_in_place():
+    """Records in page-locked host memory go to the device without a staging
+    copy (the split kernels read them over the host link): the storage and
+    the trained field equal those made from ordinary host memory."""
+    import torch
+
+    import openpgl_gb300 as pgl
+    from openpgl_gb300 import synthetic as syn
+
+    samples = syn.cube_face_samples(300000, 77, volume_fraction=0.3)
+    pinned = torch.empty(samples.nbytes, dtype=torch.uint8, pin_memory=True)
+    view = pinned.numpy().view(samples.dtype)
+    view[:] = samples
+    dev = pgl.Device()
+    a, b = pgl.SampleStorage(), pgl.SampleStorage()
+    a.add_samples(samples)
+    b.add_samples(view)
+    assert a.compare(b) and b.compare(a)
+    assert a.size_surface == b.size_surface and a.size_volume == b.size_volume
+    fa = pgl.Field(dev, pgl.FieldConfig(True, 8000))
+    fb = pgl.Field(dev, pgl.FieldConfig(True, 8000))
+    fa.update(a)
+    fb.update(b)
+    assert fa.field_bytes() == fb.field_bytes()
