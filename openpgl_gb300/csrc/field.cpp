@@ -987,7 +987,9 @@ void GpuField::runDqt(SubField *const *sides, int count) {
   std::vector<LeafTask> all;
   for (auto &k : keyed) all.push_back(k.second);
   const uint32_t T = uint32_t(all.size());
-  const int blocks = int(std::min<uint32_t>(std::max<uint32_t>(T, 1), uint32_t(2 * c.numSMs)));
+  // two blocks per SM, on the SMs the schedule leaves to the Update
+  const int sms = std::max(1, c.numSMs - std::max(0, tuning.reservedSMs));
+  const int blocks = int(std::min<uint32_t>(std::max<uint32_t>(T, 1), uint32_t(2 * sms)));
   cudaEvent_t emStart, emEnd;
   check(cudaEventCreate(&emStart), "event");
   check(cudaEventCreate(&emEnd), "event");

@@ -35,7 +35,6 @@ size_t GuidingServer::projectedBytes(size_t samples) const {
 GuidingServer::GuidingServer(GpuField *field, size_t budgetBytes, int reservedSMs)
     : field_(field), budget_(budgetBytes) {
   if (!field) throw std::runtime_error("null field");
-  if (field->surface.cfg.dqt) throw std::runtime_error("the guiding server serves mixture fields, not quadtree fields");
   Context &c = Context::get();
   // the field's EM launches leave these SMs to the query stream
   field_->tuning.reservedSMs = std::max(0, std::min(reservedSMs, c.numSMs - 1));
@@ -113,6 +112,17 @@ void GuidingServer::takeSnapshot(int slot) {
         v.nbrs = s.nbrs[k].p;
       } else {
         v.nbrs = nullptr;
+      }
+      if (f.cfg.dqt) {
+        const size_t nodes = R * size_t(f.dqtStride);
+        s.dqtHeads[k].reserve(R);
+        s.dqtNodes[k].reserve(nodes);
+        check(cudaMemcpyAsync(s.dqtHeads[k].p, f.dDqtHeads.p, R * sizeof(DqtHead), cudaMemcpyDeviceToDevice, st),
+              "snapshot quadtree heads");
+        check(cudaMemcpyAsync(s.dqtNodes[k].p, f.dDqtNodes.p, nodes * sizeof(DqtNode), cudaMemcpyDeviceToDevice, st),
+              "snapshot quadtrees");
+        v.dqtHeads = s.dqtHeads[k].p;
+        v.dqtNodes = s.dqtNodes[k].p;
       }
       check(cudaStreamSynchronize(st), "snapshot");
     } else {

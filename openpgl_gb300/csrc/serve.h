@@ -26,6 +26,8 @@ struct Snapshot {
   DevArray<RegionDir> regions[2];
   DevArray<KDNode> nodes[2];
   DevArray<Neighbours> nbrs[2];
+  DevArray<DqtHead> dqtHeads[2];  // quadtree fields: the regions' heads and trees
+  DevArray<DqtNode> dqtNodes[2];
   FieldView view[2];
   uint64_t version = 0;  // field updates folded in
   cudaEvent_t lastRead = nullptr;  // the last query launch that read it

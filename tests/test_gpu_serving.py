@@ -12,9 +12,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _trained(pgl, syn, seed, frames=1):
+def _trained(pgl, syn, seed, frames=1, dqt=False):
     dev = pgl.Device()
-    f = pgl.Field(dev, pgl.FieldConfig(True, 4000))
+    f = pgl.Field(dev, pgl.FieldConfig(True, 4000, dqt=dqt))
     st = pgl.SampleStorage()
     for k in range(frames):
         st.add_samples(syn.cube_face_samples(60000, seed + k, volume_fraction=0.25))
@@ -63,12 +63,16 @@ def test_results_alone_equal_results_in_the_mix():
     server.release()
 
 
-def test_queries_during_background_update_come_from_one_field_state():
+@pytest.mark.parametrize("dqt", [False, True])
+def test_queries_during_background_update_come_from_one_field_state(dqt):
+    """Queries served while the field trains in the background come from one
+    field state each (before or after the Update), for mixture fields and for
+    directional quadtree fields."""
     import openpgl_gb300 as pgl
     from openpgl_gb300 import synthetic as syn
 
-    dev, field = _trained(pgl, syn, 5100)
-    _, after = _trained(pgl, syn, 5100, frames=2)  # the same training plus the next frame
+    dev, field = _trained(pgl, syn, 5100, dqt=dqt)
+    _, after = _trained(pgl, syn, 5100, frames=2, dqt=dqt)  # the same training plus the next frame
     q = syn.queries(20000, 5200)
     expect = {field.iteration: field.sample_batch(q), after.iteration: after.sample_batch(q)}
     assert field.iteration + 1 == after.iteration
@@ -122,4 +126,43 @@ def test_vertices_in_the_mix_and_the_budget():
     server.add_samples(syn.cube_face_samples(20000, 5601, volume_fraction=0.25))
     server.wait_update(server.update())
     assert server.stats()["updates"] == 1
+    server.release()
+
+
+def test_quadtree_field_served_alone_equals_in_the_mix():
+    """A directional quadtree field behind the server: query and path-vertex
+    requests of mixed sizes from several threads give the direct calls'
+    bytes."""
+    import openpgl_gb300 as pgl
+    from openpgl_gb300 import synthetic as syn
+
+    dev, field = _trained(pgl, syn, 5300, frames=2, dqt=True)
+    rng = np.random.default_rng(11)
+    sizes = np.exp(rng.uniform(np.log(50), np.log(20000), size=12)).astype(int)
+    batches = [syn.queries(int(n), 5400 + i) for i, n in enumerate(sizes)]
+    verts = [syn.vertices(int(n), 5500 + i) for i, n in enumerate(sizes[:6])]
+    alone_q = [field.sample_batch(q) for q in batches]
+    alone_v = [field.sample_vertices(v) for v in verts]
+    server = pgl.GuidingServer(field, hbm_budget_bytes=256 << 20)
+    got_q, got_v = [None] * len(batches), [None] * len(verts)
+
+    def worker(k):
+        for i in range(k, len(batches), 3):
+            t, out = server.submit(batches[i])
+            server.wait(t)
+            got_q[i] = out
+        for i in range(k, len(verts), 3):
+            t, out = server.submit_vertices(verts[i])
+            server.wait(t)
+            got_v[i] = out
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(3)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    for a, b in zip(alone_q, got_q):
+        assert a.tobytes() == b.tobytes()
+    for a, b in zip(alone_v, got_v):
+        assert a.tobytes() == b.tobytes()
     server.release()
