@@ -491,10 +491,13 @@ class Field:
         self.lib.pglReleaseFieldStatistics(s)
         return text
 
-    def sample_batch(self, queries, volume=False, cosine=True):
-        """Guided queries (Init + cosine product + SamplePDF + pdfLi) in one launch."""
+    def sample_batch(self, queries, volume=False, cosine=True, out=None):
+        """Guided queries (Init + cosine product + SamplePDF + pdfLi) in one
+        launch; `out` (optional) receives the results."""
         q = np.ascontiguousarray(queries, dtype=PGL_QUERY_DTYPE)
-        out = np.zeros(len(q), dtype=QUERY_RESULT_DTYPE)
+        if out is None:
+            out = np.zeros(len(q), dtype=QUERY_RESULT_DTYPE)
+        assert out.dtype == QUERY_RESULT_DTYPE and len(out) == len(q) and out.flags.c_contiguous
         if volume:
             ok = self.lib.pglFieldSampleVolumeBatch(self.h, q.ctypes.data, len(q), out.ctypes.data)
         else:

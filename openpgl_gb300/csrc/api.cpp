@@ -740,18 +740,37 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHGDevice(PGLField field, co
   return true;
   PGL_CATCH(false)
 }
+// The device address of page-locked host memory, or null for memory the
+// device does not address (then the data is copied).
+static void *device_address(const void *host) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, host) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer)
+    return a.devicePointer;
+  (void)cudaGetLastError();
+  return nullptr;
+}
+// Queries and results in page-locked host memory are read and written in
+// place by the query kernel over the host link; others are copied.
 static bool sample_batch_host(PGLField field, bool volume, const PGLGuidedQuery *q, size_t n, PGLGuidedQueryResult *r,
                               bool cosine) {
   Context &c = Context::get();
   static thread_local DevArray<QueryIn> dq;
   static thread_local DevArray<QueryOut> dr;
-  dq.reserve(n);
-  dr.reserve(n);
-  check(cudaMemcpyAsync(dq.p, q, n * sizeof(QueryIn), cudaMemcpyHostToDevice, c.stream), "H2D queries");
-  if (!pglFieldSampleBatchDevice(field, volume, reinterpret_cast<const PGLGuidedQuery *>(dq.p), n,
-                                 reinterpret_cast<PGLGuidedQueryResult *>(dr.p), cosine, c.stream))
+  const void *qin = device_address(q);
+  void *rout = device_address(r);
+  if (!qin) {
+    dq.reserve(n);
+    check(cudaMemcpyAsync(dq.p, q, n * sizeof(QueryIn), cudaMemcpyHostToDevice, c.stream), "H2D queries");
+    qin = dq.p;
+  }
+  if (!rout) {
+    dr.reserve(n);
+    rout = dr.p;
+  }
+  if (!pglFieldSampleBatchDevice(field, volume, static_cast<const PGLGuidedQuery *>(qin), n,
+                                 static_cast<PGLGuidedQueryResult *>(rout), cosine, c.stream))
     return false;
-  check(cudaMemcpyAsync(r, dr.p, n * sizeof(QueryOut), cudaMemcpyDeviceToHost, c.stream), "D2H results");
+  if (rout == dr.p) check(cudaMemcpyAsync(r, dr.p, n * sizeof(QueryOut), cudaMemcpyDeviceToHost, c.stream), "D2H results");
   check(cudaStreamSynchronize(c.stream), "queries");
   return true;
 }
@@ -819,12 +838,22 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceVertices(PGLField field, const 
   if (n == 0) return true;
   static thread_local DevArray<QueryInS4> dv;
   static thread_local DevArray<QueryOutS4> dr;
-  dv.reserve(n);
-  dr.reserve(n);
-  check(cudaMemcpyAsync(dv.p, vertices, n * sizeof(QueryInS4), cudaMemcpyHostToDevice, c.stream), "H2D vertices");
-  launch_vertices(field, reinterpret_cast<const PGLGuidedVertex *>(dv.p), n,
-                  reinterpret_cast<PGLGuidedVertexResult *>(dr.p), c.stream);
-  check(cudaMemcpyAsync(results, dr.p, n * sizeof(QueryOutS4), cudaMemcpyDeviceToHost, c.stream), "D2H results");
+  // page-locked host buffers are read and written in place (as for queries)
+  const void *vin = device_address(vertices);
+  void *rout = device_address(results);
+  if (!vin) {
+    dv.reserve(n);
+    check(cudaMemcpyAsync(dv.p, vertices, n * sizeof(QueryInS4), cudaMemcpyHostToDevice, c.stream), "H2D vertices");
+    vin = dv.p;
+  }
+  if (!rout) {
+    dr.reserve(n);
+    rout = dr.p;
+  }
+  launch_vertices(field, static_cast<const PGLGuidedVertex *>(vin), n, static_cast<PGLGuidedVertexResult *>(rout),
+                  c.stream);
+  if (rout == dr.p)
+    check(cudaMemcpyAsync(results, dr.p, n * sizeof(QueryOutS4), cudaMemcpyDeviceToHost, c.stream), "D2H results");
   check(cudaStreamSynchronize(c.stream), "vertex queries");
   return true;
   PGL_CATCH(false)

@@ -144,3 +144,31 @@ def test_page_locked_records_are_read_in_place():
     fa.update(a)
     fb.update(b)
     assert fa.field_bytes() == fb.field_bytes()
+
+
+def test_page_locked_query_buffers_are_used_in_place():
+    """Guided queries and path vertices whose buffers are page-locked host
+    memory are read and written in place by the kernels: the same bytes as
+    with ordinary host memory."""
+    import torch
+
+    import openpgl_gb300 as pgl
+    from openpgl_gb300 import synthetic as syn
+
+    dev = pgl.Device()
+    field = pgl.Field(dev, pgl.FieldConfig(True, 8000))
+    st = pgl.SampleStorage()
+    st.add_samples(syn.cube_face_samples(200000, 81, volume_fraction=0.3))
+    field.update(st)
+    q = syn.queries(50000, 82)
+    qp = torch.from_numpy(q.view(np.uint8)).pin_memory().numpy().view(q.dtype)
+    rp = torch.empty(len(q) * 32, dtype=torch.uint8).pin_memory().numpy().view(pgl.QUERY_RESULT_DTYPE)
+    for vol in (False, True):
+        ref = field.sample_batch(q, volume=vol, cosine=not vol)
+        field.sample_batch(qp, volume=vol, cosine=not vol, out=rp)
+        assert rp.tobytes() == ref.tobytes()
+    v = syn.vertices(30000, 83)
+    vp = torch.from_numpy(v.view(np.uint8)).pin_memory().numpy().view(v.dtype)
+    ref = field.sample_vertices(v)
+    got = field.sample_vertices(vp)
+    assert got.tobytes() == ref.tobytes()
