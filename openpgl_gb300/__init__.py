@@ -704,10 +704,11 @@ class GuidingServer:
         _check(self.h, "pglNewGuidingServer")
         self._keep = {}
 
-    def submit(self, queries, volume=False, cosine=True):
+    def submit(self, queries, volume=False, cosine=True, out=None):
         """Queue a batch; returns (ticket, result array filled when done)."""
         q = np.ascontiguousarray(queries, dtype=PGL_QUERY_DTYPE)
-        out = np.zeros(len(q), dtype=QUERY_RESULT_DTYPE)
+        if out is None:
+            out = np.zeros(len(q), dtype=QUERY_RESULT_DTYPE)
         t = self.lib.pglGuidingServerSubmit(self.h, q.ctypes.data, len(q), out.ctypes.data, volume, cosine)
         _check(t != 0, "pglGuidingServerSubmit")
         self._keep[t] = (q, out)

@@ -740,15 +740,6 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHGDevice(PGLField field, co
   return true;
   PGL_CATCH(false)
 }
-// The device address of page-locked host memory, or null for memory the
-// device does not address (then the data is copied).
-static void *device_address(const void *host) {
-  cudaPointerAttributes a{};
-  if (cudaPointerGetAttributes(&a, host) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer)
-    return a.devicePointer;
-  (void)cudaGetLastError();
-  return nullptr;
-}
 // Queries and results in page-locked host memory are read and written in
 // place by the query kernel over the host link; others are copied.
 static bool sample_batch_host(PGLField field, bool volume, const PGLGuidedQuery *q, size_t n, PGLGuidedQueryResult *r,

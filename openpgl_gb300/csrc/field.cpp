@@ -250,6 +250,14 @@ void Storage::flushIfPending() {
   if (!pending_.empty()) flush();
 }
 
+void *device_address(const void *host) {
+  cudaPointerAttributes a{};
+  if (host && cudaPointerGetAttributes(&a, host) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer)
+    return a.devicePointer;
+  (void)cudaGetLastError();  // an address unknown to CUDA is not an error here
+  return nullptr;
+}
+
 // Copies n host records to the device and splits them into the surface and
 // volume arrays.  Returns after the records have been read (ingest_samples
 // synchronises), so the caller may reuse its buffer.  Records in page-locked
@@ -258,14 +266,12 @@ void Storage::flushIfPending() {
 void Storage::ingest(const PGLSampleRecord *src, size_t count) {
   Context &c = Context::get();
   const uint32_t n = uint32_t(count);
-  cudaPointerAttributes attr{};
-  if (cudaPointerGetAttributes(&attr, src) == cudaSuccess && attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+  if (const void *dsrc = device_address(src)) {
     lastH2DBytes += uint64_t(n) * sizeof(PGLSampleRecord);
     staging_.reserve(n);
-    ingestDevice(static_cast<const PGLSampleRecord *>(attr.devicePointer), count, staging_.p);
+    ingestDevice(static_cast<const PGLSampleRecord *>(dsrc), count, staging_.p);
     return;
   }
-  (void)cudaGetLastError();  // an address unknown to CUDA is not an error here
   staging_.reserve(n);
   check(cudaMemcpyAsync(staging_.p, src, size_t(n) * sizeof(PGLSampleRecord), cudaMemcpyHostToDevice, c.stream),
         "H2D samples");

@@ -64,6 +64,10 @@ struct SampleSide {
 // SampleDataStorage on the device (SampleDataStorage.h:18-324): surface and
 // volume samples as structure-of-arrays.  Samples added one by one are kept
 // in a host buffer and moved to the device in one copy when needed.
+// The device address of page-locked host memory that the device addresses
+// over the host link, or null (ordinary host memory: copy it).
+void *device_address(const void *host);
+
 class Storage {
  public:
   SampleSide surf, vol;

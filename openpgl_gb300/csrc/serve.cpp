@@ -139,6 +139,8 @@ uint64_t GuidingServer::submit(const QueryIn *in, QueryOut *out, size_t n, bool 
   r->kind = RequestKind::Query;
   r->in = in;
   r->out = out;
+  r->inDev = device_address(in);
+  r->outDev = r->inDev ? device_address(out) : nullptr;
   r->n = n;
   r->volume = volume;
   r->cosine = cosine && !volume;
@@ -168,6 +170,8 @@ uint64_t GuidingServer::submitVertices(const QueryInS4 *in, QueryOutS4 *out, siz
   r->kind = RequestKind::Vertex;
   r->in = in;
   r->out = out;
+  r->inDev = device_address(in);
+  r->outDev = r->inDev ? device_address(out) : nullptr;
   r->n = n;
   r->volume = false;
   r->cosine = true;
@@ -300,31 +304,43 @@ void GuidingServer::dispatch() {
 
     const size_t inBytes = kind == RequestKind::Vertex ? sizeof(QueryInS4) : sizeof(QueryIn);
     const size_t outBytes = kind == RequestKind::Vertex ? sizeof(QueryOutS4) : sizeof(QueryOut);
-    for (const Seg &g : slot.segs)
-      check(cudaMemcpyAsync(slot.dIn.p + g.pos * inBytes, static_cast<const unsigned char *>(g.r->in) + g.off * inBytes,
-                            g.cnt * inBytes, cudaMemcpyHostToDevice, slot.stream),
-            "H2D queries");
     QueryParams p{};
     p.f = view;
     p.cosKappa = 2.18853f;
     p.cosNorm = cosine_lobe_normalization();
     p.cosine = cosine ? 1 : 0;
-    if (kind == RequestKind::Vertex) {
-      p.samplesPerQuery = kVertexSamples;
-      check(launch_query_s4(p, reinterpret_cast<const QueryInS4 *>(slot.dIn.p),
-                            reinterpret_cast<QueryOutS4 *>(slot.dOut.p), uint32_t(total), slot.stream),
-            "vertex query launch");
+    p.samplesPerQuery = kind == RequestKind::Vertex ? kVertexSamples : 1;
+    auto launch = [&](const unsigned char *in, unsigned char *out, size_t n) {
+      if (kind == RequestKind::Vertex)
+        check(launch_query_s4(p, reinterpret_cast<const QueryInS4 *>(in), reinterpret_cast<QueryOutS4 *>(out),
+                              uint32_t(n), slot.stream),
+              "vertex query launch");
+      else
+        check(launch_query(p, reinterpret_cast<const QueryIn *>(in), reinterpret_cast<QueryOut *>(out), uint32_t(n),
+                           slot.stream),
+              "query launch");
+    };
+    // requests in page-locked host memory are read and written in place, a
+    // launch per piece; the others go through the slot's device buffers
+    bool inPlace = true;
+    for (const Seg &g : slot.segs) inPlace = inPlace && g.r->inDev && g.r->outDev;
+    if (inPlace) {
+      for (const Seg &g : slot.segs)
+        launch(static_cast<const unsigned char *>(g.r->inDev) + g.off * inBytes,
+               static_cast<unsigned char *>(g.r->outDev) + g.off * outBytes, g.cnt);
+      check(cudaEventRecord(snap_[snap].lastRead, slot.stream), "event");
     } else {
-      p.samplesPerQuery = 1;
-      check(launch_query(p, reinterpret_cast<const QueryIn *>(slot.dIn.p), reinterpret_cast<QueryOut *>(slot.dOut.p),
-                         uint32_t(total), slot.stream),
-            "query launch");
+      for (const Seg &g : slot.segs)
+        check(cudaMemcpyAsync(slot.dIn.p + g.pos * inBytes, static_cast<const unsigned char *>(g.r->in) + g.off * inBytes,
+                              g.cnt * inBytes, cudaMemcpyHostToDevice, slot.stream),
+              "H2D queries");
+      launch(slot.dIn.p, slot.dOut.p, total);
+      check(cudaEventRecord(snap_[snap].lastRead, slot.stream), "event");
+      for (const Seg &g : slot.segs)
+        check(cudaMemcpyAsync(static_cast<unsigned char *>(g.r->out) + g.off * outBytes, slot.dOut.p + g.pos * outBytes,
+                              g.cnt * outBytes, cudaMemcpyDeviceToHost, slot.stream),
+              "D2H results");
     }
-    check(cudaEventRecord(snap_[snap].lastRead, slot.stream), "event");
-    for (const Seg &g : slot.segs)
-      check(cudaMemcpyAsync(static_cast<unsigned char *>(g.r->out) + g.off * outBytes, slot.dOut.p + g.pos * outBytes,
-                            g.cnt * outBytes, cudaMemcpyDeviceToHost, slot.stream),
-            "D2H results");
     check(cudaEventRecord(slot.done, slot.stream), "event");
     slot.busy = true;
     slot.queries = total;

@@ -79,6 +79,8 @@ class GuidingServer {
     RequestKind kind;
     const void *in;
     void *out;
+    const void *inDev = nullptr;  // device addresses of page-locked request buffers (read and written in place)
+    void *outDev = nullptr;
     size_t n, sent = 0, done = 0;
     bool volume, cosine;
     int snap = -1;  // snapshot pinned at the first launch

@@ -166,3 +166,36 @@ def test_quadtree_field_served_alone_equals_in_the_mix():
     for a, b in zip(alone_v, got_v):
         assert a.tobytes() == b.tobytes()
     server.release()
+
+
+def test_page_locked_requests_are_served_in_place():
+    """Requests whose buffers are page-locked host memory are read and
+    written in place by the server's launches (no staging copies): the same
+    bytes as the direct calls, mixed with requests in ordinary memory."""
+    import torch
+
+    import openpgl_gb300 as pgl
+    from openpgl_gb300 import synthetic as syn
+
+    def pinned(a):
+        return torch.from_numpy(a.view(np.uint8)).pin_memory().numpy().view(a.dtype)
+
+    dev, field = _trained(pgl, syn, 5600, frames=2)
+    qs = [syn.queries(n, 5700 + i) for i, n in enumerate((2000, 30000, 500, 12000))]
+    vs = [syn.vertices(n, 5800 + i) for i, n in enumerate((4000, 25000))]
+    alone_q = [field.sample_batch(q) for q in qs]
+    alone_v = [field.sample_vertices(v) for v in vs]
+    server = pgl.GuidingServer(field, hbm_budget_bytes=256 << 20)
+    tickets = []
+    for i, q in enumerate(qs):
+        src = pinned(q) if i % 2 == 0 else q
+        out = pinned(np.zeros(len(q), dtype=pgl.QUERY_RESULT_DTYPE)) if i % 2 == 0 else None
+        tickets.append(("q", i, server.submit(src, out=out) if out is not None else server.submit(src)))
+    for i, v in enumerate(vs):
+        out = pinned(np.zeros(len(v), dtype=pgl.VERTEX_RESULT_DTYPE))
+        tickets.append(("v", i, server.submit_vertices(pinned(v), out=out)))
+    for kind, i, (t, out) in tickets:
+        server.wait(t)
+        ref = alone_q[i] if kind == "q" else alone_v[i]
+        assert out.tobytes() == ref.tobytes(), (kind, i)
+    server.release()
