@@ -55,8 +55,10 @@ typedef struct {
   } sample[4];
 } PGLGuidedVertexResult;
 
-// Guided queries on host buffers: copies the queries in, runs one kernel,
-// copies the results out.  Same results as the per-object calls.
+// Guided queries on host buffers: runs one kernel and returns with the
+// results written.  Page-locked buffers (cudaHostAlloc, cudaHostRegister) are
+// read and written in place by the kernel; other host memory is copied in
+// and out.  Same results as the per-object calls.
 OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceBatch(PGLField field, const PGLGuidedQuery *queries, size_t n,
                                                        PGLGuidedQueryResult *results, bool cosineProduct);
 OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatch(PGLField field, const PGLGuidedQuery *queries, size_t n,
@@ -83,8 +85,9 @@ OPENPGL_CORE_INTERFACE bool pglFieldSampleVolumeBatchHGDevice(PGLField field, co
 // vertex with SurfaceSamplingDistribution: Init, ApplyCosineProduct, then
 // SamplePDF for each of the vertex's four 2D random numbers,
 // VMMSurfaceSamplingDistribution.h:67-103), in one kernel: host buffers
-// (copies in and out, synchronises) or device buffers enqueued on
-// `cudaStream` (null: the library's stream; does not synchronise).
+// (page-locked ones used in place, others copied in and out; synchronises)
+// or device buffers enqueued on `cudaStream` (null: the library's stream;
+// does not synchronise).
 OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceVertices(PGLField field, const PGLGuidedVertex *vertices, size_t n,
                                                           PGLGuidedVertexResult *results);
 OPENPGL_CORE_INTERFACE bool pglFieldSampleSurfaceVerticesDevice(PGLField field, const PGLGuidedVertex *dVertices,
@@ -227,7 +230,9 @@ OPENPGL_CORE_INTERFACE PGLGuidingServer pglNewGuidingServerEx(PGLField field, si
                                                               int reservedSMs);
 OPENPGL_CORE_INTERFACE void pglReleaseGuidingServer(PGLGuidingServer server);
 // Queues n queries; `queries` and `results` (host memory) must stay valid until
-// the request is waited for.  Returns a ticket (0 on error).
+// the request is waited for.  When both are page-locked, the server's launches
+// read and write them in place (no staging copies).  Returns a ticket (0 on
+// error).
 OPENPGL_CORE_INTERFACE uint64_t pglGuidingServerSubmit(PGLGuidingServer server, const PGLGuidedQuery *queries,
                                                        size_t n, PGLGuidedQueryResult *results, bool volume,
                                                        bool cosineProduct);
