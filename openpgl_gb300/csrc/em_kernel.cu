@@ -85,7 +85,7 @@ struct EmShared {
   float lobeWInv[kMaxK];              // RN(1 / weight) for div_rcp
   float xch[2][kMaxK];
   uint32_t rcpTab[2048];
-  float cost[kMaxPairs];
+  float cost[kMaxK][kMaxK];  // merge cost of components i < j (cost[i][j])
   float ll;
   Unassigned un;
   int mask[kMaxK];
@@ -2033,27 +2033,41 @@ __device__ void sort_candidates(EmShared &S, const SplitState &sp) {
 // the first minimum in (i, j) scan order below the threshold.
 __device__ int perform_merging(EmShared &S, const FieldConfig &cfg) {
   const int tid = threadIdx.x;
-  __shared__ int mergeAgain, total;
-  if (tid == 0) { total = 0; mergeAgain = S.vmm.K > cfg.laneWidth ? 1 : 0; }
+  __shared__ int mergeAgain, total, lastI, lastJ;
+  if (tid == 0) { total = 0; mergeAgain = S.vmm.K > cfg.laneWidth ? 1 : 0; lastI = -1; lastJ = -1; }
   __syncthreads();
   while (mergeAgain) {
     const int K = int(S.vmm.K);
-    const int pairs = K * (K - 1) / 2;
-    for (int p = tid; p < pairs; p += kEmThreads) {
-      // p -> (i, j), i < j, in row-major order of the reference's double loop
-      int i = 0, rem = p;
-      while (rem >= K - 1 - i) { rem -= K - 1 - i; ++i; }
-      int j = i + 1 + rem;
-      S.cost[p] = merge_cost(S.vmm, i, j);
+    if (lastI < 0) {  // every pair
+      const int pairs = K * (K - 1) / 2;
+      for (int p = tid; p < pairs; p += kEmThreads) {
+        // p -> (i, j), i < j
+        int i = 0, rem = p;
+        while (rem >= K - 1 - i) { rem -= K - 1 - i; ++i; }
+        const int j = i + 1 + rem;
+        S.cost[i][j] = merge_cost(S.vmm, i, j);
+      }
+    } else {
+      // after merging lastJ into lastI (and moving the last component into
+      // slot lastJ) only the pairs with those two slots have new operands; a
+      // pair's cost depends on its two components alone, so the others keep
+      // the bits a full recomputation would give
+      const int moved = lastJ < K ? 1 : 0;  // lastJ was not the last slot
+      for (int t = tid; t < (1 + moved) * K; t += kEmThreads) {
+        const int a = t < K ? lastI : lastJ, b = t < K ? t : t - K;
+        if (b == a || (a == lastJ && b == lastI)) continue;  // (lastI, lastJ) is in the first row
+        const int i = a < b ? a : b, j = a < b ? b : a;
+        S.cost[i][j] = merge_cost(S.vmm, i, j);
+      }
     }
     __syncthreads();
     if (tid == 0) {
-      int ci = 0, cj = 0, p = 0;
+      int ci = 0, cj = 0;
       float minCost = FLT_MAX;
       bool found = false;
-      for (int i = 0; i < K - 1; ++i)
-        for (int j = i + 1; j < K; ++j, ++p) {
-          float cost = S.cost[p];
+      for (int i = 0; i < K - 1; ++i)  // the reference's row-major double loop (Merger.h:67-90)
+        for (int j = i + 1; j < K; ++j) {
+          float cost = S.cost[i][j];
           if (cost < cfg.mergeThreshold && cost < minCost && S.split.n[i] > 0.0f && S.split.n[j] > 0.0f) {
             ci = i; cj = j; minCost = cost; found = true;
           }
@@ -2067,6 +2081,8 @@ __device__ int perform_merging(EmShared &S, const FieldConfig &cfg) {
         split_merge_stats(S.split, ci, cj, wI, muI, wJ, muJ, v.w[ci], muK);
         suff_merge(S.suff, ci, cj);
         total++;
+        lastI = ci;
+        lastJ = cj;
       }
       mergeAgain = (found && S.vmm.K > cfg.laneWidth) ? 1 : 0;
     }
