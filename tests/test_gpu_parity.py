@@ -316,3 +316,67 @@ def test_path_vertex_queries(pgl):
         ok = one["ok"] == 1
         assert np.array_equal(one["pdf"][ok].view(np.uint32), got["pdf"][ok].view(np.uint32)), k
         assert np.array_equal(one["dir"][ok].view(np.uint32), got["dir"][ok].view(np.uint32)), k
+
+
+@pytest.mark.parametrize("sizes", [(1, 2, 7, 100, 50000), (0, 40000, 0, 3, 40000)])
+def test_tiny_and_empty_frames(pgl, sizes):
+    """Frames of a handful of samples, and empty frames, between ordinary
+    ones (the first Update may see a single sample: the scene bounds skip the
+    last sample, so a one-sample first frame leaves them degenerate): tree,
+    sample statistics, mixtures and queries as the oracle's after every
+    frame."""
+    from openpgl_gb300 import synthetic as syn
+
+    frames = [syn.cube_face_samples(n, 400 + i, volume_fraction=0.3) if n else
+              np.zeros(0, dtype=syn.cube_face_samples(1, 0).dtype) for i, n in enumerate(sizes)]
+    import pyoracle
+
+    dev = pgl.Device()
+    field = pgl.Field(dev, pgl.FieldConfig(True, 4000))
+    storage = pgl.SampleStorage()
+    orc = pyoracle.OracleField(4000, deterministic=True, threads=os.cpu_count() or 8)
+    q = syn.queries(4096, 499)
+    for f in frames:
+        if len(f):
+            storage.add_samples(f)
+        field.update(storage)
+        storage.clear()
+        orc.update(f)
+        assert field.iteration == orc.iteration
+        for side in ("surface", "volume"):
+            _check_field(field, orc, side)
+        for vol in (False, True):
+            _check_queries(field.sample_batch(q, volume=vol, cosine=not vol), orc.query(q, volume=vol, cosine=not vol),
+                           f"after {len(f)} samples")
+
+
+def test_explicit_scene_bounds_and_outside_queries(pgl):
+    """Scene bounds set before the first Update (pglFieldSetSceneBounds) give
+    the oracle's tree and regions; queries outside the bounds fail their
+    Init, and a negative sample1D takes the leaf's own region (no stochastic
+    neighbour choice), as in the oracle."""
+    import pyoracle
+    from openpgl_gb300 import synthetic as syn
+
+    lo, hi = (-0.5, -0.25, -1.0), (1.5, 1.25, 2.0)
+    dev = pgl.Device()
+    field = pgl.Field(dev, pgl.FieldConfig(True, 4000))
+    field.set_scene_bounds(lo, hi)
+    orc = pyoracle.OracleField(4000, deterministic=True, threads=os.cpu_count() or 8)
+    orc.set_scene_bounds(lo, hi)
+    storage = pgl.SampleStorage()
+    for i in range(2):
+        f = syn.cube_face_samples(60000, 410 + i, volume_fraction=0.25)
+        storage.add_samples(f)
+        field.update(storage)
+        storage.clear()
+        orc.update(f)
+    for side in ("surface", "volume"):
+        _check_field(field, orc, side)
+    q = syn.queries(8192, 420)
+    q["position"][:1024] += np.float32(5.0)  # outside the scene bounds
+    q["sample1d"][1024:2048] = np.float32(-1.0)  # no neighbour choice
+    for vol in (False, True):
+        out = field.sample_batch(q, volume=vol, cosine=not vol)
+        _check_queries(out, orc.query(q, volume=vol, cosine=not vol), f"volume={vol}")
+        assert not out["ok"][:1024].any()
