@@ -1330,8 +1330,9 @@ __device__ void produce_for(EmShared &S, Board &b, float *ring, const EStepShape
 // group are issued two groups before it is added (a warp issues in order, so
 // loads placed after the dependent adds would wait for them).  The products
 // of two samples share one packed multiply (each component rounded as its
-// own multiply).  The loop runs in a function of its own (its registers are
-// not shared with the rest of the kernel) on 32-bit shared-memory addresses.
+// own multiply).  The loop is inlined into the consumer's chunk loop (a call
+// per chunk, with the registers it saves and restores, measured 4 % of the
+// first Update's EM launch) and works on 32-bit shared-memory addresses.
 __device__ __forceinline__ float4 lds4(uint32_t a) {
   float4 v;
   asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
@@ -1364,7 +1365,7 @@ __device__ __forceinline__ float4 lds_if(uint32_t a) {
 }
 // Rows start at 32-bit shared addresses A, D, W (bytes); n4 samples.
 template <int kKind>
-__device__ __noinline__ float chain_rows(uint32_t A, uint32_t D, uint32_t W, int n4, float acc) {
+__device__ __forceinline__ float chain_rows(uint32_t A, uint32_t D, uint32_t W, int n4, float acc) {
   constexpr int kD = kKind == 1, kW = kKind != 2;
   // rows hold C + 4 >= 12 floats: the first two groups can be read even
   // when n4 is smaller
@@ -1424,7 +1425,7 @@ __device__ __forceinline__ void add_group2(float &acc0, float &acc1, float4 a, f
 // Rows start at 32-bit shared addresses A, D0 (kind 1 only), D1, W (bytes);
 // n4 samples; three groups of four samples in flight as in chain_rows.
 template <int kKind>
-__device__ __noinline__ float2 chain_rows2(uint32_t A, uint32_t D0, uint32_t D1, uint32_t W, int n4, float2 acc) {
+__device__ __forceinline__ float2 chain_rows2(uint32_t A, uint32_t D0, uint32_t D1, uint32_t W, int n4, float2 acc) {
   constexpr int kD0 = kKind == 1;
   float a0c = acc.x, a1c = acc.y;
   float4 a0 = lds4(A), e0 = lds_if<kD0>(D0), f0 = lds4(D1), w0 = lds4(W);
