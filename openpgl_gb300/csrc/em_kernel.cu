@@ -39,7 +39,7 @@ constexpr int kMaxPairs = kMaxK * (kMaxK - 1) / 2;
 // ring, from where the home block's loader warp copies them into the stages
 // with bulk copies.  The consumer warps add the chunks in chunk order.
 constexpr int kMaxStages = 8;                          // consumer pipeline stages
-constexpr int kMaxChunk = 384;                         // E-step samples per chunk at most (chunk divisor 1)
+constexpr int kMaxChunk = 768;                         // E-step samples per chunk at most (chunk divisor 1)
 constexpr uint32_t kRingFloats = 65536;                // ring per block (256 KB)
 constexpr uint32_t kRingMaxSlots = 64;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // longest wait before the launch fails
