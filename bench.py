@@ -65,8 +65,8 @@ EM_BYTES_PER_SAMPLE = 32
 REGION_STATE_BYTES = 3008
 # DRAM bytes (read + write) per sample of an EM launch, measured by ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum) on the first Update's launch of
-# this workload (`bench.py --em-capture`: 2,097,152 samples, 113.5 MB)
-EM_TRAFFIC_PER_SAMPLE = 54.1
+# this workload (`bench.py --em-capture`: 2,097,152 samples, 115.7 MB)
+EM_TRAFFIC_PER_SAMPLE = 55.2
 
 
 # the port against the compiled reference (CPU_8, AVX2) on x86, first frame
