@@ -1206,8 +1206,19 @@ __device__ __forceinline__ uint32_t grab_next(unsigned long long w) { return uin
 // direction x, y, z, the weight of valid samples, then w log(pdf) and the
 // four unassigned-sample terms.
 struct EStepShape {
-  int cnt, Kp, parts, P, cons0, consWarps, C, RS, stageFloats, stages, slots;
+  int cnt, Kp, parts, P, cons0, consWarps, C, C0, RS, stageFloats, stages, slots;
 };
+// Chunk k of a pass covers samples [chunk_begin, chunk_begin + chunk_size):
+// the first chunk is one producer round (the leaf's own producers make it
+// while helper blocks are still picking up the pass, and the consumers wait
+// for it), the others C samples.
+__device__ __forceinline__ uint32_t chunk_begin(const EStepShape &e, uint32_t k) {
+  return k == 0 ? 0u : uint32_t(e.C0) + (k - 1u) * uint32_t(e.C);
+}
+__device__ __forceinline__ int chunk_size(const EStepShape &e, uint32_t k) { return k == 0 ? e.C0 : e.C; }
+__device__ __forceinline__ uint32_t chunk_count(const EStepShape &e, uint32_t count) {
+  return count <= uint32_t(e.C0) ? 1u : 1u + (count - uint32_t(e.C0) + uint32_t(e.C) - 1u) / uint32_t(e.C);
+}
 __device__ __forceinline__ EStepShape estep_shape(int cnt, const EmTuning &tune) {
   EStepShape e;
   e.cnt = cnt;
@@ -1224,6 +1235,7 @@ __device__ __forceinline__ EStepShape estep_shape(int cnt, const EmTuning &tune)
   int rounds = min(kMaxChunk, fit) / slots;
   rounds = rounds < 1 ? 1 : rounds;
   e.C = ((rounds * slots) / tune.chunkDiv) & ~7;
+  e.C0 = min(e.C, slots & ~7);
   e.RS = e.C + 4;
   e.stageFloats = (e.Kp + 9) * e.RS;
   e.stages = min(min(kMaxStages, tune.stageCap), 2 * kStageFloats / e.stageFloats);
@@ -1240,15 +1252,17 @@ __device__ void produce_estep_chunk(const EmShared &S, const EStepShape &e, cons
   const int per = nthreads / e.parts;
   const int v = t % e.parts;
   const int RS = e.RS, Kp = e.Kp;
-  for (int base = 0; base < e.C; base += per) {
+  const int size = chunk_size(e, chunk);
+  const uint32_t first = chunk_begin(e, chunk);
+  for (int base = 0; base < size; base += per) {
     const int s = base + t / e.parts;
-    const uint32_t idx = chunk * uint32_t(e.C) + uint32_t(s);
-    const bool have = s < e.C && idx < count;
+    const uint32_t idx = first + uint32_t(s);
+    const bool have = s < size && idx < count;
     const float4 dw = have ? __ldcg(dirw + idx) : make_float4(0.f, 0.f, 0.f, 0.f);
     const V3 d = mk(dw.x, dw.y, dw.z);
     PartTerms T;
     part_terms(S, e.cnt, e.parts, v, have, d, T);
-    if (s < e.C) {
+    if (s < size) {
       const bool valid = have && T.valid;
       if (v < e.cnt) {
 #pragma unroll
@@ -1514,7 +1528,7 @@ __device__ __forceinline__ float2 consume_estep(EmShared &S, const EStepShape &e
     const long long w0 = clock64();
     if (!mbar_wait(&S.full[st], use_parity(S, e, k), &S.abortAt, k, S.err)) break;
     waited += clock64() - w0;
-    const int n = int(min(uint32_t(e.C), count - k * uint32_t(e.C)));
+    const int n = int(min(uint32_t(chunk_size(e, k)), count - chunk_begin(e, k)));
     estep_chunk_chain(S.pbuf + st * e.stageFloats, e, role, (n + 3) & ~3, acc);
     __syncwarp();
     if (lane == 0) {
@@ -1696,7 +1710,7 @@ __device__ void pass_estep(EmShared &S, const LeafSamples &L) {
   const int cnt = vec_count(int(S.vmm.K));
   const EStepShape e = estep_shape(cnt, S.tune);
   const int Kp = e.Kp;
-  uint32_t N = (L.count + uint32_t(e.C) - 1u) / uint32_t(e.C);
+  uint32_t N = L.count == 0 ? 0u : chunk_count(e, L.count);
   if (N > kMaxSharedChunks) {
     if (tid == 0) set_error(S.err, kErrLeafTooLarge);
     N = 0;
