@@ -28,7 +28,6 @@ namespace pgl {
 
 constexpr int kEmThreads = 512;
 constexpr int kStageFloats = 19200;  // floats per pipeline stage (two stages, 150 KB)
-constexpr int kMaxPairs = kMaxK * (kMaxK - 1) / 2;
 
 // E-step passes shared between blocks.  Every block owns a board and a ring of
 // chunk slots in global memory.  For each E-step pass the home block publishes

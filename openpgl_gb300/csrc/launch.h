@@ -36,7 +36,6 @@ cudaError_t split_samples_noalloc(const PGLSampleRecord *in, size_t n, PGLSample
                                   uint32_t *counts, cudaStream_t s);
 
 cudaError_t em_upload_tables(const LibmTables &libm);
-cudaError_t dqt_upload_tables(const LibmTables &libm);
 // The directional quadtree field type (dqt_kernels.cu): one sub-field's
 // quadtrees (a head per region, `stride` node slots per region), its
 // sorted samples and its factory arguments.
