@@ -697,8 +697,8 @@ __device__ __forceinline__ PassShape pass_shape(int Kp, int budget = kStageFloat
     consWarps = (2 * Kp + 31) / 32;
     rows = 2 * Kp;
     extra = 0;
-  } else {  // 5 Kp product chains, then (from a warp boundary) Kp chi-square chains
-    consWarps = (5 * Kp + 31) / 32 + 1;
+  } else {  // 5 Kp product chains, two per lane, then (from a warp boundary) Kp chi-square chains
+    consWarps = (5 * Kp + 63) / 64 + 1;
     rows = 7 * Kp;  // a, a w, three covariance terms, chi, 1/n
     extra = 1;      // validity
   }
@@ -966,14 +966,15 @@ __device__ __forceinline__ void distance_chain(const float *B, const PassShape &
 // group's last n (so every quotient of the group is in range).  From the
 // first group that fails (rare) the chunk is summed again with divisions,
 // which give the same bits wherever Markstein's steps were exact.
-__device__ __forceinline__ int split_chi_base(int Kp) { return ((5 * Kp + 31) / 32) * 32; }
+__device__ __forceinline__ int split_chi_base(int Kp) { return ((5 * Kp + 63) / 64) * 32; }
 __device__ __forceinline__ void split_chain(const float *B, const PassShape &sh, int c, int Kp, int n4, float n0,
-                                            float &acc, float &accN, float &cnt) {
+                                            float &acc, float &acc2, float &accN, float &cnt) {
   const int R = sh.R;
   const int chiBase = split_chi_base(Kp);
-  if (c < 5 * Kp) {
-    row_chain(B + c * R, n4, acc);
-  } else if (c >= chiBase && c < chiBase + Kp) {
+  if (c < chiBase) {  // rows c and c + chiBase (a row chain costs a few cycles per sample, the chi chain ~50)
+    if (c < 5 * Kp) row_chain(B + c * R, n4, acc);
+    if (c + chiBase < 5 * Kp) row_chain(B + (c + chiBase) * R, n4, acc2);
+  } else if (c < chiBase + Kp) {
     const int k = c - chiBase;
     const float *xr = B + (5 * Kp + k) * R, *yr = B + (6 * Kp + k) * R, *vr = B + 7 * Kp * R;
     const float accStart = acc, nStart = accN;
@@ -1034,9 +1035,9 @@ __device__ __forceinline__ void split_chain(const float *B, const PassShape &sh,
 // chunk c - 1.
 template <PassKind kind>
 __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const PassShape &sh, int cnt, float &accOut,
-                                      float &accNOut) {
+                                      float &acc2Out, float &accNOut) {
   const int tid = threadIdx.x;
-  float acc = accOut, accN = accNOut;  // the chains run on registers
+  float acc = accOut, acc2 = acc2Out, accN = accNOut;  // the chains run on registers
   const int Kp = cnt * kLanes;
   const int C = sh.C;
   const uint32_t rounds = (L.count + C - 1) / C;
@@ -1066,12 +1067,13 @@ __device__ __noinline__ void run_pass(EmShared &S, const LeafSamples &L, const P
       const int n4 = (n + 3) & ~3;
       const float *B = S.pbuf + (chunk & 1) * kStageFloats;
       if constexpr (kind == kPassDistance) distance_chain(B, sh, c, Kp, n4, acc);
-      else split_chain(B, sh, c, Kp, n4, n0, acc, accN, count);
+      else split_chain(B, sh, c, Kp, n4, n0, acc, acc2, accN, count);
       cycC += clock64() - t0;
     }
     __syncthreads();
   }
   accOut = acc;
+  acc2Out = acc2;
   accNOut = accN;
   const int probe = kind == kPassSplit ? split_chi_base(Kp) : 0;
   if (tid == 0 && kind == kPassSplit) S.prof.cycProdS += uint64_t(cycP);
@@ -1907,7 +1909,8 @@ __device__ void pass_distances(EmShared &S, const LeafSamples &L, bool init) {
   pack_lobes(S, Kp);
   __syncthreads();
   float acc = 0.0f, accN = 0.0f;
-  run_pass<kPassDistance>(S, L, sh, cnt, acc, accN);
+  float unused = 0.0f;
+  run_pass<kPassDistance>(S, L, sh, cnt, acc, unused, accN);
   // exchange: bd in xch[0][k], bw in xch[1][k]
   const int c = tid - sh.P;
   if (c >= 0 && c < 2 * Kp) S.xch[c / Kp][c % Kp] = acc;
@@ -1948,22 +1951,31 @@ __device__ void pass_split_stats(EmShared &S, const LeafSamples &L, SplitState &
   __syncthreads();
   const int c = tid - sh.P;
   const int chiBase = split_chi_base(Kp);
-  float acc = 0.0f, accN = 0.0f;
-  if (c >= 0 && c < 5 * Kp) {
-    const int r = c / Kp, k = c % Kp;
-    acc = r == 0 ? sp.sa[k] : r == 1 ? sp.sw[k] : r == 2 ? sp.cx[k] : r == 3 ? sp.cy[k] : sp.cz[k];
+  // row q < 5 Kp: r = q / Kp selects sa, sw, cx, cy, cz of lobe k = q % Kp
+  auto row_value = [&](int q) {
+    const int r = q / Kp, k = q % Kp;
+    return r == 0 ? sp.sa[k] : r == 1 ? sp.sw[k] : r == 2 ? sp.cx[k] : r == 3 ? sp.cy[k] : sp.cz[k];
+  };
+  auto row_store = [&](int q, float v) {
+    const int r = q / Kp, k = q % Kp;
+    if (r == 0) sp.sa[k] = v;
+    else if (r == 1) sp.sw[k] = v;
+    else if (r == 2) sp.cx[k] = v;
+    else if (r == 3) sp.cy[k] = v;
+    else sp.cz[k] = v;
+  };
+  float acc = 0.0f, acc2 = 0.0f, accN = 0.0f;
+  if (c >= 0 && c < chiBase) {
+    if (c < 5 * Kp) acc = row_value(c);
+    if (c + chiBase < 5 * Kp) acc2 = row_value(c + chiBase);
   } else if (c >= chiBase && c < chiBase + Kp) {
     acc = sp.chi2[c - chiBase];
     accN = sp.n[c - chiBase];
   }
-  run_pass<kPassSplit>(S, L, sh, cnt, acc, accN);
-  if (c >= 0 && c < 5 * Kp) {
-    const int r = c / Kp, k = c % Kp;
-    if (r == 0) sp.sa[k] = acc;
-    else if (r == 1) sp.sw[k] = acc;
-    else if (r == 2) sp.cx[k] = acc;
-    else if (r == 3) sp.cy[k] = acc;
-    else sp.cz[k] = acc;
+  run_pass<kPassSplit>(S, L, sh, cnt, acc, acc2, accN);
+  if (c >= 0 && c < chiBase) {
+    if (c < 5 * Kp) row_store(c, acc);
+    if (c + chiBase < 5 * Kp) row_store(c + chiBase, acc2);
   } else if (c >= chiBase && c < chiBase + Kp) {
     sp.chi2[c - chiBase] = acc;
     sp.n[c - chiBase] = accN;
