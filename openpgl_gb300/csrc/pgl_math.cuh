@@ -193,13 +193,6 @@ PGL_HD float lib_expf(float x) {
   return std::exp(x);
 #endif
 }
-PGL_HD float lib_logf(float x) {
-#ifdef __CUDA_ARCH__
-  return float(log(double(x)));
-#else
-  return std::log(x);
-#endif
-}
 PGL_HD float lib_cosf(float x) {
 #ifdef __CUDA_ARCH__
   return libm_lookup(d_libm.cosf, d_libm.numCosf, x, float(cos(double(x))));
@@ -296,10 +289,6 @@ PGL_HD float rcp_rn(float b) { return div_faithful_fix(1.0f, b, rcp_approx(b)); 
 PGL_HD float markstein_q(float a, float b, float y) {
   const float q0 = a * y;
   return fmaf_(fmaf_(-q0, b, a), y, q0);
-}
-PGL_HD bool in_div_range(float a, float q) {
-  const float aa = a < 0.0f ? -a : a, aq = q < 0.0f ? -q : q;
-  return aa >= 1e-30f && aa <= 1e30f && aq >= 1e-30f && aq <= 1e30f;
 }
 
 // fastapprox::exp
