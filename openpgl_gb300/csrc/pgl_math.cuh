@@ -166,6 +166,103 @@ PGL_HD float floorf_(float x) {
 #endif
 }
 
+// Double-float arithmetic: a value h + l held as two floats, |l| <= ulp(h)/2
+// (T. J. Dekker, "A floating-point technique for extending the available
+// precision", Numer. Math. 18, 1971), from the error-free sum (Knuth) and the
+// error-free product by FMA.
+struct DFloat {
+  float h, l;
+};
+PGL_HD DFloat df_fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+PGL_HD DFloat df_two_sum(float a, float b) {
+  const float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+PGL_HD DFloat df_two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf_(a, b, -p)};
+}
+PGL_HD DFloat df_mul(DFloat a, DFloat b) {
+  const float p = a.h * b.h;
+  float e = fmaf_(a.h, b.h, -p);
+  e = fmaf_(a.h, b.l, e);
+  e = fmaf_(a.l, b.h, e);
+  return df_fast_two_sum(p, e);
+}
+PGL_HD DFloat df_mul_f(DFloat a, float b) {
+  const float p = a.h * b;
+  return df_fast_two_sum(p, fmaf_(a.l, b, fmaf_(a.h, b, -p)));
+}
+// a + b where the sum does not cancel (|a + b| well above |a| / 2 or |b| / 2)
+PGL_HD DFloat df_add(DFloat a, DFloat b) {
+  const DFloat s = df_two_sum(a.h, b.h);
+  return df_fast_two_sum(s.h, s.l + (a.l + b.l));
+}
+
+// sin x and cos x of a float 0 <= x < 8 in double-float arithmetic, before
+// rounding: the additive reduction of W. J. Cody and W. Waite (Software
+// Manual for the Elementary Functions, 1980) by pi/2 = C1 + C2 + C3 (floats;
+// k <= 5 and |x - k C1| < 1, so fma(-k, C1, x) is exact), then the Taylor
+// series of sin r and cos r for |r| <= pi/4 (to r^15 and r^16), the leading
+// coefficients as double-floats, the tails in float.  The constants are the
+// exact values rounded to float (hi) and the remainders rounded to float (lo).
+// The relative error of either result is below 2^-41 on every float of the
+// range (checked against long double).
+PGL_HD void sincos_df_parts(float x, DFloat *s, DFloat *c) {
+  const float kf = rintf(x * 0x1.45f306p-1f);  // x * 2/pi to the nearest integer
+  const float t1 = fmaf_(-kf, 0x1.921fb6p+0f, x);
+  const DFloat p = df_two_prod(kf, -0x1.777a5cp-25f);
+  const DFloat s0 = df_two_sum(t1, -p.h);
+  const DFloat r = df_two_sum(s0.h, (s0.l - p.l) - kf * -0x1.ee59dap-50f);
+  const DFloat z = df_mul(r, r);
+  // sin r = r + r z (S1 + z (S2 + z (S3 + z T))), S_i = (-1)^i / (2i + 1)!
+  const float t = fmaf_(fmaf_(fmaf_(-0x1.ae7f3ep-41f, z.h, 0x1.612462p-33f), z.h, -0x1.ae6456p-26f), z.h,
+                        0x1.71de3ap-19f);
+  DFloat a = df_add({-0x1.a01a02p-13f, 0x1.7f97fap-39f}, df_mul_f(z, t));
+  a = df_add({0x1.111112p-7f, -0x1.dddddep-32f}, df_mul(z, a));
+  a = df_add({-0x1.555556p-3f, 0x1.555556p-28f}, df_mul(z, a));
+  const DFloat sr = df_add(r, df_mul(r, df_mul(z, a)));
+  // cos r = 1 + z (-1/2 + z (C2 + z (C3 + z T'))), C_i = (-1)^i / (2i)!
+  const float tc = fmaf_(fmaf_(fmaf_(fmaf_(0x1.ae7f3ep-45f, z.h, -0x1.93974ap-37f), z.h, 0x1.1eed8ep-29f), z.h,
+                               -0x1.27e4fcp-22f), z.h, 0x1.a01a02p-16f);
+  DFloat b = df_add({-0x1.6c16c2p-10f, 0x1.27d27ep-35f}, df_mul_f(z, tc));
+  b = df_add({0x1.555556p-5f, -0x1.555556p-30f}, df_mul(z, b));
+  b = df_add({-0.5f, 0.0f}, df_mul(z, b));
+  const DFloat cr = df_add({1.0f, 0.0f}, df_mul(z, b));
+  const DFloat nsr = {-sr.h, -sr.l}, ncr = {-cr.h, -cr.l};
+  switch (int(kf) & 3) {
+    case 0: *s = sr; *c = cr; break;
+    case 1: *s = cr; *c = nsr; break;
+    case 2: *s = nsr; *c = ncr; break;
+    default: *s = ncr; *c = sr; break;
+  }
+}
+// A double-float rounded to float by A. Ziv's test ("Fast evaluation of
+// elementary mathematical functions with correctly rounded last bit", ACM
+// TOMS 17(3), 1991): the value, widened by 2^-38 relative on either side,
+// must round to one float, which then is the exact value rounded to nearest.
+PGL_HD bool df_round_checked(DFloat v, float *out) {
+  const float e = fabsf(v.h) * 0x1p-38f;
+  const float lo = v.h + (v.l - e), hi = v.h + (v.l + e);
+  *out = lo;
+  return lo == hi;
+}
+// sin x and cos x correctly rounded for +0 <= x < 8, in float arithmetic;
+// false (outputs unspecified) where the test above cannot decide or x is
+// outside that range.  Where it returns true, both equal the double-precision
+// functions rounded once to float.
+PGL_HD bool sincos_df(float x, float *s, float *c) {
+  if (f2u(x) >= 0x41000000u) return false;  // not +0 <= x < 8 (-0 keeps its sign on the double path)
+  DFloat ds, dc;
+  sincos_df_parts(x, &ds, &dc);
+  const bool okS = df_round_checked(ds, s);
+  const bool okC = df_round_checked(dc, c);
+  return okS && okC;
+}
+
 // Single-precision exp/log/cos/sin/sincos as the host C library returns them
 // (std::exp(float) etc. on the reference side).  On the device each is
 // evaluated in double and rounded once to float: that is the correctly rounded
@@ -218,8 +315,14 @@ PGL_HD float lib_cosf_any(float x) {
   return std::cos(x);
 #endif
 }
+// On the device: the float evaluation of sincos_df where it decides (all but
+// about 3 in 100,000 inputs of [0, 2 pi]), which gives the same bits as the
+// double path below (checked on every float of [0, 8)) at a small fraction
+// of its cost: a double-precision instruction occupies a warp scheduler for
+// tens of cycles on this part.
 PGL_HD void lib_sincosf(float x, float *s, float *c) {
 #ifdef __CUDA_ARCH__
+  if (sincos_df(x, s, c)) return;
   double sd, cd;
   sincos(double(x), &sd, &cd);
   *s = float(sd);
