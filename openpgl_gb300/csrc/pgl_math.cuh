@@ -202,7 +202,7 @@ PGL_HD DFloat df_add(DFloat a, DFloat b) {
   return df_fast_two_sum(s.h, s.l + (a.l + b.l));
 }
 
-// sin x and cos x of a float 0 <= x < 8 in double-float arithmetic, before
+// sin x and cos x of a float +0 <= x < 8 in double-float arithmetic, before
 // rounding: the additive reduction of W. J. Cody and W. Waite (Software
 // Manual for the Elementary Functions, 1980) by pi/2 = C1 + C2 + C3 (floats;
 // k <= 5 and |x - k C1| < 1, so fma(-k, C1, x) is exact), then the Taylor
